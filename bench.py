@@ -1,0 +1,304 @@
+"""Benchmark of the batched GB300 propagation engine.
+
+Workload (default): the batched laser scan -- 256 hydrogen wavefunctions,
+B-splines order 7 (p = 6), N_r = 800 on [0, 400] a.u. with uniform knots,
+l_max = 40 (n_l = 41), z-linear length gauge, dt = 0.05, sharing one H0
+factorisation; per wavefunction, seeded draws (numpy default_rng(2025)) of the
+peak intensity (log-uniform 5e13..5e14 W/cm^2), wavelength (uniform
+400..2000 nm), CEP (uniform [0, 2 pi)) and sin^2 cycles (integer 2..10).
+
+One bench step = one time step of every wavefunction in the batch (all 256
+are inside their pulse for the first 2207 steps, which is where the timed
+window sits).  Metric: wavefunction-steps/s.
+
+  value      device time (CUDA events on the engine's stream) of
+             qpc_lgwz_run over the timed steps, states resident in HBM
+  e2e        the same steps through the public C ABI with host buffers:
+             qpc_lgwz_put (host -> device) + qpc_lgwz_run + qpc_lgwz_get
+             (device -> host) per timed step, wall clock
+  plain_1wf  the plain one-wavefunction-at-a-time GPU path (n_inst = 1, same
+             kernels) on the same grid and fields, device time
+  roofline   the dominant kernel (the coupling sweeps), FP64 flops per launch
+             over its CUDA-event duration, against the measured FP64 peak
+  cpu_baseline  the CPU oracle (a port of the reference's propagator) on the
+             host cores, a bounded sample of the same workload
+
+--impl reference times the reference's CPU implementation of the path (the
+oracle port: the reference itself needs x86 and MKL) on all host cores.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+# FP64 FMA peak measured on this machine's GB300 (profiles/fp64_peak_gb300.md):
+# 1.19 TFLOP/s with DFMA (FMA = 2 flops); DMMA (mma.sync f64) 1.05 TFLOP/s on the same pipe.
+FP64_PEAK_TFLOPS = 1.19
+
+
+def load_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            return json.load(fh)
+    except Exception:
+        return {}
+
+
+def c2_workload(n_inst=256, seed=2025):
+    rng = np.random.default_rng(seed)
+    inten = 10 ** rng.uniform(np.log10(5e13), np.log10(5e14), n_inst)
+    lam_nm = rng.uniform(400.0, 2000.0, n_inst)
+    cep = rng.uniform(0.0, 2 * np.pi, n_inst)
+    cyc = rng.integers(2, 11, n_inst)
+    return inten, lam_nm, cep, cyc
+
+
+def field_tables(q, inten, lam_nm, cep, cyc, dt=0.05):
+    tabs = [q.field_sinen(q.intensity_to_e0(I), q.wavelength_to_w0(l), float(c), 0.0, float(p / np.pi), dt)
+            for I, l, p, c in zip(inten, lam_nm, cep, cyc)]
+    nt = np.array([t.size - 1 for t in tabs], dtype=np.int64)
+    return tabs, nt
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self):
+        self.p = None
+        self.path = os.path.join(ROOT, "gpurun_out", "clocks_bench.csv") if os.path.isdir(os.path.join(ROOT, "gpurun_out")) else "/tmp/clocks_bench.csv"
+
+    def __enter__(self):
+        try:
+            self.fh = open(self.path, "w")
+            self.p = subprocess.Popen(
+                ["nvidia-smi", "--query-gpu=index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.fh, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+        return self
+
+    def __exit__(self, *a):
+        if self.p is not None:
+            self.p.terminate()
+            try:
+                self.p.wait(5)
+            except Exception:
+                self.p.kill()
+            self.fh.close()
+
+    def summary(self):
+        try:
+            rows = [l.split(",") for l in open(self.path).read().strip().splitlines() if l.strip()]
+        except Exception:
+            return None
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows]
+        mx = float(rows[0][2])
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({n for r in rows for n, v in zip(names, r[5:9]) if v.strip() == "Active"})
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": reasons, "samples": len(rows)}
+
+
+def setup_grid(q, n_r=800, p=6, n_l=41, rmax=400.0):
+    t = q.linear_knots(n_r, p, 0.0, rmax)
+    S, R, _, _, H = q.radial_setup(n_r, p, n_l, t)
+    c0, e = q.ground_state(S, H, n_l)
+    return S, R, H, c0
+
+
+def sweep_flops(n_r, p, live_pairs, power):
+    """FP64 flops of one coupling-sweep launch as implemented: per pair, row and
+    application, four lanes each do (2p+1) + 2p FMAs forward and 2p + 2 FMAs + 1 MUL
+    backward (FMA = 2 flops)."""
+    fma = (2 * p + 1) + 2 * p + (2 * p + 2)
+    return live_pairs * n_r * power * 4 * (2 * fma + 1)
+
+
+def run_engine(args):
+    import importlib
+    q = importlib.import_module("qpc-tdse-cpc_gb300")
+    B, n_r, p, n_l, dt = args.batch, 800, 6, 41, 0.05
+    S, R, H, c0 = setup_grid(q, n_r, p, n_l)
+    inten, lam_nm, cep, cyc = c2_workload(B)
+    tabs, nt = field_tables(q, inten, lam_nm, cep, cyc, dt)
+    K, W = args.steps, args.warmup
+    assert W + K <= nt.min(), "timed window must stay inside every pulse"
+    ftab = np.stack([t[:W + K + 1] for t in tabs])
+    state0 = np.repeat(c0[None], B, 0)
+
+    prop = q.propagator_cn_hc_lgwz().initialize(n_r, p, n_l, S, R, H, dt, n_inst=B)
+    launches0 = prop.launch_count()
+    prop.put(state0)
+    # warm-up: W steps (untimed)
+    prop.run(ftab[:, :W + 1], np.full(B, W))
+    # timed: K steps continuing from t_W (inputs resident, working set > L2)
+    q.load()
+    with Clocks() as clk:
+        launches1 = prop.launch_count()
+        prop.enable_profiling(True)
+        prop.run(ftab[:, W:W + K + 1], np.full(B, K))
+        dev_ms = prop.last_run_ms()
+        ktimes = prop.kernel_times()
+        prop.enable_profiling(False)
+        gpu_launches = prop.launch_count() - launches1
+        # e2e through the C ABI with host buffers, copies inside the timed region
+        host_in = np.ascontiguousarray(state0)
+        t0 = time.perf_counter()
+        prop.put(host_in)
+        prop.run(ftab[:, W:W + K + 1], np.full(B, K))
+        out = prop.get()
+        e2e_s = time.perf_counter() - t0
+    clocks = clk.summary()
+    value = B * K / (dev_ms * 1e-3)
+    e2e = B * K / e2e_s
+    state_bytes = state0.nbytes
+    h2d = (state_bytes + ftab[:, W:W + K + 1].nbytes) / K
+    d2h = state_bytes / K
+    # dominant kernel: coupling sweeps
+    sw_ms, sw_n = ktimes.get("sweep", (0.0, 0))
+    live_pairs = B * (n_l // 2)
+    fl = sweep_flops(n_r, p, live_pairs, 2)
+    achieved = fl / (sw_ms / max(sw_n, 1) * 1e-3) / 1e12 if sw_n else None
+    peaks = load_peaks()
+    # algorithmic bytes of one sweep launch: factors read 4x (p+1 complex per row and pair),
+    # eigenbasis state in and out, two scratch vectors written and read twice
+    sweep_bytes = live_pairs * n_r * ((p + 1) * 16 * 4 + 2 * 16 * 2 + 2 * 16 * 2 * 2)
+    roof = {"bound": "fp64", "kernel": "k_sweep", "achieved": achieved, "peak": FP64_PEAK_TFLOPS,
+            "unit": "TFLOP/s", "frac": (achieved / FP64_PEAK_TFLOPS) if achieved else None,
+            "peak_source": "measured DFMA peak, profiles/fp64_peak_gb300.md",
+            "flops_per_launch": fl, "launch_ms": sw_ms / max(sw_n, 1) if sw_n else None,
+            "traffic": None,
+            "hbm": {"achieved_gbs": sweep_bytes / (sw_ms / max(sw_n, 1) * 1e-3) / 1e9 if sw_n else None,
+                    "peak_gbs": peaks.get("hbm_gbs"), "bytes_per_launch": sweep_bytes}}
+    if roof["hbm"]["achieved_gbs"] and peaks.get("hbm_gbs"):
+        roof["hbm"]["frac"] = roof["hbm"]["achieved_gbs"] / peaks["hbm_gbs"]
+    kt = {k: {"ms_total": v[0], "launches": v[1]} for k, v in ktimes.items()}
+    prop.close()
+
+    # plain one-wavefunction GPU path, same kernels, same grid, fields of instance 0
+    Kp = min(K, 60)
+    pl = q.propagator_cn_hc_lgwz().initialize(n_r, p, n_l, S, R, H, dt, n_inst=1)
+    pl.put(c0[None])
+    pl.run(ftab[:1, :W + 1], [W])
+    pl.run(ftab[:1, W:W + Kp + 1], [Kp])
+    plain = Kp / (pl.last_run_ms() * 1e-3)
+    gpu_launches += 0
+    pl.close()
+
+    cpu = cpu_baseline(q, S, R, H, c0, ftab, dt, n_l, budget_s=args.cpu_seconds) if not args.no_cpu else None
+    line = {
+        "metric": "wavefunction-steps/s (batched, 256 wavefunctions)",
+        "value": value, "unit": "wf-steps/s", "n_gpus": 1, "steps": K, "warmup": W,
+        "ms_per_step": dev_ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "c128 (complex FP64)", "data": "synthetic (seeded laser parameters, numpy default_rng(2025))",
+        "config": {"workload": "batched laser scan: 256 H atoms, N_r=800, p=6, l_max=40, z-linear length gauge, dt=0.05",
+                   "n_inst": B, "n_r": n_r, "p": p, "n_l": n_l, "dt": dt, "parallelism": "replicas only",
+                   "l2": "working set %.1f GB > 129 MB L2 (no flush needed)" % ((B * n_l * n_r * 16 * 4 + 8 * B * (n_l // 2) * n_r * 7 * 16) / 1e9)},
+        "e2e": {"value": e2e, "unit": "wf-steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "plain_1wf": {"value": plain, "unit": "wf-steps/s", "ratio_batched_over_plain": value / plain},
+        "gpu_launches": gpu_launches,
+        "kernels": kt,
+        "roofline": roof,
+        "cpu_baseline": cpu,
+        "clocks": clocks,
+    }
+    return line
+
+
+def cpu_baseline(q, S, R, H, c0, ftab, dt, n_l, budget_s=15.0, threads=None):
+    """The CPU oracle (port of the reference's propagator_cn_hc_lgwz), one
+    wavefunction per host thread, on a bounded number of steps of the same workload."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from conftest import Oracle
+    threads = threads or os.cpu_count()
+    o = Oracle()
+    # calibrate on one instance
+    g1 = o.grid(S, R, H, dt, n_l, n_inst=1)
+    t0 = time.perf_counter()
+    o.run(g1, c0[None], ftab[:1, :4], [3], [3], threads=1)
+    per_step = (time.perf_counter() - t0) / 3
+    steps = int(max(3, min(ftab.shape[1] - 1, budget_s / per_step)))
+    g = o.grid(S, R, H, dt, n_l, n_inst=threads)
+    st = np.repeat(c0[None], threads, 0)
+    tab = ftab[:threads, :steps + 1] if ftab.shape[0] >= threads else np.repeat(ftab[:1, :steps + 1], threads, 0)
+    t0 = time.perf_counter()
+    o.run(g, st, tab, [steps] * threads, [steps] * threads, threads=threads)
+    el = time.perf_counter() - t0
+    return {"value": threads * steps / el, "unit": "wf-steps/s", "cores": threads, "kind": "port",
+            "sample": "%d wavefunctions x %d steps of the same workload, one per host thread (%.1f s)" % (threads, steps, el)}
+
+
+def run_reference(args):
+    import importlib
+    q = importlib.import_module("qpc-tdse-cpc_gb300")
+    B, n_r, p, n_l, dt = args.batch, 800, 6, 41, 0.05
+    S, R, H, c0 = setup_grid(q, n_r, p, n_l)
+    inten, lam_nm, cep, cyc = c2_workload(B)
+    tabs, nt = field_tables(q, inten, lam_nm, cep, cyc, dt)
+    ftab = np.stack([t[:args.steps + 2] for t in tabs])
+    vals = []
+    budget = max(2.0, 60.0 / max(args.steps + args.warmup, 1))
+    for i in range(args.warmup + args.steps):
+        r = cpu_baseline(q, S, R, H, c0, ftab, dt, n_l, budget_s=budget)
+        if i >= args.warmup:
+            vals.append(r["value"])
+    v = float(np.median(vals))
+    r["value"] = v
+    return {"impl": "reference", "metric": "wavefunction-steps/s (batched, 256 wavefunctions)", "value": v,
+            "unit": "wf-steps/s", "n_gpus": 0, "steps": args.steps, "warmup": args.warmup,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128 (complex FP64)",
+            "data": "synthetic (seeded laser parameters, numpy default_rng(2025))",
+            "config": {"workload": "batched laser scan: 256 H atoms, N_r=800, p=6, l_max=40, z-linear length gauge, dt=0.05",
+                       "n_inst": B},
+            "cpu_baseline": r, "e2e": {"value": v, "unit": "wf-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
+    ap.add_argument("--batch", type=int, default=256)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        print(json.dumps(run_reference(args)))
+        return
+    if world > 1:
+        # replicas only: every rank runs its own batch; value = sum over ranks
+        import torch
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        dist.barrier()
+        line = run_engine(args)
+        t = torch.tensor([line["ms_per_step"]], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        if rank == 0:
+            line["n_gpus"] = world
+            line["ms_per_step"] = float(t.item())
+            line["value"] = world * args.batch * 1e3 / line["ms_per_step"]
+            print(json.dumps(line))
+        dist.destroy_process_group()
+        return
+    print(json.dumps(run_engine(args)))
+
+
+if __name__ == "__main__":
+    main()

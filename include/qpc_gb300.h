@@ -1,0 +1,178 @@
+/*
+ * qpc_gb300.h -- C ABI of the GB300 propagation engine for QPC-TDSE.
+ *
+ * The reference (zzh535897/QPC-TDSE-CPC) has no runtime plugin API: its
+ * propagators are C++ templates selected at compile time
+ * (binsrc/sphTDSE.cpp:574-600) and called from the driver's step loop
+ * (binsrc/sphTDSE.cpp:786-831).  This header is the boundary a caller crosses
+ * instead: plain C types, host pointers, int status codes, no C++ exceptions
+ * and no torch types.  Each entry point names the reference member it replaces.
+ *
+ * Layouts (identical to the reference, so state export is a memcpy):
+ *   wavefunction  c[inst][m][l][r] complex128 (re, im interleaved)
+ *                 (spherical/coefficient/1e.hpp, recvec<comp_t,recidx<m,l,r>>)
+ *   radial band   A[r*(p+1)+k] = A(r, r+k), k = 0..p, real float64
+ *                 (spherical/operators/1e.hpp:20)
+ *   H per l       H[l][r][k] for l = 0..lmax, lmax = max|m| + n_l - 1
+ *                 (spherical/operators/1e.hpp:595-648)
+ *
+ * Status codes: 0 on success, a QPC_ERR_* value otherwise; qpc_last_error()
+ * returns a message for the calling thread's last failure.  Nothing here
+ * throws, aborts, traps a GPU or waits without a bound.
+ */
+#ifndef QPC_GB300_H
+#define QPC_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define QPC_OK 0
+#define QPC_ERR_ARGS 1      /* bad dimensions, pointers or values */
+#define QPC_ERR_NOMEM 2     /* device or host allocation failed */
+#define QPC_ERR_CUDA 3      /* a CUDA call failed */
+#define QPC_ERR_SINGULAR 4  /* a zero pivot in a factorisation */
+#define QPC_ERR_NUMERIC 5   /* non-finite value or no convergence */
+#define QPC_ERR_TIMEOUT 6   /* a bounded wait for the device ran out */
+#define QPC_ERR_STATE 7     /* call made in the wrong state */
+#define QPC_ERR_NODEVICE 8  /* no CUDA device, or not a GB300-class device */
+
+#define QPC_MAX_RANK 8      /* largest B-spline degree p the engine accepts */
+
+enum { QPC_POTENTIAL_HYDROGENIC = 0, QPC_POTENTIAL_YUKAWA = 1 };
+
+/* V(r) = -zc/r (hydrogenic, spherical/potential.hpp:9-17) or
+ * V(r) = -(zc + zs exp(-sigma r))/r (hydrogenic_yukawa, potential.hpp:19-29). */
+typedef struct qpc_potential {
+	int32_t kind;
+	double zc, zs, sigma;
+} qpc_potential;
+
+/* Grid of one batch; replaces dimension_1e<nr,mr,nl,nm,m0> (spherical/dimension/1e.hpp:20-127). */
+typedef struct qpc_dims {
+	int32_t n_r;    /* active radial B-splines   (dims_t::n_dims) */
+	int32_t p;      /* B-spline degree            (dims_t::n_diag); bands hold p+1 per row */
+	int32_t n_l;    /* l channels per m           (dims_t::l_dims); l = |m| + il */
+	int32_t n_m;    /* m channels                 (dims_t::m_dims) */
+	int32_t m0;     /* first m                    (dims_t::m_init) */
+	int32_t n_inst; /* wavefunctions advanced together (1 for the plain path) */
+} qpc_dims;
+
+const char* qpc_last_error(void);
+/* Engine version string; also reports the SM arch the library was built for. */
+const char* qpc_version(void);
+
+/* ---------------------------------------------------------------- setup (host)
+ * One-time matrix construction, done on the host as in the reference. */
+
+/* Knots of bsplines::initialize_axis_linear_step (functions/basis_bsplines.h:450-459):
+ * writes n_r + p + 3 values. */
+int qpc_linear_knots(int32_t n_r, int32_t p, double rmin, double rmax, double* knots);
+
+/* integrator_radi::integrate_0r0 / _0r1 / integrate_hc (spherical/utilities/basisfunc.hpp:63-106)
+ * on the given knots with 2p+2 Gauss-Legendre points per interval:
+ * S = <Bi|Bj>, R = <Bi|r|Bj>, Rinv = <Bi|1/r|Bj>, D = <Bi|d/dr Bj>,
+ * H[l] = <Bi|V + l(l+1)/(2 mass r^2)|Bj> + <Bi'|Bj'>/(2 mass) for l < n_lh.
+ * Any output pointer may be NULL. */
+int qpc_radial_setup(int32_t n_r, int32_t p, int32_t n_lh, const double* knots, const qpc_potential* pot,
+	double mass, double* S, double* R, double* Rinv, double* D, double* H);
+
+/* integrator_angu::integrate_cos (spherical/utilities/basisfunc.hpp:222-229): y10[il] = <l,m|cos|l+1,m>. */
+int qpc_y10_coupling(int32_t n_l, int32_t m, double* y10);
+
+/* operator_y10::solve_eigen for one m (spherical/operators/1e.hpp:304-333):
+ * lam[n_l] ascending, P[n_l][n_l] row-major with row a = eigenvector a. */
+int qpc_y10_eigen(int32_t n_l, int32_t m, double* lam, double* P);
+
+/* lu_zsb of S + i g H (algorithm/ed.h:208-289) in the engine's layout:
+ * Lrow[r][k-1] = L(r, r-k) (complex), Dinv[r] = 1/D(r) (complex).
+ * Returns the count of pivots with |D|^2 < 1e-31, or -1 on bad arguments. */
+int qpc_ldlt_csym(int32_t n, int32_t p, const double* S, const double* H, double g, double* Lrow, double* Dinv);
+
+/* gv_dsb (LAPACKE_dsbgv, algorithm/ed.h:105-112): all eigenvalues of H v = E S v
+ * ascending, and the lowest n_want S-normalised eigenvectors (rows of vec). */
+int qpc_gen_eigen(int32_t n, int32_t p, const double* S, const double* Hl, int32_t n_want, double* energy, double* vec);
+
+/* field_component_sinen<n_pow> inside field<> (structure/field.h:89-133, 245-281):
+ * *nt_out = para_nt; when f != NULL writes f(t_i), i = 0..para_nt (cap >= para_nt+1). */
+int qpc_field_sinen(int32_t n_pow, double e0, double w0, double nc, double n0, double cep, double dt,
+	int64_t cap, double* f, int64_t* nt_out);
+
+/* ---------------------------------------------------------------- propagator
+ * propagator_cn_hc_lgwz (spherical/propagator/cn_1e.hpp:549-619): length gauge,
+ * field along z, Crank-Nicolson split operator, for a batch of n_inst
+ * wavefunctions that share one grid, potential and dt.  The handle owns its
+ * device memory and one CUDA stream; calls on one handle are not re-entrant,
+ * calls on different handles may come from different threads. */
+typedef struct qpc_lgwz qpc_lgwz;
+
+/* Replaces propagator_cn_hc_lgwz::initialize(nthd, radi, angu, mass, potn, dt)
+ * (cn_1e.hpp:565-593).  S, R: [n_r][p+1]; H: [lmax+1][n_r][p+1] with
+ * lmax = max(|m0|, |m0+n_m-1|) + n_l - 1.  Builds the field-free bands and
+ * their LDL^T (cn_component_hc::initialize) and the Y10 eigensystem per m.
+ * Errors: QPC_ERR_ARGS, QPC_ERR_NODEVICE, QPC_ERR_NOMEM, QPC_ERR_SINGULAR. */
+int qpc_lgwz_create(const qpc_dims* dims, double dt, const double* S, const double* R, const double* H, qpc_lgwz** out);
+
+/* Frees everything the handle owns.  NULL is accepted. */
+int qpc_lgwz_destroy(qpc_lgwz* h);
+
+/* Copy the batch state in/out, host layout c[inst][m][l][r] complex128
+ * (what coefficient<dims_t>::data holds, coefficient/1e.hpp:11-53). */
+int qpc_lgwz_put(qpc_lgwz* h, const double* coef);
+int qpc_lgwz_get(qpc_lgwz* h, double* coef);
+/* Same, with device-resident buffers in the host layout (no host copy). */
+int qpc_lgwz_put_device(qpc_lgwz* h, const double* dev_coef);
+int qpc_lgwz_get_device(qpc_lgwz* h, double* dev_coef);
+
+/* One call of propagate(coef, ez_ti, ez_tf) (cn_1e.hpp:595-613) for every
+ * instance: f_ti[inst], f_tf[inst] are the field at t_i and t_{i+1}. */
+int qpc_lgwz_propagate(qpc_lgwz* h, const double* f_ti, const double* f_tf);
+
+/* One field-free propagate(coef) (cn_1e.hpp:615-618) for every instance. */
+int qpc_lgwz_propagate_free(qpc_lgwz* h);
+
+/* The driver loop (binsrc/sphTDSE.cpp:786-831) for the whole batch in one call:
+ * instance k takes nt_field[k] field steps with f(t_i) = ftab[k*ld + i],
+ * i = 0..nt_field[k] (nt_field[k]+1 values), then field-free steps until
+ * nt_total[k] >= nt_field[k] steps in all.  Instances advance independently,
+ * so uneven step counts are fine.  The result equals nt_total[k] single calls
+ * (within rounding: consecutive coupling half-steps are fused). */
+int qpc_lgwz_run(qpc_lgwz* h, const double* ftab, int64_t ld, const int64_t* nt_field, const int64_t* nt_total);
+
+/* S-norm per instance, sum over (m,l) of c^H S c
+ * (operator_rsym::observe, spherical/operators/1e.hpp:69-89); norm[n_inst]. */
+int qpc_lgwz_norm(qpc_lgwz* h, double* norm);
+
+/* <c| f(r) cos(theta) |c> per instance with F = <Bi|f|Bj> ([n_r][p+1])
+ * (observable_z::observe, spherical/observable/1e.hpp:26-50); out[2*inst] re, [2*inst+1] im. */
+int qpc_lgwz_dipole(qpc_lgwz* h, const double* F, double* out);
+
+/* eigenstate_sph::projection (spherical/spectrum/population_1e.hpp:29-55):
+ * proj[inst][m][il][n] = sum_r basis_l[n][r] c[inst][m][il][r] for the
+ * n_state[l] left eigenvectors (S v) of each l = 0..lmax, packed one l after
+ * another in basis (n_state[l] rows of n_r each); proj is packed the same way
+ * per (inst, m, il) with n_state[l] entries, complex. */
+int qpc_lgwz_projection(qpc_lgwz* h, const int32_t* n_state, const double* basis, double* proj);
+
+/* Time the handle's last qpc_lgwz_run on its stream, in milliseconds
+ * (CUDA events around the launched kernels). */
+int qpc_lgwz_last_run_ms(qpc_lgwz* h, double* ms);
+
+/* Kernel launches made by the handle since creation (all of them this library's own). */
+int64_t qpc_lgwz_launch_count(qpc_lgwz* h);
+
+/* Per-kernel timing of qpc_lgwz_run: when on, each launch is bracketed by CUDA
+ * events on the handle's stream and run() accumulates the elapsed times per
+ * kernel (setting it also clears the totals).  ms[QPC_NKERNEL], launches[QPC_NKERNEL]
+ * are indexed by QPC_KERNEL_*. */
+enum { QPC_KERNEL_FACTOR = 0, QPC_KERNEL_TRANSFORM_FWD = 1, QPC_KERNEL_SWEEP = 2,
+       QPC_KERNEL_TRANSFORM_BWD = 3, QPC_KERNEL_FIELDFREE = 4, QPC_NKERNEL = 5 };
+int qpc_lgwz_set_profiling(qpc_lgwz* h, int on);
+int qpc_lgwz_kernel_times(qpc_lgwz* h, double* ms, int64_t* launches);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

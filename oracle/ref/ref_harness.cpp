@@ -1,0 +1,237 @@
+// Harness that drives the UNMODIFIED reference headers (QPC-TDSE include/, read
+// in place from the reference checkout) to produce golden vectors for the
+// oracle and to time the reference's own CPU propagator.
+//
+// Test infrastructure, not product code.  Built by oracle/ref/Makefile into
+// oracle/_ref/ (never committed); only tests/golden/make_golden.py and the
+// developer run it.  MKL, GSL and HDF5 are replaced by the headers in
+// oracle/ref/shim/ (see their comments).
+//
+// Grid sizes are compile-time in the reference (dimension_1e<...>), so the
+// Makefile builds one binary per grid with -DHNR (active B-splines),
+// -DHMR (B-spline degree p), -DHNL (number of l channels), m = 0 only.
+//
+// Commands (all arrays are written as raw little-endian float64 files):
+//   setup  OUT RMAX DT ZC ZS SG
+//       S, R (=<B|r|B>), RINV, D (=<B|d/dr|B>), H[l] for l=0..NL-1, the CN bands
+//       upper/lower (lower already LDL^T-factorised by lu_zsb), the Y10 eigen-
+//       system yeig[L], yprj[L][L], the knot vector, ground state (l=0, n=0).
+//       Follows binsrc/sphTDSE.cpp:742-743 and cn_1e.hpp:565-593.
+//   field  OUT E0 W0 NC N0 CEP DT
+//       f(t_i) for i = 0..para_nt of field<field_component_sinen<2>> on 'z',
+//       as binsrc/sphTDSE.cpp:738 and structure/field.h:229-311.
+//   propagate OUT RMAX DT ZC ZS SG INIT FIELD NT NFREE NTHREADS
+//       INIT = "gs" (ground state, l=0) or a file of 2*L*NR doubles; FIELD = file
+//       of NT+1 doubles f(t_0..t_NT).  Runs propagate(coef, f[i], f[i+1]) for
+//       i < NT, then NFREE field-free steps (binsrc/sphTDSE.cpp:786-831 loop
+//       without observe/mask), and writes coef, S-norm, <z> (observable_z with
+//       f(r)=r) and the wall time of the step loop (qpc::timer semantics).
+//   proj   OUT RMAX DT ZC ZS SG COEF EMAX
+//       Projection of COEF onto field-free eigenstates with E < EMAX
+//       (eigenstate_sph::initialize + projection, population_1e.hpp:29-118).
+#include <spherical/inventory.h>
+#include <omp.h>
+#include <string>
+#include <vector>
+#include <cstring>
+
+using namespace qpc;
+using namespace qpc::spherical;
+
+#ifndef HNR
+#define HNR 64
+#endif
+#ifndef HMR
+#define HMR 6
+#endif
+#ifndef HNL
+#define HNL 6
+#endif
+
+using dims_t = dimension_1e<HNR, HMR, HNL, 1, 0>;
+
+static void dump(const std::string& dir, const char* name, const void* p, size_t ndouble)
+{
+	std::string f = dir + "/" + name + ".bin";
+	FILE* fp = std::fopen(f.c_str(), "wb");
+	if (!fp) { std::perror(f.c_str()); std::exit(2); }
+	std::fwrite(p, sizeof(double), ndouble, fp);
+	std::fclose(fp);
+}
+static std::vector<double> slurp(const char* f, size_t ndouble)
+{
+	std::vector<double> v(ndouble);
+	FILE* fp = std::fopen(f, "rb");
+	if (!fp) { std::perror(f); std::exit(2); }
+	if (std::fread(v.data(), sizeof(double), ndouble, fp) != ndouble) { std::fprintf(stderr, "short read %s\n", f); std::exit(2); }
+	std::fclose(fp);
+	return v;
+}
+
+struct potn_any
+{
+	double zc, zs, sg;
+	double operator()(double r) const noexcept
+	{
+		if (zs == 0.0) return hydrogenic{zc}(r);
+		return hydrogenic_yukawa{zc, zs, sg}(r);
+	}
+};
+
+template <class prop_t>
+static void init_prop(prop_t& prop, integrator_radi<dims_t>& radi, integrator_angu<dims_t>& angu, double rmax, double dt,
+	const potn_any& potn, size_t nthd)
+{
+	radi.initialize(0.0, rmax);
+	prop.initialize(nthd, radi, angu, 1.0, potn, dt);
+}
+
+static int cmd_setup(int argc, char** argv)
+{
+	if (argc < 8) return 1;
+	std::string out = argv[2];
+	double rmax = atof(argv[3]), dt = atof(argv[4]);
+	potn_any potn{atof(argv[5]), atof(argv[6]), atof(argv[7])};
+	auto radi = integrator_radi<dims_t>();
+	auto angu = integrator_angu<dims_t>();
+	auto prop = propagator_cn_hc_lgwz<dims_t>();
+	init_prop(prop, radi, angu, rmax, dt, potn, 1);
+
+	dump(out, "S", prop.s.sub(), dims_t::n_rsub);
+	dump(out, "R", prop.r.data, dims_t::n_rsub);
+	{
+		operator_rinv1<dims_t> ri; ri.initialize(radi); dump(out, "RINV", ri.data, dims_t::n_rsub);
+		operator_rdif1<dims_t> d; d.initialize(radi); dump(out, "D", d.data, dims_t::n_rsub);
+	}
+	std::vector<double> h((dims_t::n_lmax + 1) * dims_t::n_rsub);
+	for (size_t l = 0; l <= dims_t::n_lmax; ++l) std::memcpy(h.data() + l * dims_t::n_rsub, prop.h[l], sizeof(double) * dims_t::n_rsub);
+	dump(out, "H", h.data(), h.size());
+	dump(out, "upper", prop.prop_hc.upper.data, 2 * (dims_t::n_lmax + 1) * dims_t::n_rsub);
+	dump(out, "lower", prop.prop_hc.lower.data, 2 * (dims_t::n_lmax + 1) * dims_t::n_rsub);
+	dump(out, "yeig", prop.prop_z1.yeig.data, dims_t::m_dims * dims_t::l_dims);
+	dump(out, "yprj", prop.tran_z1.yprj.data, dims_t::m_dims * dims_t::l_dims * dims_t::l_dims);
+	dump(out, "y10", prop.y.data, dims_t::m_dims * dims_t::l_dims);
+	{
+		using base_t = typename integrator_radi<dims_t>::base_t;
+		size_t nk = dims_t::nr + dims_t::mr + 3;
+		dump(out, "knots", radi.base.knot() - 1, nk);
+		(void)sizeof(base_t);
+	}
+	auto coef = coefficient<dims_t>();
+	auto eng = coef.template initialize<1>(prop.s, prop.h, {0ul}, {0ul}, {0ul}, {comp_t{1.0}});
+	dump(out, "gs_energy", eng.data(), 1);
+	dump(out, "gs_coef", coef.data, 2 * dims_t::n_leng);
+	return 0;
+}
+
+static int cmd_field(int argc, char** argv)
+{
+	if (argc < 9) return 1;
+	std::string out = argv[2];
+	std::array<std::array<double, 5>, 0> none{};
+	std::array<std::array<double, 5>, 1> z{{{atof(argv[3]), atof(argv[4]), atof(argv[5]), atof(argv[6]), atof(argv[7])}}};
+	double dt = atof(argv[8]);
+	auto laser = create_laser_field<field_component_sinen<2>>(none, none, z, dt);
+	std::vector<double> t(laser.para_nt + 1), f(laser.para_nt + 1);
+	for (size_t i = 0; i <= laser.para_nt; ++i) { t[i] = laser.t(i); f[i] = std::get<2>(laser(t[i])); }
+	double nt = (double)laser.para_nt;
+	dump(out, "nt", &nt, 1);
+	dump(out, "t", t.data(), t.size());
+	dump(out, "f", f.data(), f.size());
+	return 0;
+}
+
+static int cmd_propagate(int argc, char** argv)
+{
+	if (argc < 13) return 1;
+	std::string out = argv[2];
+	double rmax = atof(argv[3]), dt = atof(argv[4]);
+	potn_any potn{atof(argv[5]), atof(argv[6]), atof(argv[7])};
+	const char* init = argv[8];
+	const char* field = argv[9];
+	size_t nt = strtoul(argv[10], 0, 10), nfree = strtoul(argv[11], 0, 10);
+	int nthd = atoi(argv[12]);
+	omp_set_num_threads(nthd);
+	auto radi = integrator_radi<dims_t>();
+	auto angu = integrator_angu<dims_t>();
+	auto prop = propagator_cn_hc_lgwz<dims_t>();
+	init_prop(prop, radi, angu, rmax, dt, potn, nthd);
+	auto coef = coefficient<dims_t>();
+	if (std::string(init) == "gs") {
+		coef.template initialize<1>(prop.s, prop.h, {0ul}, {0ul}, {0ul}, {comp_t{1.0}});
+	} else {
+		auto v = slurp(init, 2 * dims_t::n_leng);
+		std::memcpy((double*)coef.data, v.data(), sizeof(double) * v.size());
+	}
+	std::vector<double> f = nt ? slurp(field, nt + 1) : std::vector<double>{};
+	auto clock = timer();
+	clock.tic();
+	for (size_t it = 0; it < nt + nfree; ++it) {
+		if (it < nt) prop.propagate(coef, f[it], f[it + 1]);
+		else prop.propagate(coef);
+	}
+	clock.toc();
+	double secs = clock.get();
+	double norm = 0.0;
+	#pragma omp parallel
+	{
+		double part = 0.0;
+		prop.s.observe(coef.data, part);
+		#pragma omp atomic
+		norm += part;
+	}
+	auto obs = observable_z<dims_t>();
+	obs.initialize(radi, angu);
+	comp_t zz = obs.observe(coef.data, coef.data);
+	double z2[2] = {zz[0], zz[1]};
+	dump(out, "coef", coef.data, 2 * dims_t::n_leng);
+	dump(out, "norm", &norm, 1);
+	dump(out, "dipole", z2, 2);
+	dump(out, "seconds", &secs, 1);
+	std::printf("steps %zu threads %d seconds %.6f\n", nt + nfree, nthd, secs);
+	return 0;
+}
+
+static int cmd_proj(int argc, char** argv)
+{
+	if (argc < 10) return 1;
+	std::string out = argv[2];
+	double rmax = atof(argv[3]), dt = atof(argv[4]);
+	potn_any potn{atof(argv[5]), atof(argv[6]), atof(argv[7])};
+	auto v = slurp(argv[8], 2 * dims_t::n_leng);
+	double emax = atof(argv[9]);
+	auto radi = integrator_radi<dims_t>();
+	auto angu = integrator_angu<dims_t>();
+	auto prop = propagator_cn_hc_lgwz<dims_t>();
+	init_prop(prop, radi, angu, rmax, dt, potn, 1);
+	auto coef = coefficient<dims_t>();
+	std::memcpy((double*)coef.data, v.data(), sizeof(double) * v.size());
+	eigenstate_sph<dims_t> eig;
+	eig.initialize(prop.s, prop.h, [emax](size_t, double e, const double*) { return e < emax; });
+	std::vector<comp_t> proj; std::vector<size_t> size;
+	eig.projection(coef, proj, size);
+	std::vector<double> sz(size.begin(), size.end()), en;
+	for (size_t l = 0; l < dims_t::l_dims; ++l) for (double e : eig.val(l)) en.push_back(e);
+	dump(out, "proj", proj.data(), 2 * proj.size());
+	dump(out, "proj_nnz", sz.data(), sz.size());
+	dump(out, "proj_energy", en.data(), en.size());
+	return 0;
+}
+
+int main(int argc, char** argv)
+{
+	if (argc < 2) { std::fprintf(stderr, "usage: setup|field|propagate|proj ...\n"); return 1; }
+	try {
+		std::string c = argv[1];
+		int rc = 1;
+		if (c == "setup") rc = cmd_setup(argc, argv);
+		else if (c == "field") rc = cmd_field(argc, argv);
+		else if (c == "propagate") rc = cmd_propagate(argc, argv);
+		else if (c == "proj") rc = cmd_proj(argc, argv);
+		if (rc) std::fprintf(stderr, "bad arguments for %s\n", argv[1]);
+		return rc;
+	} catch (std::exception& e) {
+		std::fprintf(stderr, "reference threw: %s\n", e.what());
+		return 3;
+	}
+}

@@ -1,0 +1,316 @@
+"""Python host-side mirror of the QPC-TDSE propagation path, over the C ABI of
+the GB300 engine (include/qpc_gb300.h, library libqpc_gb300.so built in-tree).
+
+The names follow the reference's C++ interface for the path:
+  integrator_radi.initialize(rmin, rmax)      -> radial_setup(...)   (spherical/utilities/basisfunc.hpp:33-36)
+  operator_y10::solve_eigen                   -> y10_eigen(...)      (spherical/operators/1e.hpp:304-333)
+  coefficient::initialize (ground state)      -> ground_state(...)   (spherical/coefficient/1e.hpp:91-143)
+  field<field_component_sinen<2>>             -> field_sinen(...)    (structure/field.h:89-133, 229-311)
+  propagator_cn_hc_lgwz::initialize/propagate -> propagator_cn_hc_lgwz (spherical/propagator/cn_1e.hpp:549-619)
+
+Errors from the engine raise QpcError with the engine's message; a missing
+library or a missing GPU raises instead of falling back to anything else.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+_PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_PKG, "libqpc_gb300.so")
+
+QPC_OK = 0
+ERRORS = {1: "QPC_ERR_ARGS", 2: "QPC_ERR_NOMEM", 3: "QPC_ERR_CUDA", 4: "QPC_ERR_SINGULAR",
+          5: "QPC_ERR_NUMERIC", 6: "QPC_ERR_TIMEOUT", 7: "QPC_ERR_STATE", 8: "QPC_ERR_NODEVICE"}
+POTENTIAL_HYDROGENIC = 0
+POTENTIAL_YUKAWA = 1
+
+# every symbol include/qpc_gb300.h declares
+EXPORTS = (
+    "qpc_last_error", "qpc_version", "qpc_linear_knots", "qpc_radial_setup", "qpc_y10_coupling",
+    "qpc_y10_eigen", "qpc_ldlt_csym", "qpc_gen_eigen", "qpc_field_sinen", "qpc_lgwz_create",
+    "qpc_lgwz_destroy", "qpc_lgwz_put", "qpc_lgwz_get", "qpc_lgwz_put_device", "qpc_lgwz_get_device",
+    "qpc_lgwz_propagate", "qpc_lgwz_propagate_free", "qpc_lgwz_run", "qpc_lgwz_norm", "qpc_lgwz_dipole",
+    "qpc_lgwz_projection", "qpc_lgwz_last_run_ms", "qpc_lgwz_launch_count", "qpc_lgwz_set_profiling",
+    "qpc_lgwz_kernel_times",
+)
+KERNELS = ("factor", "transform_fwd", "sweep", "transform_bwd", "fieldfree")
+
+
+class QpcError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("%s: %s" % (ERRORS.get(code, code), msg))
+        self.code = code
+
+
+class qpc_potential(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int32), ("zc", ctypes.c_double), ("zs", ctypes.c_double), ("sigma", ctypes.c_double)]
+
+
+class qpc_dims(ctypes.Structure):
+    _fields_ = [("n_r", ctypes.c_int32), ("p", ctypes.c_int32), ("n_l", ctypes.c_int32),
+                ("n_m", ctypes.c_int32), ("m0", ctypes.c_int32), ("n_inst", ctypes.c_int32)]
+
+
+_lib = None
+
+
+def load(path=None):
+    """Load the engine library; builds it first if it is missing (the build
+    needs nvcc, not a GPU)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = path or LIB_PATH
+    if not os.path.exists(path):
+        from . import build as _b
+        _b.build_engine()
+    lib = ctypes.CDLL(path)
+    P = ctypes.c_void_p
+    i32, i64, d = ctypes.c_int32, ctypes.c_int64, ctypes.c_double
+    sig = {
+        "qpc_last_error": (ctypes.c_char_p, []),
+        "qpc_version": (ctypes.c_char_p, []),
+        "qpc_linear_knots": (ctypes.c_int, [i32, i32, d, d, P]),
+        "qpc_radial_setup": (ctypes.c_int, [i32, i32, i32, P, P, d, P, P, P, P, P]),
+        "qpc_y10_coupling": (ctypes.c_int, [i32, i32, P]),
+        "qpc_y10_eigen": (ctypes.c_int, [i32, i32, P, P]),
+        "qpc_ldlt_csym": (ctypes.c_int, [i32, i32, P, P, d, P, P]),
+        "qpc_gen_eigen": (ctypes.c_int, [i32, i32, P, P, i32, P, P]),
+        "qpc_field_sinen": (ctypes.c_int, [i32, d, d, d, d, d, d, i64, P, P]),
+        "qpc_lgwz_create": (ctypes.c_int, [P, d, P, P, P, P]),
+        "qpc_lgwz_destroy": (ctypes.c_int, [P]),
+        "qpc_lgwz_put": (ctypes.c_int, [P, P]),
+        "qpc_lgwz_get": (ctypes.c_int, [P, P]),
+        "qpc_lgwz_put_device": (ctypes.c_int, [P, P]),
+        "qpc_lgwz_get_device": (ctypes.c_int, [P, P]),
+        "qpc_lgwz_propagate": (ctypes.c_int, [P, P, P]),
+        "qpc_lgwz_propagate_free": (ctypes.c_int, [P]),
+        "qpc_lgwz_run": (ctypes.c_int, [P, P, i64, P, P]),
+        "qpc_lgwz_norm": (ctypes.c_int, [P, P]),
+        "qpc_lgwz_dipole": (ctypes.c_int, [P, P, P]),
+        "qpc_lgwz_projection": (ctypes.c_int, [P, P, P, P]),
+        "qpc_lgwz_last_run_ms": (ctypes.c_int, [P, P]),
+        "qpc_lgwz_launch_count": (ctypes.c_int64, [P]),
+        "qpc_lgwz_set_profiling": (ctypes.c_int, [P, ctypes.c_int]),
+        "qpc_lgwz_kernel_times": (ctypes.c_int, [P, P, P]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = lib
+    return lib
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+def _check(rc):
+    if rc != QPC_OK:
+        raise QpcError(rc, load().qpc_last_error().decode())
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+# ------------------------------------------------------------------ setup (host)
+
+def linear_knots(n_r, p, rmin, rmax):
+    t = np.zeros(n_r + p + 3)
+    _check(load().qpc_linear_knots(n_r, p, rmin, rmax, _ptr(t)))
+    return t
+
+
+def radial_setup(n_r, p, n_lh, knots, potential=(POTENTIAL_HYDROGENIC, 1.0, 0.0, 0.0), mass=1.0):
+    """S, R, Rinv, D as [n_r, p+1] bands and H as [n_lh, n_r, p+1]
+    (integrator_radi integrals, spherical/utilities/basisfunc.hpp:63-106)."""
+    knots = _f64(knots)
+    pot = qpc_potential(*potential)
+    S, R, Ri, D = (np.zeros((n_r, p + 1)) for _ in range(4))
+    H = np.zeros((n_lh, n_r, p + 1))
+    _check(load().qpc_radial_setup(n_r, p, n_lh, _ptr(knots), ctypes.byref(pot), mass,
+                                   _ptr(S), _ptr(R), _ptr(Ri), _ptr(D), _ptr(H)))
+    return S, R, Ri, D, H
+
+
+def y10_coupling(n_l, m=0):
+    y = np.zeros(n_l)
+    _check(load().qpc_y10_coupling(n_l, m, _ptr(y)))
+    return y
+
+
+def y10_eigen(n_l, m=0):
+    lam = np.zeros(n_l)
+    P = np.zeros((n_l, n_l))
+    _check(load().qpc_y10_eigen(n_l, m, _ptr(lam), _ptr(P)))
+    return lam, P
+
+
+def ldlt_csym(S, H, g):
+    n, ne = S.shape
+    p = ne - 1
+    Lrow = np.zeros((n, p), complex)
+    Dinv = np.zeros(n, complex)
+    bad = load().qpc_ldlt_csym(n, p, _ptr(_f64(S)), _ptr(_f64(H)), g, _ptr(Lrow), _ptr(Dinv))
+    if bad < 0:
+        raise QpcError(1, "ldlt arguments")
+    return Lrow, Dinv, bad
+
+
+def gen_eigen(S, Hl, n_want=0):
+    n, ne = S.shape
+    e = np.zeros(n)
+    v = np.zeros((max(n_want, 1), n))
+    _check(load().qpc_gen_eigen(n, ne - 1, _ptr(_f64(S)), _ptr(_f64(Hl)), n_want, _ptr(e), _ptr(v)))
+    return e, v[:n_want]
+
+
+def ground_state(S, H, n_l, n_m=1, im=0, il=0, ir=0, m0=0):
+    """coefficient::initialize for one (im, il, ir) with cf = 1: the state is the
+    ir-th eigenvector of H_l in block (im, il), zero elsewhere; returns (coef, E)."""
+    n_r = S.shape[0]
+    l = il + abs(m0 + im)
+    e, v = gen_eigen(S, H[l], ir + 1)
+    c = np.zeros((n_m, n_l, n_r), complex)
+    c[im, il] = v[ir]
+    return c, e[ir]
+
+
+def field_sinen(e0, w0, nc, n0, cep, dt, n_pow=2):
+    """f(t_i), i = 0..para_nt, of field_component_sinen<n_pow> (CEP in units of pi)."""
+    nt = ctypes.c_int64(0)
+    _check(load().qpc_field_sinen(n_pow, e0, w0, nc, n0, cep, dt, 0, None, ctypes.byref(nt)))
+    f = np.zeros(nt.value + 1)
+    _check(load().qpc_field_sinen(n_pow, e0, w0, nc, n0, cep, dt, f.size, _ptr(f), ctypes.byref(nt)))
+    return f
+
+
+def intensity_to_e0(intensity_wcm2):
+    """E0 [a.u.] = sqrt(I / 3.50944758e16 W/cm^2)."""
+    return float(np.sqrt(intensity_wcm2 / 3.50944758e16))
+
+
+def wavelength_to_w0(lambda_nm):
+    """omega [a.u.] = 45.5633525 / lambda[nm]."""
+    return 45.5633525 / lambda_nm
+
+
+# ------------------------------------------------------------------ propagator
+
+class propagator_cn_hc_lgwz:
+    """Batched GPU propagator_cn_hc_lgwz: n_inst wavefunctions on one grid.
+
+    initialize(...) mirrors propagator_cn_hc_lgwz::initialize (cn_1e.hpp:565-593);
+    propagate(f_ti, f_tf) / propagate() mirror the two propagate overloads
+    (cn_1e.hpp:595-618) for every instance at once; run(...) is the driver loop.
+    The state lives on the GPU; put()/get() copy c[inst][m][l][r] complex128.
+    """
+
+    def __init__(self):
+        self._h = None
+        self.dims = None
+
+    def initialize(self, n_r, p, n_l, S, R, H, dt, n_m=1, m0=0, n_inst=1):
+        lib = load()
+        self.close()
+        d = qpc_dims(n_r, p, n_l, n_m, m0, n_inst)
+        h = ctypes.c_void_p()
+        S, R, H = _f64(S), _f64(R), _f64(H)
+        lmax = max(abs(m0), abs(m0 + n_m - 1)) + n_l - 1
+        if H.shape[0] < lmax + 1:
+            raise QpcError(1, "H needs lmax+1 = %d blocks" % (lmax + 1))
+        _check(lib.qpc_lgwz_create(ctypes.byref(d), dt, _ptr(S), _ptr(R), _ptr(H[:lmax + 1].copy()), ctypes.byref(h)))
+        self._h = h
+        self.dims = d
+        self.shape = (n_inst, n_m, n_l, n_r)
+        return self
+
+    def close(self):
+        if self._h is not None:
+            load().qpc_lgwz_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def put(self, coef):
+        c = np.ascontiguousarray(coef, dtype=np.complex128).reshape(self.shape)
+        _check(load().qpc_lgwz_put(self._h, _ptr(c)))
+
+    def get(self):
+        c = np.zeros(self.shape, np.complex128)
+        _check(load().qpc_lgwz_get(self._h, _ptr(c)))
+        return c
+
+    def put_device(self, dev_ptr):
+        _check(load().qpc_lgwz_put_device(self._h, ctypes.c_void_p(dev_ptr)))
+
+    def get_device(self, dev_ptr):
+        _check(load().qpc_lgwz_get_device(self._h, ctypes.c_void_p(dev_ptr)))
+
+    def propagate(self, f_ti=None, f_tf=None):
+        if f_ti is None:
+            _check(load().qpc_lgwz_propagate_free(self._h))
+            return
+        a = _f64(np.broadcast_to(f_ti, (self.shape[0],)))
+        b = _f64(np.broadcast_to(f_tf, (self.shape[0],)))
+        _check(load().qpc_lgwz_propagate(self._h, _ptr(a), _ptr(b)))
+
+    def run(self, ftab, nt_field, nt_total=None):
+        nt_field = np.ascontiguousarray(np.broadcast_to(nt_field, (self.shape[0],)), dtype=np.int64)
+        nt_total = nt_field.copy() if nt_total is None else np.ascontiguousarray(
+            np.broadcast_to(nt_total, (self.shape[0],)), dtype=np.int64)
+        if ftab is None:
+            _check(load().qpc_lgwz_run(self._h, None, 1, _ptr(nt_field), _ptr(nt_total)))
+            return
+        ftab = _f64(np.atleast_2d(ftab))
+        if ftab.shape[0] != self.shape[0]:
+            ftab = _f64(np.broadcast_to(ftab, (self.shape[0], ftab.shape[1])))
+        _check(load().qpc_lgwz_run(self._h, _ptr(ftab), ftab.shape[1], _ptr(nt_field), _ptr(nt_total)))
+
+    def last_run_ms(self):
+        v = ctypes.c_double(0)
+        _check(load().qpc_lgwz_last_run_ms(self._h, ctypes.byref(v)))
+        return v.value
+
+    def launch_count(self):
+        return int(load().qpc_lgwz_launch_count(self._h))
+
+    def enable_profiling(self, on=True):
+        _check(load().qpc_lgwz_set_profiling(self._h, int(bool(on))))
+
+    def kernel_times(self):
+        """{kernel: (total ms, launches)} accumulated by run() while profiling is on."""
+        ms = np.zeros(len(KERNELS))
+        n = np.zeros(len(KERNELS), np.int64)
+        _check(load().qpc_lgwz_kernel_times(self._h, _ptr(ms), _ptr(n)))
+        return {k: (float(ms[i]), int(n[i])) for i, k in enumerate(KERNELS)}
+
+    def norm(self):
+        out = np.zeros(self.shape[0])
+        _check(load().qpc_lgwz_norm(self._h, _ptr(out)))
+        return out
+
+    def dipole(self, F):
+        out = np.zeros(2 * self.shape[0])
+        _check(load().qpc_lgwz_dipole(self._h, _ptr(_f64(F)), _ptr(out)))
+        return out[0::2] + 1j * out[1::2]
+
+    def projection(self, n_state, basis):
+        """basis: list over l = 0..lmax of arrays [n_state[l], n_r] (S v rows)."""
+        n_state = np.ascontiguousarray(n_state, dtype=np.int32)
+        packed = _f64(np.concatenate([np.asarray(b, np.float64).reshape(-1) for b in basis]))
+        B, M, L, N = self.shape
+        tot = 0
+        for im in range(M):
+            for il in range(L):
+                tot += int(n_state[il + abs(self.dims.m0 + im)])
+        out = np.zeros(B * tot, complex)
+        _check(load().qpc_lgwz_projection(self._h, _ptr(n_state), _ptr(packed), _ptr(out)))
+        return out

@@ -1,0 +1,95 @@
+"""In-tree build of the engine library (and of the CPU oracle used by the tests).
+
+Outputs (git-ignored, rebuilt on every machine; nothing compiled elsewhere is
+reused):
+  qpc-tdse-cpc_gb300/libqpc_gb300.so   engine: CUDA kernels for sm_103a + host setup
+  oracle/_build/liboracle_cn.so        CPU oracle (test infrastructure only)
+"""
+import os
+import platform
+import subprocess
+import sys
+import concurrent.futures as cf
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(PKG)
+CSRC = os.path.join(PKG, "csrc")
+LIB = os.path.join(PKG, "libqpc_gb300.so")
+OBJDIR = os.path.join(PKG, "_build")
+ORACLE_SRC = os.path.join(ROOT, "oracle", "oracle_cn.cpp")
+ORACLE_LIB = os.path.join(ROOT, "oracle", "_build", "liboracle_cn.so")
+
+NVCC_ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+
+def _nvcc():
+    for c in (os.environ.get("NVCC"), "/usr/local/cuda/bin/nvcc", "nvcc"):
+        if c and (os.path.isabs(c) and os.path.exists(c) or not os.path.isabs(c)):
+            return c
+    return "nvcc"
+
+
+def _stale(out, srcs):
+    if not os.path.exists(out):
+        return True
+    t = os.path.getmtime(out)
+    return any(os.path.getmtime(s) > t for s in srcs)
+
+
+def _run(cmd):
+    r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("build failed: %s\n%s" % (" ".join(cmd), r.stdout))
+    return r.stdout
+
+
+def build_engine(force=False, verbose=False):
+    srcs = [os.path.join(CSRC, f) for f in ("qpc_engine.cu", "qpc_setup.cpp", "qpc_internal.h")]
+    srcs.append(os.path.join(ROOT, "include", "qpc_gb300.h"))
+    if not force and not _stale(LIB, srcs):
+        return LIB
+    os.makedirs(OBJDIR, exist_ok=True)
+    o_cu = os.path.join(OBJDIR, "qpc_engine.o")
+    o_cc = os.path.join(OBJDIR, "qpc_setup.o")
+    jobs = [
+        [_nvcc()] + NVCC_ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
+                                "-c", os.path.join(CSRC, "qpc_engine.cu"), "-o", o_cu],
+        ["g++", "-O2", "-std=c++17", "-fPIC", "-c", os.path.join(CSRC, "qpc_setup.cpp"), "-o", o_cc],
+    ]
+    with cf.ThreadPoolExecutor(2) as ex:
+        outs = list(ex.map(_run, jobs))
+    _run([_nvcc()] + NVCC_ARCH + ["-shared", o_cu, o_cc, "-o", LIB + ".tmp", "-lcudart"])
+    os.replace(LIB + ".tmp", LIB)
+    if verbose:
+        print("".join(outs))
+    return LIB
+
+
+def build_oracle(force=False):
+    if not force and not _stale(ORACLE_LIB, [ORACLE_SRC]):
+        return ORACLE_LIB
+    os.makedirs(os.path.dirname(ORACLE_LIB), exist_ok=True)
+    # fma() must be the hardware instruction (exactly rounded either way); on
+    # x86-64 that needs -mfma, on aarch64 it is baseline
+    isa = ["-mfma"] if platform.machine() in ("x86_64", "AMD64") else []
+    _run(["g++", "-O3", "-std=c++17", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared"] + isa +
+         [ORACLE_SRC, "-o", ORACLE_LIB + ".tmp"])
+    os.replace(ORACLE_LIB + ".tmp", ORACLE_LIB)
+    return ORACLE_LIB
+
+
+def build_reference_oracle():
+    """Build the reference's own propagator into oracle/_ref/ when the reference
+    checkout is present (only on the development machine; never at run time on
+    a GPU machine)."""
+    ref = "/root/reference/include"
+    if not os.path.isdir(ref):
+        return None
+    _run(["make", "-C", os.path.join(ROOT, "oracle", "ref"), "-j4", "REF_INCLUDE=" + ref])
+    return os.path.join(ROOT, "oracle", "_ref")
+
+
+if __name__ == "__main__":
+    f = "--force" in sys.argv
+    print(build_engine(f, verbose=True))
+    print(build_oracle(f))

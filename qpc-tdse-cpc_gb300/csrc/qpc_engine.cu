@@ -1,0 +1,1053 @@
+// GB300 (sm_103a) propagation engine for the QPC-TDSE length-gauge
+// Crank-Nicolson step, propagator_cn_hc_lgwz (spherical/propagator/cn_1e.hpp:549-619).
+//
+// One reference step is  U = C(f_tf) F C(f_ti)  with
+//   C(f) = P^T M(f) P,  M(f) = (S + i b R)^-1 (S - i b R) per eigen-channel of Y10
+//        (b = lambda f dt/4, cn_propagate_kernel_avx1, propagate.hpp:3-98),
+//   F    = (S + i dt/2 H_l)^-1 (S - i dt/2 H_l) per (m,l) channel
+//        (cn_hc_propagate0, propagate.hpp:311-331).
+// The engine computes exactly these operators, restructured for a GPU whose
+// FP64 pipe (~1.2 TFLOP/s on GB300, one warp instruction per ~64 cycles per
+// SM sub-partition) is the binding resource:
+//   * (S + i b R)^-1 (S - i b R) z = 2 (S + i b R)^-1 (S z) - z, and likewise for
+//     F: the right-hand side is a real band times a complex vector, half the
+//     FP64 work of the complex band the reference multiplies by.
+//   * Y10 has zero diagonal, so its eigenvalues pair as +-s with eigenvectors
+//     v and D v, D = diag((-1)^il).  Then S - i b R for -s is the complex
+//     conjugate of S + i b R for +s: one LDL^T factorisation serves both
+//     channels (the second solve runs on conjugated data), and the l-space
+//     transform splits into even-l and odd-l halves (E +- O), half the FP64.
+//   * Over a run, C(f(t_i)) closes step i-1 and opens step i, and P P^T = I
+//     between them: the run applies P, M(f(t_i))^2 and P^T once per step
+//     instead of P M P^T twice.  The factorisation depends only on the field
+//     table, so it is computed for several steps ahead in one wide launch.
+//   * Each complex recurrence is split over two lanes (real part, imaginary
+//     part) and the state is kept r-major, [inst][m][r][l], so that the 32
+//     lanes of a warp read 32 consecutive doubles.
+// All arithmetic is complex FP64.  Results agree with the reference to
+// rounding; the tests hold them to 1e-10 relative L2 after full pulses.
+#include "qpc_internal.h"
+#include <cuda_runtime.h>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <cmath>
+#include <vector>
+#include <algorithm>
+#include <numeric>
+#include <string>
+#include <time.h>
+
+namespace qpc {
+
+static thread_local char g_err[512] = "";
+void set_error(const char* fmt, ...)
+{
+	va_list ap; va_start(ap, fmt);
+	vsnprintf(g_err, sizeof(g_err), fmt, ap);
+	va_end(ap);
+}
+
+#define QPC_CUDA(call) do { cudaError_t e_ = (call); if (e_ != cudaSuccess) { \
+	set_error("%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); return QPC_ERR_CUDA; } } while (0)
+
+// device status bits (never a trap)
+enum : int { ST_PIVOT = 1, ST_NONFINITE = 2 };
+
+// ============================================================================ kernels
+
+// ---------------------------------------------------------------- layout change
+// host layout [inst][m][l][r]  <->  engine layout [inst][m][r][l]
+__global__ void k_to_rmajor(const double2* __restrict__ src, double2* __restrict__ dst, int N, int L, long nblk)
+{
+	long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+	long tot = nblk * (long)N * L;
+	if (t >= tot) return;
+	long b = t / ((long)N * L);
+	int rem = (int)(t % ((long)N * L));
+	int r = rem / L, l = rem % L;
+	dst[t] = src[b * (long)N * L + (long)l * N + r];
+}
+__global__ void k_to_lmajor(const double2* __restrict__ src, double2* __restrict__ dst, int N, int L, long nblk)
+{
+	long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+	long tot = nblk * (long)N * L;
+	if (t >= tot) return;
+	long b = t / ((long)N * L);
+	int rem = (int)(t % ((long)N * L));
+	int l = rem / N, r = rem % N;
+	dst[t] = src[b * (long)N * L + (long)r * L + l];
+}
+
+// ---------------------------------------------------------------- per-instance schedule
+// Instance k: B_0 F B_1 F ... B_{nt-1} F B_nt [F ...] (nt = nt_field[k]); at loop
+// index s the coupling block is applied a_s times: 1 at s = 0 and s = nt, 2 in
+// between, 0 after nt (and always 0 when nt = 0).  F runs while s < nt_total.
+__device__ __forceinline__ int coupling_power(long s, long nt)
+{
+	if (nt <= 0 || s > nt) return 0;
+	return (s == 0 || s == nt) ? 1 : 2;
+}
+
+// ---------------------------------------------------------------- transform P (even/odd halves)
+// Vh[m][kk][il]: row kk < npair = eigenvector of +s_kk, row npair = zero-eigenvalue vector.
+// eo slots per (inst,m,r): 2k = E_k, 2k+1 = O_k, 2*npair = Z (odd L).
+// Forward: E_k = sum_{il even} v_k[il] c[il], O_k = sum_{il odd} v_k[il] c[il], Z = sum_{il even} v_0[il] c[il].
+// Backward (eo holds s_k = x_k+ + x_k-, d_k = x_k+ - x_k-, Z):
+//   c[il even] = sum_k v_k[il] s_k + v_0[il] Z,  c[il odd] = sum_k v_k[il] d_k.
+// One CTA = (inst, m, tile of TR rows).  Lane = row, warp = output slot; the
+// row tile is staged in shared memory with an odd row stride (conflict-free
+// 16-byte accesses).
+constexpr int TR = 32;
+
+__global__ void __launch_bounds__(256) k_transform(const double2* __restrict__ src, double2* __restrict__ dst,
+	const double* __restrict__ Vh, int N, int L, int M, int npair, int forward,
+	const int64_t* __restrict__ ntf, long step, int B)
+{
+	extern __shared__ double2 sm[];
+	const int ldt = L | 1;	// odd stride in 16-byte units
+	double2* tin = sm;
+	double2* tout = sm + TR * ldt;
+	int tiles = (N + TR - 1) / TR;
+	long blk = blockIdx.x;
+	int tile = (int)(blk % tiles);
+	long im_inst = blk / tiles;
+	int m = (int)(im_inst % M);
+	long inst = im_inst / M;
+	if (inst >= B) return;
+	if (coupling_power(step, ntf[inst]) == 0) return;
+	int r0 = tile * TR;
+	int nr = min(TR, N - r0);
+	const double2* s = src + (im_inst * (long)N + r0) * L;
+	double2* d = dst + (im_inst * (long)N + r0) * L;
+	for (int t = threadIdx.x; t < nr * L; t += blockDim.x) {
+		int rr = t / L, c = t % L;
+		tin[rr * ldt + c] = s[t];
+	}
+	__syncthreads();
+	const double* V = Vh + (long)m * (npair + 1) * L;
+	int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+	if (lane < nr) {
+		const double2* row = tin + lane * ldt;
+		for (int slot = warp; slot < L; slot += nw) {
+			double ar = 0.0, ai = 0.0;
+			if (forward) {
+				int kk = slot >> 1, par = slot & 1;
+				if (slot == 2 * npair) { kk = npair; par = 0; }
+				const double* v = V + (long)kk * L;
+				for (int il = par; il < L; il += 2) {
+					double w = v[il];
+					double2 c = row[il];
+					ar = fma(w, c.x, ar);
+					ai = fma(w, c.y, ai);
+				}
+			} else {
+				int il = slot, par = il & 1;
+				for (int k = 0; k < npair; ++k) {
+					double w = V[(long)k * L + il];
+					double2 c = row[2 * k + par];
+					ar = fma(w, c.x, ar);
+					ai = fma(w, c.y, ai);
+				}
+				if (!par && 2 * npair < L) {
+					double w = V[(long)npair * L + il];
+					double2 c = row[2 * npair];
+					ar = fma(w, c.x, ar);
+					ai = fma(w, c.y, ai);
+				}
+			}
+			tout[lane * ldt + slot] = make_double2(ar, ai);
+		}
+	}
+	__syncthreads();
+	for (int t = threadIdx.x; t < nr * L; t += blockDim.x) {
+		int rr = t / L, c = t % L;
+		d[t] = tout[rr * ldt + c];
+	}
+}
+
+// ---------------------------------------------------------------- coupling factorisation
+// LDL^T (no pivoting) of the complex-symmetric band S + i b R, b = lambda_k f(t_s) dt/4,
+// for every (look-ahead step j, inst, m, pair k): one lane per system, the
+// trailing (p+1)x(p+1) window of the right-looking elimination in registers.
+// Output fac[j][inst][m][r][c][k]: c < P: L(r+1+c, r); c = P: 1/D(r).
+template <int P>
+__global__ void __launch_bounds__(64) k_factor(double2* __restrict__ fac, const double* __restrict__ S, const double* __restrict__ R,
+	const double* __restrict__ lamp, const double* __restrict__ ftab, long ld, const int64_t* __restrict__ ntf,
+	long step0, int K, int B, int M, int N, int npair, double dt, int* __restrict__ status)
+{
+	constexpr int NE = P + 1;
+	long g = (long)blockIdx.x * blockDim.x + threadIdx.x;
+	long nsys = (long)K * B * M * npair;
+	if (g >= nsys) return;
+	int k = (int)(g % npair);
+	long t = g / npair;
+	int m = (int)(t % M); t /= M;
+	long inst = t % B;
+	int j = (int)(t / B);
+	long s = step0 + j;
+	if (coupling_power(s, ntf[inst]) == 0) return;
+	double f = ftab[inst * ld + s];
+	double beta = lamp[m * npair + k] * ((f * (dt * 0.5)) * 0.5);
+	double2* out = fac + ((((long)j * B + inst) * M + m) * (long)N) * NE * npair + k;
+	double wr[NE][NE], wi[NE][NE];
+#pragma unroll
+	for (int a = 0; a < NE; ++a)
+#pragma unroll
+		for (int b = 0; b <= a; ++b) {
+			// entry (a, b), b <= a: stored at S[b][a-b]
+			bool in = a < N;
+			wr[a][b] = in ? __ldg(S + b * NE + (a - b)) : 0.0;
+			wi[a][b] = in ? beta * __ldg(R + b * NE + (a - b)) : 0.0;
+		}
+	int bad = 0;
+	for (int i = 0; i < N; ++i) {
+		double dr = wr[0][0], di = wi[0][0];
+		double den = fma(dr, dr, di * di);
+		if (!(den >= 1e-31)) bad = 1;
+		double inv = 1.0 / den;
+		double rr = dr * inv, ri = -di * inv;
+		double lr[NE], li[NE];
+		double2* o = out + (long)i * NE * npair;
+#pragma unroll
+		for (int a = 1; a < NE; ++a) {
+			lr[a] = fma(wr[a][0], rr, -wi[a][0] * ri);
+			li[a] = fma(wr[a][0], ri, wi[a][0] * rr);
+			o[(long)(a - 1) * npair] = make_double2(lr[a], li[a]);
+		}
+		o[(long)P * npair] = make_double2(rr, ri);
+		double cr[NE], ci[NE];	// column 0 before the update overwrites it
+#pragma unroll
+		for (int b = 1; b < NE; ++b) { cr[b] = wr[b][0]; ci[b] = wi[b][0]; }
+#pragma unroll
+		for (int a = 1; a < NE; ++a)
+#pragma unroll
+			for (int b = 1; b <= a; ++b) {
+				// W[a-1][b-1] = W[a][b] - l_a * W[b][0]
+				double xr = cr[b], xi = ci[b];
+				wr[a - 1][b - 1] = fma(-lr[a], xr, fma(li[a], xi, wr[a][b]));
+				wi[a - 1][b - 1] = fma(-lr[a], xi, fma(-li[a], xr, wi[a][b]));
+			}
+		int rn = i + NE;
+#pragma unroll
+		for (int c = 0; c < NE; ++c) {
+			int col = i + 1 + c;
+			bool in = rn < N;
+			wr[P][c] = in ? __ldg(S + (long)col * NE + (P - c)) : 0.0;
+			wi[P][c] = in ? beta * __ldg(R + (long)col * NE + (P - c)) : 0.0;
+		}
+	}
+	if (bad) atomicOr(status, ST_PIVOT);
+}
+
+// ---------------------------------------------------------------- coupling sweeps
+// For every (inst, m, pair k): the two channels +s_k and -s_k, each split into
+// real-part and imaginary-part lanes (4 lanes per pair).  The -s_k channel is
+// solved as the conjugate problem with the +s_k factors.  With the pair's
+// factors (k_factor) the block M(f)^a (a = 1 or 2) is applied as
+//   forward:  y_r = (S z)_r - sum_k L(r, r-k) y_{r-k}
+//   backward: x_r = y_r / D_r - sum_k L(r+k, r) x_{r+k};  z_r <- 2 x_r - z_r
+// Input eo slots (E_k, O_k) give z+ = E + O, z- = E - O; output slots hold
+// s_k = z+ + z-, d_k = z+ - z- for the backward transform.
+template <int P>
+__device__ __forceinline__ double shfl(double v, int lanemask, unsigned gmask)
+{
+	return __shfl_xor_sync(gmask, v, lanemask);
+}
+
+template <int P>
+__device__ __forceinline__ void cn_forward(const double* __restrict__ S, const double2* __restrict__ fac, long fstride,
+	const double2* __restrict__ eo, long eostride, int slotE, bool fromEO, double sgnO, double conjsgn, int part,
+	const double* __restrict__ zsrc, long zstride, double* __restrict__ ydst, long ystride, int N, unsigned gmask)
+{
+	constexpr int NE = P + 1;
+	double zw[2 * P + 1];	// own part of z at rows r-P .. r+P
+	double yre[P], yim[P];	// y_{r-1} .. y_{r-P}
+#pragma unroll
+	for (int q = 0; q < 2 * P + 1; ++q) zw[q] = 0.0;
+#pragma unroll
+	for (int q = 0; q < P; ++q) { yre[q] = 0.0; yim[q] = 0.0; }
+	auto loadz = [&](int r) -> double {
+		if (r >= N) return 0.0;
+		if (fromEO) {
+			double2 e = eo[(long)r * eostride + slotE];
+			double2 o = eo[(long)r * eostride + slotE + 1];
+			double v = part ? (e.y + sgnO * o.y) * conjsgn : (e.x + sgnO * o.x);
+			return v;
+		}
+		return zsrc[(long)r * zstride];
+	};
+#pragma unroll
+	for (int q = 0; q < P; ++q) zw[P + 1 + q] = loadz(q + 1);
+	zw[P] = loadz(0);
+	for (int r = 0; r < N; ++r) {
+		// w = (S z)_r, own part
+		double w = 0.0;
+#pragma unroll
+		for (int k = P; k >= 1; --k)
+			if (r - k >= 0) w = fma(__ldg(S + (long)(r - k) * NE + k), zw[P - k], w);
+#pragma unroll
+		for (int k = 0; k <= P; ++k) w = fma(__ldg(S + (long)r * NE + k), zw[P + k], w);
+		// y_r = w - sum_k L(r, r-k) y_{r-k};  L(r, r-k) = fac[r-k][k-1]
+		double acc = w;
+#pragma unroll
+		for (int k = P; k >= 1; --k) {
+			if (r - k < 0) continue;
+			double2 lv = fac[(long)(r - k) * fstride + (long)(k - 1) * (fstride / NE)];
+			if (part == 0) acc = fma(-lv.x, yre[k - 1], fma(lv.y, yim[k - 1], acc));
+			else acc = fma(-lv.x, yim[k - 1], fma(-lv.y, yre[k - 1], acc));
+		}
+		double other = shfl<P>(acc, 1, gmask);
+		double nyr = part ? other : acc, nyi = part ? acc : other;
+		ydst[(long)r * ystride] = acc;
+#pragma unroll
+		for (int q = P - 1; q >= 1; --q) { yre[q] = yre[q - 1]; yim[q] = yim[q - 1]; }
+		yre[0] = nyr; yim[0] = nyi;
+#pragma unroll
+		for (int q = 0; q < 2 * P; ++q) zw[q] = zw[q + 1];
+		zw[2 * P] = loadz(r + P + 1);
+	}
+}
+
+template <int P>
+__global__ void __launch_bounds__(64) k_sweep(double2* __restrict__ eo, double* __restrict__ y1, double* __restrict__ y2,
+	const double2* __restrict__ fac, const double* __restrict__ S, const int64_t* __restrict__ ntf,
+	long step, int jslot, int B, int M, int N, int L, int npair)
+{
+	constexpr int NE = P + 1;
+	long g = (long)blockIdx.x * blockDim.x + threadIdx.x;
+	long tot = (long)B * M * npair * 4;
+	int lane = threadIdx.x & 31;
+	unsigned gmask = 0xFu << (lane & 28);
+	bool valid = g < tot;
+	long gg = valid ? g : tot - 1;
+	int sub = (int)(gg & 3);
+	int part = sub & 1, neg = sub >> 1;
+	long pk = gg >> 2;
+	int k = (int)(pk % npair);
+	long im_inst = pk / npair;
+	long inst = im_inst / M;
+	int a = valid ? coupling_power(step, ntf[inst]) : 0;
+	if (a == 0) return;	// the 4 lanes of a pair agree on a
+	const long eostride = L;	// in double2 per row
+	double2* eob = eo + im_inst * (long)N * L;
+	// scratch viewed as doubles: [inst][m][r][slot][part] with slot = 2k+neg
+	const long ystride = 2L * L;
+	const long yoff = im_inst * (long)N * 2 * L + (2 * k + neg) * 2 + part;
+	double* y1b = y1 + yoff;
+	double* y2b = y2 + yoff;
+	const long fstride = (long)NE * npair;	// double2 per row
+	const double2* fb = fac + (((long)jslot * B * M + im_inst) * (long)N) * NE * npair + k;
+	const double sgnO = neg ? -1.0 : 1.0;
+	const double conjsgn = neg ? -1.0 : 1.0;
+	for (int app = 0; app < a; ++app) {
+		// forward: z from eo (app 0) or y1 (app 1); y -> y2
+		cn_forward<P>(S, fb, fstride, eob, eostride, 2 * k, app == 0, sgnO, conjsgn, part, y1b, ystride, y2b, ystride, N, gmask);
+		// backward: x_r = Dinv_r y_r - sum_k L(r+k, r) x_{r+k}; z <- 2x - z
+		double xre[P], xim[P];
+#pragma unroll
+		for (int q = 0; q < P; ++q) { xre[q] = 0.0; xim[q] = 0.0; }
+		const bool last = (app == a - 1);
+		for (int r = N - 1; r >= 0; --r) {
+			double yown = y2b[(long)r * ystride];
+			double yoth = shfl<P>(yown, 1, gmask);
+			double yr = part ? yoth : yown, yi = part ? yown : yoth;
+			double2 dv = fb[(long)r * fstride + (long)P * npair];
+			double acc = part ? fma(dv.x, yi, dv.y * yr) : fma(dv.x, yr, -dv.y * yi);
+#pragma unroll
+			for (int q = 1; q <= P; ++q) {
+				if (r + q >= N) continue;
+				double2 lv = fb[(long)r * fstride + (long)(q - 1) * npair];
+				if (part == 0) acc = fma(-lv.x, xre[q - 1], fma(lv.y, xim[q - 1], acc));
+				else acc = fma(-lv.x, xim[q - 1], fma(-lv.y, xre[q - 1], acc));
+			}
+			double oth = shfl<P>(acc, 1, gmask);
+#pragma unroll
+			for (int q = P - 1; q >= 1; --q) { xre[q] = xre[q - 1]; xim[q] = xim[q - 1]; }
+			xre[0] = part ? oth : acc; xim[0] = part ? acc : oth;
+			// z (own part) of this application
+			double z;
+			if (app == 0) {
+				double2 e = eob[(long)r * eostride + 2 * k], o = eob[(long)r * eostride + 2 * k + 1];
+				z = part ? (e.y + sgnO * o.y) * conjsgn : (e.x + sgnO * o.x);
+			} else z = y1b[(long)r * ystride];
+			double zn = fma(2.0, acc, -z);
+			if (!last) {
+				y1b[(long)r * ystride] = zn;
+			} else {
+				// combine with the other sign: actual z- = conj(computed)
+				double zo = shfl<P>(zn, 2, gmask);
+				double zp = neg ? zo : zn, zm = neg ? zn : zo;	// own part of z+ and of computed z-
+				double zmact = part ? -zm : zm;
+				double outv = neg ? (zp - zmact) : (zp + zmact);	// s (neg=0) or d (neg=1)
+				double* eod = reinterpret_cast<double*>(eob + (long)r * eostride + 2 * k + neg);
+				eod[part] = outv;
+			}
+		}
+	}
+}
+
+// ---------------------------------------------------------------- field-free step
+// Every (inst, m, il) channel, real/imag split over two lanes:
+//   forward  y_r = (S c)_r - sum_k L_l(r, r-k) y_{r-k}
+//   backward x_r = y_r / D_l(r) - sum_k L_l(r+k, r) x_{r+k};  c_r <- 2 x_r - c_r
+// with L_l, D_l the LDL^T of S + i dt/2 H_l (ff[r][c][l]: c < P L(r, r-1-c), c = P 1/D).
+template <int P>
+__global__ void __launch_bounds__(64) k_fieldfree(double2* __restrict__ st, double* __restrict__ ys, const double2* __restrict__ ff,
+	const double* __restrict__ S, const int64_t* __restrict__ ntt, long step, int B, int M, int m0, int N, int L, int nlh)
+{
+	constexpr int NE = P + 1;
+	long g = (long)blockIdx.x * blockDim.x + threadIdx.x;
+	long tot = (long)B * M * L * 2;
+	int lane = threadIdx.x & 31;
+	unsigned gmask = 0x3u << (lane & 30);
+	bool valid = g < tot;
+	long gg = valid ? g : tot - 1;
+	int part = (int)(gg & 1);
+	long ch = gg >> 1;
+	int il = (int)(ch % L);
+	long im_inst = ch / L;
+	int m = (int)(im_inst % M) + m0;
+	long inst = im_inst / M;
+	if (!valid || step >= ntt[inst]) return;
+	int l = il + (m < 0 ? -m : m);
+	double* sb = reinterpret_cast<double*>(st + im_inst * (long)N * L + il) + part;
+	double* yb = ys + (im_inst * (long)N * L + il) * 2 + part;
+	const long stride = 2L * L;	// doubles per row
+	const double2* fl = ff + l;
+	const long fstride = (long)NE * nlh;
+	// forward
+	{
+		double zw[2 * P + 1];
+		double yre[P], yim[P];
+#pragma unroll
+		for (int q = 0; q < 2 * P + 1; ++q) zw[q] = 0.0;
+#pragma unroll
+		for (int q = 0; q < P; ++q) { yre[q] = 0.0; yim[q] = 0.0; }
+#pragma unroll
+		for (int q = 0; q <= P; ++q) zw[P + q] = q < N ? sb[(long)q * stride] : 0.0;
+		for (int r = 0; r < N; ++r) {
+			double w = 0.0;
+#pragma unroll
+			for (int k = P; k >= 1; --k)
+				if (r - k >= 0) w = fma(__ldg(S + (long)(r - k) * NE + k), zw[P - k], w);
+#pragma unroll
+			for (int k = 0; k <= P; ++k) w = fma(__ldg(S + (long)r * NE + k), zw[P + k], w);
+			double acc = w;
+#pragma unroll
+			for (int k = 1; k <= P; ++k) {
+				double2 lv = fl[(long)r * fstride + (long)(k - 1) * nlh];
+				if (part == 0) acc = fma(-lv.x, yre[k - 1], fma(lv.y, yim[k - 1], acc));
+				else acc = fma(-lv.x, yim[k - 1], fma(-lv.y, yre[k - 1], acc));
+			}
+			double other = __shfl_xor_sync(gmask, acc, 1);
+			yb[(long)r * stride] = acc;
+#pragma unroll
+			for (int q = P - 1; q >= 1; --q) { yre[q] = yre[q - 1]; yim[q] = yim[q - 1]; }
+			yre[0] = part ? other : acc; yim[0] = part ? acc : other;
+#pragma unroll
+			for (int q = 0; q < 2 * P; ++q) zw[q] = zw[q + 1];
+			zw[2 * P] = (r + P + 1 < N) ? sb[(long)(r + P + 1) * stride] : 0.0;
+		}
+	}
+	// backward
+	{
+		double xre[P], xim[P];
+#pragma unroll
+		for (int q = 0; q < P; ++q) { xre[q] = 0.0; xim[q] = 0.0; }
+		for (int r = N - 1; r >= 0; --r) {
+			double yown = yb[(long)r * stride];
+			double yoth = __shfl_xor_sync(gmask, yown, 1);
+			double yr = part ? yoth : yown, yi = part ? yown : yoth;
+			double2 dv = fl[(long)r * fstride + (long)P * nlh];
+			double acc = part ? fma(dv.x, yi, dv.y * yr) : fma(dv.x, yr, -dv.y * yi);
+#pragma unroll
+			for (int q = 1; q <= P; ++q) {
+				if (r + q >= N) continue;
+				double2 lv = fl[(long)(r + q) * fstride + (long)(q - 1) * nlh];
+				if (part == 0) acc = fma(-lv.x, xre[q - 1], fma(lv.y, xim[q - 1], acc));
+				else acc = fma(-lv.x, xim[q - 1], fma(-lv.y, xre[q - 1], acc));
+			}
+			double oth = __shfl_xor_sync(gmask, acc, 1);
+#pragma unroll
+			for (int q = P - 1; q >= 1; --q) { xre[q] = xre[q - 1]; xim[q] = xim[q - 1]; }
+			xre[0] = part ? oth : acc; xim[0] = part ? acc : oth;
+			double c = sb[(long)r * stride];
+			sb[(long)r * stride] = fma(2.0, acc, -c);
+		}
+	}
+}
+
+// ---------------------------------------------------------------- reductions
+// Per (inst, m, il) channel partial sums, then a fixed-order per-instance sum
+// (deterministic: the same input gives bit-identical output).
+__device__ __forceinline__ double2 band_sym_mv(const double* __restrict__ A, int NE, int N, const double2* __restrict__ x, long xs, int r)
+{
+	// (A x)_r for symmetric band A
+	double re = 0.0, im = 0.0;
+	for (int k = NE - 1; k >= 1; --k)
+		if (r - k >= 0) { double a = __ldg(A + (long)(r - k) * NE + k); double2 v = x[(long)(r - k) * xs]; re = fma(a, v.x, re); im = fma(a, v.y, im); }
+	for (int k = 0; k < NE && r + k < N; ++k) { double a = __ldg(A + (long)r * NE + k); double2 v = x[(long)(r + k) * xs]; re = fma(a, v.x, re); im = fma(a, v.y, im); }
+	return make_double2(re, im);
+}
+
+// out[ch] = c^H A c' where c = channel ch, c' = channel ch + dl (same (inst,m)); zero if out of range
+__global__ void k_band_inner(const double2* __restrict__ st, const double* __restrict__ A, int NE, int N, int L, long nch,
+	int dl, double2* __restrict__ out)
+{
+	long ch = (long)blockIdx.x * blockDim.x + threadIdx.x;
+	if (ch >= nch) return;
+	int il = (int)(ch % L);
+	int il2 = il + dl;
+	if (il2 < 0 || il2 >= L) { out[ch] = make_double2(0.0, 0.0); return; }
+	long base = (ch / L) * (long)N * L;
+	const double2* x = st + base + il;
+	const double2* y = st + base + il2;
+	double re = 0.0, im = 0.0;
+	for (int r = 0; r < N; ++r) {
+		double2 t = band_sym_mv(A, NE, N, y, L, r);
+		double2 c = x[(long)r * L];
+		re = fma(c.x, t.x, fma(c.y, t.y, re));
+		im = fma(c.x, t.y, fma(-c.y, t.x, im));
+	}
+	out[ch] = make_double2(re, im);
+}
+
+// proj[inst][m][il][n] = sum_r basis_l[n][r] c[r]
+__global__ void k_projection(const double2* __restrict__ st, const double* __restrict__ basis, const long* __restrict__ boff,
+	const int* __restrict__ nst, const long* __restrict__ poff, int N, int L, int M, int m0, long nch, int nmax,
+	double2* __restrict__ proj)
+{
+	long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+	long ch = t / nmax;
+	int n = (int)(t % nmax);
+	if (ch >= nch) return;
+	int il = (int)(ch % L);
+	int m = (int)((ch / L) % M) + m0;
+	int l = il + (m < 0 ? -m : m);
+	if (n >= nst[l]) return;
+	const double* b = basis + boff[l] + (long)n * N;
+	const double2* x = st + (ch / L) * (long)N * L + il;
+	double re = 0.0, im = 0.0;
+	for (int r = 0; r < N; ++r) { double w = __ldg(b + r); double2 c = x[(long)r * L]; re = fma(w, c.x, re); im = fma(w, c.y, im); }
+	proj[poff[ch] + n] = make_double2(re, im);
+}
+
+__global__ void k_status_check(const double2* __restrict__ st, long n, int* __restrict__ status)
+{
+	long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+	if (t >= n) return;
+	double2 v = st[t];
+	if (!isfinite(v.x) || !isfinite(v.y)) atomicOr(status, ST_NONFINITE);
+}
+
+} // namespace qpc
+
+using namespace qpc;
+
+// ============================================================================ handle
+
+struct qpc_lgwz {
+	int dev = 0;
+	qpc_dims d{};
+	int N = 0, P = 0, L = 0, M = 0, B = 0, lmax = 0, nlh = 0, npair = 0;
+	double dt = 0.0;
+	cudaStream_t stream = nullptr;
+	cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+	double* S = nullptr;      // [N][P+1]
+	double* R = nullptr;      // [N][P+1]
+	double* Vh = nullptr;     // [M][npair+1][L]
+	double* lamp = nullptr;   // [M][npair]
+	double2* ff = nullptr;    // [N][P+1][nlh]
+	double2* st = nullptr;    // [B][M][N][L]
+	double2* eo = nullptr;    // [B][M][N][L]
+	double* y1 = nullptr;     // [B][M][N][L][2]
+	double* y2 = nullptr;
+	double2* hostlay = nullptr; // [B][M][L][N] staging for layout change
+	double2* fac = nullptr;   // [K][B][M][N][P+1][npair]
+	int K = 1;
+	int* status = nullptr;
+	double2* red = nullptr;   // reduction scratch [B*M*L]
+	int64_t* ntf = nullptr;   // device [B]
+	int64_t* ntt = nullptr;
+	double* ftab = nullptr;   // device field table [B][ld]
+	size_t ftab_cap = 0;
+	long ld = 1;
+	double last_ms = 0.0;
+	int64_t launches = 0;
+	// optional per-kernel timing (CUDA events around each launch on the handle's stream)
+	bool profiling = false;
+	std::vector<cudaEvent_t> evpool;
+	std::vector<std::pair<int, int>> evuse;	// (kernel id, index of start event; end = +1)
+	double kms[QPC_NKERNEL] = {0};
+	int64_t kcount[QPC_NKERNEL] = {0};
+	std::vector<double> h_lam;   // [M][L]
+	std::vector<double> h_P;     // [M][L][L]
+	std::vector<double> h_S;
+};
+
+namespace {
+
+long state_len(const qpc_lgwz* h) { return (long)h->B * h->M * h->N * h->L; }
+
+int check_device(int* dev)
+{
+	int n = 0;
+	cudaError_t e = cudaGetDeviceCount(&n);
+	if (e != cudaSuccess || n == 0) { set_error("no CUDA device: %s", cudaGetErrorString(e)); return QPC_ERR_NODEVICE; }
+	QPC_CUDA(cudaGetDevice(dev));
+	cudaDeviceProp prop;
+	QPC_CUDA(cudaGetDeviceProperties(&prop, *dev));
+	if (prop.major * 10 + prop.minor < 100) { set_error("device %s (sm_%d%d) is not Blackwell-class", prop.name, prop.major, prop.minor); return QPC_ERR_NODEVICE; }
+	return QPC_OK;
+}
+
+template <class T> int dalloc(T** p, size_t n)
+{
+	cudaError_t e = cudaMalloc((void**)p, sizeof(T) * std::max<size_t>(n, 1));
+	if (e != cudaSuccess) { *p = nullptr; set_error("cudaMalloc(%zu bytes): %s", sizeof(T) * n, cudaGetErrorString(e)); return QPC_ERR_NOMEM; }
+	return QPC_OK;
+}
+
+int wait_stream(qpc_lgwz* h)
+{
+	// bounded wait: poll, give up after ~600 s of wall time
+	for (long it = 0;; ++it) {
+		cudaError_t e = cudaStreamQuery(h->stream);
+		if (e == cudaSuccess) return QPC_OK;
+		if (e != cudaErrorNotReady) { set_error("stream error: %s", cudaGetErrorString(e)); return QPC_ERR_CUDA; }
+		if (it > 6000000) { set_error("timed out waiting for the device"); return QPC_ERR_TIMEOUT; }
+		struct timespec ts = {0, 100000};
+		nanosleep(&ts, nullptr);
+	}
+}
+
+int read_status(qpc_lgwz* h)
+{
+	int st = 0;
+	QPC_CUDA(cudaMemcpyAsync(&st, h->status, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+	int rc = wait_stream(h);
+	if (rc) return rc;
+	if (st & ST_PIVOT) { set_error("zero pivot in a Crank-Nicolson factorisation"); return QPC_ERR_SINGULAR; }
+	if (st & ST_NONFINITE) { set_error("non-finite value in the state"); return QPC_ERR_NUMERIC; }
+	return QPC_OK;
+}
+
+#define LAUNCH(h) ((h)->launches++)
+
+struct prof_scope {
+	qpc_lgwz* h; int kind; int idx = -1;
+	prof_scope(qpc_lgwz* h_, int kind_) : h(h_), kind(kind_)
+	{
+		if (!h->profiling) return;
+		idx = (int)h->evuse.size() * 2;
+		while ((int)h->evpool.size() < idx + 2) { cudaEvent_t e; cudaEventCreate(&e); h->evpool.push_back(e); }
+		cudaEventRecord(h->evpool[idx], h->stream);
+	}
+	~prof_scope()
+	{
+		if (idx < 0) return;
+		cudaEventRecord(h->evpool[idx + 1], h->stream);
+		h->evuse.push_back({kind, idx});
+	}
+};
+
+void collect_profile(qpc_lgwz* h)
+{
+	for (auto& u : h->evuse) {
+		float ms = 0.f;
+		if (cudaEventElapsedTime(&ms, h->evpool[u.second], h->evpool[u.second + 1]) == cudaSuccess) {
+			h->kms[u.first] += ms;
+			h->kcount[u.first] += 1;
+		}
+	}
+	h->evuse.clear();
+}
+
+template <int P>
+int launch_step_kernels(qpc_lgwz* h, long step, long step0, int jslot, bool do_factor, int kfac)
+{
+	const int B = h->B, M = h->M, N = h->N, L = h->L, np = h->npair;
+	if (do_factor && np > 0) {
+		prof_scope ps(h, QPC_KERNEL_FACTOR);
+		long nsys = (long)kfac * B * M * np;
+		k_factor<P><<<(unsigned)((nsys + 63) / 64), 64, 0, h->stream>>>(h->fac, h->S, h->R, h->lamp, h->ftab, h->ld,
+			h->ntf, step0, kfac, B, M, N, np, h->dt, h->status);
+		LAUNCH(h);
+	}
+	if (np > 0 || (L & 1)) {
+		int tiles = (N + TR - 1) / TR;
+		size_t smem = sizeof(double2) * 2 * TR * (L | 1);
+		unsigned grid = (unsigned)((long)B * M * tiles);
+		{
+			prof_scope ps(h, QPC_KERNEL_TRANSFORM_FWD);
+			k_transform<<<grid, 256, smem, h->stream>>>(h->st, h->eo, h->Vh, N, L, M, np, 1, h->ntf, step, B);
+			LAUNCH(h);
+		}
+		if (np > 0) {
+			prof_scope ps(h, QPC_KERNEL_SWEEP);
+			long tot = (long)B * M * np * 4;
+			k_sweep<P><<<(unsigned)((tot + 63) / 64), 64, 0, h->stream>>>(h->eo, h->y1, h->y2, h->fac, h->S, h->ntf, step, jslot, B, M, N, L, np);
+			LAUNCH(h);
+		}
+		{
+			prof_scope ps(h, QPC_KERNEL_TRANSFORM_BWD);
+			k_transform<<<grid, 256, smem, h->stream>>>(h->eo, h->st, h->Vh, N, L, M, np, 0, h->ntf, step, B);
+			LAUNCH(h);
+		}
+	}
+	prof_scope ps(h, QPC_KERNEL_FIELDFREE);
+	long tot = (long)B * M * L * 2;
+	k_fieldfree<P><<<(unsigned)((tot + 63) / 64), 64, 0, h->stream>>>(h->st, h->y2, h->ff, h->S, h->ntt, step, B, M, h->d.m0, N, L, h->nlh);
+	LAUNCH(h);
+	return QPC_OK;
+}
+
+int launch_step(qpc_lgwz* h, long step, long step0, int jslot, bool do_factor, int kfac)
+{
+	switch (h->P) {
+	case 3: return launch_step_kernels<3>(h, step, step0, jslot, do_factor, kfac);
+	case 4: return launch_step_kernels<4>(h, step, step0, jslot, do_factor, kfac);
+	case 5: return launch_step_kernels<5>(h, step, step0, jslot, do_factor, kfac);
+	case 6: return launch_step_kernels<6>(h, step, step0, jslot, do_factor, kfac);
+	case 7: return launch_step_kernels<7>(h, step, step0, jslot, do_factor, kfac);
+	case 8: return launch_step_kernels<8>(h, step, step0, jslot, do_factor, kfac);
+	default: set_error("unsupported B-spline degree %d", h->P); return QPC_ERR_ARGS;
+	}
+}
+
+} // namespace
+
+extern "C" {
+
+const char* qpc_last_error(void) { return g_err; }
+const char* qpc_version(void) { return "qpc-gb300 engine 1 (sm_103a, complex FP64)"; }
+
+int qpc_lgwz_create(const qpc_dims* dims, double dt, const double* S, const double* R, const double* H, qpc_lgwz** out)
+{
+	if (!out) { set_error("out is NULL"); return QPC_ERR_ARGS; }
+	*out = nullptr;
+	if (!dims || !S || !R || !H) { set_error("NULL argument"); return QPC_ERR_ARGS; }
+	const qpc_dims d = *dims;
+	if (d.p < 3 || d.p > QPC_MAX_RANK || d.n_r < 2 * d.p + 2 || d.n_l < 1 || d.n_m < 1 || d.n_inst < 1 || !(dt > 0) || !std::isfinite(dt)) {
+		set_error("bad dims n_r=%d p=%d n_l=%d n_m=%d n_inst=%d dt=%g", d.n_r, d.p, d.n_l, d.n_m, d.n_inst, dt);
+		return QPC_ERR_ARGS;
+	}
+	int dev = 0;
+	if (int rc = check_device(&dev)) return rc;
+	auto* h = new (std::nothrow) qpc_lgwz();
+	if (!h) { set_error("host allocation"); return QPC_ERR_NOMEM; }
+	h->dev = dev; h->d = d; h->N = d.n_r; h->P = d.p; h->L = d.n_l; h->M = d.n_m; h->B = d.n_inst; h->dt = dt;
+	long mabs = std::max(std::labs((long)d.m0), std::labs((long)d.m0 + d.n_m - 1));
+	h->lmax = (int)(mabs + d.n_l - 1);
+	h->nlh = h->lmax + 1;
+	h->npair = d.n_l / 2;
+	const int N = h->N, P = h->P, NE = P + 1, L = h->L, M = h->M, np = h->npair;
+	int rc = QPC_OK;
+	auto fail = [&](int code) { qpc_lgwz_destroy(h); return code; };
+	if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) { set_error("stream create"); return fail(QPC_ERR_CUDA); }
+	cudaEventCreate(&h->ev0); cudaEventCreate(&h->ev1);
+	// host setup: field-free LDL^T per l, Y10 eigensystems
+	std::vector<double2> ffh((size_t)N * NE * h->nlh);
+	std::vector<double> Lrow((size_t)N * P * 2), Dinv((size_t)N * 2);
+	for (int l = 0; l < h->nlh; ++l) {
+		int bad = qpc_ldlt_csym(N, P, S, H + (size_t)l * N * NE, dt * 0.5, Lrow.data(), Dinv.data());
+		if (bad < 0) { set_error("ldlt arguments"); return fail(QPC_ERR_ARGS); }
+		if (bad > 0) { set_error("zero pivot factorising S + i dt/2 H_%d", l); return fail(QPC_ERR_SINGULAR); }
+		// store L(r, r-1-c) for the forward sweep: ff[r][c][l] = Lrow[r][c]
+		for (int r = 0; r < N; ++r) {
+			for (int c = 0; c < P; ++c)
+				ffh[((size_t)r * NE + c) * h->nlh + l] = make_double2(Lrow[2 * ((size_t)r * P + c)], Lrow[2 * ((size_t)r * P + c) + 1]);
+			ffh[((size_t)r * NE + P) * h->nlh + l] = make_double2(Dinv[2 * (size_t)r], Dinv[2 * (size_t)r + 1]);
+		}
+	}
+	h->h_lam.assign((size_t)M * L, 0.0);
+	h->h_P.assign((size_t)M * L * L, 0.0);
+	std::vector<double> Vh((size_t)M * (np + 1) * L, 0.0), lamp((size_t)M * std::max(np, 1), 0.0);
+	for (int im = 0; im < M; ++im) {
+		double* lam = h->h_lam.data() + (size_t)im * L;
+		double* Pm = h->h_P.data() + (size_t)im * L * L;
+		if ((rc = qpc_y10_eigen(L, d.m0 + im, lam, Pm))) return fail(rc);
+		for (int k = 0; k < np; ++k) {
+			int row = L - 1 - k;	// +s_k
+			lamp[(size_t)im * np + k] = lam[row];
+			for (int il = 0; il < L; ++il) Vh[((size_t)im * (np + 1) + k) * L + il] = Pm[(size_t)row * L + il];
+		}
+		if (L & 1)
+			for (int il = 0; il < L; ++il) Vh[((size_t)im * (np + 1) + np) * L + il] = Pm[(size_t)np * L + il];
+	}
+	h->h_S.assign(S, S + (size_t)N * NE);
+	// look-ahead depth for the factorisation: enough systems to fill the GPU, bounded memory
+	size_t per_step = (size_t)h->B * M * N * NE * std::max(np, 1) * sizeof(double2);
+	h->K = 1;
+	while (h->K < 8 && (long)h->K * h->B * M * np < 40000 && per_step * (h->K * 2) <= ((size_t)4 << 30)) h->K *= 2;
+	long sl = state_len(h);
+	if ((rc = dalloc(&h->S, (size_t)N * NE)) || (rc = dalloc(&h->R, (size_t)N * NE)) || (rc = dalloc(&h->Vh, Vh.size())) ||
+		(rc = dalloc(&h->lamp, lamp.size())) || (rc = dalloc(&h->ff, ffh.size())) || (rc = dalloc(&h->st, sl)) ||
+		(rc = dalloc(&h->eo, sl)) || (rc = dalloc(&h->y1, 2 * sl)) || (rc = dalloc(&h->y2, 2 * sl)) ||
+		(rc = dalloc(&h->hostlay, sl)) || (rc = dalloc(&h->fac, per_step / sizeof(double2) * h->K)) ||
+		(rc = dalloc(&h->status, 1)) || (rc = dalloc(&h->red, (size_t)h->B * M * L * 2)) ||
+		(rc = dalloc(&h->ntf, h->B)) || (rc = dalloc(&h->ntt, h->B)))
+		return fail(rc);
+	if (cudaMemcpy(h->S, S, sizeof(double) * N * NE, cudaMemcpyHostToDevice) != cudaSuccess ||
+		cudaMemcpy(h->R, R, sizeof(double) * N * NE, cudaMemcpyHostToDevice) != cudaSuccess ||
+		cudaMemcpy(h->Vh, Vh.data(), sizeof(double) * Vh.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
+		cudaMemcpy(h->lamp, lamp.data(), sizeof(double) * lamp.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
+		cudaMemcpy(h->ff, ffh.data(), sizeof(double2) * ffh.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
+		cudaMemset(h->st, 0, sizeof(double2) * sl) != cudaSuccess || cudaMemset(h->status, 0, sizeof(int)) != cudaSuccess) {
+		set_error("initial device copies failed");
+		return fail(QPC_ERR_CUDA);
+	}
+	size_t smem = sizeof(double2) * 2 * TR * (L | 1);
+	if (smem > 48 * 1024) cudaFuncSetAttribute(k_transform, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+	*out = h;
+	return QPC_OK;
+}
+
+int qpc_lgwz_destroy(qpc_lgwz* h)
+{
+	if (!h) return QPC_OK;
+	if (h->stream) cudaStreamSynchronize(h->stream);
+	cudaFree(h->S); cudaFree(h->R); cudaFree(h->Vh); cudaFree(h->lamp); cudaFree(h->ff);
+	cudaFree(h->st); cudaFree(h->eo); cudaFree(h->y1); cudaFree(h->y2); cudaFree(h->hostlay); cudaFree(h->fac);
+	cudaFree(h->status); cudaFree(h->red); cudaFree(h->ntf); cudaFree(h->ntt); cudaFree(h->ftab);
+	for (auto e : h->evpool) cudaEventDestroy(e);
+	if (h->ev0) cudaEventDestroy(h->ev0);
+	if (h->ev1) cudaEventDestroy(h->ev1);
+	if (h->stream) cudaStreamDestroy(h->stream);
+	delete h;
+	return QPC_OK;
+}
+
+static int put_common(qpc_lgwz* h, const double* src, cudaMemcpyKind kind)
+{
+	long sl = state_len(h);
+	QPC_CUDA(cudaMemcpyAsync(h->hostlay, src, sizeof(double2) * sl, kind, h->stream));
+	long nblk = (long)h->B * h->M;
+	k_to_rmajor<<<(unsigned)((sl + 255) / 256), 256, 0, h->stream>>>(h->hostlay, h->st, h->N, h->L, nblk);
+	LAUNCH(h);
+	QPC_CUDA(cudaGetLastError());
+	return wait_stream(h);
+}
+static int get_common(qpc_lgwz* h, double* dst, cudaMemcpyKind kind)
+{
+	long sl = state_len(h);
+	long nblk = (long)h->B * h->M;
+	k_to_lmajor<<<(unsigned)((sl + 255) / 256), 256, 0, h->stream>>>(h->st, h->hostlay, h->N, h->L, nblk);
+	LAUNCH(h);
+	QPC_CUDA(cudaGetLastError());
+	QPC_CUDA(cudaMemcpyAsync(dst, h->hostlay, sizeof(double2) * sl, kind, h->stream));
+	return wait_stream(h);
+}
+
+int qpc_lgwz_put(qpc_lgwz* h, const double* coef)
+{
+	if (!h || !coef) { set_error("NULL argument"); return QPC_ERR_ARGS; }
+	return put_common(h, coef, cudaMemcpyHostToDevice);
+}
+int qpc_lgwz_get(qpc_lgwz* h, double* coef)
+{
+	if (!h || !coef) { set_error("NULL argument"); return QPC_ERR_ARGS; }
+	return get_common(h, coef, cudaMemcpyDeviceToHost);
+}
+int qpc_lgwz_put_device(qpc_lgwz* h, const double* dev_coef)
+{
+	if (!h || !dev_coef) { set_error("NULL argument"); return QPC_ERR_ARGS; }
+	return put_common(h, dev_coef, cudaMemcpyDeviceToDevice);
+}
+int qpc_lgwz_get_device(qpc_lgwz* h, double* dev_coef)
+{
+	if (!h || !dev_coef) { set_error("NULL argument"); return QPC_ERR_ARGS; }
+	return get_common(h, dev_coef, cudaMemcpyDeviceToDevice);
+}
+
+int qpc_lgwz_run(qpc_lgwz* h, const double* ftab, int64_t ld, const int64_t* nt_field, const int64_t* nt_total)
+{
+	if (!h || !nt_field || !nt_total) { set_error("NULL argument"); return QPC_ERR_ARGS; }
+	const int B = h->B;
+	long smax = 0;
+	bool anyfield = false;
+	for (int k = 0; k < B; ++k) {
+		if (nt_field[k] < 0 || nt_total[k] < nt_field[k]) { set_error("instance %d: nt_field=%lld nt_total=%lld", k, (long long)nt_field[k], (long long)nt_total[k]); return QPC_ERR_ARGS; }
+		if (nt_field[k] > 0) { anyfield = true; if (ld < nt_field[k] + 1) { set_error("ld=%lld < nt_field+1", (long long)ld); return QPC_ERR_ARGS; } }
+		smax = std::max<long>(smax, std::max<long>(nt_total[k], nt_field[k] + (nt_field[k] > 0 ? 1 : 0)));
+	}
+	if (anyfield && !ftab) { set_error("ftab is NULL"); return QPC_ERR_ARGS; }
+	// field table to the device, padded to B*ld
+	size_t need = anyfield ? (size_t)B * ld : 1;
+	if (h->ftab_cap < need) {
+		cudaFree(h->ftab); h->ftab = nullptr; h->ftab_cap = 0;
+		if (int rc = dalloc(&h->ftab, need)) return rc;
+		h->ftab_cap = need;
+	}
+	if (anyfield) {
+		for (int k = 0; k < B; ++k)
+			for (int64_t i = 0; i <= nt_field[k]; ++i)
+				if (nt_field[k] > 0 && !std::isfinite(ftab[(size_t)k * ld + i])) { set_error("non-finite field value, instance %d step %lld", k, (long long)i); return QPC_ERR_ARGS; }
+		QPC_CUDA(cudaMemcpyAsync(h->ftab, ftab, sizeof(double) * need, cudaMemcpyHostToDevice, h->stream));
+	}
+	QPC_CUDA(cudaMemcpyAsync(h->ntf, nt_field, sizeof(int64_t) * B, cudaMemcpyHostToDevice, h->stream));
+	QPC_CUDA(cudaMemcpyAsync(h->ntt, nt_total, sizeof(int64_t) * B, cudaMemcpyHostToDevice, h->stream));
+	QPC_CUDA(cudaMemsetAsync(h->status, 0, sizeof(int), h->stream));
+	h->ld = anyfield ? (long)ld : 0;
+	QPC_CUDA(cudaEventRecord(h->ev0, h->stream));
+	for (long s = 0; s < smax; ++s) {
+		// factors for steps s .. s+K-1 are computed together, into slots 0..K-1
+		int j = (int)(s % h->K);
+		long kf = std::min<long>(h->K, smax - s);
+		if (int rc = launch_step(h, s, s - j, j, j == 0, (int)kf)) return rc;
+	}
+	QPC_CUDA(cudaEventRecord(h->ev1, h->stream));
+	QPC_CUDA(cudaGetLastError());
+	long sl = state_len(h);
+	k_status_check<<<(unsigned)((sl + 255) / 256), 256, 0, h->stream>>>(h->st, sl, h->status);
+	LAUNCH(h);
+	int rc = read_status(h);
+	float ms = 0.f;
+	cudaEventElapsedTime(&ms, h->ev0, h->ev1);
+	h->last_ms = ms;
+	collect_profile(h);
+	return rc;
+}
+
+int qpc_lgwz_propagate(qpc_lgwz* h, const double* f_ti, const double* f_tf)
+{
+	if (!h || !f_ti || !f_tf) { set_error("NULL argument"); return QPC_ERR_ARGS; }
+	std::vector<double> tab((size_t)h->B * 2);
+	std::vector<int64_t> nf(h->B, 1), nt(h->B, 1);
+	for (int k = 0; k < h->B; ++k) { tab[2 * (size_t)k] = f_ti[k]; tab[2 * (size_t)k + 1] = f_tf[k]; }
+	return qpc_lgwz_run(h, tab.data(), 2, nf.data(), nt.data());
+}
+
+int qpc_lgwz_propagate_free(qpc_lgwz* h)
+{
+	if (!h) { set_error("NULL argument"); return QPC_ERR_ARGS; }
+	std::vector<int64_t> nf(h->B, 0), nt(h->B, 1);
+	return qpc_lgwz_run(h, nullptr, 1, nf.data(), nt.data());
+}
+
+int qpc_lgwz_norm(qpc_lgwz* h, double* norm)
+{
+	if (!h || !norm) { set_error("NULL argument"); return QPC_ERR_ARGS; }
+	long nch = (long)h->B * h->M * h->L;
+	k_band_inner<<<(unsigned)((nch + 127) / 128), 128, 0, h->stream>>>(h->st, h->S, h->P + 1, h->N, h->L, nch, 0, h->red);
+	LAUNCH(h);
+	QPC_CUDA(cudaGetLastError());
+	std::vector<double2> part(nch);
+	QPC_CUDA(cudaMemcpyAsync(part.data(), h->red, sizeof(double2) * nch, cudaMemcpyDeviceToHost, h->stream));
+	if (int rc = wait_stream(h)) return rc;
+	long per = (long)h->M * h->L;
+	for (int k = 0; k < h->B; ++k) {
+		double s = 0.0;
+		for (long c = 0; c < per; ++c) s += part[(size_t)k * per + c].x;
+		norm[k] = s;
+	}
+	return QPC_OK;
+}
+
+int qpc_lgwz_dipole(qpc_lgwz* h, const double* F, double* out)
+{
+	if (!h || !F || !out) { set_error("NULL argument"); return QPC_ERR_ARGS; }
+	const int N = h->N, NE = h->P + 1, L = h->L, M = h->M;
+	double* dF = nullptr;
+	if (int rc = dalloc(&dF, (size_t)N * NE)) return rc;
+	long nch = (long)h->B * M * L;
+	double2* red2 = h->red + nch;
+	int rc = QPC_OK;
+	if (cudaMemcpyAsync(dF, F, sizeof(double) * N * NE, cudaMemcpyHostToDevice, h->stream) != cudaSuccess) rc = QPC_ERR_CUDA;
+	if (!rc) {
+		k_band_inner<<<(unsigned)((nch + 127) / 128), 128, 0, h->stream>>>(h->st, dF, NE, N, L, nch, -1, h->red);
+		k_band_inner<<<(unsigned)((nch + 127) / 128), 128, 0, h->stream>>>(h->st, dF, NE, N, L, nch, +1, red2);
+		h->launches += 2;
+		if (cudaGetLastError() != cudaSuccess) rc = QPC_ERR_CUDA;
+	}
+	std::vector<double2> lo(nch), hi(nch);
+	if (!rc && (cudaMemcpyAsync(lo.data(), h->red, sizeof(double2) * nch, cudaMemcpyDeviceToHost, h->stream) != cudaSuccess ||
+		cudaMemcpyAsync(hi.data(), red2, sizeof(double2) * nch, cudaMemcpyDeviceToHost, h->stream) != cudaSuccess)) rc = QPC_ERR_CUDA;
+	if (!rc) rc = wait_stream(h);
+	cudaFree(dF);
+	if (rc) { if (rc == QPC_ERR_CUDA) set_error("dipole device step failed"); return rc; }
+	std::vector<double> y(L);
+	for (int k = 0; k < h->B; ++k) {
+		double re = 0.0, im = 0.0;
+		for (int m = 0; m < M; ++m) {
+			qpc_y10_coupling(L, h->d.m0 + m, y.data());
+			for (int il = 0; il < L; ++il) {
+				size_t c = ((size_t)k * M + m) * L + il;
+				if (il > 0) { re += lo[c].x * y[il - 1]; im += lo[c].y * y[il - 1]; }
+				if (il + 1 < L) { re += hi[c].x * y[il]; im += hi[c].y * y[il]; }
+			}
+		}
+		out[2 * (size_t)k] = re; out[2 * (size_t)k + 1] = im;
+	}
+	return QPC_OK;
+}
+
+int qpc_lgwz_projection(qpc_lgwz* h, const int32_t* n_state, const double* basis, double* proj)
+{
+	if (!h || !n_state || !basis || !proj) { set_error("NULL argument"); return QPC_ERR_ARGS; }
+	const int N = h->N, L = h->L, M = h->M, nl = h->nlh;
+	std::vector<long> boff(nl + 1, 0);
+	int nmax = 0;
+	for (int l = 0; l < nl; ++l) {
+		if (n_state[l] < 0 || n_state[l] > N) { set_error("n_state[%d]=%d", l, n_state[l]); return QPC_ERR_ARGS; }
+		boff[l + 1] = boff[l] + (long)n_state[l] * N;
+		nmax = std::max(nmax, n_state[l]);
+	}
+	long nch = (long)h->B * M * L;
+	std::vector<long> poff(nch + 1, 0);
+	for (long c = 0; c < nch; ++c) {
+		int il = (int)(c % L), m = (int)((c / L) % M) + h->d.m0;
+		int l = il + (m < 0 ? -m : m);
+		poff[c + 1] = poff[c] + n_state[l];
+	}
+	if (nmax == 0) return QPC_OK;
+	double *db = nullptr; long *dbo = nullptr, *dpo = nullptr; int* dn = nullptr; double2* dp = nullptr;
+	int rc = QPC_OK;
+	if ((rc = dalloc(&db, (size_t)boff[nl])) || (rc = dalloc(&dbo, (size_t)nl + 1)) || (rc = dalloc(&dpo, (size_t)nch + 1)) ||
+		(rc = dalloc(&dn, (size_t)nl)) || (rc = dalloc(&dp, (size_t)poff[nch]))) {
+		cudaFree(db); cudaFree(dbo); cudaFree(dpo); cudaFree(dn); cudaFree(dp);
+		return rc;
+	}
+	bool ok = cudaMemcpyAsync(db, basis, sizeof(double) * boff[nl], cudaMemcpyHostToDevice, h->stream) == cudaSuccess &&
+		cudaMemcpyAsync(dbo, boff.data(), sizeof(long) * (nl + 1), cudaMemcpyHostToDevice, h->stream) == cudaSuccess &&
+		cudaMemcpyAsync(dpo, poff.data(), sizeof(long) * (nch + 1), cudaMemcpyHostToDevice, h->stream) == cudaSuccess &&
+		cudaMemcpyAsync(dn, n_state, sizeof(int) * nl, cudaMemcpyHostToDevice, h->stream) == cudaSuccess;
+	if (ok) {
+		long tot = nch * nmax;
+		k_projection<<<(unsigned)((tot + 127) / 128), 128, 0, h->stream>>>(h->st, db, dbo, dn, dpo, N, L, M, h->d.m0, nch, nmax, dp);
+		LAUNCH(h);
+		ok = cudaGetLastError() == cudaSuccess &&
+			cudaMemcpyAsync(proj, dp, sizeof(double2) * poff[nch], cudaMemcpyDeviceToHost, h->stream) == cudaSuccess;
+	}
+	rc = ok ? wait_stream(h) : QPC_ERR_CUDA;
+	if (!ok) set_error("projection device step failed");
+	cudaFree(db); cudaFree(dbo); cudaFree(dpo); cudaFree(dn); cudaFree(dp);
+	return rc;
+}
+
+int qpc_lgwz_last_run_ms(qpc_lgwz* h, double* ms)
+{
+	if (!h || !ms) { set_error("NULL argument"); return QPC_ERR_ARGS; }
+	*ms = h->last_ms;
+	return QPC_OK;
+}
+
+int64_t qpc_lgwz_launch_count(qpc_lgwz* h) { return h ? h->launches : -1; }
+
+int qpc_lgwz_set_profiling(qpc_lgwz* h, int on)
+{
+	if (!h) { set_error("NULL argument"); return QPC_ERR_ARGS; }
+	h->profiling = on != 0;
+	for (int k = 0; k < QPC_NKERNEL; ++k) { h->kms[k] = 0.0; h->kcount[k] = 0; }
+	return QPC_OK;
+}
+
+int qpc_lgwz_kernel_times(qpc_lgwz* h, double* ms, int64_t* launches)
+{
+	if (!h || !ms || !launches) { set_error("NULL argument"); return QPC_ERR_ARGS; }
+	for (int k = 0; k < QPC_NKERNEL; ++k) { ms[k] = h->kms[k]; launches[k] = h->kcount[k]; }
+	return QPC_OK;
+}
+
+} // extern "C"

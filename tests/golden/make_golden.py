@@ -1,0 +1,121 @@
+"""Generate the golden fixtures in tests/golden/ by running the reference's own
+propagator (QPC-TDSE headers compiled by oracle/ref/Makefile into oracle/_ref/).
+
+Run on the development machine, where the reference checkout exists:
+    python tests/golden/make_golden.py [/path/to/reference/include]
+The fixtures are committed; the tests only read them.
+
+Cases (hydrogen unless stated; r in [0, rmax], uniform knots, m = 0):
+  small_setup.npz   N_r=64, p=6, n_l=6, rmax=30, dt=0.05: S, R, Rinv, D, H_l,
+                    CN bands upper/lower (lu_zsb), Y10 eigensystem, knots, ground state
+  small_yukawa.npz  same grid, V = -(1 + 17 e^{-2r})/r: H_l and ground state
+  small_prop.npz    seeded random initial state, 50 field steps f_i = 0.05 sin(0.1 i),
+                    then 5 field-free steps: final coefficients, S-norm, <z>
+  c0_field.npz      f(t_i) of the C0 pulse: 800 nm (w0 = 45.5633525/800),
+                    1e14 W/cm^2 (E0 = sqrt(1e14/3.50944758e16)), sin^2, 4 cycles, dt = 0.05
+  mid_pulse.npz     N_r=160, p=6, n_l=12, rmax=80: ground state through 1 cycle of
+                    800 nm at 2e14 W/cm^2, CEP 0.5 pi
+  c0_final.npz      the C0 workload: N_r=400, p=6, n_l=21, rmax=200, ground state,
+                    the full c0 pulse (8826 steps): final coefficients, norm, <z>,
+                    projections onto field-free states with E < 2
+"""
+import json
+import os
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+REF = os.path.join(ROOT, "oracle", "_ref")
+
+
+def build(ref_include):
+    subprocess.run(["make", "-C", os.path.join(ROOT, "oracle", "ref"), "-j4", "REF_INCLUDE=" + ref_include], check=True)
+
+
+def run(binary, *args):
+    env = dict(os.environ, OPENBLAS_NUM_THREADS="1", OMP_NUM_THREADS="1")
+    out = subprocess.run([os.path.join(REF, binary)] + [str(a) for a in args], check=True, env=env,
+                         stdout=subprocess.PIPE, text=True)
+    return out.stdout
+
+
+def load(d, name, shape=None, cplx=False):
+    a = np.fromfile(os.path.join(d, name + ".bin"))
+    if cplx:
+        a = a.view(np.complex128)
+    return a.reshape(shape) if shape is not None else a
+
+
+def c0_field():
+    e0 = float(np.sqrt(1e14 / 3.50944758e16))
+    w0 = 45.5633525 / 800.0
+    return e0, w0, 4.0, 0.0, 0.0, 0.05
+
+
+def main():
+    ref_include = sys.argv[1] if len(sys.argv) > 1 else "/root/reference/include"
+    build(ref_include)
+    meta = {}
+    with tempfile.TemporaryDirectory() as d:
+        # ---- small grid setup
+        NR, P, NL, RMAX, DT = 64, 6, 6, 30.0, 0.05
+        run("ref_small", "setup", d, RMAX, DT, 1, 0, 0)
+        np.savez(os.path.join(HERE, "small_setup.npz"),
+                 n_r=NR, p=P, n_l=NL, rmax=RMAX, dt=DT,
+                 S=load(d, "S", (NR, P + 1)), R=load(d, "R", (NR, P + 1)), RINV=load(d, "RINV", (NR, P + 1)),
+                 D=load(d, "D", (NR, P + 1)), H=load(d, "H", (NL, NR, P + 1)),
+                 upper=load(d, "upper", (NL, NR, P + 1), True), lower=load(d, "lower", (NL, NR, P + 1), True),
+                 yeig=load(d, "yeig"), yprj=load(d, "yprj", (NL, NL)), y10=load(d, "y10"),
+                 knots=load(d, "knots"), gs_energy=load(d, "gs_energy"), gs_coef=load(d, "gs_coef", (NL, NR), True))
+        run("ref_small", "setup", d, RMAX, DT, 1, 17, 2)
+        np.savez(os.path.join(HERE, "small_yukawa.npz"), zc=1.0, zs=17.0, sigma=2.0,
+                 H=load(d, "H", (NL, NR, P + 1)), gs_energy=load(d, "gs_energy"), gs_coef=load(d, "gs_coef", (NL, NR), True))
+        # ---- small propagation
+        rng = np.random.default_rng(1)
+        c0 = rng.standard_normal(NL * NR) + 1j * rng.standard_normal(NL * NR)
+        c0.tofile(os.path.join(d, "init.bin"))
+        nt, nfree = 50, 5
+        f = 0.05 * np.sin(0.1 * np.arange(nt + 1))
+        f.tofile(os.path.join(d, "field.bin"))
+        run("ref_small", "propagate", d, RMAX, DT, 1, 0, 0, os.path.join(d, "init.bin"), os.path.join(d, "field.bin"), nt, nfree, 1)
+        np.savez(os.path.join(HERE, "small_prop.npz"), init=c0.reshape(NL, NR), f=f, nt=nt, nfree=nfree,
+                 coef=load(d, "coef", (NL, NR), True), norm=load(d, "norm"), dipole=load(d, "dipole"))
+        # ---- C0 field
+        e0, w0, nc, n0, cep, dt = c0_field()
+        run("ref_small", "field", d, e0, w0, nc, n0, cep, dt)
+        np.savez(os.path.join(HERE, "c0_field.npz"), e0=e0, w0=w0, nc=nc, n0=n0, cep=cep, dt=dt,
+                 nt=int(load(d, "nt")[0]), f=load(d, "f"))
+        # ---- mid grid: one cycle of 800 nm at 2e14 W/cm^2, CEP 0.5 pi
+        e0m = float(np.sqrt(2e14 / 3.50944758e16))
+        run("ref_mid", "field", d, e0m, w0, 1.0, 0.0, 0.5, 0.05)
+        fm = load(d, "f")
+        ntm = int(load(d, "nt")[0])
+        fm.tofile(os.path.join(d, "fieldm.bin"))
+        out = run("ref_mid", "propagate", d, 80.0, 0.05, 1, 0, 0, "gs", os.path.join(d, "fieldm.bin"), ntm, 0, 1)
+        meta["mid_pulse"] = out.strip()
+        np.savez(os.path.join(HERE, "mid_pulse.npz"), n_r=160, p=6, n_l=12, rmax=80.0, dt=0.05,
+                 e0=e0m, w0=w0, nc=1.0, n0=0.0, cep=0.5, nt=ntm, f=fm,
+                 coef=load(d, "coef", (12, 160), True), norm=load(d, "norm"), dipole=load(d, "dipole"))
+        # ---- C0 full pulse
+        fc = np.load(os.path.join(HERE, "c0_field.npz"))["f"]
+        ntc = fc.size - 1
+        fc.tofile(os.path.join(d, "fieldc.bin"))
+        out = run("ref_c0", "propagate", d, 200.0, 0.05, 1, 0, 0, "gs", os.path.join(d, "fieldc.bin"), ntc, 0, 1)
+        meta["c0_final"] = out.strip()
+        coef = load(d, "coef", (21, 400), True)
+        norm, dip = load(d, "norm"), load(d, "dipole")
+        coef.tofile(os.path.join(d, "c0coef.bin"))
+        run("ref_c0", "proj", d, 200.0, 0.05, 1, 0, 0, os.path.join(d, "c0coef.bin"), 2.0)
+        np.savez(os.path.join(HERE, "c0_final.npz"), n_r=400, p=6, n_l=21, rmax=200.0, dt=0.05, nt=ntc,
+                 coef=coef, norm=norm, dipole=dip, proj=load(d, "proj", None, True),
+                 proj_nnz=load(d, "proj_nnz").astype(np.int64), proj_energy=load(d, "proj_energy"))
+    with open(os.path.join(HERE, "make_golden.log.json"), "w") as fh:
+        json.dump(meta, fh, indent=1)
+
+
+if __name__ == "__main__":
+    main()

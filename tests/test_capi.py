@@ -1,0 +1,62 @@
+"""The C ABI library: loads, exports what include/qpc_gb300.h declares, and
+rejects bad arguments with status codes (no GPU needed)."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+
+
+def _declared():
+    txt = open(os.path.join(ROOT, "include", "qpc_gb300.h")).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\b(qpc_[a-z0-9_]+)\s*\(", txt)))
+
+
+def test_exports_every_declared_symbol(q):
+    lib = q.load()
+    names = _declared()
+    assert len(names) >= 20
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+    assert set(names) == set(q.EXPORTS)
+
+
+def test_library_is_in_tree(q):
+    lib = q.load()
+    assert os.path.dirname(os.path.abspath(q.LIB_PATH)).startswith(ROOT)
+    assert b"sm_103a" in lib.qpc_version()
+
+
+def test_bad_arguments_return_codes(q):
+    lib = q.load()
+    assert lib.qpc_linear_knots(10, 6, 0.0, 1.0, None) == 1
+    assert lib.qpc_radial_setup(5, 6, 1, None, None, 1.0, None, None, None, None, None) == 1
+    assert lib.qpc_lgwz_create(None, 0.05, None, None, None, None) == 1
+    d = q.qpc_dims(10, 6, 4, 1, 0, 1)  # n_r < 2p+2
+    h = ctypes.c_void_p()
+    S = np.zeros((10, 7))
+    assert lib.qpc_lgwz_create(ctypes.byref(d), 0.05, S.ctypes.data, S.ctypes.data, S.ctypes.data, ctypes.byref(h)) == 1
+    assert b"bad dims" in lib.qpc_last_error()
+    assert lib.qpc_lgwz_destroy(None) == 0
+
+
+def test_no_device_is_an_error_not_a_fallback(q):
+    torch = pytest.importorskip("torch")
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    t = q.linear_knots(32, 6, 0.0, 20.0)
+    S, R, _, _, H = q.radial_setup(32, 6, 4, t)
+    with pytest.raises(q.QpcError) as e:
+        q.propagator_cn_hc_lgwz().initialize(32, 6, 4, S, R, H, 0.05)
+    assert e.value.code == 8  # QPC_ERR_NODEVICE
+
+
+def test_field_and_setup_errors(q):
+    with pytest.raises(q.QpcError):
+        q.field_sinen(0.05, -1.0, 4, 0, 0, 0.05)
+    with pytest.raises(q.QpcError):
+        q.radial_setup(8, 6, 1, np.zeros(17))

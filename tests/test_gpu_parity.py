@@ -1,0 +1,222 @@
+"""Parity of the GB300 engine (through the C ABI) against the CPU oracle and
+the reference's golden vectors.  Tolerance: relative L2 of the coefficients
+<= 1e-10 after full pulses (the bar the path is held to); single steps and
+short runs are held to 1e-12."""
+import numpy as np
+import pytest
+
+from conftest import engine, golden, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+TOL_FULL = 1e-10
+TOL_SHORT = 1e-12
+
+
+def grid(q, n_r, p, n_l, rmax, pot=None, n_lh=None):
+    t = q.linear_knots(n_r, p, 0.0, rmax)
+    args = (n_r, p, n_lh or n_l, t) + ((pot,) if pot else ())
+    S, R, Ri, D, H = q.radial_setup(*args)
+    return S, R, H
+
+
+def rand_state(rng, *shape):
+    return rng.standard_normal(shape) + 1j * rng.standard_normal(shape)
+
+
+@pytest.fixture(scope="module")
+def small(q):
+    g = golden("small_setup")
+    return g
+
+
+def test_single_step_matches_oracle(q, oracle, small):
+    g = small
+    n_r, p, n_l, dt = int(g["n_r"]), int(g["p"]), int(g["n_l"]), float(g["dt"])
+    S, R, H = grid(q, n_r, p, n_l, float(g["rmax"]))
+    prop = q.propagator_cn_hc_lgwz().initialize(n_r, p, n_l, S, R, H, dt)
+    c0 = rand_state(np.random.default_rng(3), 1, 1, n_l, n_r)
+    prop.put(c0)
+    prop.propagate(0.03, 0.045)
+    og = oracle.grid(S, R, H, dt, n_l)
+    ref = oracle.step(og, c0, 0.03, 0.045)
+    assert rel_l2(prop.get(), ref.reshape(1, 1, n_l, n_r)) < TOL_SHORT
+    prop.propagate()  # field-free overload
+    ref = oracle.step(og, ref)
+    assert rel_l2(prop.get(), ref.reshape(1, 1, n_l, n_r)) < TOL_SHORT
+
+
+def test_golden_small_propagation(q, small):
+    """Against the reference itself: 50 field steps + 5 field-free (tests/golden/small_prop)."""
+    g = small
+    pr = golden("small_prop")
+    n_r, p, n_l, dt = int(g["n_r"]), int(g["p"]), int(g["n_l"]), float(g["dt"])
+    prop = q.propagator_cn_hc_lgwz().initialize(n_r, p, n_l, g["S"], g["R"], g["H"], dt)
+    prop.put(pr["init"][None, None])
+    nt, nf = int(pr["nt"]), int(pr["nfree"])
+    prop.run(pr["f"][None, :], [nt], [nt + nf])
+    c = prop.get()[0, 0]
+    assert rel_l2(c, pr["coef"]) < TOL_SHORT
+    assert abs(prop.norm()[0] - pr["norm"][0]) < 1e-12 * pr["norm"][0]
+    z = prop.dipole(g["R"])[0]
+    assert abs(z.real - pr["dipole"][0]) < 1e-11 * abs(pr["dipole"][0])
+
+
+def test_stepwise_equals_run(q, small):
+    """propagate() called step by step and run() over the same table agree."""
+    g = small
+    pr = golden("small_prop")
+    n_r, p, n_l, dt = int(g["n_r"]), int(g["p"]), int(g["n_l"]), float(g["dt"])
+    a = q.propagator_cn_hc_lgwz().initialize(n_r, p, n_l, g["S"], g["R"], g["H"], dt)
+    b = q.propagator_cn_hc_lgwz().initialize(n_r, p, n_l, g["S"], g["R"], g["H"], dt)
+    a.put(pr["init"][None, None])
+    b.put(pr["init"][None, None])
+    f = pr["f"]
+    for i in range(20):
+        a.propagate(f[i], f[i + 1])
+    b.run(f[None, :21], [20])
+    assert rel_l2(a.get(), b.get()) < TOL_SHORT
+
+
+def test_uneven_batch_matches_oracle(q, oracle):
+    """A batch whose instances carry their own fields and step counts (with
+    field-free tails), against the oracle instance by instance."""
+    n_r, p, n_l, dt = 96, 6, 9, 0.05
+    S, R, H = grid(q, n_r, p, n_l, 48.0)
+    B = 7
+    rng = np.random.default_rng(11)
+    nt_field = np.array([0, 1, 2, 37, 60, 15, 60])
+    nt_total = nt_field + np.array([3, 0, 5, 1, 0, 20, 7])
+    ld = nt_field.max() + 1
+    ftab = np.zeros((B, ld))
+    for k in range(B):
+        ftab[k, :nt_field[k] + 1] = rng.uniform(0.02, 0.1) * np.sin(rng.uniform(0.05, 0.2) * np.arange(nt_field[k] + 1) + rng.uniform(0, 6))
+    c0 = rand_state(rng, B, 1, n_l, n_r)
+    prop = q.propagator_cn_hc_lgwz().initialize(n_r, p, n_l, S, R, H, dt, n_inst=B)
+    prop.put(c0)
+    prop.run(ftab, nt_field, nt_total)
+    got = prop.get()
+    og = oracle.grid(S, R, H, dt, n_l, n_inst=B)
+    ref = oracle.run(og, c0, ftab, nt_field, nt_total, threads=4)
+    for k in range(B):
+        assert rel_l2(got[k], ref[k]) < TOL_SHORT, k
+    on = oracle.norm(og, ref)
+    assert np.abs(prop.norm() - on).max() < 1e-12 * on.max()
+
+
+@pytest.mark.parametrize("n_l,p,n_m,m0", [(8, 6, 1, 0), (7, 7, 1, 0), (6, 5, 3, -1), (5, 4, 2, 1)])
+def test_other_grids_match_oracle(q, oracle, n_l, p, n_m, m0):
+    """Even n_l (no zero eigenvalue), other B-spline degrees, several m."""
+    n_r, dt = 72, 0.04
+    lmax = max(abs(m0), abs(m0 + n_m - 1)) + n_l - 1
+    S, R, H = grid(q, n_r, p, n_l, 40.0, n_lh=lmax + 1)
+    rng = np.random.default_rng(5 + n_l)
+    c0 = rand_state(rng, 2, n_m, n_l, n_r)
+    nt = 12
+    ftab = 0.06 * np.sin(0.3 * np.arange(nt + 1))[None, :].repeat(2, 0)
+    ftab[1] *= -0.7
+    prop = q.propagator_cn_hc_lgwz().initialize(n_r, p, n_l, S, R, H, dt, n_m=n_m, m0=m0, n_inst=2)
+    prop.put(c0)
+    prop.run(ftab, [nt, nt], [nt, nt + 2])
+    og = oracle.grid(S, R, H, dt, n_l, n_m=n_m, m0=m0, n_inst=2)
+    ref = oracle.run(og, c0, ftab, [nt, nt], [nt, nt + 2], threads=2)
+    assert rel_l2(prop.get(), ref) < TOL_SHORT
+
+
+def test_golden_mid_pulse(q):
+    """Reference output: ground state through one 800 nm cycle at 2e14 W/cm^2."""
+    m = golden("mid_pulse")
+    n_r, p, n_l, dt = int(m["n_r"]), int(m["p"]), int(m["n_l"]), float(m["dt"])
+    S, R, H = grid(q, n_r, p, n_l, float(m["rmax"]))
+    c0, _ = q.ground_state(S, H, n_l)
+    prop = q.propagator_cn_hc_lgwz().initialize(n_r, p, n_l, S, R, H, dt)
+    prop.put(c0[None])
+    nt = int(m["nt"])
+    prop.run(m["f"][None, :], [nt])
+    c = prop.get()[0, 0]
+    ref = m["coef"]
+    sgn = np.sign(np.vdot(ref.ravel(), c.ravel()).real)
+    assert rel_l2(sgn * c, ref) < TOL_FULL
+    assert abs(prop.norm()[0] - m["norm"][0]) < 1e-10
+
+
+def test_golden_c0_full_pulse(q):
+    """The C0 workload against the reference: 8826 steps, H atom, N_r=400, l_max=20."""
+    g = golden("c0_final")
+    fz = golden("c0_field")["f"]
+    n_r, p, n_l, dt = int(g["n_r"]), int(g["p"]), int(g["n_l"]), float(g["dt"])
+    S, R, H = grid(q, n_r, p, n_l, float(g["rmax"]))
+    c0, e = q.ground_state(S, H, n_l)
+    prop = q.propagator_cn_hc_lgwz().initialize(n_r, p, n_l, S, R, H, dt)
+    prop.put(c0[None])
+    nt = fz.size - 1
+    prop.run(fz[None, :], [nt])
+    c = prop.get()[0, 0]
+    ref = g["coef"]
+    sgn = np.sign(np.vdot(ref.ravel(), c.ravel()).real)
+    err = rel_l2(sgn * c, ref)
+    drift = abs(prop.norm()[0] - 1.0)
+    print("C0 rel L2 vs reference %.3e, |1-norm| %.3e (reference %.3e)" % (err, drift, abs(g["norm"][0] - 1)))
+    assert err < TOL_FULL
+    assert drift < 1e-10
+    # dipole and projections (PES) at the end of the pulse
+    z = prop.dipole(R)[0]
+    assert abs(z.real - g["dipole"][0]) < 1e-9 * max(1.0, abs(g["dipole"][0]))
+    nnz = g["proj_nnz"]
+    basis, off = [], 0
+    for l in range(n_l):
+        e_l, v_l = q.gen_eigen(S, H[l], int(nnz[l]))
+        # left vectors S v, as eigenstate_sph stores them
+        Sv = np.zeros_like(v_l)
+        for j in range(v_l.shape[0]):
+            x = v_l[j]
+            y = np.zeros(n_r)
+            for r in range(n_r):
+                for k in range(p + 1):
+                    if r + k < n_r:
+                        y[r] += S[r, k] * x[r + k]
+                        if k:
+                            y[r + k] += S[r, k] * x[r]
+            Sv[j] = y
+        basis.append(Sv)
+    proj = prop.projection(nnz.astype(np.int32), basis)
+    # eigenvector signs are arbitrary: compare |<v|c>|^2 (what the spectrum uses)
+    assert np.abs(np.abs(proj) ** 2 - np.abs(g["proj"]) ** 2).max() < 1e-10
+
+
+def test_deterministic(q, small):
+    g = small
+    pr = golden("small_prop")
+    n_r, p, n_l, dt = int(g["n_r"]), int(g["p"]), int(g["n_l"]), float(g["dt"])
+    outs = []
+    for _ in range(2):
+        prop = q.propagator_cn_hc_lgwz().initialize(n_r, p, n_l, g["S"], g["R"], g["H"], dt, n_inst=3)
+        prop.put(np.repeat(pr["init"][None, None], 3, 0))
+        prop.run(np.repeat(pr["f"][None, :], 3, 0), [50, 20, 35])
+        outs.append((prop.get(), prop.norm()))
+    assert np.array_equal(outs[0][0], outs[1][0])
+    assert np.array_equal(outs[0][1], outs[1][1])
+
+
+def test_field_free_stationary_phase(q):
+    """A field-free eigenstate only picks up the CN phase exactly:
+    c(n dt) = ((1 - i E dt/2)/(1 + i E dt/2))^n c(0)."""
+    n_r, p, n_l, dt = 80, 6, 4, 0.05
+    S, R, H = grid(q, n_r, p, n_l, 40.0)
+    c0, e = q.ground_state(S, H, n_l)
+    prop = q.propagator_cn_hc_lgwz().initialize(n_r, p, n_l, S, R, H, dt)
+    prop.put(c0[None])
+    n = 500
+    prop.run(None, [0], [n])
+    ph = ((1 - 0.5j * e * dt) / (1 + 0.5j * e * dt)) ** n
+    assert rel_l2(prop.get()[0, 0], ph * c0) < 1e-11
+
+
+def test_zero_pivot_is_reported_not_trapped(q):
+    """A singular band (S = 0) is an error code from create, no device fault."""
+    n_r, p, n_l = 32, 6, 3
+    S = np.zeros((n_r, p + 1))
+    H = np.zeros((n_l, n_r, p + 1))
+    with pytest.raises(q.QpcError) as e:
+        q.propagator_cn_hc_lgwz().initialize(n_r, p, n_l, S, S, H, 0.05)
+    assert e.value.code == 4

@@ -1,0 +1,73 @@
+"""Pins the CPU oracle (oracle/oracle_cn.cpp) to the reference's own outputs
+(tests/golden/*, produced by running the reference headers compiled by
+oracle/ref/Makefile)."""
+import numpy as np
+
+from conftest import band_mask, golden, rel_l2
+
+
+def test_cn_bands_match_lu_zsb(oracle):
+    g = golden("small_setup")
+    n_r, p, n_l = int(g["n_r"]), int(g["p"]), int(g["n_l"])
+    grid = oracle.grid(g["S"], g["R"], g["H"], float(g["dt"]), n_l)
+    up, lo = grid._keep[4], grid._keep[5]
+    m = band_mask(n_r, p)
+    # the restatement of cn_component_hc::initialize + lu_zsb is bit-exact
+    assert np.array_equal(up[:, m], g["upper"][:, m])
+    assert np.array_equal(lo[:, m], g["lower"][:, m])
+
+
+def _reference_grid(oracle, g):
+    """Oracle grid fed with the reference's own Y10 eigensystem."""
+    grid = oracle.grid(g["S"], g["R"], g["H"], float(g["dt"]), int(g["n_l"]))
+    lam, P = grid._keep[2], grid._keep[3]
+    lam[0] = g["yeig"]
+    P[0] = g["yprj"]
+    return grid
+
+
+def test_small_propagation(oracle):
+    g = golden("small_setup")
+    pr = golden("small_prop")
+    grid = _reference_grid(oracle, g)
+    c = pr["init"].copy()
+    f = pr["f"]
+    for i in range(int(pr["nt"])):
+        c = oracle.step(grid, c, f[i], f[i + 1])
+    for _ in range(int(pr["nfree"])):
+        c = oracle.step(grid, c)
+    assert rel_l2(c, pr["coef"]) < 1e-12
+    assert abs(oracle.norm(grid, c)[0] - pr["norm"][0]) < 1e-12 * pr["norm"][0]
+    z = oracle.dipole(grid, g["R"], g["y10"], c)[0]
+    assert abs(z.real - pr["dipole"][0]) < 1e-11 * abs(pr["dipole"][0])
+
+
+def test_oracle_run_equals_steps(oracle):
+    """oracle_lgwz_run (the driver loop) equals stepping one call at a time."""
+    g = golden("small_setup")
+    pr = golden("small_prop")
+    grid = _reference_grid(oracle, g)
+    nt, nf = int(pr["nt"]), int(pr["nfree"])
+    c = oracle.run(grid, pr["init"], pr["f"][None, :], [nt], [nt + nf])
+    assert rel_l2(c, pr["coef"]) < 1e-12
+
+
+def test_c0_full_pulse(oracle):
+    """The C0 workload end to end: 8826 steps from the ground state."""
+    g = golden("c0_final")
+    fz = golden("c0_field")["f"]
+    from conftest import engine
+    q = engine()
+    n_r, p, n_l = int(g["n_r"]), int(g["p"]), int(g["n_l"])
+    t = q.linear_knots(n_r, p, 0.0, float(g["rmax"]))
+    S, R, _, _, H = q.radial_setup(n_r, p, n_l, t)
+    grid = oracle.grid(S, R, H, float(g["dt"]), n_l)
+    c0, e = q.ground_state(S, H, n_l)
+    nt = fz.size - 1
+    c = oracle.run(grid, c0, fz[None, :], [nt], [nt])
+    # the ground state's sign is arbitrary (LAPACK dsbgv vs ours): align it
+    ref = g["coef"][None]
+    sgn = np.sign(np.vdot(ref.ravel(), c.ravel()).real)
+    assert rel_l2(sgn * c, ref) < 1e-10
+    # S-norm drift over 8826 steps is rounding only (Crank-Nicolson is S-unitary)
+    assert abs(oracle.norm(grid, c)[0] - g["norm"][0]) < 1e-10
