@@ -116,12 +116,12 @@ def setup_grid(q, n_r=800, p=6, n_l=41, rmax=400.0):
     return S, R, H, c0
 
 
-def sweep_flops(n_r, p, live_pairs, power):
-    """FP64 flops of one coupling-sweep launch as implemented: per pair, row and
-    application, four lanes each do (2p+1) + 2p FMAs forward and 2p + 2 FMAs + 1 MUL
-    backward (FMA = 2 flops)."""
-    fma = (2 * p + 1) + 2 * p + (2 * p + 2)
-    return live_pairs * n_r * power * 4 * (2 * fma + 1)
+def chain_flops(n_r, p, chains, power):
+    """FP64 flops of one chain-kernel launch as implemented (FMA = 2 flops): per
+    chain, row and application, both parts do S z ((2p+1) FMA), the forward and
+    backward recurrences (2p FMA each), D^-1 y (1 MUL + 1 FMA) and 2x - z (1 FMA)."""
+    per_part = 2 * (2 * p + 1) + 2 * (2 * p) + 2 * (2 * p) + 3 + 2
+    return chains * n_r * power * 2 * per_part
 
 
 def run_engine(args):
@@ -167,13 +167,14 @@ def run_engine(args):
     # dominant kernel: coupling sweeps
     sw_ms, sw_n = ktimes.get("sweep", (0.0, 0))
     live_pairs = B * (n_l // 2)
-    fl = sweep_flops(n_r, p, live_pairs, 2)
+    fl = chain_flops(n_r, p, 2 * live_pairs, 2)
     achieved = fl / (sw_ms / max(sw_n, 1) * 1e-3) / 1e12 if sw_n else None
     peaks = load_peaks()
-    # algorithmic bytes of one sweep launch: factors read 4x (p+1 complex per row and pair),
-    # eigenbasis state in and out, two scratch vectors written and read twice
-    sweep_bytes = live_pairs * n_r * ((p + 1) * 16 * 4 + 2 * 16 * 2 + 2 * 16 * 2 * 2)
-    roof = {"bound": "fp64", "kernel": "k_sweep", "achieved": achieved, "peak": FP64_PEAK_TFLOPS,
+    # algorithmic bytes of one coupling-chain launch: the pair's factors (p+1 complex per row)
+    # read twice per application, each chain's eigen-basis vector read and written once per
+    # application and its work vector written/read by the five passes
+    sweep_bytes = live_pairs * n_r * 2 * ((p + 1) * 16 * 2 + 2 * 16 * 2 + 2 * 16 * 5)
+    roof = {"bound": "fp64", "kernel": "k_chain (coupling)", "achieved": achieved, "peak": FP64_PEAK_TFLOPS,
             "unit": "TFLOP/s", "frac": (achieved / FP64_PEAK_TFLOPS) if achieved else None,
             "peak_source": "measured DFMA peak, profiles/fp64_peak_gb300.md",
             "flops_per_launch": fl, "launch_ms": sw_ms / max(sw_n, 1) if sw_n else None,

@@ -1,0 +1,286 @@
+// Banded Crank-Nicolson chain solver for GB300.
+//
+// Every channel ("chain") of the propagation applies, a = 1 or 2 times,
+//     z <- (S + i a B)^-1 (S - i a B) z = 2 (S + i a B)^-1 (S z) - z
+// with the complex-symmetric band factorised as L D L^T (unit lower L with p
+// sub-diagonals, stored row-wise: Lrow[r][k-1] = L(r, r-k), and 1/D(r)).
+// This is the solve of cn_propagate_kernel_avx1 (coupling, propagate.hpp:3-98)
+// and of cn_hc_propagate0 (field-free, propagate.hpp:311-331) rewritten as
+//     P1  w = S z                       (rows independent)
+//     P2  y = L^-1 w                    (recurrence over r, ascending)
+//     P3  y <- D^-1 y                   (rows independent)
+//     P4  x = L^-T y                    (recurrence over r, descending)
+//     P5  z <- 2 x - z                  (rows independent)
+// GB300 issues one FP64 warp instruction per ~64 cycles per SM sub-partition,
+// whether the instruction depends on the previous one or not, so a recurrence
+// advances one row per (FP64 instructions per lane per row) x 64 cycles.  The
+// recurrences P2/P4 are therefore run column-oriented on a systolic window:
+// G lanes per real/imaginary part each keep P/G of the P pending partial sums;
+// when row c completes, its value is broadcast and every lane subtracts its
+// L(c+j, c) * y_c in 2 P/G FMAs, then the window slides by one row
+// (shuffles, no FP64).  The row-parallel passes P1/P3/P5 use all 32 lanes.
+// One warp owns CPW chains and runs all passes itself (__syncwarp between),
+// so no block-level synchronisation is needed.  G is chosen per batch size
+// by the engine's autotuner: G = P gives the shortest rows (few chains,
+// latency-bound), G = 1 the fewest idle lanes (many chains).
+#pragma once
+
+namespace qpc {
+
+// Coupling chains come in pairs (+s, -s) that share one factorisation; the
+// -s chain holds conj(z) and is solved with the +s factors.
+template <int P, int G, bool CPL>
+struct chain_cfg {
+	static constexpr int NE = P + 1;
+	static constexpr int LPC = 2 * G;	// lanes per chain: G real-part lanes, G imaginary-part lanes
+	static constexpr int CPW = CPL ? ((32 / LPC) & ~1) : (32 / LPC);
+	static constexpr int TPL = P / G;	// partial sums per lane
+	static_assert(P % G == 0, "G must divide P");
+	static_assert(CPW >= 1, "too many lanes per chain");
+};
+
+__device__ __forceinline__ int coupling_power(long s, long nt)
+{
+	if (nt <= 0 || s > nt) return 0;
+	return (s == 0 || s == nt) ? 1 : 2;
+}
+
+struct chain_desc {
+	long xoff;	// offset of the chain's element at row 0 (double2 units); row stride = L
+	long foff;	// offset of the chain's factor block (double2 units); [N][P+1]
+	int a;		// applications this step (0 = inactive)
+};
+
+template <bool CPL>
+__device__ __forceinline__ chain_desc describe(long ch, long nchains, const int64_t* __restrict__ nta, long step, int jslot,
+	int B, int M, int m0, int N, int L, int np, int NE)
+{
+	chain_desc d{0, 0, 0};
+	if (ch >= nchains) return d;
+	if (CPL) {
+		long pr = ch >> 1;
+		int sign = (int)(ch & 1);
+		int k = (int)(pr % np);
+		long im_inst = pr / np;
+		long inst = im_inst / M;
+		d.xoff = im_inst * (long)N * L + 2 * k + sign;
+		d.foff = (((long)jslot * B * M + im_inst) * np + k) * (long)N * NE;
+		d.a = coupling_power(step, nta[inst]);
+	} else {
+		int il = (int)(ch % L);
+		long im_inst = ch / L;
+		int m = (int)(im_inst % M) + m0;
+		long inst = im_inst / M;
+		int l = il + (m < 0 ? -m : m);
+		d.xoff = im_inst * (long)N * L + il;
+		d.foff = (long)l * N * NE;
+		d.a = step < nta[inst] ? 1 : 0;
+	}
+	return d;
+}
+
+__device__ __forceinline__ double part_of(double2 v, int part) { return part ? v.y : v.x; }
+
+// own part of (l * v), complex l and v
+__device__ __forceinline__ double cmul_part(double2 l, double vr, double vi, int part)
+{
+	return part ? fma(l.x, vi, l.y * vr) : fma(l.x, vr, -l.y * vi);
+}
+
+// operands for acc -= part(l * v) as two FMAs, acc = fma(-l.x, u, fma(l.y, w, acc)):
+// real part u = vr, w = vi; imaginary part u = vi, w = -vr (sign flip as an integer op)
+__device__ __forceinline__ void msub_operands(double vr, double vi, int part, double& u, double& w)
+{
+	u = part ? vi : vr;
+	w = part ? __longlong_as_double(__double_as_longlong(vr) ^ (long long)0x8000000000000000ull) : vi;
+}
+
+template <int P, int G, bool CPL>
+__global__ void __launch_bounds__(128) k_chain(double2* __restrict__ X, double2* __restrict__ Wk,
+	const double2* __restrict__ fac, const double* __restrict__ S, const int64_t* __restrict__ nta,
+	long step, int jslot, int B, int M, int m0, int N, int L, int np, long nchains)
+{
+	using C = chain_cfg<P, G, CPL>;
+	constexpr int NE = C::NE, LPC = C::LPC, CPW = C::CPW, TPL = C::TPL;
+	extern __shared__ double sS[];	// S band [N][P+1]
+	for (int t = threadIdx.x; t < N * NE; t += blockDim.x) sS[t] = S[t];
+	__syncthreads();
+	const unsigned FULL = 0xffffffffu;
+	const int lane = threadIdx.x & 31;
+	const long warp = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+	const long ch0 = warp * CPW;
+	if (ch0 >= nchains) return;
+	// chain descriptors of this warp, once, in shared memory
+	__shared__ long s_x[4][32], s_f[4][32];
+	__shared__ int s_a[4][32];
+	const int wib = threadIdx.x >> 5;
+	if (lane < CPW) {
+		chain_desc d = describe<CPL>(ch0 + lane, nchains, nta, step, jslot, B, M, m0, N, L, np, NE);
+		s_x[wib][lane] = d.xoff; s_f[wib][lane] = d.foff; s_a[wib][lane] = d.a;
+	}
+	__syncwarp();
+	auto desc = [&](int cl) { chain_desc d; d.xoff = s_x[wib][cl]; d.foff = s_f[wib][cl]; d.a = s_a[wib][cl]; return d; };
+	int amax = 0;
+#pragma unroll
+	for (int cl = 0; cl < CPW; ++cl) amax = max(amax, s_a[wib][cl]);
+	if (amax == 0) return;
+	double* Xd = reinterpret_cast<double*>(X);
+	double* Wd = reinterpret_cast<double*>(Wk);
+	const long rs = 2L * L;	// row stride in doubles
+
+	// systolic role of this lane
+	const int cls = lane / LPC;
+	const int ps = (lane % LPC) / G;
+	const int g = lane % G;
+	const int cbase = cls * LPC;
+	const bool srole = cls < CPW;
+	const chain_desc ds = srole ? desc(cls) : chain_desc{0, 0, 0};
+	const double2* fs = fac + ds.foff;
+	double* ws = Wd + 2 * ds.xoff + ps;
+
+	for (int app = 0; app < amax; ++app) {
+		// ---- P1: w = S z  (items: row r, chain cl, part)
+		for (int base = 0; base < N * CPW * 2; base += 32) {
+			int it = base + lane;
+			int part = it & 1, cl = (it >> 1) % CPW, r = (it >> 1) / CPW;
+			if (it < N * CPW * 2) {
+				chain_desc d = desc(cl);
+				if (app < d.a) {
+					const double* z = Xd + 2 * d.xoff + part;
+					double w = 0.0;
+#pragma unroll
+					for (int k = P; k >= 1; --k)
+						if (r - k >= 0) w = fma(sS[(r - k) * NE + k], z[(long)(r - k) * rs], w);
+#pragma unroll
+					for (int k = 0; k <= P; ++k)
+						if (r + k < N) w = fma(sS[r * NE + k], z[(long)(r + k) * rs], w);
+					Wd[2 * d.xoff + part + (long)r * rs] = w;
+				}
+			}
+		}
+		__syncwarp();
+		const bool act = srole && app < ds.a;
+		// ---- P2: y = L^-1 w, column-oriented systolic window (rows c+1+g*TPL+t)
+		{
+			double acc[TPL];
+#pragma unroll
+			for (int t = 0; t < TPL; ++t) {
+				int row = g * TPL + t;
+				acc[t] = (act && row < N) ? ws[(long)row * rs] : 0.0;
+			}
+			for (int c = 0; c < N; ++c) {
+				double yr = __shfl_sync(FULL, acc[0], cbase);
+				double yi = __shfl_sync(FULL, acc[0], cbase + G);
+				double u, w;
+				msub_operands(yr, yi, ps, u, w);
+				if (act && g == 0) ws[(long)c * rs] = acc[0];
+				double nxt = __shfl_sync(FULL, acc[0], (lane + 1) & 31);
+#pragma unroll
+				for (int t = 0; t < TPL - 1; ++t) acc[t] = acc[t + 1];
+				if (g == G - 1) acc[TPL - 1] = (act && c + P < N) ? ws[(long)(c + P) * rs] : 0.0;
+				else acc[TPL - 1] = nxt;
+#pragma unroll
+				for (int t = 0; t < TPL; ++t) {
+					int j = 1 + g * TPL + t;
+					int row = c + j;
+					if (act && row < N) {
+						double2 lv = fs[(long)row * NE + (j - 1)];
+						acc[t] = fma(-lv.x, u, fma(lv.y, w, acc[t]));
+					}
+				}
+			}
+		}
+		__syncwarp();
+		// ---- P3: y <- D^-1 y
+		for (int base = 0; base < N * CPW * 2; base += 32) {
+			int it = base + lane;
+			int part = it & 1, cl = (it >> 1) % CPW, r = (it >> 1) / CPW;
+			bool v = false;
+			double res = 0.0;
+			long o = 0;
+			if (it < N * CPW * 2) {
+				chain_desc d = desc(cl);
+				if (app < d.a) {
+					o = 2 * d.xoff + (long)r * rs;
+					double2 y = make_double2(Wd[o], Wd[o + 1]);
+					double2 dv = fac[d.foff + (long)r * NE + P];
+					res = cmul_part(dv, y.x, y.y, part);
+					v = true;
+				}
+			}
+			__syncwarp();
+			if (v) Wd[o + part] = res;
+		}
+		__syncwarp();
+		// ---- P4: x = L^-T y, descending (rows c-1-g*TPL-t)
+		{
+			double acc[TPL];
+#pragma unroll
+			for (int t = 0; t < TPL; ++t) {
+				int row = N - 1 - g * TPL - t;
+				acc[t] = (act && row >= 0) ? ws[(long)row * rs] : 0.0;
+			}
+			for (int c = N - 1; c >= 0; --c) {
+				double xr = __shfl_sync(FULL, acc[0], cbase);
+				double xi = __shfl_sync(FULL, acc[0], cbase + G);
+				double u, w;
+				msub_operands(xr, xi, ps, u, w);
+				if (act && g == 0) ws[(long)c * rs] = acc[0];
+				double nxt = __shfl_sync(FULL, acc[0], (lane + 1) & 31);
+#pragma unroll
+				for (int t = 0; t < TPL - 1; ++t) acc[t] = acc[t + 1];
+				if (g == G - 1) acc[TPL - 1] = (act && c - P >= 0) ? ws[(long)(c - P) * rs] : 0.0;
+				else acc[TPL - 1] = nxt;
+#pragma unroll
+				for (int t = 0; t < TPL; ++t) {
+					int j = 1 + g * TPL + t;
+					int row = c - j;
+					if (act && row >= 0) {
+						double2 lv = fs[(long)c * NE + (j - 1)];	// L(c, c-j)
+						acc[t] = fma(-lv.x, u, fma(lv.y, w, acc[t]));
+					}
+				}
+			}
+		}
+		__syncwarp();
+		// ---- P5: z <- 2x - z; after the last application of a coupling pair, emit
+		//      s = z+ + conj(z-bar), d = z+ - conj(z-bar) for the backward transform
+		if (CPL) {
+			constexpr int PPW = CPW / 2;
+			for (int base = 0; base < N * PPW * 2; base += 32) {
+				int it = base + lane;
+				int part = it & 1, pl = (it >> 1) % PPW, r = (it >> 1) / PPW;
+				if (it < N * PPW * 2) {
+					chain_desc dp = desc(2 * pl);
+					chain_desc dm = desc(2 * pl + 1);
+					if (app < dp.a) {
+						long op = 2 * dp.xoff + (long)r * rs + part, om = 2 * dm.xoff + (long)r * rs + part;
+						double zp = fma(2.0, Wd[op], -Xd[op]);
+						double zm = fma(2.0, Wd[om], -Xd[om]);
+						if (app + 1 < dp.a) { Xd[op] = zp; Xd[om] = zm; }
+						else {
+							double zc = part ? -zm : zm;	// conj(z-bar), own part
+							Xd[op] = zp + zc;
+							Xd[om] = zp - zc;
+						}
+					}
+				}
+			}
+		} else {
+			for (int base = 0; base < N * CPW * 2; base += 32) {
+				int it = base + lane;
+				int part = it & 1, cl = (it >> 1) % CPW, r = (it >> 1) / CPW;
+				if (it < N * CPW * 2) {
+					chain_desc d = desc(cl);
+					if (app < d.a) {
+						long o = 2 * d.xoff + (long)r * rs + part;
+						Xd[o] = fma(2.0, Wd[o], -Xd[o]);
+					}
+				}
+			}
+		}
+		__syncwarp();
+	}
+}
+
+} // namespace qpc

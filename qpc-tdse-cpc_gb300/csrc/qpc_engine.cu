@@ -37,6 +37,7 @@
 #include <numeric>
 #include <string>
 #include <time.h>
+#include "qpc_chain.cuh"
 
 namespace qpc {
 
@@ -79,23 +80,14 @@ __global__ void k_to_lmajor(const double2* __restrict__ src, double2* __restrict
 	dst[t] = src[b * (long)N * L + (long)r * L + l];
 }
 
-// ---------------------------------------------------------------- per-instance schedule
-// Instance k: B_0 F B_1 F ... B_{nt-1} F B_nt [F ...] (nt = nt_field[k]); at loop
-// index s the coupling block is applied a_s times: 1 at s = 0 and s = nt, 2 in
-// between, 0 after nt (and always 0 when nt = 0).  F runs while s < nt_total.
-__device__ __forceinline__ int coupling_power(long s, long nt)
-{
-	if (nt <= 0 || s > nt) return 0;
-	return (s == 0 || s == nt) ? 1 : 2;
-}
-
 // ---------------------------------------------------------------- transform P (even/odd halves)
 // Vh[m][kk][il]: row kk < npair = eigenvector of +s_kk, row npair = zero-eigenvalue vector.
-// eo slots per (inst,m,r): 2k = E_k, 2k+1 = O_k, 2*npair = Z (odd L).
-// Forward: E_k = sum_{il even} v_k[il] c[il], O_k = sum_{il odd} v_k[il] c[il], Z = sum_{il even} v_0[il] c[il].
-// Backward (eo holds s_k = x_k+ + x_k-, d_k = x_k+ - x_k-, Z):
+// Eigen-basis slots per (inst,m,r) after the forward transform:
+//   2k = z+_k = E_k + O_k,  2k+1 = conj(z-_k) = conj(E_k - O_k),  2*npair = Z (odd n_l)
+// with E_k = sum_{il even} v_k[il] c[il], O_k = sum_{il odd} v_k[il] c[il], Z = sum_{il even} v_0[il] c[il].
+// Backward (slots hold s_k = z+ + z-, d_k = z+ - z-, Z):
 //   c[il even] = sum_k v_k[il] s_k + v_0[il] Z,  c[il odd] = sum_k v_k[il] d_k.
-// One CTA = (inst, m, tile of TR rows).  Lane = row, warp = output slot; the
+// One CTA = (inst, m, tile of TR rows); lane = row, warp = output unit; the
 // row tile is staged in shared memory with an odd row stride (conflict-free
 // 16-byte accesses).
 constexpr int TR = 32;
@@ -129,20 +121,34 @@ __global__ void __launch_bounds__(256) k_transform(const double2* __restrict__ s
 	int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
 	if (lane < nr) {
 		const double2* row = tin + lane * ldt;
-		for (int slot = warp; slot < L; slot += nw) {
-			double ar = 0.0, ai = 0.0;
-			if (forward) {
-				int kk = slot >> 1, par = slot & 1;
-				if (slot == 2 * npair) { kk = npair; par = 0; }
-				const double* v = V + (long)kk * L;
-				for (int il = par; il < L; il += 2) {
+		if (forward) {
+			const int nunit = npair + (L & 1);
+			for (int u = warp; u < nunit; u += nw) {
+				const double* v = V + (long)u * L;
+				double er = 0.0, ei = 0.0, orr = 0.0, oi = 0.0;
+				for (int il = 0; il < L; il += 2) {
 					double w = v[il];
 					double2 c = row[il];
-					ar = fma(w, c.x, ar);
-					ai = fma(w, c.y, ai);
+					er = fma(w, c.x, er);
+					ei = fma(w, c.y, ei);
 				}
-			} else {
-				int il = slot, par = il & 1;
+				if (u < npair) {
+					for (int il = 1; il < L; il += 2) {
+						double w = v[il];
+						double2 c = row[il];
+						orr = fma(w, c.x, orr);
+						oi = fma(w, c.y, oi);
+					}
+					tout[lane * ldt + 2 * u] = make_double2(er + orr, ei + oi);
+					tout[lane * ldt + 2 * u + 1] = make_double2(er - orr, oi - ei);
+				} else {
+					tout[lane * ldt + 2 * npair] = make_double2(er, ei);
+				}
+			}
+		} else {
+			for (int il = warp; il < L; il += nw) {
+				int par = il & 1;
+				double ar = 0.0, ai = 0.0;
 				for (int k = 0; k < npair; ++k) {
 					double w = V[(long)k * L + il];
 					double2 c = row[2 * k + par];
@@ -155,8 +161,8 @@ __global__ void __launch_bounds__(256) k_transform(const double2* __restrict__ s
 					ar = fma(w, c.x, ar);
 					ai = fma(w, c.y, ai);
 				}
+				tout[lane * ldt + il] = make_double2(ar, ai);
 			}
-			tout[lane * ldt + slot] = make_double2(ar, ai);
 		}
 	}
 	__syncthreads();
@@ -170,35 +176,35 @@ __global__ void __launch_bounds__(256) k_transform(const double2* __restrict__ s
 // LDL^T (no pivoting) of the complex-symmetric band S + i b R, b = lambda_k f(t_s) dt/4,
 // for every (look-ahead step j, inst, m, pair k): one lane per system, the
 // trailing (p+1)x(p+1) window of the right-looking elimination in registers.
-// Output fac[j][inst][m][r][c][k]: c < P: L(r+1+c, r); c = P: 1/D(r).
+// Output, row form per system: fac[sys][r][c], c < P: L(r, r-1-c); c = P: 1/D(r),
+// sys = ((j*B + inst)*M + m)*npair + k.
 template <int P>
 __global__ void __launch_bounds__(64) k_factor(double2* __restrict__ fac, const double* __restrict__ S, const double* __restrict__ R,
 	const double* __restrict__ lamp, const double* __restrict__ ftab, long ld, const int64_t* __restrict__ ntf,
-	long step0, int K, int B, int M, int N, int npair, double dt, int* __restrict__ status)
+	long step0, int K, int B, int Blive, int M, int N, int npair, double dt, int* __restrict__ status)
 {
 	constexpr int NE = P + 1;
 	long g = (long)blockIdx.x * blockDim.x + threadIdx.x;
-	long nsys = (long)K * B * M * npair;
+	long nsys = (long)K * Blive * M * npair;
 	if (g >= nsys) return;
 	int k = (int)(g % npair);
 	long t = g / npair;
 	int m = (int)(t % M); t /= M;
-	long inst = t % B;
-	int j = (int)(t / B);
+	long inst = t % Blive;
+	int j = (int)(t / Blive);
 	long s = step0 + j;
 	if (coupling_power(s, ntf[inst]) == 0) return;
 	double f = ftab[inst * ld + s];
 	double beta = lamp[m * npair + k] * ((f * (dt * 0.5)) * 0.5);
-	double2* out = fac + ((((long)j * B + inst) * M + m) * (long)N) * NE * npair + k;
+	double2* out = fac + ((((long)j * B + inst) * M + m) * npair + k) * (long)N * NE;
 	double wr[NE][NE], wi[NE][NE];
 #pragma unroll
 	for (int a = 0; a < NE; ++a)
 #pragma unroll
 		for (int b = 0; b <= a; ++b) {
 			// entry (a, b), b <= a: stored at S[b][a-b]
-			bool in = a < N;
-			wr[a][b] = in ? __ldg(S + b * NE + (a - b)) : 0.0;
-			wi[a][b] = in ? beta * __ldg(R + b * NE + (a - b)) : 0.0;
+			wr[a][b] = __ldg(S + b * NE + (a - b));
+			wi[a][b] = beta * __ldg(R + b * NE + (a - b));
 		}
 	int bad = 0;
 	for (int i = 0; i < N; ++i) {
@@ -208,14 +214,13 @@ __global__ void __launch_bounds__(64) k_factor(double2* __restrict__ fac, const 
 		double inv = 1.0 / den;
 		double rr = dr * inv, ri = -di * inv;
 		double lr[NE], li[NE];
-		double2* o = out + (long)i * NE * npair;
+		out[(long)i * NE + P] = make_double2(rr, ri);
 #pragma unroll
 		for (int a = 1; a < NE; ++a) {
 			lr[a] = fma(wr[a][0], rr, -wi[a][0] * ri);
 			li[a] = fma(wr[a][0], ri, wi[a][0] * rr);
-			o[(long)(a - 1) * npair] = make_double2(lr[a], li[a]);
+			if (i + a < N) out[(long)(i + a) * NE + (a - 1)] = make_double2(lr[a], li[a]);
 		}
-		o[(long)P * npair] = make_double2(rr, ri);
 		double cr[NE], ci[NE];	// column 0 before the update overwrites it
 #pragma unroll
 		for (int b = 1; b < NE; ++b) { cr[b] = wr[b][0]; ci[b] = wi[b][0]; }
@@ -224,9 +229,8 @@ __global__ void __launch_bounds__(64) k_factor(double2* __restrict__ fac, const 
 #pragma unroll
 			for (int b = 1; b <= a; ++b) {
 				// W[a-1][b-1] = W[a][b] - l_a * W[b][0]
-				double xr = cr[b], xi = ci[b];
-				wr[a - 1][b - 1] = fma(-lr[a], xr, fma(li[a], xi, wr[a][b]));
-				wi[a - 1][b - 1] = fma(-lr[a], xi, fma(-li[a], xr, wi[a][b]));
+				wr[a - 1][b - 1] = fma(-lr[a], cr[b], fma(li[a], ci[b], wr[a][b]));
+				wi[a - 1][b - 1] = fma(-lr[a], ci[b], fma(-li[a], cr[b], wi[a][b]));
 			}
 		int rn = i + NE;
 #pragma unroll
@@ -238,244 +242,6 @@ __global__ void __launch_bounds__(64) k_factor(double2* __restrict__ fac, const 
 		}
 	}
 	if (bad) atomicOr(status, ST_PIVOT);
-}
-
-// ---------------------------------------------------------------- coupling sweeps
-// For every (inst, m, pair k): the two channels +s_k and -s_k, each split into
-// real-part and imaginary-part lanes (4 lanes per pair).  The -s_k channel is
-// solved as the conjugate problem with the +s_k factors.  With the pair's
-// factors (k_factor) the block M(f)^a (a = 1 or 2) is applied as
-//   forward:  y_r = (S z)_r - sum_k L(r, r-k) y_{r-k}
-//   backward: x_r = y_r / D_r - sum_k L(r+k, r) x_{r+k};  z_r <- 2 x_r - z_r
-// Input eo slots (E_k, O_k) give z+ = E + O, z- = E - O; output slots hold
-// s_k = z+ + z-, d_k = z+ - z- for the backward transform.
-template <int P>
-__device__ __forceinline__ double shfl(double v, int lanemask, unsigned gmask)
-{
-	return __shfl_xor_sync(gmask, v, lanemask);
-}
-
-template <int P>
-__device__ __forceinline__ void cn_forward(const double* __restrict__ S, const double2* __restrict__ fac, long fstride,
-	const double2* __restrict__ eo, long eostride, int slotE, bool fromEO, double sgnO, double conjsgn, int part,
-	const double* __restrict__ zsrc, long zstride, double* __restrict__ ydst, long ystride, int N, unsigned gmask)
-{
-	constexpr int NE = P + 1;
-	double zw[2 * P + 1];	// own part of z at rows r-P .. r+P
-	double yre[P], yim[P];	// y_{r-1} .. y_{r-P}
-#pragma unroll
-	for (int q = 0; q < 2 * P + 1; ++q) zw[q] = 0.0;
-#pragma unroll
-	for (int q = 0; q < P; ++q) { yre[q] = 0.0; yim[q] = 0.0; }
-	auto loadz = [&](int r) -> double {
-		if (r >= N) return 0.0;
-		if (fromEO) {
-			double2 e = eo[(long)r * eostride + slotE];
-			double2 o = eo[(long)r * eostride + slotE + 1];
-			double v = part ? (e.y + sgnO * o.y) * conjsgn : (e.x + sgnO * o.x);
-			return v;
-		}
-		return zsrc[(long)r * zstride];
-	};
-#pragma unroll
-	for (int q = 0; q < P; ++q) zw[P + 1 + q] = loadz(q + 1);
-	zw[P] = loadz(0);
-	for (int r = 0; r < N; ++r) {
-		// w = (S z)_r, own part
-		double w = 0.0;
-#pragma unroll
-		for (int k = P; k >= 1; --k)
-			if (r - k >= 0) w = fma(__ldg(S + (long)(r - k) * NE + k), zw[P - k], w);
-#pragma unroll
-		for (int k = 0; k <= P; ++k) w = fma(__ldg(S + (long)r * NE + k), zw[P + k], w);
-		// y_r = w - sum_k L(r, r-k) y_{r-k};  L(r, r-k) = fac[r-k][k-1]
-		double acc = w;
-#pragma unroll
-		for (int k = P; k >= 1; --k) {
-			if (r - k < 0) continue;
-			double2 lv = fac[(long)(r - k) * fstride + (long)(k - 1) * (fstride / NE)];
-			if (part == 0) acc = fma(-lv.x, yre[k - 1], fma(lv.y, yim[k - 1], acc));
-			else acc = fma(-lv.x, yim[k - 1], fma(-lv.y, yre[k - 1], acc));
-		}
-		double other = shfl<P>(acc, 1, gmask);
-		double nyr = part ? other : acc, nyi = part ? acc : other;
-		ydst[(long)r * ystride] = acc;
-#pragma unroll
-		for (int q = P - 1; q >= 1; --q) { yre[q] = yre[q - 1]; yim[q] = yim[q - 1]; }
-		yre[0] = nyr; yim[0] = nyi;
-#pragma unroll
-		for (int q = 0; q < 2 * P; ++q) zw[q] = zw[q + 1];
-		zw[2 * P] = loadz(r + P + 1);
-	}
-}
-
-template <int P>
-__global__ void __launch_bounds__(64) k_sweep(double2* __restrict__ eo, double* __restrict__ y1, double* __restrict__ y2,
-	const double2* __restrict__ fac, const double* __restrict__ S, const int64_t* __restrict__ ntf,
-	long step, int jslot, int B, int M, int N, int L, int npair)
-{
-	constexpr int NE = P + 1;
-	long g = (long)blockIdx.x * blockDim.x + threadIdx.x;
-	long tot = (long)B * M * npair * 4;
-	int lane = threadIdx.x & 31;
-	unsigned gmask = 0xFu << (lane & 28);
-	bool valid = g < tot;
-	long gg = valid ? g : tot - 1;
-	int sub = (int)(gg & 3);
-	int part = sub & 1, neg = sub >> 1;
-	long pk = gg >> 2;
-	int k = (int)(pk % npair);
-	long im_inst = pk / npair;
-	long inst = im_inst / M;
-	int a = valid ? coupling_power(step, ntf[inst]) : 0;
-	if (a == 0) return;	// the 4 lanes of a pair agree on a
-	const long eostride = L;	// in double2 per row
-	double2* eob = eo + im_inst * (long)N * L;
-	// scratch viewed as doubles: [inst][m][r][slot][part] with slot = 2k+neg
-	const long ystride = 2L * L;
-	const long yoff = im_inst * (long)N * 2 * L + (2 * k + neg) * 2 + part;
-	double* y1b = y1 + yoff;
-	double* y2b = y2 + yoff;
-	const long fstride = (long)NE * npair;	// double2 per row
-	const double2* fb = fac + (((long)jslot * B * M + im_inst) * (long)N) * NE * npair + k;
-	const double sgnO = neg ? -1.0 : 1.0;
-	const double conjsgn = neg ? -1.0 : 1.0;
-	for (int app = 0; app < a; ++app) {
-		// forward: z from eo (app 0) or y1 (app 1); y -> y2
-		cn_forward<P>(S, fb, fstride, eob, eostride, 2 * k, app == 0, sgnO, conjsgn, part, y1b, ystride, y2b, ystride, N, gmask);
-		// backward: x_r = Dinv_r y_r - sum_k L(r+k, r) x_{r+k}; z <- 2x - z
-		double xre[P], xim[P];
-#pragma unroll
-		for (int q = 0; q < P; ++q) { xre[q] = 0.0; xim[q] = 0.0; }
-		const bool last = (app == a - 1);
-		for (int r = N - 1; r >= 0; --r) {
-			double yown = y2b[(long)r * ystride];
-			double yoth = shfl<P>(yown, 1, gmask);
-			double yr = part ? yoth : yown, yi = part ? yown : yoth;
-			double2 dv = fb[(long)r * fstride + (long)P * npair];
-			double acc = part ? fma(dv.x, yi, dv.y * yr) : fma(dv.x, yr, -dv.y * yi);
-#pragma unroll
-			for (int q = 1; q <= P; ++q) {
-				if (r + q >= N) continue;
-				double2 lv = fb[(long)r * fstride + (long)(q - 1) * npair];
-				if (part == 0) acc = fma(-lv.x, xre[q - 1], fma(lv.y, xim[q - 1], acc));
-				else acc = fma(-lv.x, xim[q - 1], fma(-lv.y, xre[q - 1], acc));
-			}
-			double oth = shfl<P>(acc, 1, gmask);
-#pragma unroll
-			for (int q = P - 1; q >= 1; --q) { xre[q] = xre[q - 1]; xim[q] = xim[q - 1]; }
-			xre[0] = part ? oth : acc; xim[0] = part ? acc : oth;
-			// z (own part) of this application
-			double z;
-			if (app == 0) {
-				double2 e = eob[(long)r * eostride + 2 * k], o = eob[(long)r * eostride + 2 * k + 1];
-				z = part ? (e.y + sgnO * o.y) * conjsgn : (e.x + sgnO * o.x);
-			} else z = y1b[(long)r * ystride];
-			double zn = fma(2.0, acc, -z);
-			if (!last) {
-				y1b[(long)r * ystride] = zn;
-			} else {
-				// combine with the other sign: actual z- = conj(computed)
-				double zo = shfl<P>(zn, 2, gmask);
-				double zp = neg ? zo : zn, zm = neg ? zn : zo;	// own part of z+ and of computed z-
-				double zmact = part ? -zm : zm;
-				double outv = neg ? (zp - zmact) : (zp + zmact);	// s (neg=0) or d (neg=1)
-				double* eod = reinterpret_cast<double*>(eob + (long)r * eostride + 2 * k + neg);
-				eod[part] = outv;
-			}
-		}
-	}
-}
-
-// ---------------------------------------------------------------- field-free step
-// Every (inst, m, il) channel, real/imag split over two lanes:
-//   forward  y_r = (S c)_r - sum_k L_l(r, r-k) y_{r-k}
-//   backward x_r = y_r / D_l(r) - sum_k L_l(r+k, r) x_{r+k};  c_r <- 2 x_r - c_r
-// with L_l, D_l the LDL^T of S + i dt/2 H_l (ff[r][c][l]: c < P L(r, r-1-c), c = P 1/D).
-template <int P>
-__global__ void __launch_bounds__(64) k_fieldfree(double2* __restrict__ st, double* __restrict__ ys, const double2* __restrict__ ff,
-	const double* __restrict__ S, const int64_t* __restrict__ ntt, long step, int B, int M, int m0, int N, int L, int nlh)
-{
-	constexpr int NE = P + 1;
-	long g = (long)blockIdx.x * blockDim.x + threadIdx.x;
-	long tot = (long)B * M * L * 2;
-	int lane = threadIdx.x & 31;
-	unsigned gmask = 0x3u << (lane & 30);
-	bool valid = g < tot;
-	long gg = valid ? g : tot - 1;
-	int part = (int)(gg & 1);
-	long ch = gg >> 1;
-	int il = (int)(ch % L);
-	long im_inst = ch / L;
-	int m = (int)(im_inst % M) + m0;
-	long inst = im_inst / M;
-	if (!valid || step >= ntt[inst]) return;
-	int l = il + (m < 0 ? -m : m);
-	double* sb = reinterpret_cast<double*>(st + im_inst * (long)N * L + il) + part;
-	double* yb = ys + (im_inst * (long)N * L + il) * 2 + part;
-	const long stride = 2L * L;	// doubles per row
-	const double2* fl = ff + l;
-	const long fstride = (long)NE * nlh;
-	// forward
-	{
-		double zw[2 * P + 1];
-		double yre[P], yim[P];
-#pragma unroll
-		for (int q = 0; q < 2 * P + 1; ++q) zw[q] = 0.0;
-#pragma unroll
-		for (int q = 0; q < P; ++q) { yre[q] = 0.0; yim[q] = 0.0; }
-#pragma unroll
-		for (int q = 0; q <= P; ++q) zw[P + q] = q < N ? sb[(long)q * stride] : 0.0;
-		for (int r = 0; r < N; ++r) {
-			double w = 0.0;
-#pragma unroll
-			for (int k = P; k >= 1; --k)
-				if (r - k >= 0) w = fma(__ldg(S + (long)(r - k) * NE + k), zw[P - k], w);
-#pragma unroll
-			for (int k = 0; k <= P; ++k) w = fma(__ldg(S + (long)r * NE + k), zw[P + k], w);
-			double acc = w;
-#pragma unroll
-			for (int k = 1; k <= P; ++k) {
-				double2 lv = fl[(long)r * fstride + (long)(k - 1) * nlh];
-				if (part == 0) acc = fma(-lv.x, yre[k - 1], fma(lv.y, yim[k - 1], acc));
-				else acc = fma(-lv.x, yim[k - 1], fma(-lv.y, yre[k - 1], acc));
-			}
-			double other = __shfl_xor_sync(gmask, acc, 1);
-			yb[(long)r * stride] = acc;
-#pragma unroll
-			for (int q = P - 1; q >= 1; --q) { yre[q] = yre[q - 1]; yim[q] = yim[q - 1]; }
-			yre[0] = part ? other : acc; yim[0] = part ? acc : other;
-#pragma unroll
-			for (int q = 0; q < 2 * P; ++q) zw[q] = zw[q + 1];
-			zw[2 * P] = (r + P + 1 < N) ? sb[(long)(r + P + 1) * stride] : 0.0;
-		}
-	}
-	// backward
-	{
-		double xre[P], xim[P];
-#pragma unroll
-		for (int q = 0; q < P; ++q) { xre[q] = 0.0; xim[q] = 0.0; }
-		for (int r = N - 1; r >= 0; --r) {
-			double yown = yb[(long)r * stride];
-			double yoth = __shfl_xor_sync(gmask, yown, 1);
-			double yr = part ? yoth : yown, yi = part ? yown : yoth;
-			double2 dv = fl[(long)r * fstride + (long)P * nlh];
-			double acc = part ? fma(dv.x, yi, dv.y * yr) : fma(dv.x, yr, -dv.y * yi);
-#pragma unroll
-			for (int q = 1; q <= P; ++q) {
-				if (r + q >= N) continue;
-				double2 lv = fl[(long)(r + q) * fstride + (long)(q - 1) * nlh];
-				if (part == 0) acc = fma(-lv.x, xre[q - 1], fma(lv.y, xim[q - 1], acc));
-				else acc = fma(-lv.x, xim[q - 1], fma(-lv.y, xre[q - 1], acc));
-			}
-			double oth = __shfl_xor_sync(gmask, acc, 1);
-#pragma unroll
-			for (int q = P - 1; q >= 1; --q) { xre[q] = xre[q - 1]; xim[q] = xim[q - 1]; }
-			xre[0] = part ? oth : acc; xim[0] = part ? acc : oth;
-			double c = sb[(long)r * stride];
-			sb[(long)r * stride] = fma(2.0, acc, -c);
-		}
-	}
 }
 
 // ---------------------------------------------------------------- reductions
@@ -553,21 +319,21 @@ struct qpc_lgwz {
 	int N = 0, P = 0, L = 0, M = 0, B = 0, lmax = 0, nlh = 0, npair = 0;
 	double dt = 0.0;
 	cudaStream_t stream = nullptr;
-	cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+	cudaEvent_t ev0 = nullptr, ev1 = nullptr;	// brackets of qpc_lgwz_run
+	cudaEvent_t evt0 = nullptr, evt1 = nullptr;	// autotuner timing
 	double* S = nullptr;      // [N][P+1]
 	double* R = nullptr;      // [N][P+1]
 	double* Vh = nullptr;     // [M][npair+1][L]
 	double* lamp = nullptr;   // [M][npair]
-	double2* ff = nullptr;    // [N][P+1][nlh]
-	double2* st = nullptr;    // [B][M][N][L]
-	double2* eo = nullptr;    // [B][M][N][L]
-	double* y1 = nullptr;     // [B][M][N][L][2]
-	double* y2 = nullptr;
-	double2* hostlay = nullptr; // [B][M][L][N] staging for layout change
-	double2* fac = nullptr;   // [K][B][M][N][P+1][npair]
+	double2* ff = nullptr;    // field-free factors [nlh][N][P+1] (row form + 1/D)
+	double2* st = nullptr;    // state, engine layout [B][M][N][L]
+	double2* eo = nullptr;    // eigen-basis state [B][M][N][L]
+	double2* wk = nullptr;    // per-chain work vector [B][M][N][L]
+	double2* hostlay = nullptr; // [B][M][L][N] staging for layout changes
+	double2* fac = nullptr;   // coupling factors [K][B][M][npair][N][P+1]
 	int K = 1;
 	int* status = nullptr;
-	double2* red = nullptr;   // reduction scratch [B*M*L]
+	double2* red = nullptr;   // reduction scratch [2*B*M*L]
 	int64_t* ntf = nullptr;   // device [B]
 	int64_t* ntt = nullptr;
 	double* ftab = nullptr;   // device field table [B][ld]
@@ -575,6 +341,10 @@ struct qpc_lgwz {
 	long ld = 1;
 	double last_ms = 0.0;
 	int64_t launches = 0;
+	// chain-kernel lanes per part chosen by the autotuner, per (coupling?, live-instance bucket)
+	int gsel[2][32];
+	std::vector<int> gcand;
+	size_t chain_smem = 0;
 	// optional per-kernel timing (CUDA events around each launch on the handle's stream)
 	bool profiling = false;
 	std::vector<cudaEvent_t> evpool;
@@ -583,7 +353,6 @@ struct qpc_lgwz {
 	int64_t kcount[QPC_NKERNEL] = {0};
 	std::vector<double> h_lam;   // [M][L]
 	std::vector<double> h_P;     // [M][L][L]
-	std::vector<double> h_S;
 };
 
 namespace {
@@ -664,56 +433,152 @@ void collect_profile(qpc_lgwz* h)
 	h->evuse.clear();
 }
 
+// ---------------------------------------------------------------- chain launches
+template <int P, int G, bool CPL>
+void launch_chain_g(qpc_lgwz* h, double2* X, const double2* fac, const int64_t* nta, long step, int jslot, int Blive)
+{
+	using C = chain_cfg<P, G, CPL>;
+	long nchains = CPL ? (long)Blive * h->M * h->npair * 2 : (long)Blive * h->M * h->L;
+	if (nchains <= 0) return;
+	long nwarps = (nchains + C::CPW - 1) / C::CPW;
+	unsigned grid = (unsigned)((nwarps + 3) / 4);
+	k_chain<P, G, CPL><<<grid, 128, h->chain_smem, h->stream>>>(X, h->wk, fac, h->S, nta, step, jslot, h->B, h->M, h->d.m0,
+		h->N, h->L, h->npair, nchains);
+	LAUNCH(h);
+}
+
+template <int P, bool CPL>
+void launch_chain(qpc_lgwz* h, int G, double2* X, const double2* fac, const int64_t* nta, long step, int jslot, int Blive)
+{
+	switch (G) {
+	case 1: launch_chain_g<P, 1, CPL>(h, X, fac, nta, step, jslot, Blive); break;
+	case 2: if constexpr (P % 2 == 0) launch_chain_g<P, 2, CPL>(h, X, fac, nta, step, jslot, Blive); break;
+	case 3: if constexpr (P % 3 == 0) launch_chain_g<P, 3, CPL>(h, X, fac, nta, step, jslot, Blive); break;
+	case 4: if constexpr (P % 4 == 0) launch_chain_g<P, 4, CPL>(h, X, fac, nta, step, jslot, Blive); break;
+	default: launch_chain_g<P, P, CPL>(h, X, fac, nta, step, jslot, Blive); break;
+	}
+}
+
 template <int P>
-int launch_step_kernels(qpc_lgwz* h, long step, long step0, int jslot, bool do_factor, int kfac)
+void set_chain_smem_attr(size_t smem)
+{
+	auto f = [&](auto kern) { cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); };
+	f(k_chain<P, 1, true>); f(k_chain<P, 1, false>); f(k_chain<P, P, true>); f(k_chain<P, P, false>);
+	if constexpr (P % 2 == 0) { f(k_chain<P, 2, true>); f(k_chain<P, 2, false>); }
+	if constexpr (P % 3 == 0) { f(k_chain<P, 3, true>); f(k_chain<P, 3, false>); }
+	if constexpr (P % 4 == 0) { f(k_chain<P, 4, true>); f(k_chain<P, 4, false>); }
+}
+
+int live_bucket(int n) { int b = 0; while ((1 << b) < n) ++b; return b; }
+
+// Autotuner: for the current live-instance count, time every candidate G for
+// the coupling and the field-free chain kernels (two launches each, CUDA
+// events) on scratch buffers (eo / wk / the factor slot of this step, whose
+// contents are about to be overwritten) and keep the fastest.  Runs before
+// the step's forward transform, once per (kernel, live bucket).
+template <int P>
+int autotune(qpc_lgwz* h, long step, int jslot, int Bc, int Bf)
+{
+	for (int cpl = 0; cpl < 2; ++cpl) {
+		int Bl = cpl ? Bc : Bf;
+		if (Bl <= 0 || (cpl && h->npair == 0)) continue;
+		int bk = live_bucket(Bl);
+		if (h->gsel[cpl][bk]) continue;
+		float best = 1e30f;
+		int bestg = 1;
+		for (int G : h->gcand) {
+			float tot = 0.f;
+			for (int rep = 0; rep < 2; ++rep) {
+				QPC_CUDA(cudaEventRecord(h->evt0, h->stream));
+				if (cpl) launch_chain<P, true>(h, G, h->eo, h->fac, h->ntf, step, jslot, Bl);
+				else launch_chain<P, false>(h, G, h->eo, h->ff, h->ntt, step, 0, Bl);
+				QPC_CUDA(cudaEventRecord(h->evt1, h->stream));
+				if (int rc = wait_stream(h)) return rc;
+				float ms = 0.f;
+				cudaEventElapsedTime(&ms, h->evt0, h->evt1);
+				if (rep) tot += ms;
+			}
+			QPC_CUDA(cudaGetLastError());
+			if (tot < best) { best = tot; bestg = G; }
+		}
+		h->gsel[cpl][bk] = bestg;
+	}
+	return QPC_OK;
+}
+
+template <int P>
+int launch_step_kernels(qpc_lgwz* h, long step, long step0, int jslot, bool do_factor, int kfac, int Bc, int Bf, int Bfac)
 {
 	const int B = h->B, M = h->M, N = h->N, L = h->L, np = h->npair;
-	if (do_factor && np > 0) {
+	if (do_factor && np > 0 && Bfac > 0) {
 		prof_scope ps(h, QPC_KERNEL_FACTOR);
-		long nsys = (long)kfac * B * M * np;
+		long nsys = (long)kfac * Bfac * M * np;
 		k_factor<P><<<(unsigned)((nsys + 63) / 64), 64, 0, h->stream>>>(h->fac, h->S, h->R, h->lamp, h->ftab, h->ld,
-			h->ntf, step0, kfac, B, M, N, np, h->dt, h->status);
+			h->ntf, step0, kfac, B, Bfac, M, N, np, h->dt, h->status);
 		LAUNCH(h);
 	}
-	if (np > 0 || (L & 1)) {
+	if (int rc = autotune<P>(h, step, jslot, Bc, Bf)) return rc;
+	if (Bc > 0 && (np > 0 || (L & 1))) {
 		int tiles = (N + TR - 1) / TR;
 		size_t smem = sizeof(double2) * 2 * TR * (L | 1);
-		unsigned grid = (unsigned)((long)B * M * tiles);
+		unsigned grid = (unsigned)((long)Bc * M * tiles);
 		{
 			prof_scope ps(h, QPC_KERNEL_TRANSFORM_FWD);
-			k_transform<<<grid, 256, smem, h->stream>>>(h->st, h->eo, h->Vh, N, L, M, np, 1, h->ntf, step, B);
+			k_transform<<<grid, 256, smem, h->stream>>>(h->st, h->eo, h->Vh, N, L, M, np, 1, h->ntf, step, Bc);
 			LAUNCH(h);
 		}
 		if (np > 0) {
 			prof_scope ps(h, QPC_KERNEL_SWEEP);
-			long tot = (long)B * M * np * 4;
-			k_sweep<P><<<(unsigned)((tot + 63) / 64), 64, 0, h->stream>>>(h->eo, h->y1, h->y2, h->fac, h->S, h->ntf, step, jslot, B, M, N, L, np);
-			LAUNCH(h);
+			launch_chain<P, true>(h, h->gsel[1][live_bucket(Bc)], h->eo, h->fac, h->ntf, step, jslot, Bc);
 		}
 		{
 			prof_scope ps(h, QPC_KERNEL_TRANSFORM_BWD);
-			k_transform<<<grid, 256, smem, h->stream>>>(h->eo, h->st, h->Vh, N, L, M, np, 0, h->ntf, step, B);
+			k_transform<<<grid, 256, smem, h->stream>>>(h->eo, h->st, h->Vh, N, L, M, np, 0, h->ntf, step, Bc);
 			LAUNCH(h);
 		}
 	}
-	prof_scope ps(h, QPC_KERNEL_FIELDFREE);
-	long tot = (long)B * M * L * 2;
-	k_fieldfree<P><<<(unsigned)((tot + 63) / 64), 64, 0, h->stream>>>(h->st, h->y2, h->ff, h->S, h->ntt, step, B, M, h->d.m0, N, L, h->nlh);
-	LAUNCH(h);
+	if (Bf > 0) {
+		prof_scope ps(h, QPC_KERNEL_FIELDFREE);
+		launch_chain<P, false>(h, h->gsel[0][live_bucket(Bf)], h->st, h->ff, h->ntt, step, 0, Bf);
+	}
 	return QPC_OK;
 }
 
-int launch_step(qpc_lgwz* h, long step, long step0, int jslot, bool do_factor, int kfac)
+int launch_step(qpc_lgwz* h, long step, long step0, int jslot, bool do_factor, int kfac, int Bc, int Bf, int Bfac)
 {
 	switch (h->P) {
-	case 3: return launch_step_kernels<3>(h, step, step0, jslot, do_factor, kfac);
-	case 4: return launch_step_kernels<4>(h, step, step0, jslot, do_factor, kfac);
-	case 5: return launch_step_kernels<5>(h, step, step0, jslot, do_factor, kfac);
-	case 6: return launch_step_kernels<6>(h, step, step0, jslot, do_factor, kfac);
-	case 7: return launch_step_kernels<7>(h, step, step0, jslot, do_factor, kfac);
-	case 8: return launch_step_kernels<8>(h, step, step0, jslot, do_factor, kfac);
+	case 3: return launch_step_kernels<3>(h, step, step0, jslot, do_factor, kfac, Bc, Bf, Bfac);
+	case 4: return launch_step_kernels<4>(h, step, step0, jslot, do_factor, kfac, Bc, Bf, Bfac);
+	case 5: return launch_step_kernels<5>(h, step, step0, jslot, do_factor, kfac, Bc, Bf, Bfac);
+	case 6: return launch_step_kernels<6>(h, step, step0, jslot, do_factor, kfac, Bc, Bf, Bfac);
+	case 7: return launch_step_kernels<7>(h, step, step0, jslot, do_factor, kfac, Bc, Bf, Bfac);
+	case 8: return launch_step_kernels<8>(h, step, step0, jslot, do_factor, kfac, Bc, Bf, Bfac);
 	default: set_error("unsupported B-spline degree %d", h->P); return QPC_ERR_ARGS;
 	}
+}
+
+void set_smem_attrs(qpc_lgwz* h)
+{
+	switch (h->P) {
+	case 3: set_chain_smem_attr<3>(h->chain_smem); break;
+	case 4: set_chain_smem_attr<4>(h->chain_smem); break;
+	case 5: set_chain_smem_attr<5>(h->chain_smem); break;
+	case 6: set_chain_smem_attr<6>(h->chain_smem); break;
+	case 7: set_chain_smem_attr<7>(h->chain_smem); break;
+	case 8: set_chain_smem_attr<8>(h->chain_smem); break;
+	}
+}
+
+// reorder instances on the device: dst[k] = src[perm[k]] (whole instance blocks)
+int permute_instances(qpc_lgwz* h, const std::vector<int>& perm, bool inverse)
+{
+	size_t blk = sizeof(double2) * (size_t)h->M * h->N * h->L;
+	for (int k = 0; k < h->B; ++k) {
+		int from = inverse ? k : perm[k], to = inverse ? perm[k] : k;
+		QPC_CUDA(cudaMemcpyAsync((char*)h->eo + blk * to, (const char*)h->st + blk * from, blk, cudaMemcpyDeviceToDevice, h->stream));
+	}
+	std::swap(h->st, h->eo);
+	return QPC_OK;
 }
 
 } // namespace
@@ -746,7 +611,7 @@ int qpc_lgwz_create(const qpc_dims* dims, double dt, const double* S, const doub
 	int rc = QPC_OK;
 	auto fail = [&](int code) { qpc_lgwz_destroy(h); return code; };
 	if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) { set_error("stream create"); return fail(QPC_ERR_CUDA); }
-	cudaEventCreate(&h->ev0); cudaEventCreate(&h->ev1);
+	cudaEventCreate(&h->ev0); cudaEventCreate(&h->ev1); cudaEventCreate(&h->evt0); cudaEventCreate(&h->evt1);
 	// host setup: field-free LDL^T per l, Y10 eigensystems
 	std::vector<double2> ffh((size_t)N * NE * h->nlh);
 	std::vector<double> Lrow((size_t)N * P * 2), Dinv((size_t)N * 2);
@@ -754,11 +619,11 @@ int qpc_lgwz_create(const qpc_dims* dims, double dt, const double* S, const doub
 		int bad = qpc_ldlt_csym(N, P, S, H + (size_t)l * N * NE, dt * 0.5, Lrow.data(), Dinv.data());
 		if (bad < 0) { set_error("ldlt arguments"); return fail(QPC_ERR_ARGS); }
 		if (bad > 0) { set_error("zero pivot factorising S + i dt/2 H_%d", l); return fail(QPC_ERR_SINGULAR); }
-		// store L(r, r-1-c) for the forward sweep: ff[r][c][l] = Lrow[r][c]
+		// row form per l: ff[l][r][c] = L(r, r-1-c), ff[l][r][P] = 1/D(r)
 		for (int r = 0; r < N; ++r) {
 			for (int c = 0; c < P; ++c)
-				ffh[((size_t)r * NE + c) * h->nlh + l] = make_double2(Lrow[2 * ((size_t)r * P + c)], Lrow[2 * ((size_t)r * P + c) + 1]);
-			ffh[((size_t)r * NE + P) * h->nlh + l] = make_double2(Dinv[2 * (size_t)r], Dinv[2 * (size_t)r + 1]);
+				ffh[((size_t)l * N + r) * NE + c] = make_double2(Lrow[2 * ((size_t)r * P + c)], Lrow[2 * ((size_t)r * P + c) + 1]);
+			ffh[((size_t)l * N + r) * NE + P] = make_double2(Dinv[2 * (size_t)r], Dinv[2 * (size_t)r + 1]);
 		}
 	}
 	h->h_lam.assign((size_t)M * L, 0.0);
@@ -776,15 +641,14 @@ int qpc_lgwz_create(const qpc_dims* dims, double dt, const double* S, const doub
 		if (L & 1)
 			for (int il = 0; il < L; ++il) Vh[((size_t)im * (np + 1) + np) * L + il] = Pm[(size_t)np * L + il];
 	}
-	h->h_S.assign(S, S + (size_t)N * NE);
 	// look-ahead depth for the factorisation: enough systems to fill the GPU, bounded memory
 	size_t per_step = (size_t)h->B * M * N * NE * std::max(np, 1) * sizeof(double2);
 	h->K = 1;
-	while (h->K < 8 && (long)h->K * h->B * M * np < 40000 && per_step * (h->K * 2) <= ((size_t)4 << 30)) h->K *= 2;
+	while (h->K < 8 && (long)h->K * h->B * M * np < 40000 && per_step * (h->K * 2) <= ((size_t)8 << 30)) h->K *= 2;
 	long sl = state_len(h);
 	if ((rc = dalloc(&h->S, (size_t)N * NE)) || (rc = dalloc(&h->R, (size_t)N * NE)) || (rc = dalloc(&h->Vh, Vh.size())) ||
 		(rc = dalloc(&h->lamp, lamp.size())) || (rc = dalloc(&h->ff, ffh.size())) || (rc = dalloc(&h->st, sl)) ||
-		(rc = dalloc(&h->eo, sl)) || (rc = dalloc(&h->y1, 2 * sl)) || (rc = dalloc(&h->y2, 2 * sl)) ||
+		(rc = dalloc(&h->eo, sl)) || (rc = dalloc(&h->wk, sl)) ||
 		(rc = dalloc(&h->hostlay, sl)) || (rc = dalloc(&h->fac, per_step / sizeof(double2) * h->K)) ||
 		(rc = dalloc(&h->status, 1)) || (rc = dalloc(&h->red, (size_t)h->B * M * L * 2)) ||
 		(rc = dalloc(&h->ntf, h->B)) || (rc = dalloc(&h->ntt, h->B)))
@@ -800,6 +664,11 @@ int qpc_lgwz_create(const qpc_dims* dims, double dt, const double* S, const doub
 	}
 	size_t smem = sizeof(double2) * 2 * TR * (L | 1);
 	if (smem > 48 * 1024) cudaFuncSetAttribute(k_transform, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+	h->chain_smem = sizeof(double) * (size_t)N * NE;
+	if (h->chain_smem > 200 * 1024) { set_error("n_r=%d too large for the shared-memory S band", N); return fail(QPC_ERR_ARGS); }
+	set_smem_attrs(h);
+	std::memset(h->gsel, 0, sizeof(h->gsel));
+	for (int g = 1; g <= P; ++g) if (P % g == 0 && (g <= 4 || g == P)) h->gcand.push_back(g);
 	*out = h;
 	return QPC_OK;
 }
@@ -809,9 +678,11 @@ int qpc_lgwz_destroy(qpc_lgwz* h)
 	if (!h) return QPC_OK;
 	if (h->stream) cudaStreamSynchronize(h->stream);
 	cudaFree(h->S); cudaFree(h->R); cudaFree(h->Vh); cudaFree(h->lamp); cudaFree(h->ff);
-	cudaFree(h->st); cudaFree(h->eo); cudaFree(h->y1); cudaFree(h->y2); cudaFree(h->hostlay); cudaFree(h->fac);
+	cudaFree(h->st); cudaFree(h->eo); cudaFree(h->wk); cudaFree(h->hostlay); cudaFree(h->fac);
 	cudaFree(h->status); cudaFree(h->red); cudaFree(h->ntf); cudaFree(h->ntt); cudaFree(h->ftab);
 	for (auto e : h->evpool) cudaEventDestroy(e);
+	if (h->evt0) cudaEventDestroy(h->evt0);
+	if (h->evt1) cudaEventDestroy(h->evt1);
 	if (h->ev0) cudaEventDestroy(h->ev0);
 	if (h->ev1) cudaEventDestroy(h->ev1);
 	if (h->stream) cudaStreamDestroy(h->stream);
@@ -886,19 +757,42 @@ int qpc_lgwz_run(qpc_lgwz* h, const double* ftab, int64_t ld, const int64_t* nt_
 				if (nt_field[k] > 0 && !std::isfinite(ftab[(size_t)k * ld + i])) { set_error("non-finite field value, instance %d step %lld", k, (long long)i); return QPC_ERR_ARGS; }
 		QPC_CUDA(cudaMemcpyAsync(h->ftab, ftab, sizeof(double) * need, cudaMemcpyHostToDevice, h->stream));
 	}
-	QPC_CUDA(cudaMemcpyAsync(h->ntf, nt_field, sizeof(int64_t) * B, cudaMemcpyHostToDevice, h->stream));
-	QPC_CUDA(cudaMemcpyAsync(h->ntt, nt_total, sizeof(int64_t) * B, cudaMemcpyHostToDevice, h->stream));
+	// Instances are processed in decreasing order of nt_field (then nt_total):
+	// the instances still in their pulse at step s are then a prefix, and
+	// launches cover only that prefix.
+	std::vector<int> perm(B);
+	std::iota(perm.begin(), perm.end(), 0);
+	std::stable_sort(perm.begin(), perm.end(), [&](int x, int y) {
+		return nt_field[x] != nt_field[y] ? nt_field[x] > nt_field[y] : nt_total[x] > nt_total[y]; });
+	bool ident = true;
+	for (int k = 0; k < B; ++k) ident &= perm[k] == k;
+	std::vector<int64_t> pf(B), pt(B);
+	for (int k = 0; k < B; ++k) { pf[k] = nt_field[perm[k]]; pt[k] = nt_total[perm[k]]; }
+	if (anyfield && !ident) {
+		std::vector<double> tab((size_t)B * ld);
+		for (int k = 0; k < B; ++k) std::memcpy(tab.data() + (size_t)k * ld, ftab + (size_t)perm[k] * ld, sizeof(double) * ld);
+		QPC_CUDA(cudaMemcpyAsync(h->ftab, tab.data(), sizeof(double) * tab.size(), cudaMemcpyHostToDevice, h->stream));
+		if (int rc = wait_stream(h)) return rc;
+	}
+	QPC_CUDA(cudaMemcpyAsync(h->ntf, pf.data(), sizeof(int64_t) * B, cudaMemcpyHostToDevice, h->stream));
+	QPC_CUDA(cudaMemcpyAsync(h->ntt, pt.data(), sizeof(int64_t) * B, cudaMemcpyHostToDevice, h->stream));
 	QPC_CUDA(cudaMemsetAsync(h->status, 0, sizeof(int), h->stream));
+	if (!ident) if (int rc = permute_instances(h, perm, false)) return rc;
 	h->ld = anyfield ? (long)ld : 0;
+	// live prefixes per step: coupling (nt_field >= s, nt_field > 0) and field-free (nt_total > s)
+	auto coupling_live = [&](long s) { int n = 0; while (n < B && pf[n] > 0 && pf[n] >= s) ++n; return n; };
+	auto free_live = [&](long s) { int n = B; while (n > 0 && pt[n - 1] <= s) --n; return n; };
 	QPC_CUDA(cudaEventRecord(h->ev0, h->stream));
 	for (long s = 0; s < smax; ++s) {
 		// factors for steps s .. s+K-1 are computed together, into slots 0..K-1
 		int j = (int)(s % h->K);
 		long kf = std::min<long>(h->K, smax - s);
-		if (int rc = launch_step(h, s, s - j, j, j == 0, (int)kf)) return rc;
+		int Bc = coupling_live(s), Bf = free_live(s);
+		if (int rc = launch_step(h, s, s - j, j, j == 0, (int)kf, Bc, Bf, Bc)) return rc;
 	}
 	QPC_CUDA(cudaEventRecord(h->ev1, h->stream));
 	QPC_CUDA(cudaGetLastError());
+	if (!ident) if (int rc = permute_instances(h, perm, true)) return rc;
 	long sl = state_len(h);
 	k_status_check<<<(unsigned)((sl + 255) / 256), 256, 0, h->stream>>>(h->st, sl, h->status);
 	LAUNCH(h);
