@@ -184,6 +184,7 @@ def run_engine(args):
     if roof["hbm"]["achieved_gbs"] and peaks.get("hbm_gbs"):
         roof["hbm"]["frac"] = roof["hbm"]["achieved_gbs"] / peaks["hbm_gbs"]
     kt = {k: {"ms_total": v[0], "launches": v[1]} for k, v in ktimes.items()}
+    tuning = prop.tuning()
     prop.close()
 
     # plain one-wavefunction GPU path, same kernels, same grid, fields of instance 0
@@ -193,6 +194,7 @@ def run_engine(args):
     pl.run(ftab[:1, :W + 1], [W])
     pl.run(ftab[:1, W:W + Kp + 1], [Kp])
     plain = Kp / (pl.last_run_ms() * 1e-3)
+    tuning_plain = pl.tuning()
     gpu_launches += 0
     pl.close()
 
@@ -209,6 +211,7 @@ def run_engine(args):
         "plain_1wf": {"value": plain, "unit": "wf-steps/s", "ratio_batched_over_plain": value / plain},
         "gpu_launches": gpu_launches,
         "kernels": kt,
+        "tuning": {"batched": tuning, "plain": tuning_plain},
         "roofline": roof,
         "cpu_baseline": cpu,
         "clocks": clocks,

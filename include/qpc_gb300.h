@@ -170,6 +170,12 @@ int64_t qpc_lgwz_launch_count(qpc_lgwz* h);
 enum { QPC_KERNEL_FACTOR = 0, QPC_KERNEL_TRANSFORM_FWD = 1, QPC_KERNEL_SWEEP = 2,
        QPC_KERNEL_TRANSFORM_BWD = 3, QPC_KERNEL_FIELDFREE = 4, QPC_NKERNEL = 5 };
 int qpc_lgwz_set_profiling(qpc_lgwz* h, int on);
+
+/* Tuning state: out[0] = factorisation look-ahead (steps); out[1+b], out[33+b] =
+ * lanes per real/imaginary part chosen by the autotuner for the coupling and the
+ * field-free chain kernels at live-instance bucket b (2^(b-1) < live <= 2^b; 0 = not tuned yet).
+ * out must hold 65 values. */
+int qpc_lgwz_get_tuning(qpc_lgwz* h, int32_t* out);
 int qpc_lgwz_kernel_times(qpc_lgwz* h, double* ms, int64_t* launches);
 
 #ifdef __cplusplus

@@ -32,7 +32,7 @@ EXPORTS = (
     "qpc_lgwz_destroy", "qpc_lgwz_put", "qpc_lgwz_get", "qpc_lgwz_put_device", "qpc_lgwz_get_device",
     "qpc_lgwz_propagate", "qpc_lgwz_propagate_free", "qpc_lgwz_run", "qpc_lgwz_norm", "qpc_lgwz_dipole",
     "qpc_lgwz_projection", "qpc_lgwz_last_run_ms", "qpc_lgwz_launch_count", "qpc_lgwz_set_profiling",
-    "qpc_lgwz_kernel_times",
+    "qpc_lgwz_kernel_times", "qpc_lgwz_get_tuning",
 )
 KERNELS = ("factor", "transform_fwd", "sweep", "transform_bwd", "fieldfree")
 
@@ -94,6 +94,7 @@ def load(path=None):
         "qpc_lgwz_launch_count": (ctypes.c_int64, [P]),
         "qpc_lgwz_set_profiling": (ctypes.c_int, [P, ctypes.c_int]),
         "qpc_lgwz_kernel_times": (ctypes.c_int, [P, P, P]),
+        "qpc_lgwz_get_tuning": (ctypes.c_int, [P, P]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -284,6 +285,14 @@ class propagator_cn_hc_lgwz:
 
     def enable_profiling(self, on=True):
         _check(load().qpc_lgwz_set_profiling(self._h, int(bool(on))))
+
+    def tuning(self):
+        """{"lookahead": K, "coupling": {bucket: G}, "fieldfree": {bucket: G}} (G = lanes per part)."""
+        out = np.zeros(65, np.int32)
+        _check(load().qpc_lgwz_get_tuning(self._h, _ptr(out)))
+        return {"lookahead": int(out[0]),
+                "coupling": {b: int(out[1 + b]) for b in range(32) if out[1 + b]},
+                "fieldfree": {b: int(out[33 + b]) for b in range(32) if out[33 + b]}}
 
     def kernel_times(self):
         """{kernel: (total ms, launches)} accumulated by run() while profiling is on."""

@@ -35,6 +35,9 @@ struct chain_cfg {
 	static constexpr int LPC = 2 * G;	// lanes per chain: G real-part lanes, G imaginary-part lanes
 	static constexpr int CPW = CPL ? ((32 / LPC) & ~1) : (32 / LPC);
 	static constexpr int TPL = P / G;	// partial sums per lane
+	// prefetch distance (columns) of the recurrences: a row costs 2*TPL FP64
+	// instructions (~128*TPL cycles); memory latency is ~600-800 cycles
+	static constexpr int PD = TPL >= 6 ? 1 : (TPL >= 3 ? 2 : (TPL == 2 ? 3 : 4));
 	static_assert(P % G == 0, "G must divide P");
 	static_assert(CPW >= 1, "too many lanes per chain");
 };
@@ -101,7 +104,7 @@ __global__ void __launch_bounds__(128) k_chain(double2* __restrict__ X, double2*
 	long step, int jslot, int B, int M, int m0, int N, int L, int np, long nchains)
 {
 	using C = chain_cfg<P, G, CPL>;
-	constexpr int NE = C::NE, LPC = C::LPC, CPW = C::CPW, TPL = C::TPL;
+	constexpr int NE = C::NE, LPC = C::LPC, CPW = C::CPW, TPL = C::TPL, PD = C::PD;
 	extern __shared__ double sS[];	// S band [N][P+1]
 	for (int t = threadIdx.x; t < N * NE; t += blockDim.x) sS[t] = S[t];
 	__syncthreads();
@@ -160,7 +163,9 @@ __global__ void __launch_bounds__(128) k_chain(double2* __restrict__ X, double2*
 		}
 		__syncwarp();
 		const bool act = srole && app < ds.a;
-		// ---- P2: y = L^-1 w, column-oriented systolic window (rows c+1+g*TPL+t)
+		// ---- P2: y = L^-1 w, column-oriented systolic window (rows c+1+g*TPL+t).
+		// The factor entries of column c and the value entering the window are
+		// fetched PD columns ahead into a register ring.
 		{
 			double acc[TPL];
 #pragma unroll
@@ -168,25 +173,35 @@ __global__ void __launch_bounds__(128) k_chain(double2* __restrict__ X, double2*
 				int row = g * TPL + t;
 				acc[t] = (act && row < N) ? ws[(long)row * rs] : 0.0;
 			}
-			for (int c = 0; c < N; ++c) {
-				double yr = __shfl_sync(FULL, acc[0], cbase);
-				double yi = __shfl_sync(FULL, acc[0], cbase + G);
-				double u, w;
-				msub_operands(yr, yi, ps, u, w);
-				if (act && g == 0) ws[(long)c * rs] = acc[0];
-				double nxt = __shfl_sync(FULL, acc[0], (lane + 1) & 31);
-#pragma unroll
-				for (int t = 0; t < TPL - 1; ++t) acc[t] = acc[t + 1];
-				if (g == G - 1) acc[TPL - 1] = (act && c + P < N) ? ws[(long)(c + P) * rs] : 0.0;
-				else acc[TPL - 1] = nxt;
+			double2 lr[PD][TPL];
+			double wr[PD];
+			auto fetch = [&](int c, double2* l, double& we) {
 #pragma unroll
 				for (int t = 0; t < TPL; ++t) {
-					int j = 1 + g * TPL + t;
-					int row = c + j;
-					if (act && row < N) {
-						double2 lv = fs[(long)row * NE + (j - 1)];
-						acc[t] = fma(-lv.x, u, fma(lv.y, w, acc[t]));
-					}
+					int j = 1 + g * TPL + t, row = c + j;
+					l[t] = (act && row < N) ? fs[(long)row * NE + (j - 1)] : make_double2(0.0, 0.0);
+				}
+				we = (act && g == G - 1 && c + P < N) ? ws[(long)(c + P) * rs] : 0.0;
+			};
+#pragma unroll
+			for (int d = 0; d < PD; ++d) fetch(d, lr[d], wr[d]);
+			for (int c0 = 0; c0 < N; c0 += PD) {
+#pragma unroll
+				for (int d = 0; d < PD; ++d) {
+					const int c = c0 + d;
+					if (c >= N) break;
+					double yr = __shfl_sync(FULL, acc[0], cbase);
+					double yi = __shfl_sync(FULL, acc[0], cbase + G);
+					double u, w;
+					msub_operands(yr, yi, ps, u, w);
+					if (act && g == 0) ws[(long)c * rs] = acc[0];
+					double nxt = __shfl_sync(FULL, acc[0], (lane + 1) & 31);
+#pragma unroll
+					for (int t = 0; t < TPL - 1; ++t) acc[t] = acc[t + 1];
+					acc[TPL - 1] = (g == G - 1) ? wr[d] : nxt;
+#pragma unroll
+					for (int t = 0; t < TPL; ++t) acc[t] = fma(-lr[d][t].x, u, fma(lr[d][t].y, w, acc[t]));
+					fetch(c + PD, lr[d], wr[d]);
 				}
 			}
 		}
@@ -212,7 +227,7 @@ __global__ void __launch_bounds__(128) k_chain(double2* __restrict__ X, double2*
 			if (v) Wd[o + part] = res;
 		}
 		__syncwarp();
-		// ---- P4: x = L^-T y, descending (rows c-1-g*TPL-t)
+		// ---- P4: x = L^-T y, descending (rows c-1-g*TPL-t), same ring prefetch
 		{
 			double acc[TPL];
 #pragma unroll
@@ -220,25 +235,35 @@ __global__ void __launch_bounds__(128) k_chain(double2* __restrict__ X, double2*
 				int row = N - 1 - g * TPL - t;
 				acc[t] = (act && row >= 0) ? ws[(long)row * rs] : 0.0;
 			}
-			for (int c = N - 1; c >= 0; --c) {
-				double xr = __shfl_sync(FULL, acc[0], cbase);
-				double xi = __shfl_sync(FULL, acc[0], cbase + G);
-				double u, w;
-				msub_operands(xr, xi, ps, u, w);
-				if (act && g == 0) ws[(long)c * rs] = acc[0];
-				double nxt = __shfl_sync(FULL, acc[0], (lane + 1) & 31);
-#pragma unroll
-				for (int t = 0; t < TPL - 1; ++t) acc[t] = acc[t + 1];
-				if (g == G - 1) acc[TPL - 1] = (act && c - P >= 0) ? ws[(long)(c - P) * rs] : 0.0;
-				else acc[TPL - 1] = nxt;
+			double2 lr[PD][TPL];
+			double wr[PD];
+			auto fetch = [&](int c, double2* l, double& we) {
 #pragma unroll
 				for (int t = 0; t < TPL; ++t) {
-					int j = 1 + g * TPL + t;
-					int row = c - j;
-					if (act && row >= 0) {
-						double2 lv = fs[(long)c * NE + (j - 1)];	// L(c, c-j)
-						acc[t] = fma(-lv.x, u, fma(lv.y, w, acc[t]));
-					}
+					int j = 1 + g * TPL + t, row = c - j;
+					l[t] = (act && row >= 0) ? fs[(long)c * NE + (j - 1)] : make_double2(0.0, 0.0);	// L(c, c-j)
+				}
+				we = (act && g == G - 1 && c - P >= 0) ? ws[(long)(c - P) * rs] : 0.0;
+			};
+#pragma unroll
+			for (int d = 0; d < PD; ++d) fetch(N - 1 - d, lr[d], wr[d]);
+			for (int c0 = N - 1; c0 >= 0; c0 -= PD) {
+#pragma unroll
+				for (int d = 0; d < PD; ++d) {
+					const int c = c0 - d;
+					if (c < 0) break;
+					double xr = __shfl_sync(FULL, acc[0], cbase);
+					double xi = __shfl_sync(FULL, acc[0], cbase + G);
+					double u, w;
+					msub_operands(xr, xi, ps, u, w);
+					if (act && g == 0) ws[(long)c * rs] = acc[0];
+					double nxt = __shfl_sync(FULL, acc[0], (lane + 1) & 31);
+#pragma unroll
+					for (int t = 0; t < TPL - 1; ++t) acc[t] = acc[t + 1];
+					acc[TPL - 1] = (g == G - 1) ? wr[d] : nxt;
+#pragma unroll
+					for (int t = 0; t < TPL; ++t) acc[t] = fma(-lr[d][t].x, u, fma(lr[d][t].y, w, acc[t]));
+					fetch(c - PD, lr[d], wr[d]);
 				}
 			}
 		}

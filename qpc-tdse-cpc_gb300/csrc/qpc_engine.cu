@@ -643,8 +643,10 @@ int qpc_lgwz_create(const qpc_dims* dims, double dt, const double* S, const doub
 	}
 	// look-ahead depth for the factorisation: enough systems to fill the GPU, bounded memory
 	size_t per_step = (size_t)h->B * M * N * NE * std::max(np, 1) * sizeof(double2);
+	// look-ahead depth of the coupling factorisation: ~40k independent systems per
+	// launch (fills every FP64 pipe even for one wavefunction), at most 4 GB
 	h->K = 1;
-	while (h->K < 8 && (long)h->K * h->B * M * np < 40000 && per_step * (h->K * 2) <= ((size_t)8 << 30)) h->K *= 2;
+	while (h->K < 4096 && (long)h->K * h->B * M * np < 40000 && per_step * (h->K * 2) <= ((size_t)4 << 30)) h->K *= 2;
 	long sl = state_len(h);
 	if ((rc = dalloc(&h->S, (size_t)N * NE)) || (rc = dalloc(&h->R, (size_t)N * NE)) || (rc = dalloc(&h->Vh, Vh.size())) ||
 		(rc = dalloc(&h->lamp, lamp.size())) || (rc = dalloc(&h->ff, ffh.size())) || (rc = dalloc(&h->st, sl)) ||
@@ -934,6 +936,14 @@ int qpc_lgwz_set_profiling(qpc_lgwz* h, int on)
 	if (!h) { set_error("NULL argument"); return QPC_ERR_ARGS; }
 	h->profiling = on != 0;
 	for (int k = 0; k < QPC_NKERNEL; ++k) { h->kms[k] = 0.0; h->kcount[k] = 0; }
+	return QPC_OK;
+}
+
+int qpc_lgwz_get_tuning(qpc_lgwz* h, int32_t* out)
+{
+	if (!h || !out) { set_error("NULL argument"); return QPC_ERR_ARGS; }
+	out[0] = h->K;
+	for (int b = 0; b < 32; ++b) { out[1 + b] = h->gsel[1][b]; out[33 + b] = h->gsel[0][b]; }
 	return QPC_OK;
 }
 
