@@ -101,8 +101,9 @@ __device__ __forceinline__ void msub_operands(double vr, double vi, int part, do
 template <int P, int G, bool CPL>
 __global__ void __launch_bounds__(128) k_chain(double2* __restrict__ X, double2* __restrict__ Wk,
 	const double2* __restrict__ fac, const double* __restrict__ S, const int64_t* __restrict__ nta,
-	long step, int jslot, int B, int M, int m0, int N, int L, int np, long nchains)
+	long step, int jslot, int B, int M, int m0, int N, int L, int np, long chbase, long nchains)
 {
+	// chains [chbase, nchains) of this launch (an instance group); nchains is an end index
 	using C = chain_cfg<P, G, CPL>;
 	constexpr int NE = C::NE, LPC = C::LPC, CPW = C::CPW, TPL = C::TPL, PD = C::PD;
 	extern __shared__ double sS[];	// S band [N][P+1]
@@ -111,7 +112,7 @@ __global__ void __launch_bounds__(128) k_chain(double2* __restrict__ X, double2*
 	const unsigned FULL = 0xffffffffu;
 	const int lane = threadIdx.x & 31;
 	const long warp = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-	const long ch0 = warp * CPW;
+	const long ch0 = chbase + warp * CPW;
 	if (ch0 >= nchains) return;
 	// chain descriptors of this warp, once, in shared memory
 	__shared__ long s_x[4][32], s_f[4][32];

@@ -37,6 +37,7 @@
 #include <numeric>
 #include <string>
 #include <time.h>
+#include <cstdlib>
 #include "qpc_chain.cuh"
 
 namespace qpc {
@@ -94,8 +95,9 @@ constexpr int TR = 32;
 
 __global__ void __launch_bounds__(256) k_transform(const double2* __restrict__ src, double2* __restrict__ dst,
 	const double* __restrict__ Vh, int N, int L, int M, int npair, int forward,
-	const int64_t* __restrict__ ntf, long step, int B)
+	const int64_t* __restrict__ ntf, long step, int b0, int B)
 {
+	// instances [b0, b0+B) of this launch (an instance group)
 	extern __shared__ double2 sm[];
 	const int ldt = L | 1;	// odd stride in 16-byte units
 	double2* tin = sm;
@@ -103,10 +105,10 @@ __global__ void __launch_bounds__(256) k_transform(const double2* __restrict__ s
 	int tiles = (N + TR - 1) / TR;
 	long blk = blockIdx.x;
 	int tile = (int)(blk % tiles);
-	long im_inst = blk / tiles;
+	long im_inst = (long)b0 * M + blk / tiles;
 	int m = (int)(im_inst % M);
 	long inst = im_inst / M;
-	if (inst >= B) return;
+	if (inst >= b0 + B) return;
 	if (coupling_power(step, ntf[inst]) == 0) return;
 	int r0 = tile * TR;
 	int nr = min(TR, N - r0);
@@ -181,7 +183,7 @@ __global__ void __launch_bounds__(256) k_transform(const double2* __restrict__ s
 template <int P>
 __global__ void __launch_bounds__(64) k_factor(double2* __restrict__ fac, const double* __restrict__ S, const double* __restrict__ R,
 	const double* __restrict__ lamp, const double* __restrict__ ftab, long ld, const int64_t* __restrict__ ntf,
-	long step0, int K, int B, int Blive, int M, int N, int npair, double dt, int* __restrict__ status)
+	long step0, int K, int B, int b0, int Blive, int M, int N, int npair, double dt, int* __restrict__ status)
 {
 	constexpr int NE = P + 1;
 	long g = (long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -190,7 +192,7 @@ __global__ void __launch_bounds__(64) k_factor(double2* __restrict__ fac, const 
 	int k = (int)(g % npair);
 	long t = g / npair;
 	int m = (int)(t % M); t /= M;
-	long inst = t % Blive;
+	long inst = b0 + t % Blive;
 	int j = (int)(t / Blive);
 	long s = step0 + j;
 	if (coupling_power(s, ntf[inst]) == 0) return;
@@ -321,6 +323,12 @@ struct qpc_lgwz {
 	cudaStream_t stream = nullptr;
 	cudaEvent_t ev0 = nullptr, ev1 = nullptr;	// brackets of qpc_lgwz_run
 	cudaEvent_t evt0 = nullptr, evt1 = nullptr;	// autotuner timing
+	// instance groups advance on their own streams, so that the kernels of one
+	// group fill the FP64 pipes the other group leaves idle
+	static constexpr int MAXNS = 4;
+	int NS = 1;
+	cudaStream_t gs[MAXNS] = {nullptr, nullptr, nullptr, nullptr};
+	cudaEvent_t gev[MAXNS] = {nullptr, nullptr, nullptr, nullptr};
 	double* S = nullptr;      // [N][P+1]
 	double* R = nullptr;      // [N][P+1]
 	double* Vh = nullptr;     // [M][npair+1][L]
@@ -378,11 +386,11 @@ template <class T> int dalloc(T** p, size_t n)
 	return QPC_OK;
 }
 
-int wait_stream(qpc_lgwz* h)
+int wait_on(cudaStream_t st)
 {
 	// bounded wait: poll, give up after ~600 s of wall time
 	for (long it = 0;; ++it) {
-		cudaError_t e = cudaStreamQuery(h->stream);
+		cudaError_t e = cudaStreamQuery(st);
 		if (e == cudaSuccess) return QPC_OK;
 		if (e != cudaErrorNotReady) { set_error("stream error: %s", cudaGetErrorString(e)); return QPC_ERR_CUDA; }
 		if (it > 6000000) { set_error("timed out waiting for the device"); return QPC_ERR_TIMEOUT; }
@@ -390,6 +398,8 @@ int wait_stream(qpc_lgwz* h)
 		nanosleep(&ts, nullptr);
 	}
 }
+
+int wait_stream(qpc_lgwz* h) { return wait_on(h->stream); }
 
 int read_status(qpc_lgwz* h)
 {
@@ -405,18 +415,18 @@ int read_status(qpc_lgwz* h)
 #define LAUNCH(h) ((h)->launches++)
 
 struct prof_scope {
-	qpc_lgwz* h; int kind; int idx = -1;
-	prof_scope(qpc_lgwz* h_, int kind_) : h(h_), kind(kind_)
+	qpc_lgwz* h; int kind; cudaStream_t st; int idx = -1;
+	prof_scope(qpc_lgwz* h_, int kind_, cudaStream_t st_) : h(h_), kind(kind_), st(st_)
 	{
 		if (!h->profiling) return;
 		idx = (int)h->evuse.size() * 2;
 		while ((int)h->evpool.size() < idx + 2) { cudaEvent_t e; cudaEventCreate(&e); h->evpool.push_back(e); }
-		cudaEventRecord(h->evpool[idx], h->stream);
+		cudaEventRecord(h->evpool[idx], st);
 	}
 	~prof_scope()
 	{
 		if (idx < 0) return;
-		cudaEventRecord(h->evpool[idx + 1], h->stream);
+		cudaEventRecord(h->evpool[idx + 1], st);
 		h->evuse.push_back({kind, idx});
 	}
 };
@@ -435,27 +445,29 @@ void collect_profile(qpc_lgwz* h)
 
 // ---------------------------------------------------------------- chain launches
 template <int P, int G, bool CPL>
-void launch_chain_g(qpc_lgwz* h, double2* X, const double2* fac, const int64_t* nta, long step, int jslot, int Blive)
+void launch_chain_g(qpc_lgwz* h, cudaStream_t st, int b0, double2* X, const double2* fac, const int64_t* nta, long step, int jslot, int cnt)
 {
 	using C = chain_cfg<P, G, CPL>;
-	long nchains = CPL ? (long)Blive * h->M * h->npair * 2 : (long)Blive * h->M * h->L;
-	if (nchains <= 0) return;
-	long nwarps = (nchains + C::CPW - 1) / C::CPW;
+	long per = CPL ? (long)h->M * h->npair * 2 : (long)h->M * h->L;
+	long nch = (long)cnt * per;
+	if (nch <= 0) return;
+	long chbase = (long)b0 * per;
+	long nwarps = (nch + C::CPW - 1) / C::CPW;
 	unsigned grid = (unsigned)((nwarps + 3) / 4);
-	k_chain<P, G, CPL><<<grid, 128, h->chain_smem, h->stream>>>(X, h->wk, fac, h->S, nta, step, jslot, h->B, h->M, h->d.m0,
-		h->N, h->L, h->npair, nchains);
+	k_chain<P, G, CPL><<<grid, 128, h->chain_smem, st>>>(X, h->wk, fac, h->S, nta, step, jslot, h->B, h->M, h->d.m0,
+		h->N, h->L, h->npair, chbase, chbase + nch);
 	LAUNCH(h);
 }
 
 template <int P, bool CPL>
-void launch_chain(qpc_lgwz* h, int G, double2* X, const double2* fac, const int64_t* nta, long step, int jslot, int Blive)
+void launch_chain(qpc_lgwz* h, cudaStream_t st, int b0, int G, double2* X, const double2* fac, const int64_t* nta, long step, int jslot, int cnt)
 {
 	switch (G) {
-	case 1: launch_chain_g<P, 1, CPL>(h, X, fac, nta, step, jslot, Blive); break;
-	case 2: if constexpr (P % 2 == 0) launch_chain_g<P, 2, CPL>(h, X, fac, nta, step, jslot, Blive); break;
-	case 3: if constexpr (P % 3 == 0) launch_chain_g<P, 3, CPL>(h, X, fac, nta, step, jslot, Blive); break;
-	case 4: if constexpr (P % 4 == 0) launch_chain_g<P, 4, CPL>(h, X, fac, nta, step, jslot, Blive); break;
-	default: launch_chain_g<P, P, CPL>(h, X, fac, nta, step, jslot, Blive); break;
+	case 1: launch_chain_g<P, 1, CPL>(h, st, b0, X, fac, nta, step, jslot, cnt); break;
+	case 2: if constexpr (P % 2 == 0) launch_chain_g<P, 2, CPL>(h, st, b0, X, fac, nta, step, jslot, cnt); break;
+	case 3: if constexpr (P % 3 == 0) launch_chain_g<P, 3, CPL>(h, st, b0, X, fac, nta, step, jslot, cnt); break;
+	case 4: if constexpr (P % 4 == 0) launch_chain_g<P, 4, CPL>(h, st, b0, X, fac, nta, step, jslot, cnt); break;
+	default: launch_chain_g<P, P, CPL>(h, st, b0, X, fac, nta, step, jslot, cnt); break;
 	}
 }
 
@@ -477,82 +489,113 @@ int live_bucket(int n) { int b = 0; while ((1 << b) < n) ++b; return b; }
 // contents are about to be overwritten) and keep the fastest.  Runs before
 // the step's forward transform, once per (kernel, live bucket).
 template <int P>
-int autotune(qpc_lgwz* h, long step, int jslot, int Bc, int Bf)
+int autotune_one(qpc_lgwz* h, int cpl, long step, int jslot, int Bl)
 {
-	for (int cpl = 0; cpl < 2; ++cpl) {
-		int Bl = cpl ? Bc : Bf;
-		if (Bl <= 0 || (cpl && h->npair == 0)) continue;
-		int bk = live_bucket(Bl);
-		if (h->gsel[cpl][bk]) continue;
-		float best = 1e30f;
-		int bestg = 1;
-		for (int G : h->gcand) {
-			float tot = 0.f;
-			for (int rep = 0; rep < 2; ++rep) {
-				QPC_CUDA(cudaEventRecord(h->evt0, h->stream));
-				if (cpl) launch_chain<P, true>(h, G, h->eo, h->fac, h->ntf, step, jslot, Bl);
-				else launch_chain<P, false>(h, G, h->eo, h->ff, h->ntt, step, 0, Bl);
-				QPC_CUDA(cudaEventRecord(h->evt1, h->stream));
-				if (int rc = wait_stream(h)) return rc;
-				float ms = 0.f;
-				cudaEventElapsedTime(&ms, h->evt0, h->evt1);
-				if (rep) tot += ms;
-			}
-			QPC_CUDA(cudaGetLastError());
-			if (tot < best) { best = tot; bestg = G; }
+	int bk = live_bucket(Bl);
+	if (Bl <= 0 || h->gsel[cpl][bk]) return QPC_OK;
+	float best = 1e30f;
+	int bestg = 1;
+	for (int G : h->gcand) {
+		float tot = 0.f;
+		for (int rep = 0; rep < 2; ++rep) {
+			QPC_CUDA(cudaEventRecord(h->evt0, h->stream));
+			if (cpl) launch_chain<P, true>(h, h->stream, 0, G, h->eo, h->fac, h->ntf, step, jslot, Bl);
+			else launch_chain<P, false>(h, h->stream, 0, G, h->eo, h->ff, h->ntt, step, 0, Bl);
+			QPC_CUDA(cudaEventRecord(h->evt1, h->stream));
+			if (int rc = wait_stream(h)) return rc;
+			float ms = 0.f;
+			cudaEventElapsedTime(&ms, h->evt0, h->evt1);
+			if (rep) tot += ms;
 		}
-		h->gsel[cpl][bk] = bestg;
+		QPC_CUDA(cudaGetLastError());
+		if (tot < best) { best = tot; bestg = G; }
+	}
+	h->gsel[cpl][bk] = bestg;
+	return QPC_OK;
+}
+
+// Autotuner: for a live-instance count not seen before, time every candidate G
+// of the coupling and the field-free chain kernels (two launches each, CUDA
+// events) on scratch buffers (eo, wk and this step's factor slot, whose
+// contents are overwritten before use) and keep the fastest.  Runs with all
+// group streams idle, before the step's forward transforms.
+template <int P>
+int autotune(qpc_lgwz* h, long step, int jslot, const int* Bc, const int* Bf)
+{
+	bool need = false;
+	for (int g = 0; g < h->NS; ++g) {
+		if (Bc[g] > 0 && h->npair > 0 && !h->gsel[1][live_bucket(Bc[g])]) need = true;
+		if (Bf[g] > 0 && !h->gsel[0][live_bucket(Bf[g])]) need = true;
+	}
+	if (!need) return QPC_OK;
+	for (int g = 0; g < h->NS; ++g)
+		if (int rc = wait_on(h->gs[g])) return rc;
+	for (int g = 0; g < h->NS; ++g) {
+		if (h->npair > 0) if (int rc = autotune_one<P>(h, 1, step, jslot, Bc[g])) return rc;
+		if (int rc = autotune_one<P>(h, 0, step, jslot, Bf[g])) return rc;
 	}
 	return QPC_OK;
 }
 
+// All kernels of loop index `step` for the instance group [b0, b0+...) on stream st:
+// Bc instances in their pulse (coupling), Bf with field-free work, factor look-ahead
+// for Bfac instances when do_factor.
 template <int P>
-int launch_step_kernels(qpc_lgwz* h, long step, long step0, int jslot, bool do_factor, int kfac, int Bc, int Bf, int Bfac)
+void launch_group_step(qpc_lgwz* h, cudaStream_t st, int b0, long step, long step0, int jslot, bool do_factor, int kfac,
+	int Bc, int Bf, int Bfac)
 {
 	const int B = h->B, M = h->M, N = h->N, L = h->L, np = h->npair;
 	if (do_factor && np > 0 && Bfac > 0) {
-		prof_scope ps(h, QPC_KERNEL_FACTOR);
+		prof_scope ps(h, QPC_KERNEL_FACTOR, st);
 		long nsys = (long)kfac * Bfac * M * np;
-		k_factor<P><<<(unsigned)((nsys + 63) / 64), 64, 0, h->stream>>>(h->fac, h->S, h->R, h->lamp, h->ftab, h->ld,
-			h->ntf, step0, kfac, B, Bfac, M, N, np, h->dt, h->status);
+		k_factor<P><<<(unsigned)((nsys + 63) / 64), 64, 0, st>>>(h->fac, h->S, h->R, h->lamp, h->ftab, h->ld,
+			h->ntf, step0, kfac, B, b0, Bfac, M, N, np, h->dt, h->status);
 		LAUNCH(h);
 	}
-	if (int rc = autotune<P>(h, step, jslot, Bc, Bf)) return rc;
 	if (Bc > 0 && (np > 0 || (L & 1))) {
 		int tiles = (N + TR - 1) / TR;
 		size_t smem = sizeof(double2) * 2 * TR * (L | 1);
 		unsigned grid = (unsigned)((long)Bc * M * tiles);
 		{
-			prof_scope ps(h, QPC_KERNEL_TRANSFORM_FWD);
-			k_transform<<<grid, 256, smem, h->stream>>>(h->st, h->eo, h->Vh, N, L, M, np, 1, h->ntf, step, Bc);
+			prof_scope ps(h, QPC_KERNEL_TRANSFORM_FWD, st);
+			k_transform<<<grid, 256, smem, st>>>(h->st, h->eo, h->Vh, N, L, M, np, 1, h->ntf, step, b0, Bc);
 			LAUNCH(h);
 		}
 		if (np > 0) {
-			prof_scope ps(h, QPC_KERNEL_SWEEP);
-			launch_chain<P, true>(h, h->gsel[1][live_bucket(Bc)], h->eo, h->fac, h->ntf, step, jslot, Bc);
+			prof_scope ps(h, QPC_KERNEL_SWEEP, st);
+			launch_chain<P, true>(h, st, b0, h->gsel[1][live_bucket(Bc)], h->eo, h->fac, h->ntf, step, jslot, Bc);
 		}
 		{
-			prof_scope ps(h, QPC_KERNEL_TRANSFORM_BWD);
-			k_transform<<<grid, 256, smem, h->stream>>>(h->eo, h->st, h->Vh, N, L, M, np, 0, h->ntf, step, Bc);
+			prof_scope ps(h, QPC_KERNEL_TRANSFORM_BWD, st);
+			k_transform<<<grid, 256, smem, st>>>(h->eo, h->st, h->Vh, N, L, M, np, 0, h->ntf, step, b0, Bc);
 			LAUNCH(h);
 		}
 	}
 	if (Bf > 0) {
-		prof_scope ps(h, QPC_KERNEL_FIELDFREE);
-		launch_chain<P, false>(h, h->gsel[0][live_bucket(Bf)], h->st, h->ff, h->ntt, step, 0, Bf);
+		prof_scope ps(h, QPC_KERNEL_FIELDFREE, st);
+		launch_chain<P, false>(h, st, b0, h->gsel[0][live_bucket(Bf)], h->st, h->ff, h->ntt, step, 0, Bf);
 	}
+}
+
+template <int P>
+int launch_step_t(qpc_lgwz* h, long step, long step0, int jslot, bool do_factor, int kfac, const int* gb,
+	const int* Bc, const int* Bf)
+{
+	if (int rc = autotune<P>(h, step, jslot, Bc, Bf)) return rc;
+	for (int g = 0; g < h->NS; ++g)
+		launch_group_step<P>(h, h->gs[g], gb[g], step, step0, jslot, do_factor, kfac, Bc[g], Bf[g], Bc[g]);
 	return QPC_OK;
 }
 
-int launch_step(qpc_lgwz* h, long step, long step0, int jslot, bool do_factor, int kfac, int Bc, int Bf, int Bfac)
+int launch_step(qpc_lgwz* h, long step, long step0, int jslot, bool do_factor, int kfac, const int* gb, const int* Bc, const int* Bf)
 {
 	switch (h->P) {
-	case 3: return launch_step_kernels<3>(h, step, step0, jslot, do_factor, kfac, Bc, Bf, Bfac);
-	case 4: return launch_step_kernels<4>(h, step, step0, jslot, do_factor, kfac, Bc, Bf, Bfac);
-	case 5: return launch_step_kernels<5>(h, step, step0, jslot, do_factor, kfac, Bc, Bf, Bfac);
-	case 6: return launch_step_kernels<6>(h, step, step0, jslot, do_factor, kfac, Bc, Bf, Bfac);
-	case 7: return launch_step_kernels<7>(h, step, step0, jslot, do_factor, kfac, Bc, Bf, Bfac);
-	case 8: return launch_step_kernels<8>(h, step, step0, jslot, do_factor, kfac, Bc, Bf, Bfac);
+	case 3: return launch_step_t<3>(h, step, step0, jslot, do_factor, kfac, gb, Bc, Bf);
+	case 4: return launch_step_t<4>(h, step, step0, jslot, do_factor, kfac, gb, Bc, Bf);
+	case 5: return launch_step_t<5>(h, step, step0, jslot, do_factor, kfac, gb, Bc, Bf);
+	case 6: return launch_step_t<6>(h, step, step0, jslot, do_factor, kfac, gb, Bc, Bf);
+	case 7: return launch_step_t<7>(h, step, step0, jslot, do_factor, kfac, gb, Bc, Bf);
+	case 8: return launch_step_t<8>(h, step, step0, jslot, do_factor, kfac, gb, Bc, Bf);
 	default: set_error("unsupported B-spline degree %d", h->P); return QPC_ERR_ARGS;
 	}
 }
@@ -612,6 +655,12 @@ int qpc_lgwz_create(const qpc_dims* dims, double dt, const double* S, const doub
 	auto fail = [&](int code) { qpc_lgwz_destroy(h); return code; };
 	if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) { set_error("stream create"); return fail(QPC_ERR_CUDA); }
 	cudaEventCreate(&h->ev0); cudaEventCreate(&h->ev1); cudaEventCreate(&h->evt0); cudaEventCreate(&h->evt1);
+	h->NS = d.n_inst >= 2 ? 2 : 1;
+	if (const char* e = getenv("QPC_STREAMS")) h->NS = std::max(1, std::min(qpc_lgwz::MAXNS, std::min(d.n_inst, atoi(e))));
+	for (int g = 0; g < h->NS; ++g) {
+		if (cudaStreamCreateWithFlags(&h->gs[g], cudaStreamNonBlocking) != cudaSuccess) { set_error("stream create"); return fail(QPC_ERR_CUDA); }
+		cudaEventCreateWithFlags(&h->gev[g], cudaEventDisableTiming);
+	}
 	// host setup: field-free LDL^T per l, Y10 eigensystems
 	std::vector<double2> ffh((size_t)N * NE * h->nlh);
 	std::vector<double> Lrow((size_t)N * P * 2), Dinv((size_t)N * 2);
@@ -683,6 +732,10 @@ int qpc_lgwz_destroy(qpc_lgwz* h)
 	cudaFree(h->st); cudaFree(h->eo); cudaFree(h->wk); cudaFree(h->hostlay); cudaFree(h->fac);
 	cudaFree(h->status); cudaFree(h->red); cudaFree(h->ntf); cudaFree(h->ntt); cudaFree(h->ftab);
 	for (auto e : h->evpool) cudaEventDestroy(e);
+	for (int g = 0; g < qpc_lgwz::MAXNS; ++g) {
+		if (h->gs[g]) { cudaStreamSynchronize(h->gs[g]); cudaStreamDestroy(h->gs[g]); }
+		if (h->gev[g]) cudaEventDestroy(h->gev[g]);
+	}
 	if (h->evt0) cudaEventDestroy(h->evt0);
 	if (h->evt1) cudaEventDestroy(h->evt1);
 	if (h->ev0) cudaEventDestroy(h->ev0);
@@ -781,16 +834,46 @@ int qpc_lgwz_run(qpc_lgwz* h, const double* ftab, int64_t ld, const int64_t* nt_
 	QPC_CUDA(cudaMemsetAsync(h->status, 0, sizeof(int), h->stream));
 	if (!ident) if (int rc = permute_instances(h, perm, false)) return rc;
 	h->ld = anyfield ? (long)ld : 0;
-	// live prefixes per step: coupling (nt_field >= s, nt_field > 0) and field-free (nt_total > s)
-	auto coupling_live = [&](long s) { int n = 0; while (n < B && pf[n] > 0 && pf[n] >= s) ++n; return n; };
-	auto free_live = [&](long s) { int n = B; while (n > 0 && pt[n - 1] <= s) --n; return n; };
+	// Instance groups (contiguous in the sorted order, balanced by work) on their
+	// own streams; within a group, the instances still in their pulse at step s
+	// are a prefix, and the field-free ones lie below a bound.
+	const int NS = h->NS;
+	std::vector<int> gb(NS + 1, 0);
+	{
+		double tot = 0.0;
+		for (int k = 0; k < B; ++k) tot += (double)pt[k] + 2.0 * pf[k];
+		double acc = 0.0;
+		int g = 1;
+		for (int k = 0; k < B && g < NS; ++k) {
+			acc += (double)pt[k] + 2.0 * pf[k];
+			if (acc >= tot * g / NS) gb[g++] = k + 1;
+		}
+		for (; g < NS; ++g) gb[g] = B;
+		gb[NS] = B;
+		for (int q = 1; q <= NS; ++q) gb[q] = std::max(gb[q], gb[q - 1]);
+	}
+	std::vector<int> Bc(NS), Bf(NS);
+	auto live_counts = [&](long s) {
+		for (int g = 0; g < NS; ++g) {
+			int n = 0;
+			while (gb[g] + n < gb[g + 1] && pf[gb[g] + n] > 0 && pf[gb[g] + n] >= s) ++n;
+			int f = gb[g + 1] - gb[g];
+			while (f > 0 && pt[gb[g] + f - 1] <= s) --f;
+			Bc[g] = n; Bf[g] = f;
+		}
+	};
 	QPC_CUDA(cudaEventRecord(h->ev0, h->stream));
+	for (int g = 0; g < NS; ++g) QPC_CUDA(cudaStreamWaitEvent(h->gs[g], h->ev0, 0));
 	for (long s = 0; s < smax; ++s) {
 		// factors for steps s .. s+K-1 are computed together, into slots 0..K-1
 		int j = (int)(s % h->K);
 		long kf = std::min<long>(h->K, smax - s);
-		int Bc = coupling_live(s), Bf = free_live(s);
-		if (int rc = launch_step(h, s, s - j, j, j == 0, (int)kf, Bc, Bf, Bc)) return rc;
+		live_counts(s);
+		if (int rc = launch_step(h, s, s - j, j, j == 0, (int)kf, gb.data(), Bc.data(), Bf.data())) return rc;
+	}
+	for (int g = 0; g < NS; ++g) {
+		QPC_CUDA(cudaEventRecord(h->gev[g], h->gs[g]));
+		QPC_CUDA(cudaStreamWaitEvent(h->stream, h->gev[g], 0));
 	}
 	QPC_CUDA(cudaEventRecord(h->ev1, h->stream));
 	QPC_CUDA(cudaGetLastError());
