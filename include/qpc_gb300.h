@@ -178,6 +178,32 @@ int qpc_lgwz_set_profiling(qpc_lgwz* h, int on);
 int qpc_lgwz_get_tuning(qpc_lgwz* h, int32_t* out);
 int qpc_lgwz_kernel_times(qpc_lgwz* h, double* ms, int64_t* launches);
 
+/* ---------------------------------------------------------------- no device allocation
+ * No counterpart in the reference (it has no device code).  For callers that
+ * cannot call cudaMalloc -- a framework that owns every device allocation
+ * through its own pool, code running while a stream is being captured, or an
+ * embedding with a fixed device-memory budget -- this entry point performs the
+ * field-free Crank-Nicolson step propagate(coef) of cn_1e.hpp:615-618 on
+ * buffers the caller owns, and allocates nothing: its scratch is a fixed array
+ * of 2 * QPC_NOALLOC_MAX_ELEMS complex128 values (32 MiB) compiled into the
+ * library, which every GPU that loads the library holds until the process exits.
+ *   coef  device, [n_inst][n_m][n_l][n_r] complex128, in/out
+ *   S     device, [n_r][p+1] overlap band
+ *   ffac  device, [lmax+1][n_r][p+1] complex128: the LDL^T factors of S + i dt/2 H_l,
+ *         entries 0..p-1 of row r = L(r, r-1-c) and entry p = 1/D(r)
+ *         (what qpc_ldlt_csym returns, packed per l)
+ *   stream  a cudaStream_t (NULL = legacy default stream); the call only enqueues work
+ * Limit: n_inst*n_m*n_l*n_r + ceil(n_inst/2) <= QPC_NOALLOC_MAX_ELEMS, otherwise
+ * QPC_ERR_ARGS with a message.  The first call on a device looks up the
+ * scratch's device address (cudaGetSymbolAddress) with that device current;
+ * make that first call before any stream capture.  All calls on a device share
+ * the one scratch array and it keeps the previous call's contents, so calls
+ * that overlap on the GPU (different streams or host threads) race: serialise
+ * them.  Nothing in the scratch needs to start at zero: every call writes what
+ * it later reads. */
+#define QPC_NOALLOC_MAX_ELEMS (1L << 20)
+int qpc_fieldfree_noalloc(const qpc_dims* dims, const double* S, const double* ffac, double* coef, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

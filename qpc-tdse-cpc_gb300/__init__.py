@@ -32,8 +32,9 @@ EXPORTS = (
     "qpc_lgwz_destroy", "qpc_lgwz_put", "qpc_lgwz_get", "qpc_lgwz_put_device", "qpc_lgwz_get_device",
     "qpc_lgwz_propagate", "qpc_lgwz_propagate_free", "qpc_lgwz_run", "qpc_lgwz_norm", "qpc_lgwz_dipole",
     "qpc_lgwz_projection", "qpc_lgwz_last_run_ms", "qpc_lgwz_launch_count", "qpc_lgwz_set_profiling",
-    "qpc_lgwz_kernel_times", "qpc_lgwz_get_tuning",
+    "qpc_lgwz_kernel_times", "qpc_lgwz_get_tuning", "qpc_fieldfree_noalloc",
 )
+NOALLOC_MAX_ELEMS = 1 << 20
 KERNELS = ("factor", "transform_fwd", "sweep", "transform_bwd", "fieldfree")
 
 
@@ -95,6 +96,7 @@ def load(path=None):
         "qpc_lgwz_set_profiling": (ctypes.c_int, [P, ctypes.c_int]),
         "qpc_lgwz_kernel_times": (ctypes.c_int, [P, P, P]),
         "qpc_lgwz_get_tuning": (ctypes.c_int, [P, P]),
+        "qpc_fieldfree_noalloc": (ctypes.c_int, [P, P, P, P, P]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -197,6 +199,27 @@ def intensity_to_e0(intensity_wcm2):
 def wavelength_to_w0(lambda_nm):
     """omega [a.u.] = 45.5633525 / lambda[nm]."""
     return 45.5633525 / lambda_nm
+
+
+def fieldfree_factors(S, H, dt, lmax):
+    """Host-packed LDL^T factors of S + i dt/2 H_l for l = 0..lmax, [lmax+1][n_r][p+1]
+    complex128 (L(r, r-1-c) for c < p, 1/D(r) last), as qpc_fieldfree_noalloc takes them."""
+    n_r, ne = S.shape
+    p = ne - 1
+    out = np.zeros((lmax + 1, n_r, ne), complex)
+    for l in range(lmax + 1):
+        Lrow, Dinv, bad = ldlt_csym(S, H[l], dt * 0.5)
+        if bad:
+            raise QpcError(4, "zero pivot factorising S + i dt/2 H_%d" % l)
+        out[l, :, :p] = Lrow
+        out[l, :, p] = Dinv
+    return out
+
+
+def fieldfree_noalloc(dims, S_dev, ffac_dev, coef_dev, stream=0):
+    """qpc_fieldfree_noalloc on caller-owned device buffers (raw device pointers)."""
+    _check(load().qpc_fieldfree_noalloc(ctypes.byref(dims), ctypes.c_void_p(S_dev), ctypes.c_void_p(ffac_dev),
+                                        ctypes.c_void_p(coef_dev), ctypes.c_void_p(stream)))
 
 
 # ------------------------------------------------------------------ propagator
