@@ -124,6 +124,25 @@ def chain_flops(n_r, p, chains, power):
     return chains * n_r * power * 2 * per_part
 
 
+def path_flops(n_r, p, n_l, power=2):
+    """FP64 flops of one wavefunction-step of the batched run (FMA = 2): coupling
+    chains (n_l - n_l%2 chains, M^2), field-free chains (n_l), the complex-symmetric
+    LDL^T of each channel pair (~217 flops per row) and both l-space transforms."""
+    npair = n_l // 2
+    chains_c = chain_flops(n_r, p, 2 * npair, power)
+    chains_f = chain_flops(n_r, p, n_l, 1)
+    factor = npair * n_r * (4 * p * (p + 1) // 2 * 2 + 6 * p + 13)
+    even, odd = (n_l + 1) // 2, n_l // 2
+    fwd = npair * (2 * 2 * (even + odd) + 4) + (n_l % 2) * 2 * 2 * even
+    bwd = even * 2 * 2 * (npair + n_l % 2) + odd * 2 * 2 * npair
+    return chains_c + chains_f + factor + n_r * (fwd + bwd)
+
+
+# DRAM bytes per chain-row of the coupling chain kernel (both applications), from the
+# ncu capture summarised in profiles/k_chain_c2.md
+TRAFFIC_PER_CHAIN_ROW = None
+
+
 def run_engine(args):
     import importlib
     q = importlib.import_module("qpc-tdse-cpc_gb300")
@@ -164,23 +183,34 @@ def run_engine(args):
     state_bytes = state0.nbytes
     h2d = (state_bytes + ftab[:, W:W + K + 1].nbytes) / K
     d2h = state_bytes / K
-    # dominant kernel: coupling sweeps
+    # dominant kernel: the coupling chains.  Its launches in the timed region cover
+    # all live instances once per step (split over the instance-group streams), so
+    # the flops of one launch are the step's coupling flops over the launches per step.
     sw_ms, sw_n = ktimes.get("sweep", (0.0, 0))
     live_pairs = B * (n_l // 2)
-    fl = chain_flops(n_r, p, 2 * live_pairs, 2)
-    achieved = fl / (sw_ms / max(sw_n, 1) * 1e-3) / 1e12 if sw_n else None
+    launches_per_step = max(sw_n / max(K, 1), 1.0)
+    fl_step = chain_flops(n_r, p, 2 * live_pairs, 2)
+    fl = fl_step / launches_per_step
+    launch_ms = sw_ms / max(sw_n, 1) if sw_n else None
+    achieved = fl / (launch_ms * 1e-3) / 1e12 if sw_n else None
     peaks = load_peaks()
-    # algorithmic bytes of one coupling-chain launch: the pair's factors (p+1 complex per row)
-    # read twice per application, each chain's eigen-basis vector read and written once per
-    # application and its work vector written/read by the five passes
-    sweep_bytes = live_pairs * n_r * 2 * ((p + 1) * 16 * 2 + 2 * 16 * 2 + 2 * 16 * 5)
-    roof = {"bound": "fp64", "kernel": "k_chain (coupling)", "achieved": achieved, "peak": FP64_PEAK_TFLOPS,
-            "unit": "TFLOP/s", "frac": (achieved / FP64_PEAK_TFLOPS) if achieved else None,
-            "peak_source": "measured DFMA peak, profiles/fp64_peak_gb300.md",
-            "flops_per_launch": fl, "launch_ms": sw_ms / max(sw_n, 1) if sw_n else None,
-            "traffic": None,
-            "hbm": {"achieved_gbs": sweep_bytes / (sw_ms / max(sw_n, 1) * 1e-3) / 1e9 if sw_n else None,
-                    "peak_gbs": peaks.get("hbm_gbs"), "bytes_per_launch": sweep_bytes}}
+    # algorithmic bytes of the coupling chains per step: each pair's factors (p+1
+    # complex per row) read twice per application, each chain's eigen-basis vector
+    # read and written once per application, its work vector through the five passes
+    sweep_bytes = live_pairs * n_r * 2 * ((p + 1) * 16 * 2 + 2 * 16 * 2 + 2 * 16 * 5) / launches_per_step
+    # the whole step: every kernel's FP64 flops per wavefunction-step
+    step_flops = path_flops(n_r, p, n_l) * B
+    path_tflops = step_flops / (dev_ms / K * 1e-3) / 1e12
+    roof = {"bound": "fp64", "kernel": "k_chain<6,G,coupling> (coupling CN chains)", "achieved": achieved,
+            "peak": FP64_PEAK_TFLOPS, "unit": "TFLOP/s", "frac": (achieved / FP64_PEAK_TFLOPS) if achieved else None,
+            "peak_source": "measured DFMA peak, profiles/fp64_peak_gb300.md (MEASURED_PEAKS.json has no FP64 figure)",
+            "flops_per_launch": fl, "launch_ms": launch_ms, "concurrent_streams": launches_per_step,
+            "traffic": (TRAFFIC_PER_CHAIN_ROW * 2 * live_pairs * n_r / launches_per_step) if TRAFFIC_PER_CHAIN_ROW else None,
+            "traffic_source": "ncu dram__bytes_read+write of k_chain coupling launches, profiles/k_chain_c2.md, scaled by chain-rows",
+            "hbm": {"achieved_gbs": sweep_bytes / (launch_ms * 1e-3) / 1e9 if sw_n else None,
+                    "peak_gbs": peaks.get("hbm_gbs"), "bytes_per_launch": sweep_bytes},
+            "path": {"flops_per_wf_step": path_flops(n_r, p, n_l), "achieved_tflops": path_tflops,
+                     "frac": path_tflops / FP64_PEAK_TFLOPS}}
     if roof["hbm"]["achieved_gbs"] and peaks.get("hbm_gbs"):
         roof["hbm"]["frac"] = roof["hbm"]["achieved_gbs"] / peaks["hbm_gbs"]
     kt = {k: {"ms_total": v[0], "launches": v[1]} for k, v in ktimes.items()}
