@@ -140,7 +140,7 @@ def path_flops(n_r, p, n_l, power=2):
 
 # DRAM bytes per chain-row of the coupling chain kernel (both applications), from the
 # ncu capture summarised in profiles/k_chain_c2.md
-TRAFFIC_PER_CHAIN_ROW = None
+TRAFFIC_PER_CHAIN_ROW = 84.0
 
 
 def run_engine(args):

@@ -141,6 +141,13 @@ int qpc_lgwz_propagate_free(qpc_lgwz* h);
  * (within rounding: consecutive coupling half-steps are fused). */
 int qpc_lgwz_run(qpc_lgwz* h, const double* ftab, int64_t ld, const int64_t* nt_field, const int64_t* nt_total);
 
+/* qpc_lgwz_run that also records, for every instance k and step s < nt_total[k],
+ * zlist[k*ldz + s] = Re <psi_k(t_s)| f(r) cos(theta) |psi_k(t_s)> with F = <Bi|f|Bj>
+ * ([n_r][p+1]; f(r) = r gives the dipole), the observation the driver makes before
+ * each step (obsv::observe, binsrc/sphTDSE.cpp:515-521 and 794).  ldz >= max nt_total. */
+int qpc_lgwz_run_dipole(qpc_lgwz* h, const double* ftab, int64_t ld, const int64_t* nt_field, const int64_t* nt_total,
+	const double* F, double* zlist, int64_t ldz);
+
 /* S-norm per instance, sum over (m,l) of c^H S c
  * (operator_rsym::observe, spherical/operators/1e.hpp:69-89); norm[n_inst]. */
 int qpc_lgwz_norm(qpc_lgwz* h, double* norm);

@@ -34,6 +34,7 @@
 #include <string>
 #include <vector>
 #include <cstring>
+#include <cstdlib>
 
 using namespace qpc;
 using namespace qpc::spherical;
@@ -164,14 +165,21 @@ static int cmd_propagate(int argc, char** argv)
 		std::memcpy((double*)coef.data, v.data(), sizeof(double) * v.size());
 	}
 	std::vector<double> f = nt ? slurp(field, nt + 1) : std::vector<double>{};
+	// optional per-step observation, as the driver does before each step (sphTDSE.cpp:794)
+	const bool record = std::getenv("QPC_REF_RECORD_Z") != nullptr;
+	auto obs_rec = observable_z<dims_t>();
+	if (record) obs_rec.initialize(radi, angu);
+	std::vector<double> zl;
 	auto clock = timer();
 	clock.tic();
 	for (size_t it = 0; it < nt + nfree; ++it) {
+		if (record) zl.push_back(obs_rec.observe(coef.data, coef.data)[0]);
 		if (it < nt) prop.propagate(coef, f[it], f[it + 1]);
 		else prop.propagate(coef);
 	}
 	clock.toc();
 	double secs = clock.get();
+	if (record) dump(out, "zlist", zl.data(), zl.size());
 	double norm = 0.0;
 	#pragma omp parallel
 	{

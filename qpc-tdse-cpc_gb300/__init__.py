@@ -32,7 +32,7 @@ EXPORTS = (
     "qpc_lgwz_destroy", "qpc_lgwz_put", "qpc_lgwz_get", "qpc_lgwz_put_device", "qpc_lgwz_get_device",
     "qpc_lgwz_propagate", "qpc_lgwz_propagate_free", "qpc_lgwz_run", "qpc_lgwz_norm", "qpc_lgwz_dipole",
     "qpc_lgwz_projection", "qpc_lgwz_last_run_ms", "qpc_lgwz_launch_count", "qpc_lgwz_set_profiling",
-    "qpc_lgwz_kernel_times", "qpc_lgwz_get_tuning", "qpc_fieldfree_noalloc",
+    "qpc_lgwz_kernel_times", "qpc_lgwz_get_tuning", "qpc_fieldfree_noalloc", "qpc_lgwz_run_dipole",
 )
 NOALLOC_MAX_ELEMS = 1 << 20
 KERNELS = ("factor", "transform_fwd", "sweep", "transform_bwd", "fieldfree")
@@ -97,6 +97,7 @@ def load(path=None):
         "qpc_lgwz_kernel_times": (ctypes.c_int, [P, P, P]),
         "qpc_lgwz_get_tuning": (ctypes.c_int, [P, P]),
         "qpc_fieldfree_noalloc": (ctypes.c_int, [P, P, P, P, P]),
+        "qpc_lgwz_run_dipole": (ctypes.c_int, [P, P, i64, P, P, P, P, i64]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -297,6 +298,24 @@ class propagator_cn_hc_lgwz:
         if ftab.shape[0] != self.shape[0]:
             ftab = _f64(np.broadcast_to(ftab, (self.shape[0], ftab.shape[1])))
         _check(load().qpc_lgwz_run(self._h, _ptr(ftab), ftab.shape[1], _ptr(nt_field), _ptr(nt_total)))
+
+    def run_dipole(self, ftab, nt_field, nt_total, F):
+        """run() that also returns zlist[inst, s] = <psi(t_s)| f(r) cos(theta) |psi(t_s)>
+        for s < nt_total[inst] (F = <B|f|B>, f(r) = r for the dipole)."""
+        nt_field = np.ascontiguousarray(np.broadcast_to(nt_field, (self.shape[0],)), dtype=np.int64)
+        nt_total = np.ascontiguousarray(np.broadcast_to(nt_total, (self.shape[0],)), dtype=np.int64)
+        ldz = int(max(1, nt_total.max()))
+        z = np.zeros((self.shape[0], ldz))
+        if ftab is None:
+            tab, ld = None, 1
+        else:
+            tab = _f64(np.atleast_2d(ftab))
+            if tab.shape[0] != self.shape[0]:
+                tab = _f64(np.broadcast_to(tab, (self.shape[0], tab.shape[1])))
+            ld = tab.shape[1]
+        _check(load().qpc_lgwz_run_dipole(self._h, _ptr(tab), ld, _ptr(nt_field), _ptr(nt_total),
+                                          _ptr(_f64(F)), _ptr(z), ldz))
+        return z
 
     def last_run_ms(self):
         v = ctypes.c_double(0)

@@ -101,9 +101,13 @@ __device__ __forceinline__ void msub_operands(double vr, double vi, int part, do
 template <int P, int G, bool CPL>
 __global__ void __launch_bounds__(128) k_chain(double2* __restrict__ X, double2* __restrict__ Wk,
 	const double2* __restrict__ fac, const double* __restrict__ S, const int64_t* __restrict__ nta,
-	long step, int jslot, int B, int M, int m0, int N, int L, int np, long chbase, long nchains)
+	long step, int jslot, int B, int M, int m0, int N, int L, int np, long chbase, long nchains,
+	const double* __restrict__ Fo = nullptr, double* __restrict__ obs = nullptr)
 {
-	// chains [chbase, nchains) of this launch (an instance group); nchains is an end index
+	// chains [chbase, nchains) of this launch (an instance group); nchains is an end index.
+	// Fo/obs (coupling chains only, optional): obs[chain] = <z|F|z> of the chain's vector at
+	// the point where it represents the wavefunction at t_step -- before the first
+	// application at step 0, after the first of two applications otherwise.
 	using C = chain_cfg<P, G, CPL>;
 	constexpr int NE = C::NE, LPC = C::LPC, CPW = C::CPW, TPL = C::TPL, PD = C::PD;
 	extern __shared__ double sS[];	// S band [N][P+1]
@@ -142,7 +146,43 @@ __global__ void __launch_bounds__(128) k_chain(double2* __restrict__ X, double2*
 	const double2* fs = fac + ds.foff;
 	double* ws = Wd + 2 * ds.xoff + ps;
 
+	// observation pass: every lane has a fixed (chain, part) when CPW divides 16
+	auto observe = [&](int app, int pos) {
+		if constexpr (CPL && (16 % CPW == 0)) {
+			double acc = 0.0;
+			for (int base = 0; base < N * CPW * 2; base += 32) {
+				int it = base + lane;
+				int part = it & 1, cl = (it >> 1) % CPW, r = (it >> 1) / CPW;
+				if (it < N * CPW * 2) {
+					chain_desc d = desc(cl);
+					bool on = d.a > 0 && app == 0 && ((pos == 0 && step == 0) || (pos == 1 && d.a == 2));
+					if (on) {
+						const double* z = Xd + 2 * d.xoff + part;
+						double t = 0.0;
+#pragma unroll
+						for (int k = P; k >= 1; --k)
+							if (r - k >= 0) t = fma(__ldg(Fo + (r - k) * NE + k), z[(long)(r - k) * rs], t);
+#pragma unroll
+						for (int k = 0; k <= P; ++k)
+							if (r + k < N) t = fma(__ldg(Fo + r * NE + k), z[(long)(r + k) * rs], t);
+						acc = fma(z[(long)r * rs], t, acc);
+					}
+				}
+			}
+			// lanes of one chain differ in bit 0 (part) and in the bits above log2(CPW)+1
+			for (int mk = 2 * CPW; mk < 32; mk <<= 1) acc += __shfl_xor_sync(FULL, acc, mk);
+			acc += __shfl_xor_sync(FULL, acc, 1);
+			if (lane < 2 * CPW && !(lane & 1)) {
+				int cl = lane >> 1;
+				chain_desc d = desc(cl);
+				bool on = d.a > 0 && app == 0 && ((pos == 0 && step == 0) || (pos == 1 && d.a == 2));
+				if (on) obs[ch0 + cl] = acc;
+			}
+		}
+	};
+
 	for (int app = 0; app < amax; ++app) {
+		if (obs && app == 0) { observe(0, 0); __syncwarp(); }
 		// ---- P1: w = S z  (items: row r, chain cl, part)
 		for (int base = 0; base < N * CPW * 2; base += 32) {
 			int it = base + lane;
@@ -306,6 +346,7 @@ __global__ void __launch_bounds__(128) k_chain(double2* __restrict__ X, double2*
 			}
 		}
 		__syncwarp();
+		if (obs && app == 0) { observe(0, 1); __syncwarp(); }
 	}
 }
 

@@ -301,6 +301,63 @@ __global__ void k_projection(const double2* __restrict__ st, const double* __res
 	proj[poff[ch] + n] = make_double2(re, im);
 }
 
+// In-loop dipole, l basis: per channel of instances with nt_field <= step < nt_total,
+// dl = 2 y10(m,il) Re <c_il|F|c_il+1>  (observable_z::observe, observable/1e.hpp:26-50)
+__global__ void k_dipole_lbasis(const double2* __restrict__ st, const double* __restrict__ F, const double* __restrict__ y10,
+	const int64_t* __restrict__ ntf, const int64_t* __restrict__ ntt, long step, int b0, int cnt, int M, int N, int L, int NE,
+	double* __restrict__ dl)
+{
+	long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+	if (t >= (long)cnt * M * L) return;
+	long ch = (long)b0 * M * L + t;
+	int il = (int)(ch % L);
+	long im_inst = ch / L;
+	int m = (int)(im_inst % M);
+	long inst = im_inst / M;
+	if (!(step >= ntf[inst] && step < ntt[inst])) return;
+	double v = 0.0;
+	if (il + 1 < L) {
+		const double2* x = st + im_inst * (long)N * L + il;
+		const double2* y = x + 1;
+		double re = 0.0;
+		for (int r = 0; r < N; ++r) {
+			double tr = 0.0, ti = 0.0;
+			for (int k = NE - 1; k >= 1; --k)
+				if (r - k >= 0) { double a = __ldg(F + (long)(r - k) * NE + k); double2 w = y[(long)(r - k) * L]; tr = fma(a, w.x, tr); ti = fma(a, w.y, ti); }
+			for (int k = 0; k < NE && r + k < N; ++k) { double a = __ldg(F + (long)r * NE + k); double2 w = y[(long)(r + k) * L]; tr = fma(a, w.x, tr); ti = fma(a, w.y, ti); }
+			double2 c = x[(long)r * L];
+			re = fma(c.x, tr, fma(c.y, ti, re));
+		}
+		v = 2.0 * y10[m * L + il] * re;
+	}
+	dl[ch] = v;
+}
+
+// Per instance of [b0, b0+cnt) with step < nt_total: the dipole at t_step, from the
+// eigen-basis observation of the coupling chains (sum_k s_k (<z+|F|z+> - <z-|F|z->))
+// while the instance is in its pulse, from the l-basis terms otherwise; fixed
+// summation order.
+__global__ void k_dipole_combine(const double* __restrict__ obs, const double* __restrict__ dl, const double* __restrict__ lamp,
+	const int64_t* __restrict__ ntf, const int64_t* __restrict__ ntt, long step, int b0, int cnt, int M, int L, int np,
+	double* __restrict__ zdev, long ldz)
+{
+	int t = blockIdx.x * blockDim.x + threadIdx.x;
+	if (t >= cnt) return;
+	long inst = b0 + t;
+	if (step >= ntt[inst] && !(ntf[inst] > 0 && step < ntf[inst])) return;
+	double v = 0.0;
+	if (ntf[inst] > 0 && step < ntf[inst]) {
+		for (int m = 0; m < M; ++m)
+			for (int k = 0; k < np; ++k) {
+				long c = ((inst * M + m) * np + k) * 2;
+				v += lamp[m * np + k] * (obs[c] - obs[c + 1]);
+			}
+	} else {
+		for (long c = inst * M * L; c < (inst + 1) * M * L; ++c) v += dl[c];
+	}
+	zdev[inst * ldz + step] = v;
+}
+
 __global__ void k_status_check(const double2* __restrict__ st, long n, int* __restrict__ status)
 {
 	long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -342,6 +399,15 @@ struct qpc_lgwz {
 	int K = 1;
 	int* status = nullptr;
 	double2* red = nullptr;   // reduction scratch [2*B*M*L]
+	// in-loop dipole (qpc_lgwz_run_dipole)
+	double* obsF = nullptr;   // device band of <B|f|B> [N][P+1]
+	double* obs = nullptr;    // per coupling chain [B][M][npair][2]
+	double* dl = nullptr;     // per channel [B][M][L]
+	double* y10d = nullptr;   // [M][L]
+	double* zdev = nullptr;   // [B][ldz]
+	size_t zcap = 0;
+	long ldz = 0;
+	bool observing = false;
 	int64_t* ntf = nullptr;   // device [B]
 	int64_t* ntt = nullptr;
 	double* ftab = nullptr;   // device field table [B][ld]
@@ -454,8 +520,9 @@ void launch_chain_g(qpc_lgwz* h, cudaStream_t st, int b0, double2* X, const doub
 	long chbase = (long)b0 * per;
 	long nwarps = (nch + C::CPW - 1) / C::CPW;
 	unsigned grid = (unsigned)((nwarps + 3) / 4);
+	bool ob = CPL && h->observing;
 	k_chain<P, G, CPL><<<grid, 128, h->chain_smem, st>>>(X, h->wk, fac, h->S, nta, step, jslot, h->B, h->M, h->d.m0,
-		h->N, h->L, h->npair, chbase, chbase + nch);
+		h->N, h->L, h->npair, chbase, chbase + nch, ob ? h->obsF : nullptr, ob ? h->obs : nullptr);
 	LAUNCH(h);
 }
 
@@ -495,6 +562,9 @@ int autotune_one(qpc_lgwz* h, int cpl, long step, int jslot, int Bl)
 	if (Bl <= 0 || h->gsel[cpl][bk]) return QPC_OK;
 	float best = 1e30f;
 	int bestg = 1;
+	const bool obs_saved = h->observing;
+	h->observing = false;	// trials write nothing but scratch
+	struct restore { qpc_lgwz* h; bool v; ~restore() { h->observing = v; } } rs{h, obs_saved};
 	for (int G : h->gcand) {
 		float tot = 0.f;
 		for (int rep = 0; rep < 2; ++rep) {
@@ -569,6 +639,18 @@ void launch_group_step(qpc_lgwz* h, cudaStream_t st, int b0, long step, long ste
 			prof_scope ps(h, QPC_KERNEL_TRANSFORM_BWD, st);
 			k_transform<<<grid, 256, smem, st>>>(h->eo, h->st, h->Vh, N, L, M, np, 0, h->ntf, step, b0, Bc);
 			LAUNCH(h);
+		}
+	}
+	if (h->observing) {
+		// the dipole at t_step of every instance with step < nt_total (before its field-free step)
+		int cnt = std::max(Bc, Bf);
+		if (cnt > 0) {
+			long nch = (long)cnt * M * L;
+			k_dipole_lbasis<<<(unsigned)((nch + 127) / 128), 128, 0, st>>>(h->st, h->obsF, h->y10d, h->ntf, h->ntt, step, b0, cnt,
+				M, N, L, h->P + 1, h->dl);
+			k_dipole_combine<<<(unsigned)((cnt + 127) / 128), 128, 0, st>>>(h->obs, h->dl, h->lamp, h->ntf, h->ntt, step, b0, cnt,
+				M, L, np, h->zdev, h->ldz);
+			h->launches += 2;
 		}
 	}
 	if (Bf > 0) {
@@ -731,6 +813,7 @@ int qpc_lgwz_destroy(qpc_lgwz* h)
 	cudaFree(h->S); cudaFree(h->R); cudaFree(h->Vh); cudaFree(h->lamp); cudaFree(h->ff);
 	cudaFree(h->st); cudaFree(h->eo); cudaFree(h->wk); cudaFree(h->hostlay); cudaFree(h->fac);
 	cudaFree(h->status); cudaFree(h->red); cudaFree(h->ntf); cudaFree(h->ntt); cudaFree(h->ftab);
+	cudaFree(h->obsF); cudaFree(h->obs); cudaFree(h->dl); cudaFree(h->y10d); cudaFree(h->zdev);
 	for (auto e : h->evpool) cudaEventDestroy(e);
 	for (int g = 0; g < qpc_lgwz::MAXNS; ++g) {
 		if (h->gs[g]) { cudaStreamSynchronize(h->gs[g]); cudaStreamDestroy(h->gs[g]); }
@@ -787,9 +870,11 @@ int qpc_lgwz_get_device(qpc_lgwz* h, double* dev_coef)
 	return get_common(h, dev_coef, cudaMemcpyDeviceToDevice);
 }
 
-int qpc_lgwz_run(qpc_lgwz* h, const double* ftab, int64_t ld, const int64_t* nt_field, const int64_t* nt_total)
+static int run_impl(qpc_lgwz* h, const double* ftab, int64_t ld, const int64_t* nt_field, const int64_t* nt_total,
+	const double* F, double* zlist, int64_t ldz)
 {
 	if (!h || !nt_field || !nt_total) { set_error("NULL argument"); return QPC_ERR_ARGS; }
+	h->observing = false;
 	const int B = h->B;
 	long smax = 0;
 	bool anyfield = false;
@@ -834,6 +919,32 @@ int qpc_lgwz_run(qpc_lgwz* h, const double* ftab, int64_t ld, const int64_t* nt_
 	QPC_CUDA(cudaMemsetAsync(h->status, 0, sizeof(int), h->stream));
 	if (!ident) if (int rc = permute_instances(h, perm, false)) return rc;
 	h->ld = anyfield ? (long)ld : 0;
+	if (F) {
+		const int N = h->N, NE = h->P + 1, M = h->M, L = h->L;
+		long ntmax = 0;
+		for (int k = 0; k < B; ++k) ntmax = std::max<long>(ntmax, nt_total[k]);
+		if (!zlist || ldz < ntmax) { set_error("zlist NULL or ldz=%lld < max nt_total=%ld", (long long)ldz, ntmax); return QPC_ERR_ARGS; }
+		if (!h->obsF) {
+			std::vector<double> y((size_t)M * L);
+			for (int m = 0; m < M; ++m) qpc_y10_coupling(L, h->d.m0 + m, y.data() + (size_t)m * L);
+			int rc;
+			if ((rc = dalloc(&h->obsF, (size_t)N * NE)) || (rc = dalloc(&h->obs, (size_t)B * M * std::max(h->npair, 1) * 2)) ||
+				(rc = dalloc(&h->dl, (size_t)B * M * L)) || (rc = dalloc(&h->y10d, (size_t)M * L)))
+				return rc;
+			QPC_CUDA(cudaMemcpyAsync(h->y10d, y.data(), sizeof(double) * y.size(), cudaMemcpyHostToDevice, h->stream));
+			if (int rc2 = wait_stream(h)) return rc2;
+		}
+		if (h->zcap < (size_t)B * ldz) {
+			cudaFree(h->zdev); h->zdev = nullptr; h->zcap = 0;
+			if (int rc = dalloc(&h->zdev, (size_t)B * ldz)) return rc;
+			h->zcap = (size_t)B * ldz;
+		}
+		QPC_CUDA(cudaMemcpyAsync(h->obsF, F, sizeof(double) * N * NE, cudaMemcpyHostToDevice, h->stream));
+		QPC_CUDA(cudaMemsetAsync(h->zdev, 0, sizeof(double) * B * ldz, h->stream));
+		if (int rc = wait_stream(h)) return rc;
+		h->ldz = ldz;
+		h->observing = true;
+	}
 	// Instance groups (contiguous in the sorted order, balanced by work) on their
 	// own streams; within a group, the instances still in their pulse at step s
 	// are a prefix, and the field-free ones lie below a bound.
@@ -877,6 +988,7 @@ int qpc_lgwz_run(qpc_lgwz* h, const double* ftab, int64_t ld, const int64_t* nt_
 	}
 	QPC_CUDA(cudaEventRecord(h->ev1, h->stream));
 	QPC_CUDA(cudaGetLastError());
+	h->observing = false;
 	if (!ident) if (int rc = permute_instances(h, perm, true)) return rc;
 	long sl = state_len(h);
 	k_status_check<<<(unsigned)((sl + 255) / 256), 256, 0, h->stream>>>(h->st, sl, h->status);
@@ -886,7 +998,25 @@ int qpc_lgwz_run(qpc_lgwz* h, const double* ftab, int64_t ld, const int64_t* nt_
 	cudaEventElapsedTime(&ms, h->ev0, h->ev1);
 	h->last_ms = ms;
 	collect_profile(h);
+	if (F && rc == QPC_OK) {
+		std::vector<double> zh((size_t)B * ldz);
+		QPC_CUDA(cudaMemcpyAsync(zh.data(), h->zdev, sizeof(double) * zh.size(), cudaMemcpyDeviceToHost, h->stream));
+		if (int rc2 = wait_stream(h)) return rc2;
+		for (int k = 0; k < B; ++k) std::memcpy(zlist + (size_t)perm[k] * ldz, zh.data() + (size_t)k * ldz, sizeof(double) * ldz);
+	}
 	return rc;
+}
+
+int qpc_lgwz_run(qpc_lgwz* h, const double* ftab, int64_t ld, const int64_t* nt_field, const int64_t* nt_total)
+{
+	return run_impl(h, ftab, ld, nt_field, nt_total, nullptr, nullptr, 0);
+}
+
+int qpc_lgwz_run_dipole(qpc_lgwz* h, const double* ftab, int64_t ld, const int64_t* nt_field, const int64_t* nt_total,
+	const double* F, double* zlist, int64_t ldz)
+{
+	if (!F) { set_error("F is NULL"); return QPC_ERR_ARGS; }
+	return run_impl(h, ftab, ld, nt_field, nt_total, F, zlist, ldz);
 }
 
 int qpc_lgwz_propagate(qpc_lgwz* h, const double* f_ti, const double* f_tf)

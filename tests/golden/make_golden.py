@@ -10,11 +10,12 @@ Cases (hydrogen unless stated; r in [0, rmax], uniform knots, m = 0):
                     CN bands upper/lower (lu_zsb), Y10 eigensystem, knots, ground state
   small_yukawa.npz  same grid, V = -(1 + 17 e^{-2r})/r: H_l and ground state
   small_prop.npz    seeded random initial state, 50 field steps f_i = 0.05 sin(0.1 i),
-                    then 5 field-free steps: final coefficients, S-norm, <z>
+                    then 5 field-free steps: final coefficients, S-norm, <z>, per-step <z>
   c0_field.npz      f(t_i) of the C0 pulse: 800 nm (w0 = 45.5633525/800),
                     1e14 W/cm^2 (E0 = sqrt(1e14/3.50944758e16)), sin^2, 4 cycles, dt = 0.05
   mid_pulse.npz     N_r=160, p=6, n_l=12, rmax=80: ground state through 1 cycle of
-                    800 nm at 2e14 W/cm^2, CEP 0.5 pi
+                    800 nm at 2e14 W/cm^2, CEP 0.5 pi, then 200 field-free steps; the
+                    driver's per-step <z> (z_list) included
   c0_final.npz      the C0 workload: N_r=400, p=6, n_l=21, rmax=200, ground state,
                     the full c0 pulse (8826 steps): final coefficients, norm, <z>,
                     projections onto field-free states with E < 2
@@ -36,8 +37,10 @@ def build(ref_include):
     subprocess.run(["make", "-C", os.path.join(ROOT, "oracle", "ref"), "-j4", "REF_INCLUDE=" + ref_include], check=True)
 
 
-def run(binary, *args):
+def run(binary, *args, record_z=False):
     env = dict(os.environ, OPENBLAS_NUM_THREADS="1", OMP_NUM_THREADS="1")
+    if record_z:
+        env["QPC_REF_RECORD_Z"] = "1"
     out = subprocess.run([os.path.join(REF, binary)] + [str(a) for a in args], check=True, env=env,
                          stdout=subprocess.PIPE, text=True)
     return out.stdout
@@ -81,9 +84,11 @@ def main():
         nt, nfree = 50, 5
         f = 0.05 * np.sin(0.1 * np.arange(nt + 1))
         f.tofile(os.path.join(d, "field.bin"))
-        run("ref_small", "propagate", d, RMAX, DT, 1, 0, 0, os.path.join(d, "init.bin"), os.path.join(d, "field.bin"), nt, nfree, 1)
+        run("ref_small", "propagate", d, RMAX, DT, 1, 0, 0, os.path.join(d, "init.bin"), os.path.join(d, "field.bin"), nt, nfree, 1,
+            record_z=True)
         np.savez(os.path.join(HERE, "small_prop.npz"), init=c0.reshape(NL, NR), f=f, nt=nt, nfree=nfree,
-                 coef=load(d, "coef", (NL, NR), True), norm=load(d, "norm"), dipole=load(d, "dipole"))
+                 coef=load(d, "coef", (NL, NR), True), norm=load(d, "norm"), dipole=load(d, "dipole"),
+                 zlist=load(d, "zlist"))
         # ---- C0 field
         e0, w0, nc, n0, cep, dt = c0_field()
         run("ref_small", "field", d, e0, w0, nc, n0, cep, dt)
@@ -95,11 +100,12 @@ def main():
         fm = load(d, "f")
         ntm = int(load(d, "nt")[0])
         fm.tofile(os.path.join(d, "fieldm.bin"))
-        out = run("ref_mid", "propagate", d, 80.0, 0.05, 1, 0, 0, "gs", os.path.join(d, "fieldm.bin"), ntm, 0, 1)
+        out = run("ref_mid", "propagate", d, 80.0, 0.05, 1, 0, 0, "gs", os.path.join(d, "fieldm.bin"), ntm, 200, 1, record_z=True)
         meta["mid_pulse"] = out.strip()
         np.savez(os.path.join(HERE, "mid_pulse.npz"), n_r=160, p=6, n_l=12, rmax=80.0, dt=0.05,
-                 e0=e0m, w0=w0, nc=1.0, n0=0.0, cep=0.5, nt=ntm, f=fm,
-                 coef=load(d, "coef", (12, 160), True), norm=load(d, "norm"), dipole=load(d, "dipole"))
+                 e0=e0m, w0=w0, nc=1.0, n0=0.0, cep=0.5, nt=ntm, nfree=200, f=fm,
+                 coef=load(d, "coef", (12, 160), True), norm=load(d, "norm"), dipole=load(d, "dipole"),
+                 zlist=load(d, "zlist"))
         # ---- C0 full pulse
         fc = np.load(os.path.join(HERE, "c0_field.npz"))["f"]
         ntc = fc.size - 1

@@ -124,20 +124,73 @@ def test_other_grids_match_oracle(q, oracle, n_l, p, n_m, m0):
 
 
 def test_golden_mid_pulse(q):
-    """Reference output: ground state through one 800 nm cycle at 2e14 W/cm^2."""
+    """Reference output: ground state through one 800 nm cycle at 2e14 W/cm^2, then
+    200 field-free steps, with the driver's per-step <z> (z_list)."""
     m = golden("mid_pulse")
     n_r, p, n_l, dt = int(m["n_r"]), int(m["p"]), int(m["n_l"]), float(m["dt"])
     S, R, H = grid(q, n_r, p, n_l, float(m["rmax"]))
     c0, _ = q.ground_state(S, H, n_l)
     prop = q.propagator_cn_hc_lgwz().initialize(n_r, p, n_l, S, R, H, dt)
     prop.put(c0[None])
-    nt = int(m["nt"])
-    prop.run(m["f"][None, :], [nt])
+    nt, nf = int(m["nt"]), int(m["nfree"])
+    z = prop.run_dipole(m["f"][None, :], [nt], [nt + nf], R)[0]
     c = prop.get()[0, 0]
     ref = m["coef"]
     sgn = np.sign(np.vdot(ref.ravel(), c.ravel()).real)
     assert rel_l2(sgn * c, ref) < TOL_FULL
     assert abs(prop.norm()[0] - m["norm"][0]) < 1e-10
+    # <z>(t_i) at every step; the dipole is even in the state's sign
+    zr = m["zlist"]
+    assert z.shape == zr.shape
+    assert np.abs(z - zr).max() < 1e-10 * np.abs(zr).max()
+
+
+def test_golden_small_dipole_list(q, small):
+    """Per-step <z> of a random state through 50 field + 5 field-free steps, against the reference."""
+    g = small
+    pr = golden("small_prop")
+    n_r, p, n_l, dt = int(g["n_r"]), int(g["p"]), int(g["n_l"]), float(g["dt"])
+    prop = q.propagator_cn_hc_lgwz().initialize(n_r, p, n_l, g["S"], g["R"], g["H"], dt, n_inst=2)
+    prop.put(np.repeat(pr["init"][None, None], 2, 0))
+    nt, nf = int(pr["nt"]), int(pr["nfree"])
+    z = prop.run_dipole(np.repeat(pr["f"][None, :], 2, 0), [nt, nt], [nt + nf, nt + nf], g["R"])
+    zr = pr["zlist"]
+    for k in range(2):
+        assert np.abs(z[k] - zr).max() < 1e-11 * np.abs(zr).max()
+    assert rel_l2(prop.get()[0, 0], pr["coef"]) < TOL_SHORT
+
+
+def test_dipole_list_uneven_batch(q, oracle):
+    """In-loop dipole for instances with their own pulses and field-free tails
+    (the eigen-basis observation inside the coupling solve and the l-basis one
+    after the pulse), against the oracle stepped one call at a time."""
+    n_r, p, n_l, dt = 80, 6, 7, 0.05
+    S, R, H = grid(q, n_r, p, n_l, 40.0)
+    rng = np.random.default_rng(19)
+    B = 4
+    nt_field = np.array([0, 1, 9, 14])
+    nt_total = nt_field + np.array([4, 3, 0, 2])
+    ld = nt_field.max() + 1
+    ftab = 0.05 * rng.standard_normal((B, ld))
+    c0 = rand_state(rng, B, 1, n_l, n_r)
+    prop = q.propagator_cn_hc_lgwz().initialize(n_r, p, n_l, S, R, H, dt, n_inst=B)
+    prop.put(c0)
+    z = prop.run_dipole(ftab, nt_field, nt_total, R)
+    og = oracle.grid(S, R, H, dt, n_l, n_inst=1)
+    y10 = q.y10_coupling(n_l, 0)
+    for k in range(B):
+        c = c0[k:k + 1].copy()
+        zr = []
+        for s in range(nt_total[k]):
+            zr.append(oracle.dipole(og, R, y10, c)[0].real)
+            if s < nt_field[k]:
+                c = oracle.step(og, c, ftab[k, s], ftab[k, s + 1])
+            else:
+                c = oracle.step(og, c)
+        zr = np.array(zr)
+        assert np.abs(z[k, :nt_total[k]] - zr).max() < 1e-11 * max(1.0, np.abs(zr).max()), k
+        assert np.all(z[k, nt_total[k]:] == 0.0)
+        assert rel_l2(prop.get()[k], c.reshape(1, n_l, n_r)) < TOL_SHORT
 
 
 def test_golden_c0_full_pulse(q):

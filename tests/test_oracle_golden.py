@@ -42,6 +42,20 @@ def test_small_propagation(oracle):
     assert abs(z.real - pr["dipole"][0]) < 1e-11 * abs(pr["dipole"][0])
 
 
+def test_oracle_dipole_list(oracle):
+    """The oracle's <z> before every step equals the driver's z_list (observable_z)."""
+    g = golden("small_setup")
+    pr = golden("small_prop")
+    grid = _reference_grid(oracle, g)
+    c = pr["init"].copy()
+    f = pr["f"]
+    zl = []
+    for i in range(int(pr["nt"]) + int(pr["nfree"])):
+        zl.append(oracle.dipole(grid, g["R"], g["y10"], c)[0].real)
+        c = oracle.step(grid, c, f[i], f[i + 1]) if i < int(pr["nt"]) else oracle.step(grid, c)
+    assert np.abs(np.array(zl) - pr["zlist"]).max() < 1e-11 * np.abs(pr["zlist"]).max()
+
+
 def test_oracle_run_equals_steps(oracle):
     """oracle_lgwz_run (the driver loop) equals stepping one call at a time."""
     g = golden("small_setup")
