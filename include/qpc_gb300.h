@@ -163,6 +163,20 @@ int qpc_lgwz_dipole(qpc_lgwz* h, const double* F, double* out);
  * per (inst, m, il) with n_state[l] entries, complex. */
 int qpc_lgwz_projection(qpc_lgwz* h, const int32_t* n_state, const double* basis, double* proj);
 
+/* ---------------------------------------------------------------- spectra (host)
+ * Harmonic spectrum of one wavefunction from its per-step dipole z(t_i), t_i = t0 + i dt
+ * (the reference's analysis/plot_hhs.m): D(w) = DFT(-z window) dt/2pi with a sin^2
+ * window on (tmin, tmax), S(w) = 4 pi^2 w^{+2 | -2} |D|^2 / c^2 (dipole_type 1 | 2),
+ * w_k = 2 pi k/(n dt), k < ceil(n/2) values written to omega and spectrum. */
+int qpc_hhg_spectrum(const double* z, int64_t n, double t0, double dt, double tmin, double tmax, int32_t dipole_type,
+	double* omega, double* spectrum);
+
+/* Photoelectron energy spectrum (|proj|^2 binned over [emin, emax) per unit energy) and
+ * ionization yield 1 - sum_{energy < thres} |proj|^2 (ionization_sph::measure_ioyd,
+ * spectrum/ionization_1e.hpp:15-51) from n projections (complex) with their energies. */
+int qpc_pes_bin(const double* proj, const double* energy, int64_t n, double emin, double emax, int32_t nbins, double thres,
+	double* pes, double* bound, double* yield);
+
 /* Time the handle's last qpc_lgwz_run on its stream, in milliseconds
  * (CUDA events around the launched kernels). */
 int qpc_lgwz_last_run_ms(qpc_lgwz* h, double* ms);

@@ -33,6 +33,7 @@ EXPORTS = (
     "qpc_lgwz_propagate", "qpc_lgwz_propagate_free", "qpc_lgwz_run", "qpc_lgwz_norm", "qpc_lgwz_dipole",
     "qpc_lgwz_projection", "qpc_lgwz_last_run_ms", "qpc_lgwz_launch_count", "qpc_lgwz_set_profiling",
     "qpc_lgwz_kernel_times", "qpc_lgwz_get_tuning", "qpc_fieldfree_noalloc", "qpc_lgwz_run_dipole",
+    "qpc_hhg_spectrum", "qpc_pes_bin",
 )
 NOALLOC_MAX_ELEMS = 1 << 20
 KERNELS = ("factor", "transform_fwd", "sweep", "transform_bwd", "fieldfree")
@@ -98,6 +99,8 @@ def load(path=None):
         "qpc_lgwz_get_tuning": (ctypes.c_int, [P, P]),
         "qpc_fieldfree_noalloc": (ctypes.c_int, [P, P, P, P, P]),
         "qpc_lgwz_run_dipole": (ctypes.c_int, [P, P, i64, P, P, P, P, i64]),
+        "qpc_hhg_spectrum": (ctypes.c_int, [P, i64, d, d, d, d, i32, P, P]),
+        "qpc_pes_bin": (ctypes.c_int, [P, P, i64, d, d, i32, d, P, P, P]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -221,6 +224,53 @@ def fieldfree_noalloc(dims, S_dev, ffac_dev, coef_dev, stream=0):
     """qpc_fieldfree_noalloc on caller-owned device buffers (raw device pointers)."""
     _check(load().qpc_fieldfree_noalloc(ctypes.byref(dims), ctypes.c_void_p(S_dev), ctypes.c_void_p(ffac_dev),
                                         ctypes.c_void_p(coef_dev), ctypes.c_void_p(stream)))
+
+
+def hhg_spectrum(z, dt, t0=0.0, tmin=None, tmax=None, dipole_type=1):
+    """(omega, S(omega)) from a per-step dipole list (analysis/plot_hhs.m restated);
+    the sin^2 window spans (tmin, tmax), by default the whole record."""
+    z = _f64(z)
+    n = z.size
+    tmin = t0 if tmin is None else tmin
+    tmax = t0 + dt * (n - 1) if tmax is None else tmax
+    nh = (n + 1) // 2
+    w, s = np.zeros(nh), np.zeros(nh)
+    _check(load().qpc_hhg_spectrum(_ptr(z), n, t0, dt, tmin, tmax, dipole_type, _ptr(w), _ptr(s)))
+    return w, s
+
+
+def pes_bin(proj, energy, emin, emax, nbins, thres=0.0):
+    """(pes[nbins], bound population, ionization yield) from projections and their energies."""
+    pr = np.ascontiguousarray(proj, dtype=np.complex128)
+    en = _f64(energy)
+    pes = np.zeros(max(nbins, 1))
+    b, y = ctypes.c_double(0), ctypes.c_double(0)
+    _check(load().qpc_pes_bin(_ptr(pr), _ptr(en), pr.size, emin, emax, nbins, thres, _ptr(pes), ctypes.byref(b), ctypes.byref(y)))
+    return pes[:nbins], b.value, y.value
+
+
+def left_eigenbasis(S, H, lmax, emax):
+    """eigenstate_sph::initialize (population_1e.hpp:58-118): per l = 0..lmax the field-free
+    eigenstates with E < emax, stored as left vectors S v; returns (n_state, basis list, energies)."""
+    n_r, ne = S.shape
+    p = ne - 1
+    n_state, basis, energies = [], [], []
+    for l in range(lmax + 1):
+        e, _ = gen_eigen(S, H[l], 0)
+        k = int((e < emax).sum())
+        e, v = gen_eigen(S, H[l], k)
+        Sv = np.zeros_like(v)
+        for j in range(k):
+            x = v[j]
+            y = S[:, 0] * x
+            for d in range(1, p + 1):
+                y[:-d] += S[:-d, d] * x[d:]
+                y[d:] += S[:-d, d] * x[:-d]
+            Sv[j] = y
+        n_state.append(k)
+        basis.append(Sv)
+        energies.append(e[:k])
+    return np.array(n_state, np.int32), basis, energies
 
 
 # ------------------------------------------------------------------ propagator

@@ -45,7 +45,7 @@ def _run(cmd):
 
 def build_engine(force=False, verbose=False):
     srcs = [os.path.join(CSRC, f) for f in ("qpc_engine.cu", "qpc_setup.cpp", "qpc_internal.h", "qpc_chain.cuh",
-                                             "qpc_noalloc.cu")]
+                                             "qpc_noalloc.cu", "qpc_spectra.cpp")]
     srcs.append(os.path.join(ROOT, "include", "qpc_gb300.h"))
     if not force and not _stale(LIB, srcs):
         return LIB
@@ -53,15 +53,17 @@ def build_engine(force=False, verbose=False):
     o_cu = os.path.join(OBJDIR, "qpc_engine.o")
     o_na = os.path.join(OBJDIR, "qpc_noalloc.o")
     o_cc = os.path.join(OBJDIR, "qpc_setup.o")
+    o_sp = os.path.join(OBJDIR, "qpc_spectra.o")
     nv = [_nvcc()] + NVCC_ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC"]
     jobs = [
         nv + ["-c", os.path.join(CSRC, "qpc_engine.cu"), "-o", o_cu],
         nv + ["-c", os.path.join(CSRC, "qpc_noalloc.cu"), "-o", o_na],
         ["g++", "-O2", "-std=c++17", "-fPIC", "-c", os.path.join(CSRC, "qpc_setup.cpp"), "-o", o_cc],
+        ["g++", "-O2", "-std=c++17", "-fPIC", "-c", os.path.join(CSRC, "qpc_spectra.cpp"), "-o", o_sp],
     ]
-    with cf.ThreadPoolExecutor(3) as ex:
+    with cf.ThreadPoolExecutor(4) as ex:
         outs = list(ex.map(_run, jobs))
-    _run([_nvcc()] + NVCC_ARCH + ["-shared", o_cu, o_na, o_cc, "-o", LIB + ".tmp", "-lcudart"])
+    _run([_nvcc()] + NVCC_ARCH + ["-shared", o_cu, o_na, o_cc, o_sp, "-o", LIB + ".tmp", "-lcudart"])
     os.replace(LIB + ".tmp", LIB)
     if verbose:
         print("".join(outs))
