@@ -95,6 +95,12 @@ int qpc_ldlt_csym(int32_t n, int32_t p, const double* S, const double* H, double
  * ascending, and the lowest n_want S-normalised eigenvectors (rows of vec). */
 int qpc_gen_eigen(int32_t n, int32_t p, const double* S, const double* Hl, int32_t n_want, double* energy, double* vec);
 
+/* lu_dsb (LAPACKE_dpbtrf 'L', algorithm/ed.h:182-193) as operator_sc::initialize uses it
+ * (spherical/operators/1e.hpp:1233-1244): S = L L^T with L(r+k, r) at L[r*(p+1)+k], the
+ * layout of operator_sc::cholesky(); entries past the last row are zero.  Returns 0, -1 on
+ * bad arguments, or 1 + the row of the first non-positive pivot. */
+int qpc_cholesky_band(int32_t n, int32_t p, const double* S, double* L);
+
 /* field_component_sinen<n_pow> inside field<> (structure/field.h:89-133, 245-281):
  * *nt_out = para_nt; when f != NULL writes f(t_i), i = 0..para_nt (cap >= para_nt+1). */
 int qpc_field_sinen(int32_t n_pow, double e0, double w0, double nc, double n0, double cep, double dt,
@@ -198,6 +204,46 @@ int qpc_lgwz_set_profiling(qpc_lgwz* h, int on);
  * out must hold 65 values. */
 int qpc_lgwz_get_tuning(qpc_lgwz* h, int32_t* out);
 int qpc_lgwz_kernel_times(qpc_lgwz* h, double* ms, int64_t* launches);
+
+/* ---------------------------------------------------------------- Arnoldi propagator
+ * Replaces propagator_hc_lgwz (spherical/propagator/la_1e.hpp:390-444) with
+ * propagate<1>(coef, dt) = propagator_arnoldi::propagate1 (la_1e.hpp:312-335):
+ * per step w -> exp(-i dt S^-1 H) w in the Krylov space of S^-1 H built in the
+ * S metric, H = H_l + ez R Y10, at most kmax vectors, expansion stopped when
+ * <v|S|v> < 1e-13 (la_1e.hpp:223).  ez is the field member of the reference
+ * class (la_1e.hpp:401), here given per instance and step.  S^-1 is the
+ * per-(m,l)-channel Cholesky solve that operator_sc::inverse_sub performs
+ * (operators/1e.hpp:1247-1251); the shipped operator_sc::inverse_all
+ * (operators/1e.hpp:1253-1260) offsets channel i by i*n_r while stepping i by
+ * n_r and so does not apply S^-1 to the (m,l) channels.
+ * A handle holds n_inst wavefunctions on one radial grid and runs them as one
+ * batch on its own CUDA stream; calls on different handles are independent.
+ *   S, R   [n_r][p+1] overlap and <B|r|B> bands
+ *   H      [h_per_instance ? n_inst : 1][lmax+1][n_r][p+1], lmax = max|m| + n_l - 1
+ *          (operator_hc, operators/1e.hpp:595-648); per instance allows one
+ *          potential per wavefunction on a shared grid
+ *   y10    [n_m][n_l] <l,m|cos|l+1,m> (operator_y10, qpc_y10_coupling per m)
+ *   emin, emax  the criterion thresholds (arnoldi_workspace, la_1e.hpp:54-62) */
+typedef struct qpc_arnoldi qpc_arnoldi;
+int qpc_arnoldi_create(const qpc_dims* dims, const double* S, const double* R, const double* H, int32_t h_per_instance,
+	const double* y10, double dt, int32_t kmax, double emin, double emax, qpc_arnoldi** out);
+int qpc_arnoldi_destroy(qpc_arnoldi* h);
+/* state transfer, [n_inst][n_m][n_l][n_r] complex128, host or device pointers */
+int qpc_arnoldi_put(qpc_arnoldi* h, const double* coef);
+int qpc_arnoldi_get(qpc_arnoldi* h, double* coef);
+int qpc_arnoldi_put_device(qpc_arnoldi* h, const double* dev_coef);
+int qpc_arnoldi_get_device(qpc_arnoldi* h, double* dev_coef);
+/* nt[k] steps of instance k with ez = ez[k*ld + s] during step s (nt[k] <= ld).  crit
+ * and msub (either may be NULL) receive, at [k*ld + s], criterion() (la_1e.hpp:296-310:
+ * 0 when |x_{m-1}|^2 > emax, 1 when > emin, else 2) and the Krylov dimension m of each
+ * step; -1 for steps an instance does not take. */
+int qpc_arnoldi_run(qpc_arnoldi* h, const double* ez, int64_t ld, const int64_t* nt, int8_t* crit, int8_t* msub);
+/* one step of every instance with ez[k]; crit[k] as above (may be NULL) */
+int qpc_arnoldi_propagate(qpc_arnoldi* h, const double* ez, int8_t* crit);
+/* S-norm per instance (operator_sc::observe, operators/1e.hpp:69-79) */
+int qpc_arnoldi_norm(qpc_arnoldi* h, double* norm);
+/* device time of the last run (CUDA events) and the kernel launches it made */
+int qpc_arnoldi_last_run(qpc_arnoldi* h, float* ms, int64_t* launches);
 
 /* ---------------------------------------------------------------- no device allocation
  * No counterpart in the reference (it has no device code).  For callers that

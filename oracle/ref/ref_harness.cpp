@@ -14,7 +14,8 @@
 // Commands (all arrays are written as raw little-endian float64 files):
 //   setup  OUT RMAX DT ZC ZS SG
 //       S, R (=<B|r|B>), RINV, D (=<B|d/dr|B>), H[l] for l=0..NL-1, the CN bands
-//       upper/lower (lower already LDL^T-factorised by lu_zsb), the Y10 eigen-
+//       upper/lower (lower already LDL^T-factorised by lu_zsb), the Cholesky factor
+//       of S (operator_sc::initialize, operators/1e.hpp:1233-1244), the Y10 eigen-
 //       system yeig[L], yprj[L][L], the knot vector, ground state (l=0, n=0).
 //       Follows binsrc/sphTDSE.cpp:742-743 and cn_1e.hpp:565-593.
 //   field  OUT E0 W0 NC N0 CEP DT
@@ -26,6 +27,9 @@
 //       i < NT, then NFREE field-free steps (binsrc/sphTDSE.cpp:786-831 loop
 //       without observe/mask), and writes coef, S-norm, <z> (observable_z with
 //       f(r)=r) and the wall time of the step loop (qpc::timer semantics).
+//   arnoldi OUT RMAX DT ZC ZS SG INIT FIELD NT KMAX EMIN EMAX
+//       NT steps of the Arnoldi propagator propagator_hc_lgwz (la_1e.hpp:390-444)
+//       with ez = FIELD[i] during step i; see cmd_arnoldi.
 //   proj   OUT RMAX DT ZC ZS SG COEF EMAX
 //       Projection of COEF onto field-free eigenstates with E < EMAX
 //       (eigenstate_sph::initialize + projection, population_1e.hpp:29-118).
@@ -99,6 +103,7 @@ static int cmd_setup(int argc, char** argv)
 	init_prop(prop, radi, angu, rmax, dt, potn, 1);
 
 	dump(out, "S", prop.s.sub(), dims_t::n_rsub);
+	dump(out, "chol", prop.s.cholesky(), dims_t::n_rsub);
 	dump(out, "R", prop.r.data, dims_t::n_rsub);
 	{
 		operator_rinv1<dims_t> ri; ri.initialize(radi); dump(out, "RINV", ri.data, dims_t::n_rsub);
@@ -226,9 +231,77 @@ static int cmd_proj(int argc, char** argv)
 	return 0;
 }
 
+// ---------------------------------------------------------------- Arnoldi (la_1e.hpp)
+// The reference's propagator_hc_lgwz (la_1e.hpp:390-444) runs through the unmodified
+// propagator_arnoldi::propagate1 (la_1e.hpp:312-335) but with a correct S^-1:
+// operator_sc::inverse_all (operators/1e.hpp:1253-1260) steps i by n_dims and then
+// offsets by i*n_dims, so it solves channels n_dims^2 apart.  fixed_sc solves each
+// (m,l) channel with the reference's own inverse_sub (operators/1e.hpp:1247-1251).
+namespace qpc { namespace spherical {
+template <class dims_t>
+struct fixed_sc {
+	const operator_sc<dims_t>* s = nullptr;
+	void observe(const comp_t* w, double& norm) const noexcept { s->observe(w, norm); }
+	void inverse_all(comp_t* u) const noexcept
+	{
+		#pragma omp for
+		for (size_t c = 0; c < dims_t::m_dims * dims_t::l_dims; ++c) s->inverse_sub(u + c * dims_t::n_dims);
+	}
+};
+template <class dims_t>
+struct type_of_inverse_all_t<fixed_sc<dims_t>> : public std::integral_constant<int, 0> {};
+
+template <class dims_t>
+struct harness_hc_lgwz : public propagator_hc_lgwz<dims_t> {
+	fixed_sc<dims_t> oper_s;	// shadows the base's operator_sc for propagate1's CRTP lookup
+	using propagator_hc_lgwz<dims_t>::propagator_hc_lgwz;
+	int step(coefficient<dims_t>& w, double dt, size_t nthreads)
+	{
+		oper_s.s = &this->propagator_hc_lgwz<dims_t>::oper_s;
+		return this->template propagate1<harness_hc_lgwz<dims_t>>(w, dt, nthreads);
+	}
+};
+}}
+
+//   arnoldi OUT RMAX DT ZC ZS SG INIT FIELD NT KMAX EMIN EMAX
+//       NT Arnoldi steps of length DT with ez = FIELD[i] (NT values), from INIT
+//       ("gs" or a file); writes coef and the criterion code of every step.
+static int cmd_arnoldi(int argc, char** argv)
+{
+	if (argc < 14) return 1;
+	std::string out = argv[2];
+	double rmax = atof(argv[3]), dt = atof(argv[4]);
+	potn_any potn{atof(argv[5]), atof(argv[6]), atof(argv[7])};
+	const char* init = argv[8];
+	const char* field = argv[9];
+	size_t nt = strtoul(argv[10], 0, 10), kmax = strtoul(argv[11], 0, 10);
+	double emin = atof(argv[12]), emax = atof(argv[13]);
+	omp_set_num_threads(1);
+	auto radi = integrator_radi<dims_t>();
+	auto angu = integrator_angu<dims_t>();
+	radi.initialize(0.0, rmax);
+	auto prop = harness_hc_lgwz<dims_t>(kmax, emin, emax);
+	prop.initialize(radi, angu, 1.0, potn);
+	auto coef = coefficient<dims_t>();
+	if (std::string(init) == "gs") {
+		coef.template initialize<1>(prop.propagator_hc_lgwz<dims_t>::oper_s, prop.oper_h, {0ul}, {0ul}, {0ul}, {comp_t{1.0}});
+	} else {
+		auto v = slurp(init, 2 * dims_t::n_leng);
+		std::memcpy((double*)coef.data, v.data(), sizeof(double) * v.size());
+	}
+	std::vector<double> f = slurp(field, nt), crit(nt);
+	for (size_t it = 0; it < nt; ++it) {
+		prop.ez = f[it];
+		crit[it] = prop.step(coef, dt, 1);
+	}
+	dump(out, "coef", coef.data, 2 * dims_t::n_leng);
+	dump(out, "crit", crit.data(), crit.size());
+	return 0;
+}
+
 int main(int argc, char** argv)
 {
-	if (argc < 2) { std::fprintf(stderr, "usage: setup|field|propagate|proj ...\n"); return 1; }
+	if (argc < 2) { std::fprintf(stderr, "usage: setup|field|propagate|proj|arnoldi ...\n"); return 1; }
 	try {
 		std::string c = argv[1];
 		int rc = 1;
@@ -236,6 +309,7 @@ int main(int argc, char** argv)
 		else if (c == "field") rc = cmd_field(argc, argv);
 		else if (c == "propagate") rc = cmd_propagate(argc, argv);
 		else if (c == "proj") rc = cmd_proj(argc, argv);
+		else if (c == "arnoldi") rc = cmd_arnoldi(argc, argv);
 		if (rc) std::fprintf(stderr, "bad arguments for %s\n", argv[1]);
 		return rc;
 	} catch (std::exception& e) {

@@ -118,9 +118,21 @@ QPC_SHIM_VML(vdLn) QPC_SHIM_VML(vdLog10) QPC_SHIM_VML(vdCos) QPC_SHIM_VML(vdSin)
 QPC_SHIM_VML(vdAsin) QPC_SHIM_VML(vdAtan) QPC_SHIM_VML(vdCosh) QPC_SHIM_VML(vdSinh) QPC_SHIM_VML(vdTanh) QPC_SHIM_VML(vdAcosh)
 QPC_SHIM_VML(vdAsinh) QPC_SHIM_VML(vdAtanh)
 QPC_SHIM_VML(vzSqrt) QPC_SHIM_VML(vzTanh) QPC_SHIM_VML(vzTan) QPC_SHIM_VML(vzSinh) QPC_SHIM_VML(vzSin) QPC_SHIM_VML(vzPow)
-QPC_SHIM_VML(vzLog10) QPC_SHIM_VML(vzLn) QPC_SHIM_VML(vzExp) QPC_SHIM_VML(vzCosh) QPC_SHIM_VML(vzCos) QPC_SHIM_VML(vzConj)
+QPC_SHIM_VML(vzLog10) QPC_SHIM_VML(vzLn) QPC_SHIM_VML(vzCosh) QPC_SHIM_VML(vzCos) QPC_SHIM_VML(vzConj)
 QPC_SHIM_VML(vzCIS) QPC_SHIM_VML(vzAtanh) QPC_SHIM_VML(vzAtan) QPC_SHIM_VML(vzAsinh) QPC_SHIM_VML(vzAsin) QPC_SHIM_VML(vzArg)
 QPC_SHIM_VML(vzAcosh) QPC_SHIM_VML(vzAcos) QPC_SHIM_VML(vzAbs) QPC_SHIM_VML(vzMul) QPC_SHIM_VML(vzDiv)
+
+// complex exponential of n values (the Arnoldi propagator's exp(-i dt a_k), la_1e.hpp:163-167)
+static inline void vzExp(long long n, const MKL_Complex16* a, MKL_Complex16* y)
+{
+	const double* x = reinterpret_cast<const double*>(a);
+	double* z = reinterpret_cast<double*>(y);
+	for (long long i = 0; i < n; ++i) {
+		std::complex<double> e = std::exp(std::complex<double>(x[2 * i], x[2 * i + 1]));
+		z[2 * i] = e.real();
+		z[2 * i + 1] = e.imag();
+	}
+}
 
 static inline void mkl_set_num_threads(int) {}
 static inline int mkl_get_max_threads() { return 1; }

@@ -33,7 +33,9 @@ EXPORTS = (
     "qpc_lgwz_propagate", "qpc_lgwz_propagate_free", "qpc_lgwz_run", "qpc_lgwz_norm", "qpc_lgwz_dipole",
     "qpc_lgwz_projection", "qpc_lgwz_last_run_ms", "qpc_lgwz_launch_count", "qpc_lgwz_set_profiling",
     "qpc_lgwz_kernel_times", "qpc_lgwz_get_tuning", "qpc_fieldfree_noalloc", "qpc_lgwz_run_dipole",
-    "qpc_hhg_spectrum", "qpc_pes_bin",
+    "qpc_hhg_spectrum", "qpc_pes_bin", "qpc_cholesky_band", "qpc_arnoldi_create", "qpc_arnoldi_destroy",
+    "qpc_arnoldi_put", "qpc_arnoldi_get", "qpc_arnoldi_put_device", "qpc_arnoldi_get_device", "qpc_arnoldi_run",
+    "qpc_arnoldi_propagate", "qpc_arnoldi_norm", "qpc_arnoldi_last_run",
 )
 NOALLOC_MAX_ELEMS = 1 << 20
 KERNELS = ("factor", "transform_fwd", "sweep", "transform_bwd", "fieldfree")
@@ -101,6 +103,17 @@ def load(path=None):
         "qpc_lgwz_run_dipole": (ctypes.c_int, [P, P, i64, P, P, P, P, i64]),
         "qpc_hhg_spectrum": (ctypes.c_int, [P, i64, d, d, d, d, i32, P, P]),
         "qpc_pes_bin": (ctypes.c_int, [P, P, i64, d, d, i32, d, P, P, P]),
+        "qpc_cholesky_band": (ctypes.c_int, [i32, i32, P, P]),
+        "qpc_arnoldi_create": (ctypes.c_int, [P, P, P, P, i32, P, d, i32, d, d, P]),
+        "qpc_arnoldi_destroy": (ctypes.c_int, [P]),
+        "qpc_arnoldi_put": (ctypes.c_int, [P, P]),
+        "qpc_arnoldi_get": (ctypes.c_int, [P, P]),
+        "qpc_arnoldi_put_device": (ctypes.c_int, [P, P]),
+        "qpc_arnoldi_get_device": (ctypes.c_int, [P, P]),
+        "qpc_arnoldi_run": (ctypes.c_int, [P, P, i64, P, P, P]),
+        "qpc_arnoldi_propagate": (ctypes.c_int, [P, P, P]),
+        "qpc_arnoldi_norm": (ctypes.c_int, [P, P]),
+        "qpc_arnoldi_last_run": (ctypes.c_int, [P, P, P]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -415,3 +428,112 @@ class propagator_cn_hc_lgwz:
         out = np.zeros(B * tot, complex)
         _check(load().qpc_lgwz_projection(self._h, _ptr(n_state), _ptr(packed), _ptr(out)))
         return out
+
+
+def cholesky_band(S, p):
+    """S = L L^T, L(r+k, r) at [r, k] (operator_sc::cholesky(), operators/1e.hpp:1233-1244)."""
+    S = _f64(S)
+    n = S.size // (p + 1)
+    L = np.zeros((n, p + 1))
+    rc = load().qpc_cholesky_band(n, p, _ptr(S), _ptr(L))
+    if rc:
+        raise QpcError(4 if rc > 0 else 1, "cholesky_band: %d" % rc)
+    return L
+
+
+class propagator_hc_lgwz:
+    """Batched GPU Arnoldi propagator, propagator_hc_lgwz of spherical/propagator/la_1e.hpp:390-444
+    with propagate<1>(coef, dt) (propagator_arnoldi::propagate1, la_1e.hpp:312-335).
+
+    propagator_hc_lgwz(kmax, emin, emax) mirrors the constructor (arnoldi_workspace,
+    la_1e.hpp:54-62); initialize(...) takes the grid, the bands and dt; the field
+    member ez of the reference class is given per instance to propagate(ez) or as a
+    table to run().  H may be [lmax+1][n_r][p+1] (shared) or [n_inst][lmax+1][n_r][p+1]
+    (one potential per wavefunction).  propagate() and run() return the criterion()
+    codes (0: dt should be smaller, 1: keep, 2: dt may grow).
+    """
+
+    def __init__(self, kmax, emin, emax):
+        if not (emin <= emax and emin > 0 and emax > 0):
+            raise QpcError(1, "invalid parameters for arnoldi propagator")
+        self.kmax, self.emin, self.emax = int(kmax), float(emin), float(emax)
+        self._h = None
+        self.ez = 0.0
+
+    def initialize(self, n_r, p, n_l, S, R, H, y10, dt, n_m=1, m0=0, n_inst=1):
+        lib = load()
+        self.close()
+        d = qpc_dims(n_r, p, n_l, n_m, m0, n_inst)
+        lmax = max(abs(m0), abs(m0 + n_m - 1)) + n_l - 1
+        H = _f64(H)
+        per = H.ndim == 4
+        H = _f64(H[:, :lmax + 1] if per else H[:lmax + 1])
+        y10 = _f64(np.broadcast_to(np.asarray(y10, np.float64).reshape(-1, n_l), (n_m, n_l)))
+        h = ctypes.c_void_p()
+        _check(lib.qpc_arnoldi_create(ctypes.byref(d), _ptr(_f64(S)), _ptr(_f64(R)), _ptr(H), int(per), _ptr(y10),
+                                      float(dt), self.kmax, self.emin, self.emax, ctypes.byref(h)))
+        self._h = h
+        self.dims = d
+        self.dt = float(dt)
+        self.shape = (n_inst, n_m, n_l, n_r)
+        return self
+
+    def close(self):
+        if self._h is not None:
+            load().qpc_arnoldi_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def put(self, coef):
+        c = np.ascontiguousarray(coef, dtype=np.complex128).reshape(self.shape)
+        _check(load().qpc_arnoldi_put(self._h, _ptr(c)))
+
+    def get(self):
+        c = np.zeros(self.shape, np.complex128)
+        _check(load().qpc_arnoldi_get(self._h, _ptr(c)))
+        return c
+
+    def put_device(self, dev_ptr):
+        _check(load().qpc_arnoldi_put_device(self._h, ctypes.c_void_p(dev_ptr)))
+
+    def get_device(self, dev_ptr):
+        _check(load().qpc_arnoldi_get_device(self._h, ctypes.c_void_p(dev_ptr)))
+
+    def propagate(self, ez=None):
+        ez = self.ez if ez is None else ez
+        e = _f64(np.broadcast_to(ez, (self.shape[0],)))
+        crit = np.zeros(self.shape[0], np.int8)
+        _check(load().qpc_arnoldi_propagate(self._h, _ptr(e), _ptr(crit)))
+        return crit
+
+    def run(self, eztab, nt=None, want_msub=False):
+        """eztab[inst, s] = ez during step s; nt[inst] steps (default: all columns).
+        Returns crit[inst, s] (and msub[inst, s]); -1 where an instance took no step."""
+        tab = _f64(np.atleast_2d(eztab))
+        if tab.shape[0] != self.shape[0]:
+            tab = _f64(np.broadcast_to(tab, (self.shape[0], tab.shape[1])))
+        ld = tab.shape[1]
+        nt = np.full(self.shape[0], ld, np.int64) if nt is None else np.ascontiguousarray(
+            np.broadcast_to(nt, (self.shape[0],)), dtype=np.int64)
+        crit = np.zeros((self.shape[0], ld), np.int8)
+        ms = np.zeros((self.shape[0], ld), np.int8)
+        _check(load().qpc_arnoldi_run(self._h, _ptr(tab), ld, _ptr(nt), _ptr(crit), _ptr(ms)))
+        return (crit, ms) if want_msub else crit
+
+    def norm(self):
+        out = np.zeros(self.shape[0])
+        _check(load().qpc_arnoldi_norm(self._h, _ptr(out)))
+        return out
+
+    def last_run(self):
+        """(device ms of the last run, kernel launches it made)"""
+        ms = ctypes.c_float(0)
+        n = ctypes.c_int64(0)
+        _check(load().qpc_arnoldi_last_run(self._h, ctypes.byref(ms), ctypes.byref(n)))
+        return ms.value, n.value
+

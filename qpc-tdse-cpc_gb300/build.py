@@ -16,7 +16,7 @@ ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 LIB = os.path.join(PKG, "libqpc_gb300.so")
 OBJDIR = os.path.join(PKG, "_build")
-ORACLE_SRC = os.path.join(ROOT, "oracle", "oracle_cn.cpp")
+ORACLE_SRCS = [os.path.join(ROOT, "oracle", f) for f in ("oracle_cn.cpp", "oracle_arnoldi.cpp")]
 ORACLE_LIB = os.path.join(ROOT, "oracle", "_build", "liboracle_cn.so")
 
 NVCC_ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -45,7 +45,7 @@ def _run(cmd):
 
 def build_engine(force=False, verbose=False):
     srcs = [os.path.join(CSRC, f) for f in ("qpc_engine.cu", "qpc_setup.cpp", "qpc_internal.h", "qpc_chain.cuh",
-                                             "qpc_noalloc.cu", "qpc_spectra.cpp")]
+                                             "qpc_noalloc.cu", "qpc_spectra.cpp", "qpc_arnoldi.cu", "qpc_cuda_util.cuh")]
     srcs.append(os.path.join(ROOT, "include", "qpc_gb300.h"))
     if not force and not _stale(LIB, srcs):
         return LIB
@@ -54,16 +54,18 @@ def build_engine(force=False, verbose=False):
     o_na = os.path.join(OBJDIR, "qpc_noalloc.o")
     o_cc = os.path.join(OBJDIR, "qpc_setup.o")
     o_sp = os.path.join(OBJDIR, "qpc_spectra.o")
+    o_ar = os.path.join(OBJDIR, "qpc_arnoldi.o")
     nv = [_nvcc()] + NVCC_ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC"]
     jobs = [
         nv + ["-c", os.path.join(CSRC, "qpc_engine.cu"), "-o", o_cu],
         nv + ["-c", os.path.join(CSRC, "qpc_noalloc.cu"), "-o", o_na],
+        nv + ["-c", os.path.join(CSRC, "qpc_arnoldi.cu"), "-o", o_ar],
         ["g++", "-O2", "-std=c++17", "-fPIC", "-c", os.path.join(CSRC, "qpc_setup.cpp"), "-o", o_cc],
         ["g++", "-O2", "-std=c++17", "-fPIC", "-c", os.path.join(CSRC, "qpc_spectra.cpp"), "-o", o_sp],
     ]
-    with cf.ThreadPoolExecutor(4) as ex:
+    with cf.ThreadPoolExecutor(5) as ex:
         outs = list(ex.map(_run, jobs))
-    _run([_nvcc()] + NVCC_ARCH + ["-shared", o_cu, o_na, o_cc, o_sp, "-o", LIB + ".tmp", "-lcudart"])
+    _run([_nvcc()] + NVCC_ARCH + ["-shared", o_cu, o_na, o_ar, o_cc, o_sp, "-o", LIB + ".tmp", "-lcudart"])
     os.replace(LIB + ".tmp", LIB)
     if verbose:
         print("".join(outs))
@@ -71,14 +73,14 @@ def build_engine(force=False, verbose=False):
 
 
 def build_oracle(force=False):
-    if not force and not _stale(ORACLE_LIB, [ORACLE_SRC]):
+    if not force and not _stale(ORACLE_LIB, ORACLE_SRCS):
         return ORACLE_LIB
     os.makedirs(os.path.dirname(ORACLE_LIB), exist_ok=True)
     # fma() must be the hardware instruction (exactly rounded either way); on
     # x86-64 that needs -mfma, on aarch64 it is baseline
     isa = ["-mfma"] if platform.machine() in ("x86_64", "AMD64") else []
     _run(["g++", "-O3", "-std=c++17", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared"] + isa +
-         [ORACLE_SRC, "-o", ORACLE_LIB + ".tmp"])
+         ORACLE_SRCS + ["-o", ORACLE_LIB + ".tmp"])
     os.replace(ORACLE_LIB + ".tmp", ORACLE_LIB)
     return ORACLE_LIB
 

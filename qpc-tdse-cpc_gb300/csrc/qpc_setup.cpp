@@ -352,6 +352,32 @@ int qpc_ldlt_csym(int32_t n, int32_t p, const double* S, const double* H, double
 	return bad;
 }
 
+// banded Cholesky S = G G^T, G lower, row form G[i][i-k] at g[i*(p+1)+k] (right-hand
+// loop over the band, the column-by-column algorithm of Golub & Van Loan 4.3.5);
+// returns 0, or 1 + the row of the first non-positive pivot
+static int chol_band_rows(int n, int p, const double* S, double* g)
+{
+	const int ne = p + 1;
+	for (size_t i = 0; i < (size_t)n * ne; ++i) g[i] = 0.0;
+	for (int i = 0; i < n; ++i) {
+		for (int k = p; k >= 0; --k) {
+			int j = i - k;
+			if (j < 0) continue;
+			double s = S[(size_t)j * ne + k];	// S(j, i)
+			for (int q = 1; q <= p; ++q) {
+				int c = j - q;	// column c < j, need G[i][c], G[j][c]
+				if (c < 0 || i - c > p) continue;
+				s -= g[(size_t)i * ne + (i - c)] * g[(size_t)j * ne + (j - c)];
+			}
+			if (k == 0) {
+				if (!(s > 0)) return i + 1;
+				g[(size_t)i * ne] = std::sqrt(s);
+			} else g[(size_t)i * ne + k] = s / g[(size_t)j * ne];
+		}
+	}
+	return 0;
+}
+
 // Eigenpairs of the generalized banded problem H v = E S v for one l block,
 // the gv_dsb (LAPACKE_dsbgv) call of the reference (algorithm/ed.h:105-112,
 // used by coefficient::initialize, spherical/coefficient/1e.hpp:91-143, and
@@ -367,22 +393,7 @@ int qpc_gen_eigen(int32_t n, int32_t p, const double* S, const double* Hl, int32
 	const int ne = p + 1;
 	// banded Cholesky, G lower: G[i][i-k] stored g[i*ne+k]
 	std::vector<double> g((size_t)n * ne, 0.0);
-	for (int i = 0; i < n; ++i) {
-		for (int k = p; k >= 0; --k) {
-			int j = i - k;
-			if (j < 0) continue;
-			double s = S[(size_t)j * ne + k];	// S(j, i)
-			for (int q = 1; q <= p; ++q) {
-				int c = j - q;	// column c < j, need G[i][c], G[j][c]
-				if (c < 0 || i - c > p) continue;
-				s -= g[(size_t)i * ne + (i - c)] * g[(size_t)j * ne + (j - c)];
-			}
-			if (k == 0) {
-				if (!(s > 0)) return QPC_ERR_SINGULAR;
-				g[(size_t)i * ne] = std::sqrt(s);
-			} else g[(size_t)i * ne + k] = s / g[(size_t)j * ne];
-		}
-	}
+	if (chol_band_rows(n, p, S, g.data())) return QPC_ERR_SINGULAR;
 	// C = G^-1 H G^-T : first X = G^-1 H (dense n x n), then C = G^-1 X^T
 	std::vector<double> X((size_t)n * n, 0.0), C((size_t)n * n, 0.0);
 	auto hval = [&](int r, int c) { int a = std::min(r, c), k = std::abs(r - c); return k > p ? 0.0 : Hl[(size_t)a * ne + k]; };
@@ -494,6 +505,20 @@ int qpc_gen_eigen(int32_t n, int32_t p, const double* S, const double* Hl, int32
 		}
 	}
 	return QPC_OK;
+}
+
+// lu_dsb (LAPACKE_dpbtrf 'L', algorithm/ed.h:182-193) in operator_sc's layout
+// (operators/1e.hpp:1233-1244): L(r+k, r) at L[r*(p+1)+k], zero past the last row
+int qpc_cholesky_band(int32_t n, int32_t p, const double* S, double* L)
+{
+	if (n < 1 || p < 0 || !S || !L) return -1;
+	const int ne = p + 1;
+	std::vector<double> g((size_t)n * ne);
+	int bad = chol_band_rows(n, p, S, g.data());
+	if (bad) return bad;
+	for (int r = 0; r < n; ++r)
+		for (int k = 0; k <= p; ++k) L[(size_t)r * ne + k] = r + k < n ? g[(size_t)(r + k) * ne + k] : 0.0;
+	return 0;
 }
 
 // E(t) of one field_component_sinen<n> (structure/field.h:89-133):

@@ -97,6 +97,55 @@ class Oracle:
         return out[0::2] + 1j * out[1::2]
 
 
+class ArnoldiGrid(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_int32) for n in ("n_r", "p", "n_l", "n_m", "m0", "n_inst", "kmax", "h_per_inst")] + \
+               [(n, ctypes.c_double) for n in ("dt", "emin", "emax")] + \
+               [(n, ctypes.c_void_p) for n in ("S", "chol", "R", "H", "y10")]
+
+
+class ArnoldiOracle:
+    """The CPU Arnoldi oracle (oracle/oracle_arnoldi.cpp), used only as the checker."""
+
+    def __init__(self):
+        from importlib import import_module
+        b = import_module("qpc-tdse-cpc_gb300.build")
+        self.lib = ctypes.CDLL(b.build_oracle())
+        self.lib.oracle_chol_band.restype = ctypes.c_int
+        self.lib.oracle_arnoldi_run.restype = ctypes.c_int
+
+    def chol(self, S):
+        S = np.ascontiguousarray(S, dtype=float)
+        L = np.zeros_like(S)
+        assert self.lib.oracle_chol_band(S.shape[0], S.shape[1] - 1, _p(S), _p(L)) == 0
+        return L
+
+    def grid(self, S, R, H, y10, dt, n_l, kmax=12, emin=1e-14, emax=1e-8, n_m=1, m0=0, n_inst=1, chol=None):
+        """H [lmax+1][n_r][p+1] shared, or [n_inst][lmax+1][n_r][p+1] per instance."""
+        n_r, ne = S.shape
+        lmax = max(abs(m0), abs(m0 + n_m - 1)) + n_l - 1
+        H = np.asarray(H, float)
+        per = H.ndim == 4
+        Hc = np.ascontiguousarray(H[:, :lmax + 1] if per else H[:lmax + 1])
+        y = np.ascontiguousarray(np.broadcast_to(np.asarray(y10, float).reshape(-1, n_l), (n_m, n_l)))
+        L = self.chol(S) if chol is None else np.ascontiguousarray(chol, dtype=float)
+        keep = [np.ascontiguousarray(S, dtype=float), L, np.ascontiguousarray(R, dtype=float), Hc, y]
+        g = ArnoldiGrid(n_r, ne - 1, n_l, n_m, m0, n_inst, kmax, int(per), dt, emin, emax, *[_p(a) for a in keep])
+        g._keep = keep
+        return g
+
+    def run(self, g, coef, eztab, nt=None, threads=1):
+        """Returns (coef, crit[inst, s], msub[inst, s])."""
+        c = np.ascontiguousarray(coef, dtype=complex).copy()
+        tab = np.ascontiguousarray(np.broadcast_to(np.atleast_2d(eztab), (g.n_inst, np.atleast_2d(eztab).shape[1])), dtype=float)
+        ld = tab.shape[1]
+        nt = np.full(g.n_inst, ld, np.int64) if nt is None else np.ascontiguousarray(np.broadcast_to(nt, (g.n_inst,)), dtype=np.int64)
+        crit = np.full((g.n_inst, ld), -1, np.int8)
+        ms = np.full((g.n_inst, ld), -1, np.int8)
+        rc = self.lib.oracle_arnoldi_run(ctypes.byref(g), _p(c), _p(tab), ctypes.c_long(ld), _p(nt), _p(crit), _p(ms), threads)
+        assert rc == 0
+        return c, crit, ms
+
+
 @pytest.fixture(scope="session")
 def q():
     return engine()
@@ -105,6 +154,11 @@ def q():
 @pytest.fixture(scope="session")
 def oracle():
     return Oracle()
+
+
+@pytest.fixture(scope="session")
+def aoracle():
+    return ArnoldiOracle()
 
 
 def rel_l2(a, b):

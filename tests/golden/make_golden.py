@@ -2,7 +2,8 @@
 propagator (QPC-TDSE headers compiled by oracle/ref/Makefile into oracle/_ref/).
 
 Run on the development machine, where the reference checkout exists:
-    python tests/golden/make_golden.py [/path/to/reference/include]
+    python tests/golden/make_golden.py [/path/to/reference/include] [--arnoldi]
+(--arnoldi regenerates only the Arnoldi fixtures.)
 The fixtures are committed; the tests only read them.
 
 Cases (hydrogen unless stated; r in [0, rmax], uniform knots, m = 0):
@@ -19,6 +20,15 @@ Cases (hydrogen unless stated; r in [0, rmax], uniform knots, m = 0):
   c0_final.npz      the C0 workload: N_r=400, p=6, n_l=21, rmax=200, ground state,
                     the full c0 pulse (8826 steps): final coefficients, norm, <z>,
                     projections onto field-free states with E < 2
+  arnoldi_small.npz the Arnoldi propagator propagator_hc_lgwz (la_1e.hpp) on the small
+                    grid, kmax = 12, emin = 1e-14, emax = 1e-8, with the reference's
+                    Cholesky factor of S: ground state through 3000 steps of dt = 0.01
+                    under ez(t) = 0.05 sin(0.057 t) sin^2(pi t/30) ("conv"); from that
+                    state 1 and 3 steps of dt = 0.1 at ez = 0.05 ("step1", "step3") and
+                    1 step with the Yukawa Hamiltonian ("ystep1"); the ground state
+                    through 10 field-free steps of dt = 0.1 (Krylov breakdown, "bd")
+  arnoldi_mid.npz   the same propagator on the mid grid from the mid_pulse final state:
+                    1 and 2 steps of dt = 0.1 at ez = 0.03, kmax = 12
 """
 import json
 import os
@@ -59,9 +69,50 @@ def c0_field():
     return e0, w0, 4.0, 0.0, 0.0, 0.05
 
 
+def arnoldi(d):
+    """Arnoldi fixtures (see the module docstring)."""
+    NR, P, NL, RMAX = 64, 6, 6, 30.0
+    K, EMIN, EMAX = 12, 1e-14, 1e-8
+    run("ref_small", "setup", d, RMAX, 0.1, 1, 0, 0)
+    chol = load(d, "chol", (NR, P + 1))
+    out = {"kmax": K, "emin": EMIN, "emax": EMAX, "chol": chol}
+
+    def arn(binary, init, ez, dt, tag, rmax=RMAX, pot=(1, 0, 0), shape=(NL, NR)):
+        ez = np.asarray(ez, np.float64)
+        ez.tofile(os.path.join(d, "ez.bin"))
+        if not isinstance(init, str):
+            np.asarray(init, np.complex128).tofile(os.path.join(d, "ainit.bin"))
+            init = os.path.join(d, "ainit.bin")
+        run(binary, "arnoldi", d, rmax, dt, pot[0], pot[1], pot[2], init, os.path.join(d, "ez.bin"), ez.size, K, EMIN, EMAX)
+        out[tag + "_ez"] = ez
+        out[tag + "_dt"] = dt
+        out[tag + "_coef"] = load(d, "coef", shape, True)
+        out[tag + "_crit"] = load(d, "crit").astype(np.int8)
+        return out[tag + "_coef"]
+
+    t = 0.01 * np.arange(3000)
+    conv = arn("ref_small", "gs", 0.05 * np.sin(0.057 * t) * np.sin(np.pi * t / 30.0) ** 2, 0.01, "conv")
+    arn("ref_small", conv, [0.05], 0.1, "step1")
+    arn("ref_small", conv, [0.05] * 3, 0.1, "step3")
+    arn("ref_small", conv, [0.05], 0.1, "ystep1", pot=(1, 17, 2))
+    arn("ref_small", "gs", np.zeros(10), 0.1, "bd")
+    np.savez(os.path.join(HERE, "arnoldi_small.npz"), **out)
+    # mid grid, from the CN mid-pulse final state
+    out = {"kmax": K, "emin": EMIN, "emax": EMAX}
+    mid = np.load(os.path.join(HERE, "mid_pulse.npz"))["coef"]
+    out["init"] = mid
+    arn("ref_mid", mid, [0.03], 0.1, "step1", rmax=80.0, shape=(12, 160))
+    arn("ref_mid", mid, [0.03] * 2, 0.1, "step2", rmax=80.0, shape=(12, 160))
+    np.savez(os.path.join(HERE, "arnoldi_mid.npz"), **out)
+
+
 def main():
-    ref_include = sys.argv[1] if len(sys.argv) > 1 else "/root/reference/include"
+    ref_include = sys.argv[1] if len(sys.argv) > 1 and not sys.argv[1].startswith("--") else "/root/reference/include"
     build(ref_include)
+    if "--arnoldi" in sys.argv:
+        with tempfile.TemporaryDirectory() as d:
+            arnoldi(d)
+        return
     meta = {}
     with tempfile.TemporaryDirectory() as d:
         # ---- small grid setup
@@ -119,6 +170,7 @@ def main():
         np.savez(os.path.join(HERE, "c0_final.npz"), n_r=400, p=6, n_l=21, rmax=200.0, dt=0.05, nt=ntc,
                  coef=coef, norm=norm, dipole=dip, proj=load(d, "proj", None, True),
                  proj_nnz=load(d, "proj_nnz").astype(np.int64), proj_energy=load(d, "proj_energy"))
+        arnoldi(d)
     with open(os.path.join(HERE, "make_golden.log.json"), "w") as fh:
         json.dump(meta, fh, indent=1)
 
