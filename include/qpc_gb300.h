@@ -146,6 +146,13 @@ int qpc_lgwz_propagate_free(qpc_lgwz* h);
  * so uneven step counts are fine.  The result equals nt_total[k] single calls
  * (within rounding: consecutive coupling half-steps are fused). */
 int qpc_lgwz_run(qpc_lgwz* h, const double* ftab, int64_t ld, const int64_t* nt_field, const int64_t* nt_total);
+/* qpc_lgwz_run on n distinct handles at once, each from its own host thread on its
+ * own streams: handle i takes (ftab[i], ld[i], nt_field[i], nt_total[i]).  For
+ * batches on different grids (the driver loop of sphTDSE.cpp:786-831 for several
+ * dimension_1e instantiations side by side).  Returns the first failing handle's
+ * status (its index in *failed when failed != NULL, else -1). */
+int qpc_lgwz_run_many(int32_t n, qpc_lgwz* const* hs, const double* const* ftab, const int64_t* ld,
+	const int64_t* const* nt_field, const int64_t* const* nt_total, int32_t* failed);
 
 /* qpc_lgwz_run that also records, for every instance k and step s < nt_total[k],
  * zlist[k*ldz + s] = Re <psi_k(t_s)| f(r) cos(theta) |psi_k(t_s)> with F = <Bi|f|Bj>

@@ -35,7 +35,7 @@ EXPORTS = (
     "qpc_lgwz_kernel_times", "qpc_lgwz_get_tuning", "qpc_fieldfree_noalloc", "qpc_lgwz_run_dipole",
     "qpc_hhg_spectrum", "qpc_pes_bin", "qpc_cholesky_band", "qpc_arnoldi_create", "qpc_arnoldi_destroy",
     "qpc_arnoldi_put", "qpc_arnoldi_get", "qpc_arnoldi_put_device", "qpc_arnoldi_get_device", "qpc_arnoldi_run",
-    "qpc_arnoldi_propagate", "qpc_arnoldi_norm", "qpc_arnoldi_last_run",
+    "qpc_arnoldi_propagate", "qpc_arnoldi_norm", "qpc_arnoldi_last_run", "qpc_lgwz_run_many",
 )
 NOALLOC_MAX_ELEMS = 1 << 20
 KERNELS = ("factor", "transform_fwd", "sweep", "transform_bwd", "fieldfree")
@@ -104,6 +104,7 @@ def load(path=None):
         "qpc_hhg_spectrum": (ctypes.c_int, [P, i64, d, d, d, d, i32, P, P]),
         "qpc_pes_bin": (ctypes.c_int, [P, P, i64, d, d, i32, d, P, P, P]),
         "qpc_cholesky_band": (ctypes.c_int, [i32, i32, P, P]),
+        "qpc_lgwz_run_many": (ctypes.c_int, [i32, P, P, P, P, P, P]),
         "qpc_arnoldi_create": (ctypes.c_int, [P, P, P, P, i32, P, d, i32, d, d, P]),
         "qpc_arnoldi_destroy": (ctypes.c_int, [P]),
         "qpc_arnoldi_put": (ctypes.c_int, [P, P]),
@@ -428,6 +429,33 @@ class propagator_cn_hc_lgwz:
         out = np.zeros(B * tot, complex)
         _check(load().qpc_lgwz_projection(self._h, _ptr(n_state), _ptr(packed), _ptr(out)))
         return out
+
+
+def run_many(props, ftabs, nt_field, nt_total=None):
+    """propagator_cn_hc_lgwz.run on several handles at once (qpc_lgwz_run_many): one host
+    thread per handle, so that batches on different grids share the GPU."""
+    n = len(props)
+    keep = []
+    H = (ctypes.c_void_p * n)()
+    F = (ctypes.c_void_p * n)()
+    LD = np.zeros(n, np.int64)
+    NF = (ctypes.c_void_p * n)()
+    NT = (ctypes.c_void_p * n)()
+    for i, pr in enumerate(props):
+        B = pr.shape[0]
+        nf = np.ascontiguousarray(np.broadcast_to(nt_field[i], (B,)), dtype=np.int64)
+        ntt = nf.copy() if nt_total is None else np.ascontiguousarray(np.broadcast_to(nt_total[i], (B,)), dtype=np.int64)
+        tab = _f64(np.atleast_2d(ftabs[i]))
+        if tab.shape[0] != B:
+            tab = _f64(np.broadcast_to(tab, (B, tab.shape[1])))
+        keep += [nf, ntt, tab]
+        H[i] = pr._h.value
+        F[i] = tab.ctypes.data
+        LD[i] = tab.shape[1]
+        NF[i] = nf.ctypes.data
+        NT[i] = ntt.ctypes.data
+    failed = ctypes.c_int32(-1)
+    _check(load().qpc_lgwz_run_many(n, H, F, _ptr(LD), NF, NT, ctypes.byref(failed)))
 
 
 def cholesky_band(S, p):

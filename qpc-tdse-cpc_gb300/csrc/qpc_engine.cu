@@ -38,6 +38,7 @@
 #include <numeric>
 #include <string>
 #include <time.h>
+#include <thread>
 #include <cstdlib>
 #include "qpc_chain.cuh"
 
@@ -739,12 +740,15 @@ int qpc_lgwz_create(const qpc_dims* dims, double dt, const double* S, const doub
 		if (L & 1)
 			for (int il = 0; il < L; ++il) Vh[((size_t)im * (np + 1) + np) * L + il] = Pm[(size_t)np * L + il];
 	}
-	// look-ahead depth for the factorisation: enough systems to fill the GPU, bounded memory
-	size_t per_step = (size_t)h->B * M * N * NE * std::max(np, 1) * sizeof(double2);
 	// look-ahead depth of the coupling factorisation: ~40k independent systems per
-	// launch (fills every FP64 pipe even for one wavefunction), at most 4 GB
+	// launch (fills every FP64 pipe even for one wavefunction), in at most
+	// min(4 GB, max(256 MB, 64 MB per wavefunction)) of factors, so that many small
+	// handles can share one GPU; QPC_FAC_BYTES overrides the bound
+	size_t per_step = (size_t)h->B * M * N * NE * std::max(np, 1) * sizeof(double2);
+	size_t fac_cap = std::min<size_t>((size_t)4 << 30, std::max<size_t>((size_t)256 << 20, (size_t)h->B * (64 << 20)));
+	if (const char* e = getenv("QPC_FAC_BYTES")) fac_cap = std::max<size_t>(per_step, (size_t)atoll(e));
 	h->K = 1;
-	while (h->K < 4096 && (long)h->K * h->B * M * np < 40000 && per_step * (h->K * 2) <= ((size_t)4 << 30)) h->K *= 2;
+	while (h->K < 4096 && (long)h->K * h->B * M * np < 40000 && per_step * (h->K * 2) <= fac_cap) h->K *= 2;
 	long sl = state_len(h);
 	if ((rc = dalloc(&h->S, (size_t)N * NE)) || (rc = dalloc(&h->R, (size_t)N * NE)) || (rc = dalloc(&h->Vh, Vh.size())) ||
 		(rc = dalloc(&h->lamp, lamp.size())) || (rc = dalloc(&h->ff, ffh.size())) || (rc = dalloc(&h->st, sl)) ||
@@ -841,6 +845,7 @@ static int run_impl(qpc_lgwz* h, const double* ftab, int64_t ld, const int64_t* 
 	const double* F, double* zlist, int64_t ldz)
 {
 	if (!h || !nt_field || !nt_total) { set_error("NULL argument"); return QPC_ERR_ARGS; }
+	QPC_CUDA(cudaSetDevice(h->dev));
 	h->observing = false;
 	const int B = h->B;
 	long smax = 0;
@@ -977,6 +982,35 @@ static int run_impl(qpc_lgwz* h, const double* ftab, int64_t ld, const int64_t* 
 int qpc_lgwz_run(qpc_lgwz* h, const double* ftab, int64_t ld, const int64_t* nt_field, const int64_t* nt_total)
 {
 	return run_impl(h, ftab, ld, nt_field, nt_total, nullptr, nullptr, 0);
+}
+
+// Several handles at once: one host thread per handle, each driving its handle's
+// own streams, so that batches on different grids share the GPU.
+int qpc_lgwz_run_many(int32_t n, qpc_lgwz* const* hs, const double* const* ftab, const int64_t* ld,
+	const int64_t* const* nt_field, const int64_t* const* nt_total, int32_t* failed)
+{
+	if (failed) *failed = -1;
+	if (n < 0 || (n > 0 && (!hs || !ld || !nt_field || !nt_total))) { set_error("NULL argument"); return QPC_ERR_ARGS; }
+	for (int i = 0; i < n; ++i)
+		for (int j = 0; j < i; ++j)
+			if (hs[i] == hs[j]) { set_error("handle %d appears twice", i); return QPC_ERR_ARGS; }
+	std::vector<int> rc(n, QPC_OK);
+	std::vector<std::string> msg(n);
+	std::vector<std::thread> th;
+	th.reserve(n);
+	for (int i = 0; i < n; ++i)
+		th.emplace_back([&, i] {
+			rc[i] = qpc_lgwz_run(hs[i], ftab ? ftab[i] : nullptr, ld[i], nt_field[i], nt_total[i]);
+			if (rc[i]) msg[i] = qpc_last_error();
+		});
+	for (auto& t : th) t.join();
+	for (int i = 0; i < n; ++i)
+		if (rc[i]) {
+			if (failed) *failed = i;
+			set_error("handle %d: %s", i, msg[i].c_str());
+			return rc[i];
+		}
+	return QPC_OK;
 }
 
 int qpc_lgwz_run_dipole(qpc_lgwz* h, const double* ftab, int64_t ld, const int64_t* nt_field, const int64_t* nt_total,
