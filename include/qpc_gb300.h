@@ -252,6 +252,31 @@ int qpc_arnoldi_norm(qpc_arnoldi* h, double* norm);
 /* device time of the last run (CUDA events) and the kernel launches it made */
 int qpc_arnoldi_last_run(qpc_arnoldi* h, float* ms, int64_t* launches);
 
+/* ---------------------------------------------------------------- surrogate network
+ * No counterpart in the reference.  An ensemble of n_members MLPs, each
+ * n_in -> n_layers x n_hidden (GELU) -> n_out, trained on the GPU with Adam:
+ * bfloat16 operands, fp32 accumulation on the tensor cores, fp32 master weights,
+ * biases, activations before rounding, loss gradient and optimiser state.  Loss:
+ * mean squared error over rows and outputs.  Rows are float32 [n][n_in], targets
+ * float32 [n][n_out]; n_hidden must be a multiple of 16 and n_out of 8. */
+typedef struct qpc_mlp qpc_mlp;
+int qpc_mlp_create(int32_t n_in, int32_t n_hidden, int32_t n_layers, int32_t n_out, int32_t n_members, uint64_t seed,
+	qpc_mlp** out);
+int qpc_mlp_destroy(qpc_mlp* h);
+/* parameters per member; flat fp32 order W_0 [n_hidden][K0] (K0 = n_in rounded up to 16,
+ * columns >= n_in unused), b_0, W_1, b_1, ..., W_last [n_out][n_hidden], b_last */
+int qpc_mlp_param_count(qpc_mlp* h, int64_t* n);
+int qpc_mlp_get_params(qpc_mlp* h, int32_t member, float* params);
+int qpc_mlp_set_params(qpc_mlp* h, int32_t member, const float* params);
+/* loss[member] and, if grad != NULL, grad[member][param_count] on the same n rows; no update */
+int qpc_mlp_loss_grad(qpc_mlp* h, const float* X, const float* Y, int32_t n, float* loss, float* grad);
+/* epochs of Adam (lr, beta 0.9 / 0.999, eps 1e-8) over minibatches of `batch` rows, each
+ * member on its own shuffle drawn from seed; loss_hist [epochs][members] or NULL */
+int qpc_mlp_train(qpc_mlp* h, const float* X, const float* Y, int32_t n, int32_t epochs, int32_t batch, float lr, uint64_t seed,
+	float* loss_hist);
+/* out [members][n][n_out] */
+int qpc_mlp_predict(qpc_mlp* h, const float* X, int32_t n, float* out);
+
 /* ---------------------------------------------------------------- no device allocation
  * No counterpart in the reference (it has no device code).  For callers that
  * cannot call cudaMalloc -- a framework that owns every device allocation

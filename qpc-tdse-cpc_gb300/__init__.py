@@ -36,6 +36,8 @@ EXPORTS = (
     "qpc_hhg_spectrum", "qpc_pes_bin", "qpc_cholesky_band", "qpc_arnoldi_create", "qpc_arnoldi_destroy",
     "qpc_arnoldi_put", "qpc_arnoldi_get", "qpc_arnoldi_put_device", "qpc_arnoldi_get_device", "qpc_arnoldi_run",
     "qpc_arnoldi_propagate", "qpc_arnoldi_norm", "qpc_arnoldi_last_run", "qpc_lgwz_run_many",
+    "qpc_mlp_create", "qpc_mlp_destroy", "qpc_mlp_param_count", "qpc_mlp_get_params", "qpc_mlp_set_params",
+    "qpc_mlp_loss_grad", "qpc_mlp_train", "qpc_mlp_predict",
 )
 NOALLOC_MAX_ELEMS = 1 << 20
 KERNELS = ("factor", "transform_fwd", "sweep", "transform_bwd", "fieldfree")
@@ -105,6 +107,14 @@ def load(path=None):
         "qpc_pes_bin": (ctypes.c_int, [P, P, i64, d, d, i32, d, P, P, P]),
         "qpc_cholesky_band": (ctypes.c_int, [i32, i32, P, P]),
         "qpc_lgwz_run_many": (ctypes.c_int, [i32, P, P, P, P, P, P]),
+        "qpc_mlp_create": (ctypes.c_int, [i32, i32, i32, i32, i32, ctypes.c_uint64, P]),
+        "qpc_mlp_destroy": (ctypes.c_int, [P]),
+        "qpc_mlp_param_count": (ctypes.c_int, [P, P]),
+        "qpc_mlp_get_params": (ctypes.c_int, [P, i32, P]),
+        "qpc_mlp_set_params": (ctypes.c_int, [P, i32, P]),
+        "qpc_mlp_loss_grad": (ctypes.c_int, [P, P, P, i32, P, P]),
+        "qpc_mlp_train": (ctypes.c_int, [P, P, P, i32, i32, i32, ctypes.c_float, ctypes.c_uint64, P]),
+        "qpc_mlp_predict": (ctypes.c_int, [P, P, i32, P]),
         "qpc_arnoldi_create": (ctypes.c_int, [P, P, P, P, i32, P, d, i32, d, d, P]),
         "qpc_arnoldi_destroy": (ctypes.c_int, [P]),
         "qpc_arnoldi_put": (ctypes.c_int, [P, P]),
@@ -564,4 +574,63 @@ class propagator_hc_lgwz:
         n = ctypes.c_int64(0)
         _check(load().qpc_arnoldi_last_run(self._h, ctypes.byref(ms), ctypes.byref(n)))
         return ms.value, n.value
+
+
+class mlp_ensemble:
+    """GPU-trained ensemble MLP (qpc_mlp): members x (n_in -> n_layers x n_hidden GELU -> n_out),
+    bf16 operands with fp32 accumulation, Adam."""
+
+    def __init__(self, n_in, n_out, n_hidden=256, n_layers=4, n_members=5, seed=0):
+        self._h = None
+        h = ctypes.c_void_p()
+        _check(load().qpc_mlp_create(n_in, n_hidden, n_layers, n_out, n_members, ctypes.c_uint64(seed), ctypes.byref(h)))
+        self._h = h
+        self.n_in, self.n_out, self.n_hidden, self.n_layers, self.n_members = n_in, n_out, n_hidden, n_layers, n_members
+        n = ctypes.c_int64(0)
+        _check(load().qpc_mlp_param_count(h, ctypes.byref(n)))
+        self.n_params = n.value
+
+    def close(self):
+        if self._h is not None:
+            load().qpc_mlp_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def get_params(self, member):
+        out = np.zeros(self.n_params, np.float32)
+        _check(load().qpc_mlp_get_params(self._h, member, _ptr(out)))
+        return out
+
+    def set_params(self, member, flat):
+        f = np.ascontiguousarray(flat, dtype=np.float32)
+        assert f.size == self.n_params
+        _check(load().qpc_mlp_set_params(self._h, member, _ptr(f)))
+
+    def loss_grad(self, X, Y):
+        X = np.ascontiguousarray(X, dtype=np.float32)
+        Y = np.ascontiguousarray(Y, dtype=np.float32)
+        loss = np.zeros(self.n_members, np.float32)
+        grad = np.zeros((self.n_members, self.n_params), np.float32)
+        _check(load().qpc_mlp_loss_grad(self._h, _ptr(X), _ptr(Y), X.shape[0], _ptr(loss), _ptr(grad)))
+        return loss, grad
+
+    def train(self, X, Y, epochs, batch=256, lr=1e-3, seed=1):
+        X = np.ascontiguousarray(X, dtype=np.float32)
+        Y = np.ascontiguousarray(Y, dtype=np.float32)
+        hist = np.zeros((epochs, self.n_members), np.float32)
+        _check(load().qpc_mlp_train(self._h, _ptr(X), _ptr(Y), X.shape[0], epochs, batch, ctypes.c_float(lr),
+                                    ctypes.c_uint64(seed), _ptr(hist)))
+        return hist
+
+    def predict(self, X):
+        """[members][n][n_out]"""
+        X = np.ascontiguousarray(X, dtype=np.float32)
+        out = np.zeros((self.n_members, X.shape[0], self.n_out), np.float32)
+        _check(load().qpc_mlp_predict(self._h, _ptr(X), X.shape[0], _ptr(out)))
+        return out
 

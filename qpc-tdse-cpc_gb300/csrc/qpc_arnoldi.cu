@@ -28,6 +28,7 @@
 #include <cmath>
 #include <vector>
 #include <algorithm>
+#include <cstdlib>
 
 namespace qpc {
 namespace {
@@ -36,7 +37,7 @@ constexpr int AR_THREADS = 256;
 constexpr int AR_PER_THREAD = 4;
 constexpr int AR_TILE = AR_THREADS * AR_PER_THREAD; // elements per block of the element-wise kernels
 constexpr int AR_KMAX = 32;                          // largest Krylov dimension accepted
-constexpr int CH_THREADS = 64;                       // real recurrences per block of k_ar_sinv
+constexpr int CH_THREADS = 32;                       // real recurrences per block of k_ar_sinv
 
 // per-instance state of the expansion within one step
 enum : int { AR_LIVE = 0, AR_BROKEN = 1, AR_IDLE = 2 };
@@ -45,6 +46,7 @@ enum : int { ARS_NONFINITE = 2, ARS_NOCONV = 4, ARS_ZERO = 8 };
 
 struct ar_args {
 	int N, P, L, M, m0, nch, nlh, B, kmax, nbe;
+	int b0;       // first instance of the group a launch covers (blockIdx.y / blockIdx.x offset)
 	long n;       // complex elements per instance
 	long hstride; // doubles between the Hamiltonians of consecutive instances (0: shared)
 	double dt, emin, emax;
@@ -151,7 +153,7 @@ __global__ void k_ar_to_lmajor(const double2* __restrict__ src, double2* __restr
 //        expansion with m = k+1; else sfac = 1/sqrt(nu), b[k+1] = sqrt(nu).
 __global__ void __launch_bounds__(AR_THREADS) k_ar_snorm(ar_args g, const double2* __restrict__ src, int k, long step)
 {
-	const int b = blockIdx.y;
+	const int b = g.b0 + blockIdx.y;
 	if (k < 0) {
 		if (step >= g.nt[b]) {
 			if (blockIdx.x == 0 && threadIdx.x == 0) g.flag[b] = AR_IDLE;
@@ -219,21 +221,25 @@ __global__ void __launch_bounds__(AR_THREADS) k_ar_snorm(ar_args g, const double
 // u_k = sfac * src (stored as U[k]); dst = H u_k (multiply, la_1e.hpp:420-434:
 // symb_mul_vecd of H_l, then + (R u_{l-1}) ez y10(m,l-1), + (R u_{l+1}) ez y10(m,l));
 // x_i = <u_i|dst> for i <= k (orthogonalize_ip, la_1e.hpp:204-209), a[k] = Re x_k.
+// The band sums run on the unscaled src and are scaled once, H (s x) = s (H x): the
+// same value to rounding, for a third of the FP64 instructions.
 __global__ void __launch_bounds__(AR_THREADS) k_ar_expand(ar_args g, const double2* __restrict__ src, double2* __restrict__ dst,
 	int k, long step)
 {
-	const int b = blockIdx.y;
+	const int b = g.b0 + blockIdx.y;
 	if (g.flag[b] != AR_LIVE) return;
 	__shared__ double2 sm[32];
 	const int P = g.P, nch = g.nch, N = g.N, L = g.L;
 	const long n = g.n;
 	const double s = g.sfac[b];
 	const double ez = g.ez[(long)b * g.ld + step];
-	const double2* x = src + (long)b * n;
+	const double2* __restrict__ x = src + (long)b * n;
 	double2* y = dst + (long)b * n;
 	double2* Uk = g.U + ((long)b * g.kmax + k) * n;
-	const double* H = g.H + (long)b * g.hstride;
+	const double* __restrict__ H = g.H + (long)b * g.hstride;
+	const double* __restrict__ Rb = g.R;
 	double2 yv[AR_PER_THREAD], uv[AR_PER_THREAD];
+#pragma unroll
 	for (int j = 0; j < AR_PER_THREAD; ++j) {
 		yv[j] = uv[j] = make_double2(0.0, 0.0);
 		long e = (long)blockIdx.x * AR_TILE + j * AR_THREADS + threadIdx.x;
@@ -241,29 +247,41 @@ __global__ void __launch_bounds__(AR_THREADS) k_ar_expand(ar_args g, const doubl
 		int r = (int)(e / nch), ch = (int)(e - (long)r * nch);
 		int im = ch / L, il = ch - im * L;
 		int l = il + abs(g.m0 + im);
-		auto u = [&](long idx) { return rmul(x[idx], s); };
-		double2 ue = u(e);
+		double2 ue = rmul(x[e], s);
 		Uk[e] = ue;
 		uv[j] = ue;
-		// H_l band: lower neighbours j ascending, then the row itself and the upper ones
+		// H_l band: lower neighbours q ascending, then the row itself and the upper ones
 		double2 t = make_double2(0.0, 0.0);
-		for (int q = 1; q <= P && q <= r; ++q) t = cadd(t, rmul(u(e - (long)q * nch), H[((long)(r - q) * (P + 1) + q) * g.nlh + l]));
-		for (int q = 0; q <= P && r + q < N; ++q) t = cadd(t, rmul(u(e + (long)q * nch), H[((long)r * (P + 1) + q) * g.nlh + l]));
-		double2 acc = t;
-		if (il > 0) {
-			double c = ez * g.y10[im * L + il - 1];
-			double2 t2 = make_double2(0.0, 0.0);
-			for (int q = 1; q <= P && q <= r; ++q) t2 = cadd(t2, rmul(u(e - 1 - (long)q * nch), g.R[(long)(r - q) * (P + 1) + q]));
-			for (int q = 0; q <= P && r + q < N; ++q) t2 = cadd(t2, rmul(u(e - 1 + (long)q * nch), g.R[(long)r * (P + 1) + q]));
-			acc = cadd(acc, rmul(t2, c));
+		for (int q = 1; q <= P && q <= r; ++q) {
+			double h = H[((long)(r - q) * (P + 1) + q) * g.nlh + l];
+			double2 v = x[e - (long)q * nch];
+			t.x = fma(v.x, h, t.x); t.y = fma(v.y, h, t.y);
 		}
-		if (il < L - 1) {
-			double c = ez * g.y10[im * L + il];
-			double2 t3 = make_double2(0.0, 0.0);
-			for (int q = 1; q <= P && q <= r; ++q) t3 = cadd(t3, rmul(u(e + 1 - (long)q * nch), g.R[(long)(r - q) * (P + 1) + q]));
-			for (int q = 0; q <= P && r + q < N; ++q) t3 = cadd(t3, rmul(u(e + 1 + (long)q * nch), g.R[(long)r * (P + 1) + q]));
-			acc = cadd(acc, rmul(t3, c));
+		for (int q = 0; q <= P && r + q < N; ++q) {
+			double h = H[((long)r * (P + 1) + q) * g.nlh + l];
+			double2 v = x[e + (long)q * nch];
+			t.x = fma(v.x, h, t.x); t.y = fma(v.y, h, t.y);
 		}
+		// R band on the l-1 and l+1 channels of the same m
+		double2 t2 = make_double2(0.0, 0.0), t3 = make_double2(0.0, 0.0);
+		const bool lo = il > 0, hi = il < L - 1;
+		for (int q = 1; q <= P && q <= r; ++q) {
+			double rq = Rb[(long)(r - q) * (P + 1) + q];
+			long o = e - (long)q * nch;
+			if (lo) { double2 v = x[o - 1]; t2.x = fma(v.x, rq, t2.x); t2.y = fma(v.y, rq, t2.y); }
+			if (hi) { double2 v = x[o + 1]; t3.x = fma(v.x, rq, t3.x); t3.y = fma(v.y, rq, t3.y); }
+		}
+		for (int q = 0; q <= P && r + q < N; ++q) {
+			double rq = Rb[(long)r * (P + 1) + q];
+			long o = e + (long)q * nch;
+			if (lo) { double2 v = x[o - 1]; t2.x = fma(v.x, rq, t2.x); t2.y = fma(v.y, rq, t2.y); }
+			if (hi) { double2 v = x[o + 1]; t3.x = fma(v.x, rq, t3.x); t3.y = fma(v.y, rq, t3.y); }
+		}
+		const double clo = lo ? ez * g.y10[im * L + il - 1] : 0.0;
+		const double chi = hi ? ez * g.y10[im * L + il] : 0.0;
+		double2 acc;
+		acc.x = fma(t3.x, chi, fma(t2.x, clo, t.x)) * s;
+		acc.y = fma(t3.y, chi, fma(t2.y, clo, t.y)) * s;
 		y[e] = acc;
 		yv[j] = acc;
 	}
@@ -298,51 +316,81 @@ __global__ void __launch_bounds__(AR_THREADS) k_ar_expand(ar_args g, const doubl
 // operator_sc::inverse_sub (operators/1e.hpp:1247-1251).  One lane per real
 // recurrence (channel, real or imaginary part); the previous P values of each
 // sweep stay in registers.  Lrow[r][j-1] = L(r, r-j), Lcol[r][k-1] = L(r+k, r)
-// (zero outside the matrix), dinv[r] = 1/L(r,r).
-template <int P>
-__global__ void __launch_bounds__(CH_THREADS) k_ar_sinv(ar_args g, double2* __restrict__ vbuf)
+// (zero outside the matrix), dinv[r] = 1/L(r,r).  The rows advance in tiles of
+// SV_D: the next tile's values are loaded while the current one is solved, and
+// the factor rows of the next tile are staged in shared memory by the block.
+constexpr int SV_D = 8;
+
+template <int P, bool FWD>
+__device__ __forceinline__ void sinv_sweep(const ar_args& g, double* v, long stride, bool act,
+	double (*Lt)[SV_D][P + 1])
 {
-	const int b = blockIdx.y;
-	if (g.flag[b] != AR_LIVE) return;
-	const int c = blockIdx.x * CH_THREADS + threadIdx.x;
-	if (c >= 2 * g.nch) return;
 	const int N = g.N;
-	const long stride = 2L * g.nch;
-	double* v = reinterpret_cast<double*>(vbuf + (long)b * g.n) + c;
+	const double* __restrict__ Lf = FWD ? g.Lrow : g.Lcol;
+	const int ntile = (N + SV_D - 1) / SV_D;
+	auto row = [&](int t, int j) { return FWD ? t * SV_D + j : N - 1 - (t * SV_D + j); };
+	auto stage = [&](int t, int buf) {
+		for (int i = threadIdx.x; i < SV_D * (P + 1); i += blockDim.x) {
+			int j = i / (P + 1), c = i - j * (P + 1);
+			int r = row(t, j);
+			double val = 0.0;
+			if (t * SV_D + j < N) val = c < P ? Lf[(long)r * P + c] : g.dinv[r];
+			Lt[buf][j][c] = val;
+		}
+	};
 	double w[P];
 #pragma unroll
 	for (int j = 0; j < P; ++j) w[j] = 0.0;
-	for (int r = 0; r < N; ++r) {
-		double x = v[(long)r * stride];
-		const double* lr = g.Lrow + (long)r * P;
+	double cur[SV_D], nxt[SV_D];
 #pragma unroll
-		for (int j = 0; j < P; ++j) x = fma(-w[j], lr[j], x);
-		x *= g.dinv[r];
+	for (int j = 0; j < SV_D; ++j) cur[j] = (act && j < N) ? v[(long)row(0, j) * stride] : 0.0;
+	stage(0, 0);
+	__syncthreads();
+	for (int t = 0; t < ntile; ++t) {
+		const int buf = t & 1;
+		if (t + 1 < ntile) {
 #pragma unroll
-		for (int j = P - 1; j > 0; --j) w[j] = w[j - 1];
-		w[0] = x;
-		v[(long)r * stride] = x;
+			for (int j = 0; j < SV_D; ++j) nxt[j] = (act && (t + 1) * SV_D + j < N) ? v[(long)row(t + 1, j) * stride] : 0.0;
+			stage(t + 1, buf ^ 1);
+		}
+#pragma unroll
+		for (int j = 0; j < SV_D; ++j) {
+			if (t * SV_D + j < N) {
+				double x = cur[j];
+#pragma unroll
+				for (int q = 0; q < P; ++q) x = fma(-w[q], Lt[buf][j][q], x);
+				x *= Lt[buf][j][P];
+#pragma unroll
+				for (int q = P - 1; q > 0; --q) w[q] = w[q - 1];
+				w[0] = x;
+				if (act) v[(long)row(t, j) * stride] = x;
+			}
+		}
+		__syncthreads();
+#pragma unroll
+		for (int j = 0; j < SV_D; ++j) cur[j] = nxt[j];
 	}
-#pragma unroll
-	for (int j = 0; j < P; ++j) w[j] = 0.0;
-	for (int r = N - 1; r >= 0; --r) {
-		double x = v[(long)r * stride];
-		const double* lc = g.Lcol + (long)r * P;
-#pragma unroll
-		for (int j = 0; j < P; ++j) x = fma(-w[j], lc[j], x);
-		x *= g.dinv[r];
-#pragma unroll
-		for (int j = P - 1; j > 0; --j) w[j] = w[j - 1];
-		w[0] = x;
-		v[(long)r * stride] = x;
-	}
+}
+
+template <int P>
+__global__ void __launch_bounds__(CH_THREADS) k_ar_sinv(ar_args g, double2* __restrict__ vbuf)
+{
+	const int b = g.b0 + blockIdx.y;
+	if (g.flag[b] != AR_LIVE) return;
+	__shared__ double Lt[2][SV_D][P + 1];
+	const int c = blockIdx.x * CH_THREADS + threadIdx.x;
+	const bool act = c < 2 * g.nch;
+	const long stride = 2L * g.nch;
+	double* v = reinterpret_cast<double*>(vbuf + (long)b * g.n) + (act ? c : 0);
+	sinv_sweep<P, true>(g, v, stride, act, Lt);
+	sinv_sweep<P, false>(g, v, stride, act, Lt);
 }
 
 // ---------------------------------------------------------------- Gram-Schmidt
 // v -= u_i x_i for i <= k with i == k or |x_i|^2 > 4e-27, i ascending (la_1e.hpp:212-219)
 __global__ void __launch_bounds__(AR_THREADS) k_ar_orth(ar_args g, double2* __restrict__ vbuf, int k)
 {
-	const int b = blockIdx.y;
+	const int b = g.b0 + blockIdx.y;
 	if (g.flag[b] != AR_LIVE) return;
 	__shared__ double2 xs[AR_KMAX];
 	__shared__ int use[AR_KMAX];
@@ -373,7 +421,7 @@ __global__ void __launch_bounds__(AR_THREADS) k_ar_orth(ar_args g, double2* __re
 // Then x_j = b0 sum_i z_i[0] exp(-i dt d_i) z_i[j].
 __global__ void __launch_bounds__(32) k_ar_small(ar_args g, long step)
 {
-	const int b = blockIdx.x, lane = threadIdx.x;
+	const int b = g.b0 + blockIdx.x, lane = threadIdx.x;
 	const int fl = g.flag[b];
 	if (fl == AR_IDLE) return;
 	const int m = fl == AR_BROKEN ? g.msub[b] : g.kmax;
@@ -453,7 +501,7 @@ __global__ void __launch_bounds__(32) k_ar_small(ar_args g, long step)
 // w = sum_{i<m} u_i x_i (eliminate_sub, la_1e.hpp:176-193)
 __global__ void __launch_bounds__(AR_THREADS) k_ar_combine(ar_args g)
 {
-	const int b = blockIdx.y;
+	const int b = g.b0 + blockIdx.y;
 	const int fl = g.flag[b];
 	if (fl == AR_IDLE) return;
 	const int m = fl == AR_BROKEN ? g.msub[b] : g.kmax;
@@ -486,8 +534,8 @@ struct qpc_arnoldi {
 	int P = 0, nch = 0, nlh = 0, kmax = 0, nbe = 0, hper = 0;
 	long n = 0;
 	double dt = 0, emin = 0, emax = 0;
-	cudaStream_t stream = nullptr;
-	cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+	cudaStream_t stream = nullptr, stream2 = nullptr;	// stream2: second instance group (n_inst >= 2)
+	cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr;
 	double *S = nullptr, *R = nullptr, *Lrow = nullptr, *Lcol = nullptr, *dinv = nullptr, *H = nullptr, *y10 = nullptr;
 	double2 *X = nullptr, *U = nullptr, *V0 = nullptr, *V1 = nullptr, *tmp = nullptr;
 	double2* partX = nullptr;
@@ -517,7 +565,9 @@ void ar_free(qpc_arnoldi* h)
 		if (p) cudaFree(p);
 	if (h->ev0) cudaEventDestroy(h->ev0);
 	if (h->ev1) cudaEventDestroy(h->ev1);
+	if (h->ev2) cudaEventDestroy(h->ev2);
 	if (h->stream) cudaStreamDestroy(h->stream);
+	if (h->stream2) cudaStreamDestroy(h->stream2);
 	delete h;
 }
 
@@ -525,7 +575,7 @@ ar_args make_args(qpc_arnoldi* h)
 {
 	ar_args g{};
 	g.N = h->d.n_r; g.P = h->P; g.L = h->d.n_l; g.M = h->d.n_m; g.m0 = h->d.m0; g.nch = h->nch; g.nlh = h->nlh;
-	g.B = h->d.n_inst; g.kmax = h->kmax; g.nbe = h->nbe; g.n = h->n;
+	g.B = h->d.n_inst; g.kmax = h->kmax; g.nbe = h->nbe; g.n = h->n; g.b0 = 0;
 	g.hstride = h->hper ? (long)h->d.n_r * (h->P + 1) * h->nlh : 0;
 	g.dt = h->dt; g.emin = h->emin; g.emax = h->emax;
 	g.S = h->S; g.R = h->R; g.Lrow = h->Lrow; g.Lcol = h->Lcol; g.dinv = h->dinv; g.H = h->H; g.y10 = h->y10;
@@ -536,9 +586,9 @@ ar_args make_args(qpc_arnoldi* h)
 	return g;
 }
 
-void launch_sinv(const ar_args& g, double2* v, cudaStream_t st)
+void launch_sinv(const ar_args& g, int Bg, double2* v, cudaStream_t st)
 {
-	dim3 grid((2 * g.nch + CH_THREADS - 1) / CH_THREADS, g.B);
+	dim3 grid((2 * g.nch + CH_THREADS - 1) / CH_THREADS, Bg);
 	switch (g.P) {
 	case 1: k_ar_sinv<1><<<grid, CH_THREADS, 0, st>>>(g, v); break;
 	case 2: k_ar_sinv<2><<<grid, CH_THREADS, 0, st>>>(g, v); break;
@@ -551,11 +601,10 @@ void launch_sinv(const ar_args& g, double2* v, cudaStream_t st)
 	}
 }
 
-// one Arnoldi step of every live instance: 4 kmax launches
-long launch_step(qpc_arnoldi* h, const ar_args& g, long step)
+// one Arnoldi step of instances [g.b0, g.b0 + Bg) on stream st: 4 kmax launches
+long launch_step(qpc_arnoldi* h, const ar_args& g, int Bg, cudaStream_t st, long step)
 {
-	cudaStream_t st = h->stream;
-	dim3 ge(g.nbe, g.B);
+	dim3 ge(g.nbe, Bg);
 	long nl = 0;
 	k_ar_snorm<<<ge, AR_THREADS, 0, st>>>(g, h->X, -1, step); ++nl;
 	double2* src = h->X;
@@ -563,12 +612,12 @@ long launch_step(qpc_arnoldi* h, const ar_args& g, long step)
 		double2* dst = (k & 1) ? h->V1 : h->V0;
 		k_ar_expand<<<ge, AR_THREADS, 0, st>>>(g, src, dst, k, step); ++nl;
 		if (k == g.kmax - 1) break; // u_kmax is never used (eliminate_sub sums i < m)
-		launch_sinv(g, dst, st); ++nl;
+		launch_sinv(g, Bg, dst, st); ++nl;
 		k_ar_orth<<<ge, AR_THREADS, 0, st>>>(g, dst, k); ++nl;
 		k_ar_snorm<<<ge, AR_THREADS, 0, st>>>(g, dst, k, step); ++nl;
 		src = dst;
 	}
-	k_ar_small<<<g.B, 32, 0, st>>>(g, step); ++nl;
+	k_ar_small<<<Bg, 32, 0, st>>>(g, step); ++nl;
 	k_ar_combine<<<ge, AR_THREADS, 0, st>>>(g); ++nl;
 	return nl;
 }
@@ -648,6 +697,9 @@ int qpc_arnoldi_create(const qpc_dims* dims, const double* S, const double* R, c
 	QPC_CUDA(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
 	QPC_CUDA(cudaEventCreate(&h->ev0));
 	QPC_CUDA(cudaEventCreate(&h->ev1));
+	QPC_CUDA(cudaEventCreateWithFlags(&h->ev2, cudaEventDisableTiming));
+	if (B >= 2 && !(getenv("QPC_STREAMS") && atoi(getenv("QPC_STREAMS")) == 1))
+		QPC_CUDA(cudaStreamCreateWithFlags(&h->stream2, cudaStreamNonBlocking));
 	const long nst = (long)B * h->n;
 	if ((rc = dalloc(&h->S, (size_t)N * NE)) || (rc = dalloc(&h->R, (size_t)N * NE)) || (rc = dalloc(&h->Lrow, (size_t)N * P)) ||
 		(rc = dalloc(&h->Lcol, (size_t)N * P)) || (rc = dalloc(&h->dinv, (size_t)N)) || (rc = dalloc(&h->H, Hr.size())) ||
@@ -761,9 +813,24 @@ int qpc_arnoldi_run(qpc_arnoldi* h, const double* ez, int64_t ld, const int64_t*
 		QPC_CUDA(cudaMemsetAsync(h->msub_out, 0xff, cap, h->stream));
 	} else g.crit = g.msub_out = nullptr;
 	long nl = 0;
+	// two instance groups on two streams: the latency-bound S^-1 sweeps of one group
+	// overlap the band products of the other (instances never interact)
+	const int ng = h->stream2 ? 2 : 1;
+	int gb[3] = {0, ng == 2 ? (B + 1) / 2 : B, B};
+	cudaStream_t gs[2] = {h->stream, h->stream2};
 	QPC_CUDA(cudaEventRecord(h->ev0, h->stream));
-	for (long s = 0; s < ntmax; ++s) nl += launch_step(h, g, s);
+	if (ng == 2) QPC_CUDA(cudaStreamWaitEvent(h->stream2, h->ev0, 0));
+	for (long s = 0; s < ntmax; ++s)
+		for (int q = 0; q < ng; ++q) {
+			ar_args gq = g;
+			gq.b0 = gb[q];
+			nl += launch_step(h, gq, gb[q + 1] - gb[q], gs[q], s);
+		}
 	QPC_CUDA(cudaGetLastError());
+	if (ng == 2) {
+		QPC_CUDA(cudaEventRecord(h->ev2, h->stream2));
+		QPC_CUDA(cudaStreamWaitEvent(h->stream, h->ev2, 0));
+	}
 	QPC_CUDA(cudaEventRecord(h->ev1, h->stream));
 	if (int rc = wait_on(h->stream)) return rc;
 	cudaEventElapsedTime(&h->last_ms, h->ev0, h->ev1);

@@ -39,6 +39,8 @@
 #include <string>
 #include <time.h>
 #include <thread>
+#include <mutex>
+#include <map>
 #include <cstdlib>
 #include "qpc_chain.cuh"
 
@@ -650,8 +652,25 @@ int launch_step(qpc_lgwz* h, long step, long step0, int jslot, bool do_factor, i
 	}
 }
 
-void set_smem_attrs(qpc_lgwz* h)
+// The dynamic shared-memory limit is a property of the kernel on a device, shared by
+// every handle: it only ever grows, to the largest size any handle on that device needs.
+std::mutex g_attr_mu;
+std::map<std::pair<int, int>, size_t> g_attr_max;	// (device, kernel family) -> limit set
+
+bool raise_attr(int dev, int family, size_t smem)
 {
+	std::lock_guard<std::mutex> lk(g_attr_mu);
+	size_t& cur = g_attr_max[{dev, family}];
+	if (smem <= cur) return false;
+	cur = smem;
+	return true;
+}
+
+void set_smem_attrs(qpc_lgwz* h, size_t tr_smem)
+{
+	if (tr_smem > 48 * 1024 && raise_attr(h->dev, 0, tr_smem))
+		cudaFuncSetAttribute(k_transform, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tr_smem);
+	if (!raise_attr(h->dev, h->P, h->chain_smem)) return;
 	switch (h->P) {
 	case 3: set_chain_smem_attr<3>(h->chain_smem); break;
 	case 4: set_chain_smem_attr<4>(h->chain_smem); break;
@@ -767,10 +786,9 @@ int qpc_lgwz_create(const qpc_dims* dims, double dt, const double* S, const doub
 		return fail(QPC_ERR_CUDA);
 	}
 	size_t smem = sizeof(double2) * 2 * TR * (L | 1);
-	if (smem > 48 * 1024) cudaFuncSetAttribute(k_transform, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 	h->chain_smem = sizeof(double) * (size_t)N * NE;
 	if (h->chain_smem > 200 * 1024) { set_error("n_r=%d too large for the shared-memory S band", N); return fail(QPC_ERR_ARGS); }
-	set_smem_attrs(h);
+	set_smem_attrs(h, smem);
 	std::memset(h->gsel, 0, sizeof(h->gsel));
 	for (int g = 1; g <= P; ++g) if (P % g == 0 && (g <= 4 || g == P)) h->gcand.push_back(g);
 	*out = h;
