@@ -1,0 +1,192 @@
+"""Learned surrogate for the laser scan: laser parameters -> photoelectron and harmonic
+spectra, with the batched TDSE engine as the label generator and the fallback.
+
+No counterpart in the reference.  Pieces:
+  * draw_params      the batched laser scan's parameter distribution: peak intensity
+                     log-uniform in [5e13, 5e14] W/cm^2, wavelength uniform in
+                     [400, 2000] nm, CEP uniform in [0, 2 pi), integer sin^2 cycles 2..10,
+                     ellipticity 0 (the length-gauge engine is z-linear).
+  * features         6 network inputs: log10(I / 1e14 W/cm^2), (lambda - 1200)/800,
+                     sin CEP, cos CEP, (cycles - 6)/4, ellipticity.
+  * tdse_spectra     runs the batched Crank-Nicolson engine (hydrogen, B-splines of
+                     degree 6, N_r = 800 on [0, 400], l < 41, dt = 0.05) from the ground
+                     state through each pulse, recording <z>(t) in the loop, then projects
+                     on the field-free eigenstates.  Labels:
+                       PES  256 bins on [0, 3.17 U_p): sum |<E_n|psi>|^2 g(E - E_n) with a
+                            Gaussian g of width 3.17 U_p / 128 (the box's discrete
+                            continuum broadened), times U_p, as log10(max(., 1e-10));
+                       HHG  harmonic orders 1..128: mean of S(w) (plot_hhs.m restated,
+                            sin^2 window over the pulse) over w / w0 in [q - 1/2, q + 1/2),
+                            as log10(max(., 1e-30)).
+  * Surrogate        a 5-member ensemble of 6 -> 4 x 256 GELU -> 384 MLPs trained on the GPU
+                     (qpc_mlp: bfloat16 operands, fp32 accumulation, Adam) on standardised
+                     targets; query() answers from the ensemble mean when the members agree
+                     (mean over outputs of the standard deviation, in standardised units,
+                     below the threshold) and the ellipticity is 0, and runs the TDSE engine
+                     for every other query.
+"""
+import importlib
+import time
+
+import numpy as np
+
+C2_GRID = dict(n_r=800, p=6, n_l=41, rmax=400.0, dt=0.05)
+N_PES, N_HHG = 256, 128
+
+
+def _q():
+    return importlib.import_module(__name__.rsplit(".", 1)[0])
+
+
+def draw_params(n, seed):
+    rng = np.random.default_rng(seed)
+    return {
+        "intensity": 10 ** rng.uniform(np.log10(5e13), np.log10(5e14), n),
+        "wavelength": rng.uniform(400.0, 2000.0, n),
+        "cep": rng.uniform(0.0, 2 * np.pi, n),
+        "cycles": rng.integers(2, 11, n).astype(np.float64),
+        "ellipticity": np.zeros(n),
+    }
+
+
+def features(p):
+    return np.stack([np.log10(p["intensity"] / 1e14), (p["wavelength"] - 1200.0) / 800.0, np.sin(p["cep"]), np.cos(p["cep"]),
+                     (p["cycles"] - 6.0) / 4.0, p["ellipticity"]], axis=1).astype(np.float32)
+
+
+def up(p):
+    """Ponderomotive energy E0^2 / (4 w^2) per parameter set [a.u.]"""
+    q = _q()
+    e0 = np.array([q.intensity_to_e0(i) for i in p["intensity"]])
+    w0 = np.array([q.wavelength_to_w0(l) for l in p["wavelength"]])
+    return e0 ** 2 / (4 * w0 ** 2)
+
+
+class _Setup:
+    """Grid, matrices, ground state and field-free eigenbasis of one TDSE grid."""
+
+    def __init__(self, grid, emax):
+        q = _q()
+        g = dict(grid)
+        self.g = g
+        kn = q.linear_knots(g["n_r"], g["p"], 0.0, g["rmax"])
+        self.S, self.R, _, _, self.H = q.radial_setup(g["n_r"], g["p"], g["n_l"], kn)
+        self.c0, self.e0 = q.ground_state(self.S, self.H, g["n_l"])
+        self.n_state, self.basis, self.energies = q.left_eigenbasis(self.S, self.H, g["n_l"] - 1, emax)
+        self.energy = np.concatenate(self.energies)
+
+
+def _pes_label(proj, energy, u):
+    """Gaussian-broadened PES on [0, 3.17 U_p), 256 bins, in units of 1/U_p, log10."""
+    emax = 3.17 * u
+    edges = np.linspace(0.0, emax, N_PES + 1)
+    centres = 0.5 * (edges[1:] + edges[:-1])
+    w = np.abs(proj) ** 2
+    keep = (energy > -0.5 * emax) & (energy < 1.5 * emax)
+    sig = emax / 128.0
+    d = (centres[:, None] - energy[keep][None, :]) / sig
+    dens = (np.exp(-0.5 * d * d) / (sig * np.sqrt(2 * np.pi))) @ w[keep]
+    return np.log10(np.maximum(dens * u, 1e-10))
+
+
+def _hhg_label(z, dt, w0):
+    q = _q()
+    n = z.size
+    om, s = q.hhg_spectrum(z, dt, 0.0, 0.0, dt * (n - 1))
+    h = om / w0
+    out = np.full(N_HHG, 1e-30)
+    for k in range(N_HHG):
+        sel = (h >= k + 0.5) & (h < k + 1.5)
+        if sel.any():
+            out[k] = max(float(s[sel].mean()), 1e-30)
+    return np.log10(out)
+
+
+def tdse_spectra(p, grid=C2_GRID, batch=256, setup=None, log=None):
+    """PES and HHG labels [n][256], [n][128] for parameter sets p (ellipticity must be 0),
+    from the batched engine in batches of `batch`.  Returns (pes, hhg, info)."""
+    q = _q()
+    n = len(p["intensity"])
+    if np.any(p["ellipticity"] != 0):
+        raise ValueError("the TDSE engine here is z-linear: ellipticity must be 0")
+    u = up(p)
+    if setup is None:
+        setup = _Setup(grid, emax=max(3.17 * float(u.max()) * 1.5, 1.0))
+    g = setup.g
+    pes = np.zeros((n, N_PES), np.float32)
+    hhg = np.zeros((n, N_HHG), np.float32)
+    wf_steps, t_run = 0, 0.0
+    prop = None
+    for b0 in range(0, n, batch):
+        idx = np.arange(b0, min(n, b0 + batch))
+        B = idx.size
+        tabs = [q.field_sinen(q.intensity_to_e0(p["intensity"][i]), q.wavelength_to_w0(p["wavelength"][i]), p["cycles"][i], 0.0,
+                              p["cep"][i] / np.pi, g["dt"]) for i in idx]
+        nt = np.array([t.size - 1 for t in tabs], np.int64)
+        ftab = np.zeros((B, int(nt.max()) + 1))
+        for k, t in enumerate(tabs):
+            ftab[k, :t.size] = t
+        if prop is None or prop.shape[0] != B:
+            prop = q.propagator_cn_hc_lgwz().initialize(g["n_r"], g["p"], g["n_l"], setup.S, setup.R, setup.H, g["dt"], n_inst=B)
+        prop.put(np.broadcast_to(setup.c0, (B,) + setup.c0.shape))
+        t0 = time.time()
+        z = prop.run_dipole(ftab, nt, nt, setup.R)
+        t_run += time.time() - t0
+        wf_steps += int(nt.sum())
+        proj = prop.projection(setup.n_state, setup.basis).reshape(B, -1)
+        for k, i in enumerate(idx):
+            pes[i] = _pes_label(proj[k], setup.energy, u[i])
+            hhg[i] = _hhg_label(z[k, :nt[k]], g["dt"], q.wavelength_to_w0(p["wavelength"][i]))
+        if log:
+            log("batch %d-%d: %d wf-steps, %.1f s" % (idx[0], idx[-1], int(nt.sum()), time.time() - t0))
+    return pes, hhg, {"wf_steps": wf_steps, "run_s": t_run}
+
+
+class Surrogate:
+    """Ensemble MLP surrogate with TDSE fallback."""
+
+    def __init__(self, n_members=5, n_hidden=256, n_layers=4, seed=0):
+        self.n_members, self.n_hidden, self.n_layers, self.seed = n_members, n_hidden, n_layers, seed
+        self.net = None
+
+    def fit(self, p, pes, hhg, epochs=400, batch=256, lr=1e-3):
+        q = _q()
+        X = features(p)
+        Y = np.concatenate([pes, hhg], axis=1).astype(np.float64)
+        self.mu = Y.mean(axis=0)
+        self.sd = np.maximum(Y.std(axis=0), 1e-3)
+        Yn = ((Y - self.mu) / self.sd).astype(np.float32)
+        self.net = q.mlp_ensemble(X.shape[1], Y.shape[1], self.n_hidden, self.n_layers, self.n_members, self.seed)
+        return self.net.train(X, Yn, epochs, batch, lr, seed=self.seed + 1)
+
+    def predict(self, p):
+        """(mean [n][384], disagreement [n]) in label units; disagreement is the mean over
+        outputs of the members' standard deviation in standardised units."""
+        y = self.net.predict(features(p)).astype(np.float64)
+        mean = y.mean(axis=0) * self.sd + self.mu
+        dis = y.std(axis=0).mean(axis=1)
+        return mean, dis
+
+    def calibrate(self, p_val, y_val, quantile=0.9):
+        """Threshold on the disagreement: the given quantile over a validation set."""
+        _, dis = self.predict(p_val)
+        self.threshold = float(np.quantile(dis, quantile))
+        return self.threshold
+
+    def query(self, p, threshold=None, setup=None):
+        """Spectra [n][384] for parameter sets p, and the mask of queries the TDSE answered.
+        Out-of-trust queries (disagreement above the threshold, or ellipticity != 0) go to
+        the TDSE engine; a nonzero ellipticity needs an elliptical propagator and raises."""
+        thr = self.threshold if threshold is None else threshold
+        mean, dis = self.predict(p)
+        fall = (dis > thr) | (p["ellipticity"] != 0)
+        if fall.any():
+            sub = {k: v[fall] for k, v in p.items()}
+            pes, hhg, _ = tdse_spectra(sub, setup=setup)
+            mean[fall] = np.concatenate([pes, hhg], axis=1)
+        return mean, fall
+
+
+def rel_l2(pred, ref):
+    """per-row relative L2 error of log-scaled spectra"""
+    return np.linalg.norm(pred - ref, axis=1) / np.linalg.norm(ref, axis=1)
