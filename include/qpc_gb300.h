@@ -95,6 +95,12 @@ int qpc_ldlt_csym(int32_t n, int32_t p, const double* S, const double* H, double
  * ascending, and the lowest n_want S-normalised eigenvectors (rows of vec). */
 int qpc_gen_eigen(int32_t n, int32_t p, const double* S, const double* Hl, int32_t n_want, double* energy, double* vec);
 
+/* Angular couplings of propagator_cn_hc_vgwr (cn_1e.hpp:836-890) on the channels
+ * ch = im*n_l + il: comp 0 = x1 (Y11, mult 1), 1 = x2 (Q11, mult -i), 2 = y1 (Y11, mult -i),
+ * 3 = y2 (Q11, mult 1) (operator_y11/q11::solve_eigen, operators/1e.hpp:336-523).
+ * lam[N_ch] ascending and P[N_ch][N_ch] complex with P Z P^H = diag(lam). */
+int qpc_vgwr_angular(int32_t n_l, int32_t n_m, int32_t m0, int32_t comp, double* lam, double* P);
+
 /* lu_dsb (LAPACKE_dpbtrf 'L', algorithm/ed.h:182-193) as operator_sc::initialize uses it
  * (spherical/operators/1e.hpp:1233-1244): S = L L^T with L(r+k, r) at L[r*(p+1)+k], the
  * layout of operator_sc::cholesky(); entries past the last row are zero.  Returns 0, -1 on
@@ -211,6 +217,27 @@ int qpc_lgwz_set_profiling(qpc_lgwz* h, int on);
  * out must hold 65 values. */
 int qpc_lgwz_get_tuning(qpc_lgwz* h, int32_t* out);
 int qpc_lgwz_kernel_times(qpc_lgwz* h, double* ms, int64_t* launches);
+
+/* ---------------------------------------------------------------- velocity gauge, elliptical
+ * Replaces propagator_cn_hc_vgwr (spherical/propagator/cn_1e.hpp:812-951): initialize with
+ * S, Rinv = <B|1/r|B>, D = <B_i|d/dr B_j> (upper entries of the anti-symmetric band) and H
+ * [lmax+1][n_r][p+1]; propagate(coef, ax_ti, ax_tf, ay_ti, ay_tf) and propagate(coef)
+ * (cn_1e.hpp:903-950) per instance; run() the driver loop (sphTDSE.cpp:930-950 for the
+ * elliptical pulse) with atab[inst][s][2] = (A_x, A_y)(t_s), s = 0..nt_field[inst].
+ * The four coupling transforms are dense n_m n_l x n_m n_l matrices (cuBLAS GEMMs). */
+typedef struct qpc_vgwr qpc_vgwr;
+int qpc_vgwr_create(const qpc_dims* dims, double dt, const double* S, const double* Rinv, const double* D, const double* H,
+	qpc_vgwr** out);
+int qpc_vgwr_destroy(qpc_vgwr* h);
+int qpc_vgwr_put(qpc_vgwr* h, const double* coef);
+int qpc_vgwr_get(qpc_vgwr* h, double* coef);
+int qpc_vgwr_put_device(qpc_vgwr* h, const double* dev_coef);
+int qpc_vgwr_get_device(qpc_vgwr* h, double* dev_coef);
+int qpc_vgwr_propagate(qpc_vgwr* h, const double* ax_ti, const double* ax_tf, const double* ay_ti, const double* ay_tf);
+int qpc_vgwr_propagate_free(qpc_vgwr* h);
+int qpc_vgwr_run(qpc_vgwr* h, const double* atab, int64_t ld, const int64_t* nt_field, const int64_t* nt_total);
+int qpc_vgwr_norm(qpc_vgwr* h, double* norm);
+int qpc_vgwr_last_run(qpc_vgwr* h, float* ms, int64_t* launches);
 
 /* ---------------------------------------------------------------- Arnoldi propagator
  * Replaces propagator_hc_lgwz (spherical/propagator/la_1e.hpp:390-444) with

@@ -122,8 +122,8 @@ void hc_channel(int n, int p, const cx* up, const cx* lo, cx* c, cx* w)
 	}
 }
 
-// ---------------------------------------------------------------- coupling CN (propagate.hpp:3-98), symflag = 0
-void cn_channel(int n, int p, const double* smat, const double* rmat, cx ifet, cx* z, cx* y, cx* u)
+// ---------------------------------------------------------------- coupling CN (propagate.hpp:3-98), symflag 0 or 1
+void cn_channel(int n, int p, const double* smat, const double* rmat, cx ifet, cx* z, cx* y, cx* u, bool anti = false)
 {
 	const int ne = p + 1;
 	cx a[2 * 16 + 1], b[2 * 16 + 1];
@@ -135,8 +135,9 @@ void cn_channel(int n, int p, const double* smat, const double* rmat, cx ifet, c
 			else {
 				double s = smat[k], r = rmat[k];
 				cx fr = cmul(ifet, r);
-				a[_j] = csub({s, 0.0}, fr);
-				b[_j] = cadd({s, 0.0}, fr);
+				// symflag = 1: r is the upper entry of an anti-symmetric band (propagate.hpp:45-47)
+				a[_j] = anti ? cadd({s, 0.0}, fr) : csub({s, 0.0}, fr);
+				b[_j] = anti ? csub({s, 0.0}, fr) : cadd({s, 0.0}, fr);
 			}
 		}
 		for (int j = 0; j < ne; ++j) {
@@ -348,6 +349,136 @@ void oracle_dipole(const oracle_lgwz* g, const double* F, const double* y10, con
 			}
 		out[2 * k] = s.re;
 		out[2 * k + 1] = s.im;
+	}
+}
+
+// ---------------------------------------------------------------- velocity gauge, elliptical
+// propagator_cn_hc_vgwr::propagate (cn_1e.hpp:903-945): four coupling components, each a
+// dense (m,l) transform and one banded CN per eigen-channel, around the field-free step.
+//   x1: P_x1 (real), cn_hm_propagate2 with D (anti-symmetric), f = -A_x/2
+//   x2: P_x2 P_x1^H, cn_hm_propagate1 with 1/r, f = +A_x/2
+//   y1: P_y1 P_x2^H, propagate2 with D, f = -A_y/2
+//   y2: P_y2 P_y1^H, propagate1 with 1/r, f = -A_y/2, then P_y2^H
+// then the field-free step and the mirror image with the t_f values.  Component steps are
+// dt/2 (cn_1e.hpp:869-872); propagate1 uses ifet = i lam f step/2, propagate2 ifet = -lam f
+// step/2 (propagate.hpp:443-568).
+struct oracle_vgwr {
+	int32_t n_r, p, n_l, n_m, m0, n_inst;
+	double dt;
+	const double* S;      // [n_r][p+1]
+	const double* Rinv;   // [n_r][p+1]  <B|1/r|B>
+	const double* D;      // [n_r][p+1]  <B_i|d/dr B_j>, upper entries of an anti-symmetric band
+	const double* upper;  // [lmax+1][n_r][p+1] complex, S - i dt/2 H_l
+	const double* lower;  // [lmax+1][n_r][p+1] complex, lu_zsb(S + i dt/2 H_l)
+	const double* lam[4]; // [N_ch] eigenvalues of x1, x2, y1, y2
+	const double* P[4];   // [N_ch][N_ch] complex, P Z P^H = diag(lam)
+};
+
+// dst[k][r] = sum_ch A[k][ch] src[ch][r] (A complex N x N, conj_t: use A^H)
+static void dense_apply(int N, int nr, const cx* A, bool herm, const cx* src, cx* dst)
+{
+	for (int k = 0; k < N; ++k)
+		for (int r = 0; r < nr; ++r) dst[(long)k * nr + r] = {0.0, 0.0};
+	for (int k = 0; k < N; ++k)
+		for (int c = 0; c < N; ++c) {
+			cx a = herm ? cx{A[(long)c * N + k].re, -A[(long)c * N + k].im} : A[(long)k * N + c];
+			if (a.re == 0.0 && a.im == 0.0) continue;
+			const cx* s = src + (long)c * nr;
+			cx* d = dst + (long)k * nr;
+			for (int r = 0; r < nr; ++r) d[r] = cadd(d[r], cmul(a, s[r]));
+		}
+}
+
+static std::vector<cx> merge(int N, const cx* L, const cx* R)
+{	// L R^H
+	std::vector<cx> M((size_t)N * N, cx{0.0, 0.0});
+	for (int i = 0; i < N; ++i)
+		for (int j = 0; j < N; ++j) {
+			cx s = {0.0, 0.0};
+			for (int k = 0; k < N; ++k) s = cadd(s, cmul(L[(long)i * N + k], cx{R[(long)j * N + k].re, -R[(long)j * N + k].im}));
+			M[(size_t)i * N + j] = s;
+		}
+	return M;
+}
+
+static void vg_component(const oracle_vgwr* g, cx* w, int comp, double f, std::vector<cx>& y, std::vector<cx>& u)
+{
+	const int N = g->n_l * g->n_m, nr = g->n_r, p = g->p;
+	const double step = g->dt * 0.5;
+	const bool anti = comp == 0 || comp == 2;
+	const double frdt = f * step;
+	for (int c = 0; c < N; ++c) {
+		double lam = g->lam[comp][c];
+		cx ifet = anti ? cx{lam * (-frdt / 2), 0.0} : cx{lam * 0.0, lam * (frdt / 2)};
+		cn_channel(nr, p, g->S, anti ? g->D : g->Rinv, ifet, w + (long)c * nr, y.data(), u.data(), anti);
+	}
+}
+
+void oracle_vgwr_step(const oracle_vgwr* g, double* coef, const double* ax_ti, const double* ax_tf, const double* ay_ti,
+	const double* ay_tf, int nthreads)
+{
+	const int N = g->n_l * g->n_m, nr = g->n_r, p = g->p;
+	const long per = (long)N * nr;
+	const cx* P[4] = {(const cx*)g->P[0], (const cx*)g->P[1], (const cx*)g->P[2], (const cx*)g->P[3]};
+	std::vector<cx> m12 = merge(N, P[1], P[0]), m23 = merge(N, P[2], P[1]), m34 = merge(N, P[3], P[2]);
+	#pragma omp parallel for num_threads(nthreads) schedule(dynamic, 1)
+	for (int k = 0; k < g->n_inst; ++k) {
+		cx* c = (cx*)coef + k * per;
+		std::vector<cx> w(per), y(nr), u((size_t)nr * p), wk(nr);
+		if (!ax_ti) {
+			for (int im = 0; im < g->n_m; ++im)
+				for (int il = 0; il < g->n_l; ++il) {
+					long l = lof(im, il, g->m0);
+					cx* z = c + ((long)im * g->n_l + il) * nr;
+					hc_channel(nr, p, (const cx*)g->upper + l * nr * (p + 1), (const cx*)g->lower + l * nr * (p + 1), z, wk.data());
+				}
+			continue;
+		}
+		const double axi = ax_ti[k] / 2.0, axf = ax_tf[k] / 2.0, ayi = ay_ti[k] / 2.0, ayf = ay_tf[k] / 2.0;
+		dense_apply(N, nr, P[0], false, c, w.data());
+		vg_component(g, w.data(), 0, -axi, y, u);
+		dense_apply(N, nr, m12.data(), false, w.data(), c);
+		vg_component(g, c, 1, axi, y, u);
+		dense_apply(N, nr, m23.data(), false, c, w.data());
+		vg_component(g, w.data(), 2, -ayi, y, u);
+		dense_apply(N, nr, m34.data(), false, w.data(), c);
+		vg_component(g, c, 3, -ayi, y, u);
+		dense_apply(N, nr, P[3], true, c, w.data());
+		for (int im = 0; im < g->n_m; ++im)
+			for (int il = 0; il < g->n_l; ++il) {
+				long l = lof(im, il, g->m0);
+				cx* z = w.data() + ((long)im * g->n_l + il) * nr;
+				hc_channel(nr, p, (const cx*)g->upper + l * nr * (p + 1), (const cx*)g->lower + l * nr * (p + 1), z, wk.data());
+			}
+		dense_apply(N, nr, P[3], false, w.data(), c);
+		vg_component(g, c, 3, -ayf, y, u);
+		dense_apply(N, nr, m34.data(), true, c, w.data());
+		vg_component(g, w.data(), 2, -ayf, y, u);
+		dense_apply(N, nr, m23.data(), true, w.data(), c);
+		vg_component(g, c, 1, axf, y, u);
+		dense_apply(N, nr, m12.data(), true, c, w.data());
+		vg_component(g, w.data(), 0, -axf, y, u);
+		dense_apply(N, nr, P[0], true, w.data(), c);
+	}
+}
+
+// nt_total steps per instance: step s < nt_field uses (A_x, A_y) at t_s and t_{s+1} from
+// atab[(inst*ld + s)*2 + {0,1}], later steps are field-free
+void oracle_vgwr_run(const oracle_vgwr* g, double* coef, const double* atab, long ld, const int64_t* nt_field,
+	const int64_t* nt_total, int nthreads)
+{
+	const long per = (long)g->n_l * g->n_m * g->n_r;
+	#pragma omp parallel for num_threads(nthreads) schedule(dynamic, 1)
+	for (int k = 0; k < g->n_inst; ++k) {
+		oracle_vgwr one = *g;
+		one.n_inst = 1;
+		double* c = coef + 2 * k * per;
+		for (long s = 0; s < nt_total[k]; ++s) {
+			if (s < nt_field[k]) {
+				const double* a = atab + (k * ld + s) * 2;
+				oracle_vgwr_step(&one, c, a, a + 2, a + 1, a + 3, 1);
+			} else oracle_vgwr_step(&one, c, nullptr, nullptr, nullptr, nullptr, 1);
+		}
 	}
 }
 

@@ -9,7 +9,8 @@
 //
 // Grid sizes are compile-time in the reference (dimension_1e<...>), so the
 // Makefile builds one binary per grid with -DHNR (active B-splines),
-// -DHMR (B-spline degree p), -DHNL (number of l channels), m = 0 only.
+// -DHMR (B-spline degree p), -DHNL (number of l channels per m), -DHNM (number
+// of m channels) and -DHM0 (first m).
 //
 // Commands (all arrays are written as raw little-endian float64 files):
 //   setup  OUT RMAX DT ZC ZS SG
@@ -30,6 +31,11 @@
 //   arnoldi OUT RMAX DT ZC ZS SG INIT FIELD NT KMAX EMIN EMAX
 //       NT steps of the Arnoldi propagator propagator_hc_lgwz (la_1e.hpp:390-444)
 //       with ez = FIELD[i] during step i; see cmd_arnoldi.
+//   vgwr   OUT RMAX DT ZC ZS SG INIT FIELD NT NFREE
+//       the velocity-gauge elliptical propagator propagator_cn_hc_vgwr
+//       (cn_1e.hpp:812-951): FIELD holds NT+1 rows (A_x, A_y) at t_0..t_NT; runs
+//       propagate(coef, ax_i, ax_i+1, ay_i, ay_i+1) for i < NT, then NFREE field-free
+//       steps; writes coef, the S-norm and the eigenvalues of the four couplings.
 //   proj   OUT RMAX DT ZC ZS SG COEF EMAX
 //       Projection of COEF onto field-free eigenstates with E < EMAX
 //       (eigenstate_sph::initialize + projection, population_1e.hpp:29-118).
@@ -52,8 +58,14 @@ using namespace qpc::spherical;
 #ifndef HNL
 #define HNL 6
 #endif
+#ifndef HNM
+#define HNM 1
+#endif
+#ifndef HM0
+#define HM0 0
+#endif
 
-using dims_t = dimension_1e<HNR, HMR, HNL, 1, 0>;
+using dims_t = dimension_1e<HNR, HMR, HNL, HNM, HM0>;
 
 static void dump(const std::string& dir, const char* name, const void* p, size_t ndouble)
 {
@@ -299,6 +311,46 @@ static int cmd_arnoldi(int argc, char** argv)
 	return 0;
 }
 
+static int cmd_vgwr(int argc, char** argv)
+{
+	if (argc < 12) return 1;
+	std::string out = argv[2];
+	double rmax = atof(argv[3]), dt = atof(argv[4]);
+	potn_any potn{atof(argv[5]), atof(argv[6]), atof(argv[7])};
+	const char* init = argv[8];
+	const char* field = argv[9];
+	size_t nt = strtoul(argv[10], 0, 10), nfree = strtoul(argv[11], 0, 10);
+	omp_set_num_threads(1);
+	auto radi = integrator_radi<dims_t>();
+	auto angu = integrator_angu<dims_t>();
+	auto prop = propagator_cn_hc_vgwr<dims_t>();
+	init_prop(prop, radi, angu, rmax, dt, potn, 1);
+	auto coef = coefficient<dims_t>();
+	auto v = slurp(init, 2 * dims_t::n_leng);
+	std::memcpy((double*)coef.data, v.data(), sizeof(double) * v.size());
+	std::vector<double> f = nt ? slurp(field, 2 * (nt + 1)) : std::vector<double>{};
+	for (size_t it = 0; it < nt + nfree; ++it) {
+		if (it < nt) prop.propagate(coef, f[2 * it], f[2 * it + 2], f[2 * it + 1], f[2 * it + 3]);
+		else prop.propagate(coef);
+	}
+	dump(out, "coef", coef.data, 2 * dims_t::n_leng);
+	double norm = 0.0;
+	#pragma omp parallel
+	{
+		double part = 0.0;
+		prop.s.observe(coef.data, part);
+		#pragma omp atomic
+		norm += part;
+	}
+	dump(out, "norm", &norm, 1);
+	const size_t nc = dims_t::m_dims * dims_t::l_dims;
+	dump(out, "zeig_x1", prop.prop_x1.zeig.data, nc);
+	dump(out, "zeig_x2", prop.prop_x2.zeig.data, nc);
+	dump(out, "zeig_y1", prop.prop_y1.zeig.data, nc);
+	dump(out, "zeig_y2", prop.prop_y2.zeig.data, nc);
+	return 0;
+}
+
 int main(int argc, char** argv)
 {
 	if (argc < 2) { std::fprintf(stderr, "usage: setup|field|propagate|proj|arnoldi ...\n"); return 1; }
@@ -310,6 +362,7 @@ int main(int argc, char** argv)
 		else if (c == "propagate") rc = cmd_propagate(argc, argv);
 		else if (c == "proj") rc = cmd_proj(argc, argv);
 		else if (c == "arnoldi") rc = cmd_arnoldi(argc, argv);
+		else if (c == "vgwr") rc = cmd_vgwr(argc, argv);
 		if (rc) std::fprintf(stderr, "bad arguments for %s\n", argv[1]);
 		return rc;
 	} catch (std::exception& e) {

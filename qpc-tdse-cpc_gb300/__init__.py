@@ -37,7 +37,9 @@ EXPORTS = (
     "qpc_arnoldi_put", "qpc_arnoldi_get", "qpc_arnoldi_put_device", "qpc_arnoldi_get_device", "qpc_arnoldi_run",
     "qpc_arnoldi_propagate", "qpc_arnoldi_norm", "qpc_arnoldi_last_run", "qpc_lgwz_run_many",
     "qpc_mlp_create", "qpc_mlp_destroy", "qpc_mlp_param_count", "qpc_mlp_get_params", "qpc_mlp_set_params",
-    "qpc_mlp_loss_grad", "qpc_mlp_train", "qpc_mlp_predict",
+    "qpc_mlp_loss_grad", "qpc_mlp_train", "qpc_mlp_predict", "qpc_vgwr_angular", "qpc_vgwr_create",
+    "qpc_vgwr_destroy", "qpc_vgwr_put", "qpc_vgwr_get", "qpc_vgwr_put_device", "qpc_vgwr_get_device",
+    "qpc_vgwr_propagate", "qpc_vgwr_propagate_free", "qpc_vgwr_run", "qpc_vgwr_norm", "qpc_vgwr_last_run",
 )
 NOALLOC_MAX_ELEMS = 1 << 20
 KERNELS = ("factor", "transform_fwd", "sweep", "transform_bwd", "fieldfree")
@@ -108,6 +110,18 @@ def load(path=None):
         "qpc_cholesky_band": (ctypes.c_int, [i32, i32, P, P]),
         "qpc_lgwz_run_many": (ctypes.c_int, [i32, P, P, P, P, P, P]),
         "qpc_mlp_create": (ctypes.c_int, [i32, i32, i32, i32, i32, ctypes.c_uint64, P]),
+        "qpc_vgwr_angular": (ctypes.c_int, [i32, i32, i32, i32, P, P]),
+        "qpc_vgwr_create": (ctypes.c_int, [P, d, P, P, P, P, P]),
+        "qpc_vgwr_destroy": (ctypes.c_int, [P]),
+        "qpc_vgwr_put": (ctypes.c_int, [P, P]),
+        "qpc_vgwr_get": (ctypes.c_int, [P, P]),
+        "qpc_vgwr_put_device": (ctypes.c_int, [P, P]),
+        "qpc_vgwr_get_device": (ctypes.c_int, [P, P]),
+        "qpc_vgwr_propagate": (ctypes.c_int, [P, P, P, P, P]),
+        "qpc_vgwr_propagate_free": (ctypes.c_int, [P]),
+        "qpc_vgwr_run": (ctypes.c_int, [P, P, i64, P, P]),
+        "qpc_vgwr_norm": (ctypes.c_int, [P, P]),
+        "qpc_vgwr_last_run": (ctypes.c_int, [P, P, P]),
         "qpc_mlp_destroy": (ctypes.c_int, [P]),
         "qpc_mlp_param_count": (ctypes.c_int, [P, P]),
         "qpc_mlp_get_params": (ctypes.c_int, [P, i32, P]),
@@ -468,6 +482,19 @@ def run_many(props, ftabs, nt_field, nt_total=None):
     _check(load().qpc_lgwz_run_many(n, H, F, _ptr(LD), NF, NT, ctypes.byref(failed)))
 
 
+VGWR_COMPONENTS = ("x1", "x2", "y1", "y2")
+
+
+def vgwr_angular(n_l, n_m, m0, comp):
+    """(lam[N_ch], P[N_ch][N_ch] complex) of coupling component comp (0..3 = x1, x2, y1, y2)
+    of propagator_cn_hc_vgwr: P Z P^H = diag(lam)."""
+    N = n_l * n_m
+    lam = np.zeros(N)
+    P = np.zeros((N, N), complex)
+    _check(load().qpc_vgwr_angular(n_l, n_m, m0, comp, _ptr(lam), _ptr(P)))
+    return lam, P
+
+
 def cholesky_band(S, p):
     """S = L L^T, L(r+k, r) at [r, k] (operator_sc::cholesky(), operators/1e.hpp:1233-1244)."""
     S = _f64(S)
@@ -633,4 +660,81 @@ class mlp_ensemble:
         out = np.zeros((self.n_members, X.shape[0], self.n_out), np.float32)
         _check(load().qpc_mlp_predict(self._h, _ptr(X), X.shape[0], _ptr(out)))
         return out
+
+
+class propagator_cn_hc_vgwr:
+    """Batched GPU propagator_cn_hc_vgwr (velocity gauge, elliptical; cn_1e.hpp:812-951).
+
+    initialize(...) mirrors the reference's initialize (S, 1/r, D = <B|d/dr|B>, H_l per l);
+    propagate(ax_ti, ax_tf, ay_ti, ay_tf) and propagate() the two overloads (cn_1e.hpp:903-950)
+    for every instance; run(atab, nt_field, nt_total) the driver loop with atab[inst, s] =
+    (A_x(t_s), A_y(t_s)).  State c[inst][m][l][r] complex128."""
+
+    def __init__(self):
+        self._h = None
+
+    def initialize(self, n_r, p, n_l, n_m, m0, S, Rinv, D, H, dt, n_inst=1):
+        lib = load()
+        self.close()
+        d = qpc_dims(n_r, p, n_l, n_m, m0, n_inst)
+        lmax = max(abs(m0), abs(m0 + n_m - 1)) + n_l - 1
+        H = _f64(H)
+        if H.shape[0] < lmax + 1:
+            raise QpcError(1, "H needs lmax+1 = %d blocks" % (lmax + 1))
+        h = ctypes.c_void_p()
+        _check(lib.qpc_vgwr_create(ctypes.byref(d), dt, _ptr(_f64(S)), _ptr(_f64(Rinv)), _ptr(_f64(D)), _ptr(_f64(H[:lmax + 1])),
+                                   ctypes.byref(h)))
+        self._h = h
+        self.dims = d
+        self.shape = (n_inst, n_m, n_l, n_r)
+        return self
+
+    def close(self):
+        if self._h is not None:
+            load().qpc_vgwr_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def put(self, coef):
+        c = np.ascontiguousarray(coef, dtype=np.complex128).reshape(self.shape)
+        _check(load().qpc_vgwr_put(self._h, _ptr(c)))
+
+    def get(self):
+        c = np.zeros(self.shape, np.complex128)
+        _check(load().qpc_vgwr_get(self._h, _ptr(c)))
+        return c
+
+    def propagate(self, ax_ti=None, ax_tf=None, ay_ti=None, ay_tf=None):
+        if ax_ti is None:
+            _check(load().qpc_vgwr_propagate_free(self._h))
+            return
+        B = self.shape[0]
+        a = [_f64(np.broadcast_to(v, (B,))) for v in (ax_ti, ax_tf, ay_ti, ay_tf)]
+        _check(load().qpc_vgwr_propagate(self._h, *[_ptr(v) for v in a]))
+
+    def run(self, atab, nt_field, nt_total=None):
+        """atab [inst][steps+1][2] (A_x, A_y at t_s)"""
+        B = self.shape[0]
+        tab = _f64(np.asarray(atab, np.float64).reshape(-1 if np.ndim(atab) == 3 else 1, np.shape(atab)[-2], 2))
+        if tab.shape[0] != B:
+            tab = _f64(np.broadcast_to(tab, (B,) + tab.shape[1:]))
+        nf = np.ascontiguousarray(np.broadcast_to(nt_field, (B,)), dtype=np.int64)
+        ntt = nf.copy() if nt_total is None else np.ascontiguousarray(np.broadcast_to(nt_total, (B,)), dtype=np.int64)
+        _check(load().qpc_vgwr_run(self._h, _ptr(tab), tab.shape[1], _ptr(nf), _ptr(ntt)))
+
+    def norm(self):
+        out = np.zeros(self.shape[0])
+        _check(load().qpc_vgwr_norm(self._h, _ptr(out)))
+        return out
+
+    def last_run(self):
+        ms = ctypes.c_float(0)
+        n = ctypes.c_int64(0)
+        _check(load().qpc_vgwr_last_run(self._h, ctypes.byref(ms), ctypes.byref(n)))
+        return ms.value, n.value
 

@@ -46,7 +46,7 @@ def _run(cmd):
 def build_engine(force=False, verbose=False):
     srcs = [os.path.join(CSRC, f) for f in ("qpc_engine.cu", "qpc_setup.cpp", "qpc_internal.h", "qpc_chain.cuh",
                                              "qpc_noalloc.cu", "qpc_spectra.cpp", "qpc_arnoldi.cu", "qpc_cuda_util.cuh",
-                                             "qpc_mlp.cu")]
+                                             "qpc_mlp.cu", "qpc_vgwr.cu")]
     srcs.append(os.path.join(ROOT, "include", "qpc_gb300.h"))
     if not force and not _stale(LIB, srcs):
         return LIB
@@ -57,18 +57,20 @@ def build_engine(force=False, verbose=False):
     o_sp = os.path.join(OBJDIR, "qpc_spectra.o")
     o_ar = os.path.join(OBJDIR, "qpc_arnoldi.o")
     o_ml = os.path.join(OBJDIR, "qpc_mlp.o")
+    o_vg = os.path.join(OBJDIR, "qpc_vgwr.o")
     nv = [_nvcc()] + NVCC_ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC"]
     jobs = [
         nv + ["-c", os.path.join(CSRC, "qpc_engine.cu"), "-o", o_cu],
         nv + ["-c", os.path.join(CSRC, "qpc_noalloc.cu"), "-o", o_na],
         nv + ["-c", os.path.join(CSRC, "qpc_arnoldi.cu"), "-o", o_ar],
         nv + ["-c", os.path.join(CSRC, "qpc_mlp.cu"), "-o", o_ml],
+        nv + ["-c", os.path.join(CSRC, "qpc_vgwr.cu"), "-o", o_vg],
         ["g++", "-O2", "-std=c++17", "-fPIC", "-c", os.path.join(CSRC, "qpc_setup.cpp"), "-o", o_cc],
         ["g++", "-O2", "-std=c++17", "-fPIC", "-c", os.path.join(CSRC, "qpc_spectra.cpp"), "-o", o_sp],
     ]
-    with cf.ThreadPoolExecutor(6) as ex:
+    with cf.ThreadPoolExecutor(7) as ex:
         outs = list(ex.map(_run, jobs))
-    _run([_nvcc()] + NVCC_ARCH + ["-shared", o_cu, o_na, o_ar, o_ml, o_cc, o_sp, "-o", LIB + ".tmp", "-lcudart"])
+    _run([_nvcc()] + NVCC_ARCH + ["-shared", o_cu, o_na, o_ar, o_ml, o_vg, o_cc, o_sp, "-o", LIB + ".tmp", "-lcudart", "-lcublas"])
     os.replace(LIB + ".tmp", LIB)
     if verbose:
         print("".join(outs))

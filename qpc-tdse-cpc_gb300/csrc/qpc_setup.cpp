@@ -378,43 +378,15 @@ static int chol_band_rows(int n, int p, const double* S, double* g)
 	return 0;
 }
 
-// Eigenpairs of the generalized banded problem H v = E S v for one l block,
-// the gv_dsb (LAPACKE_dsbgv) call of the reference (algorithm/ed.h:105-112,
-// used by coefficient::initialize, spherical/coefficient/1e.hpp:91-143, and
-// eigenstate_sph::initialize, spherical/spectrum/population_1e.hpp:58-118).
-// Eigenvalues ascending; vec row j = eigenvector j, S-normalised.
-// Method: Cholesky S = G G^T (banded), C = G^-1 H G^-T (dense), Householder
-// tridiagonalisation and implicit QL with Wilkinson shifts (Golub & Van Loan
-// 8.3), back-transformed by G^-T.  n_want <= n: only the lowest n_want vectors
-// are written (all eigenvalues are).
-int qpc_gen_eigen(int32_t n, int32_t p, const double* S, const double* Hl, int32_t n_want, double* energy, double* vec)
+// Eigen-decomposition of a dense real symmetric matrix a (n x n, row-major, both
+// triangles): Householder tridiagonalisation and implicit QL with Wilkinson shifts
+// (Golub & Van Loan 8.3).  On return d holds the eigenvalues (unsorted) and column i
+// of a the eigenvector of d[i].  Returns QPC_OK or QPC_ERR_NUMERIC.
+static int sym_eigen(int n, std::vector<double>& a, std::vector<double>& d)
 {
-	if (n < 2 * p + 2 || p < 1 || !S || !Hl || !energy || n_want < 0 || n_want > n || (n_want && !vec)) return QPC_ERR_ARGS;
-	const int ne = p + 1;
-	// banded Cholesky, G lower: G[i][i-k] stored g[i*ne+k]
-	std::vector<double> g((size_t)n * ne, 0.0);
-	if (chol_band_rows(n, p, S, g.data())) return QPC_ERR_SINGULAR;
-	// C = G^-1 H G^-T : first X = G^-1 H (dense n x n), then C = G^-1 X^T
-	std::vector<double> X((size_t)n * n, 0.0), C((size_t)n * n, 0.0);
-	auto hval = [&](int r, int c) { int a = std::min(r, c), k = std::abs(r - c); return k > p ? 0.0 : Hl[(size_t)a * ne + k]; };
-	for (int col = 0; col < n; ++col) {
-		for (int i = 0; i < n; ++i) {
-			double s = hval(i, col);
-			for (int k = 1; k <= p && i - k >= 0; ++k) s -= g[(size_t)i * ne + k] * X[(size_t)(i - k) * n + col];
-			X[(size_t)i * n + col] = s / g[(size_t)i * ne];
-		}
-	}
-	for (int col = 0; col < n; ++col) {
-		for (int i = 0; i < n; ++i) {
-			double s = X[(size_t)col * n + i];
-			for (int k = 1; k <= p && i - k >= 0; ++k) s -= g[(size_t)i * ne + k] * C[(size_t)(i - k) * n + col];
-			C[(size_t)i * n + col] = s / g[(size_t)i * ne];
-		}
-	}
-	for (int i = 0; i < n; ++i) for (int j = 0; j < i; ++j) { double m = 0.5 * (C[(size_t)i * n + j] + C[(size_t)j * n + i]); C[(size_t)i * n + j] = m; C[(size_t)j * n + i] = m; }
+	d.assign(n, 0.0);
+	std::vector<double> e(n);
 	// Householder tridiagonalisation, accumulating Q in C (rows of Q^T)
-	std::vector<double> d(n), e(n);
-	std::vector<double>& a = C;
 	for (int i = n - 1; i > 0; --i) {
 		int l = i - 1;
 		double h = 0.0, scale = 0.0;
@@ -490,6 +462,46 @@ int qpc_gen_eigen(int32_t n, int32_t p, const double* S, const double* Hl, int32
 			}
 		} while (m != l);
 	}
+	return QPC_OK;
+}
+
+// Eigenpairs of the generalized banded problem H v = E S v for one l block,
+// the gv_dsb (LAPACKE_dsbgv) call of the reference (algorithm/ed.h:105-112,
+// used by coefficient::initialize, spherical/coefficient/1e.hpp:91-143, and
+// eigenstate_sph::initialize, spherical/spectrum/population_1e.hpp:58-118).
+// Eigenvalues ascending; vec row j = eigenvector j, S-normalised.
+// Method: Cholesky S = G G^T (banded), C = G^-1 H G^-T (dense), Householder
+// tridiagonalisation and implicit QL with Wilkinson shifts (Golub & Van Loan
+// 8.3), back-transformed by G^-T.  n_want <= n: only the lowest n_want vectors
+// are written (all eigenvalues are).
+int qpc_gen_eigen(int32_t n, int32_t p, const double* S, const double* Hl, int32_t n_want, double* energy, double* vec)
+{
+	if (n < 2 * p + 2 || p < 1 || !S || !Hl || !energy || n_want < 0 || n_want > n || (n_want && !vec)) return QPC_ERR_ARGS;
+	const int ne = p + 1;
+	// banded Cholesky, G lower: G[i][i-k] stored g[i*ne+k]
+	std::vector<double> g((size_t)n * ne, 0.0);
+	if (chol_band_rows(n, p, S, g.data())) return QPC_ERR_SINGULAR;
+	// C = G^-1 H G^-T : first X = G^-1 H (dense n x n), then C = G^-1 X^T
+	std::vector<double> X((size_t)n * n, 0.0), C((size_t)n * n, 0.0);
+	auto hval = [&](int r, int c) { int a = std::min(r, c), k = std::abs(r - c); return k > p ? 0.0 : Hl[(size_t)a * ne + k]; };
+	for (int col = 0; col < n; ++col) {
+		for (int i = 0; i < n; ++i) {
+			double s = hval(i, col);
+			for (int k = 1; k <= p && i - k >= 0; ++k) s -= g[(size_t)i * ne + k] * X[(size_t)(i - k) * n + col];
+			X[(size_t)i * n + col] = s / g[(size_t)i * ne];
+		}
+	}
+	for (int col = 0; col < n; ++col) {
+		for (int i = 0; i < n; ++i) {
+			double s = X[(size_t)col * n + i];
+			for (int k = 1; k <= p && i - k >= 0; ++k) s -= g[(size_t)i * ne + k] * C[(size_t)(i - k) * n + col];
+			C[(size_t)i * n + col] = s / g[(size_t)i * ne];
+		}
+	}
+	for (int i = 0; i < n; ++i) for (int j = 0; j < i; ++j) { double m = 0.5 * (C[(size_t)i * n + j] + C[(size_t)j * n + i]); C[(size_t)i * n + j] = m; C[(size_t)j * n + i] = m; }
+	std::vector<double> d;
+	if (int rc = sym_eigen(n, C, d)) return rc;
+	std::vector<double>& a = C;
 	std::vector<int> idx(n);
 	for (int i = 0; i < n; ++i) idx[i] = i;
 	std::sort(idx.begin(), idx.end(), [&](int x, int y) { return d[x] < d[y]; });
@@ -519,6 +531,96 @@ int qpc_cholesky_band(int32_t n, int32_t p, const double* S, double* L)
 	for (int r = 0; r < n; ++r)
 		for (int k = 0; k <= p; ++k) L[(size_t)r * ne + k] = r + k < n ? g[(size_t)(r + k) * ne + k] : 0.0;
 	return 0;
+}
+
+// Angular couplings of the velocity-gauge elliptical propagator propagator_cn_hc_vgwr
+// (cn_1e.hpp:836-890) on the channels ch = im*n_l + il (m = m0 + im, l = |m| + il):
+//   comp 0 (x1): Y11 (sin e^{-i phi}, integrate_sinexp1/2), mult 1
+//   comp 1 (x2): Q11 (-cos L_- - sin e^{-i phi}(1 - L_z), integrate_coslm1/2, sign -1), mult -i
+//   comp 2 (y1): Y11, mult -i
+//   comp 3 (y2): Q11, mult 1
+// (basisfunc.hpp:243-299, operators/1e.hpp:336-523).  Z(j, i) = mult * outer(m, l) for
+// j = (m+1, l+1) and mult * inner(m, l) for j = (m+1, l-1) when j is on the grid, Z(i, j)
+// = conj Z(j, i).  Output: lam[k] ascending and P[k][ch] complex (rows = conjugated
+// eigenvectors, P Z P^H = diag(lam)), the transform construct applies
+// (cn_transform_hm, cn_1e.hpp:151-293, after solve_eigen and conjugate()).
+// Method: Z couples m only to m +- 1 and keeps il mod 2, and D^H Z D is real symmetric
+// for D = diag(phi_m), phi_m = 1 (mult 1) or i^(m - m0) (mult -i); each il-parity block
+// of the real matrix is diagonalised by sym_eigen.  Eigenvectors of degenerate
+// eigenvalues differ from LAPACK's; the propagator depends only on the spectral
+// projectors.
+int qpc_vgwr_angular(int32_t n_l, int32_t n_m, int32_t m0, int32_t comp, double* lam, double* P)
+{
+	if (n_l < 1 || n_m < 1 || comp < 0 || comp > 3 || !lam || !P) return QPC_ERR_ARGS;
+	const int N = n_l * n_m;
+	const bool q11 = comp == 1 || comp == 3;
+	const bool imag = comp == 1 || comp == 2;	// mult = -i
+	auto outer = [&](long m, long l) {
+		return q11 ? -std::sqrt(double((l + m + 1) * (l + m + 2)) / double((2 * l + 1) * (2 * l + 3))) * (l + 1)
+			: -std::sqrt(double((l + m + 2) * (l + m + 1)) / double((2 * l + 1) * (2 * l + 3)));
+	};
+	auto inner = [&](long m, long l) {
+		return q11 ? -std::sqrt(double((l - m) * (l - m - 1)) / double((2 * l + 1) * (2 * l - 1))) * l
+			: +std::sqrt(double((l - m) * (l - m - 1)) / double((2 * l + 1) * (2 * l - 1)));
+	};
+	// real symmetric D^H Z D: Z(j,i) = mult * sgn * e with sgn = -1 for Q11 (operator_q11,
+	// sign < 0); the phase adds a factor conj(phi_{m+1}) (-i) phi_m = -1 when mult = -i
+	const double fac = (q11 ? -1.0 : 1.0) * (imag ? -1.0 : 1.0);
+	std::vector<double> Zr((size_t)N * N, 0.0);
+	for (int im = 0; im + 1 < n_m; ++im)
+		for (int il = 0; il < n_l; ++il) {
+			long m = m0 + im, l = il + std::labs(m);
+			long m2 = m + 1;
+			for (int sgn = -1; sgn <= 1; sgn += 2) {
+				long l2 = l + sgn;
+				long il2 = l2 - std::labs(m2);
+				if (l2 < 0 || il2 < 0 || il2 >= n_l) continue;
+				double v = fac * (sgn > 0 ? outer(m, l) : inner(m, l));
+				int i = im * n_l + il, j = (im + 1) * n_l + (int)il2;
+				Zr[(size_t)j * N + i] = v;
+				Zr[(size_t)i * N + j] = v;
+			}
+		}
+	// eigenvectors block by block (il parity)
+	std::vector<double> evals;
+	std::vector<std::vector<double>> evecs;	// full-length real vectors
+	for (int par = 0; par < 2; ++par) {
+		std::vector<int> idx;
+		for (int ch = 0; ch < N; ++ch) if ((ch % n_l) % 2 == par) idx.push_back(ch);
+		const int nb = (int)idx.size();
+		if (!nb) continue;
+		std::vector<double> a((size_t)nb * nb), d;
+		for (int r = 0; r < nb; ++r)
+			for (int c = 0; c < nb; ++c) a[(size_t)r * nb + c] = Zr[(size_t)idx[r] * N + idx[c]];
+		if (int rc = sym_eigen(nb, a, d)) return rc;
+		for (int k = 0; k < nb; ++k) {
+			std::vector<double> v(N, 0.0);
+			for (int r = 0; r < nb; ++r) v[idx[r]] = a[(size_t)r * nb + k];
+			evals.push_back(d[k]);
+			evecs.push_back(std::move(v));
+		}
+	}
+	std::vector<int> ord(N);
+	for (int k = 0; k < N; ++k) ord[k] = k;
+	std::stable_sort(ord.begin(), ord.end(), [&](int x, int y) { return evals[x] < evals[y]; });
+	for (int k = 0; k < N; ++k) {
+		lam[k] = evals[ord[k]];
+		const std::vector<double>& v = evecs[ord[k]];
+		for (int ch = 0; ch < N; ++ch) {
+			// P[k][ch] = conj(phi_m) v[ch], phi_m = i^(im) when mult = -i
+			int im = ch / n_l, r4 = imag ? im & 3 : 0;
+			double re = 0.0, imv = 0.0;
+			switch (r4) {	// conj(i^r4) = (-i)^r4
+			case 0: re = v[ch]; break;
+			case 1: imv = -v[ch]; break;
+			case 2: re = -v[ch]; break;
+			default: imv = v[ch]; break;
+			}
+			P[2 * ((size_t)k * N + ch)] = re;
+			P[2 * ((size_t)k * N + ch) + 1] = imv;
+		}
+	}
+	return QPC_OK;
 }
 
 // E(t) of one field_component_sinen<n> (structure/field.h:89-133):

@@ -1,0 +1,591 @@
+// GB300 (sm_103a) engine for the QPC-TDSE velocity-gauge elliptical Crank-Nicolson step,
+// propagator_cn_hc_vgwr (spherical/propagator/cn_1e.hpp:812-951).
+//
+// One step with vector potential (A_x, A_y) is, with a = A/2 (cn_1e.hpp:911-914),
+//   C_x1(-a_x) C_x2(a_x) C_y1(-a_y) C_y2(-a_y)  F  C_y2(-a_y') C_y1(-a_y') C_x2(a_x') C_x1(-a_x')
+// (the mirror half with the t_f values), where each coupling C_c(f) = P_c^H M_c(f) P_c is a
+// dense (m,l) transform to the eigenbasis of the angular operator Z_c (Y11 or Q11 times
+// 1 or -i) and one banded CN per eigen-channel:
+//   M(f) = (S + ifet O)^-1 (S - ifet O),  O = 1/r (symmetric, ifet = i lam f dt/8) for x2, y2,
+//                                          O = d/dr (anti-symmetric, ifet = -lam f dt/8) for x1, y1
+// (cn_hm_propagate1/2, propagate.hpp:443-568; component step dt/2), and consecutive
+// transforms are merged, P_x2 P_x1^H etc. (cn_1e.hpp:884-889).  F is the field-free CN of
+// every (m,l) channel.
+//
+// GB300 mapping: the transforms are dense GEMMs, N_ch x N_ch times N_ch x N_r per
+// wavefunction (N_ch = n_m n_l up to 7381): they run as cuBLAS DGEMM (real P_x1, P_y2, on
+// the state viewed as 2 N_r reals) and ZGEMM (merged, complex), strided over the live
+// wavefunctions.  The banded CN of each eigen-channel runs one chain per thread: the LU of
+// S + ifet O is formed row by row with the previous p rows of U in registers, the forward
+// substitution fused, U rows kept in a scratch buffer for the backward substitution.
+// The field-free step uses the LDL^T factors of S + i dt/2 H_l (qpc_ldlt_csym) as
+// x = 2 (S + i dt/2 H)^-1 S c - c.  State layout [inst][m][l][r] complex128, the
+// reference's own.  All arithmetic is complex FP64.
+#include "qpc_internal.h"
+#include "qpc_cuda_util.cuh"
+#include <cuda_runtime.h>
+#include <cublas_v2.h>
+#include <cmath>
+#include <vector>
+#include <algorithm>
+#include <numeric>
+
+namespace qpc {
+namespace {
+
+constexpr int VG_THREADS = 64;
+
+__device__ __forceinline__ double2 cmul(double2 x, double2 y)
+{
+	return make_double2(fma(y.x, x.x, -(y.y * x.y)), fma(y.x, x.y, y.y * x.x));
+}
+__device__ __forceinline__ double2 csub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ double2 crcp(double2 y)
+{
+	double d = fma(y.x, y.x, y.y * y.y);
+	return make_double2(y.x / d, -y.y / d);
+}
+
+// one coupling component on the live prefix of instances: z := (S + ifet O)^-1 (S - ifet O) z
+// per (instance, eigen-channel), ifet = lam[ch] * coef * f_inst with coef complex
+// (anti = O anti-symmetric with O(r, r+k) = band[r][k] for k > 0).
+// f_inst = sgn * A[(inst*ld + step + tofs)*2 + axis] / 2.
+template <int P>
+__global__ void __launch_bounds__(VG_THREADS) k_vg_cn(double2* __restrict__ state, double2* __restrict__ ubuf, const double* __restrict__ S,
+	const double* __restrict__ O, bool anti, const double* __restrict__ lam, double2 coef, const double* __restrict__ atab, long ld,
+	long step, int tofs, int axis, double sgn, const int* __restrict__ perm, int N, int nch, int nlive)
+{
+	const long t = (long)blockIdx.x * VG_THREADS + threadIdx.x;
+	if (t >= (long)nlive * nch) return;
+	const int k = (int)(t / nch), ch = (int)(t - (long)k * nch);
+	const double f = sgn * atab[((long)perm[k] * ld + step + tofs) * 2 + axis] / 2.0;
+	const double lm = lam[ch] * f;
+	const double2 ifet = make_double2(lm * coef.x, lm * coef.y);
+	double2* z = state + t * N;
+	double2* U = ubuf + t * (long)N * (P + 1);
+	constexpr int NE = P + 1;
+	// window: U rows of the previous P rows (row i-1-q at slot q), entries c = 0..P for column row+c
+	double2 Uw[P][NE];
+	double2 yw[P];
+#pragma unroll
+	for (int q = 0; q < P; ++q) {
+		yw[q] = make_double2(0.0, 0.0);
+#pragma unroll
+		for (int c = 0; c < NE; ++c) Uw[q][c] = make_double2(0.0, 0.0);
+	}
+	for (int i = 0; i < N; ++i) {
+		// row i of A+ and rhs = (A- z)_i; lower entries at columns i-P..i-1 (index q = i-col-1)
+		double2 lo[P], up[NE];
+		double2 rhs = make_double2(0.0, 0.0);
+#pragma unroll
+		for (int q = 0; q < P; ++q) {
+			int j = q + 1;
+			lo[q] = make_double2(0.0, 0.0);
+			if (i - j >= 0) {
+				double s = S[(long)(i - j) * NE + j], o = O[(long)(i - j) * NE + j];
+				double ol = anti ? -o : o;
+				double2 fo = make_double2(ifet.x * ol, ifet.y * ol);
+				lo[q] = make_double2(s + fo.x, fo.y);
+				double2 am = make_double2(s - fo.x, -fo.y);
+				double2 pr = cmul(am, z[i - j]);
+				rhs.x += pr.x; rhs.y += pr.y;
+			}
+		}
+#pragma unroll
+		for (int c = 0; c < NE; ++c) {
+			up[c] = make_double2(0.0, 0.0);
+			if (i + c < N) {
+				double s = S[(long)i * NE + c], o = O[(long)i * NE + c];
+				double2 fo = make_double2(ifet.x * o, ifet.y * o);
+				up[c] = make_double2(s + fo.x, fo.y);
+				double2 am = make_double2(s - fo.x, -fo.y);
+				double2 pr = cmul(am, z[i + c]);
+				rhs.x += pr.x; rhs.y += pr.y;
+			}
+		}
+		// eliminate columns i-P .. i-1 in ascending order (q = P-1 .. 0); multiplier l_q
+		double2 lq[P];
+#pragma unroll
+		for (int qq = P - 1; qq >= 0; --qq) {
+			// column col = i-1-qq; its U row sits at window slot qq with U(col, col) = Uw[qq][0]
+			double2 a = lo[qq];
+			lq[qq] = make_double2(0.0, 0.0);
+			if (i - 1 - qq < 0) continue;
+			double2 l = cmul(a, crcp(Uw[qq][0]));
+			lq[qq] = l;
+			// update the remaining entries of row i: columns col+1 .. col+P
+#pragma unroll
+			for (int c = 1; c < NE; ++c) {
+				int dc = c - 1 - qq;	// column col+c relative to i (negative: lower, >= 0: upper)
+				if (dc < 0) lo[-dc - 1] = csub(lo[-dc - 1], cmul(l, Uw[qq][c]));
+				else if (dc < NE) up[dc] = csub(up[dc], cmul(l, Uw[qq][c]));
+			}
+		}
+		// forward substitution y_i = rhs_i - sum_q l_q y_{i-1-q}
+		double2 y = rhs;
+#pragma unroll
+		for (int q = 0; q < P; ++q) y = csub(y, cmul(lq[q], yw[q]));
+		// shift the windows, store U row i and y_i
+#pragma unroll
+		for (int q = P - 1; q > 0; --q) {
+			yw[q] = yw[q - 1];
+#pragma unroll
+			for (int c = 0; c < NE; ++c) Uw[q][c] = Uw[q - 1][c];
+		}
+		yw[0] = y;
+#pragma unroll
+		for (int c = 0; c < NE; ++c) {
+			Uw[0][c] = up[c];
+			U[(long)i * NE + c] = up[c];
+		}
+		z[i] = y;
+	}
+	// backward substitution x_i = (y_i - sum_c U(i, i+c) x_{i+c}) / U(i, i)
+	double2 xw[P];
+#pragma unroll
+	for (int q = 0; q < P; ++q) xw[q] = make_double2(0.0, 0.0);
+	for (int i = N - 1; i >= 0; --i) {
+		double2 v = z[i];
+#pragma unroll
+		for (int c = 1; c < NE; ++c) v = csub(v, cmul(U[(long)i * NE + c], xw[c - 1]));
+		double2 x = cmul(v, crcp(U[(long)i * NE]));
+#pragma unroll
+		for (int q = P - 1; q > 0; --q) xw[q] = xw[q - 1];
+		xw[0] = x;
+		z[i] = x;
+	}
+}
+
+// field-free step of every (instance, m, l) channel whose instance is still running:
+// x = 2 (S + i dt/2 H_l)^-1 S c - c with the LDL^T factors Lrow[l][r][k-1] = L(r, r-k),
+// Dinv[l][r] (qpc_ldlt_csym); y kept in the scratch buffer
+template <int P>
+__global__ void __launch_bounds__(VG_THREADS) k_vg_ff(double2* __restrict__ state, double2* __restrict__ ybuf, const double* __restrict__ S,
+	const double2* __restrict__ Lrow, const double2* __restrict__ Dinv, const long long* __restrict__ ntt, const int* __restrict__ perm,
+	long step, int N, int nl, int nm, int m0, int nlh, int B)
+{
+	const long t = (long)blockIdx.x * VG_THREADS + threadIdx.x;
+	const int nch = nl * nm;
+	if (t >= (long)B * nch) return;
+	const int k = (int)(t / nch), ch = (int)(t - (long)k * nch);
+	if (step >= ntt[perm[k]]) return;
+	const int im = ch / nl, il = ch - im * nl;
+	const int l = il + abs(m0 + im);
+	constexpr int NE = P + 1;
+	double2* c = state + t * N;
+	double2* y = ybuf + t * N;
+	const double2* L = Lrow + (long)l * N * P;
+	const double2* Di = Dinv + (long)l * N;
+	double2 w[P];
+#pragma unroll
+	for (int q = 0; q < P; ++q) w[q] = make_double2(0.0, 0.0);
+	for (int i = 0; i < N; ++i) {
+		double2 s = make_double2(0.0, 0.0);
+#pragma unroll
+		for (int j = 1; j <= P; ++j)
+			if (i - j >= 0) { double b = S[(long)(i - j) * NE + j]; double2 v = c[i - j]; s.x = fma(b, v.x, s.x); s.y = fma(b, v.y, s.y); }
+#pragma unroll
+		for (int j = 0; j <= P; ++j)
+			if (i + j < N) { double b = S[(long)i * NE + j]; double2 v = c[i + j]; s.x = fma(b, v.x, s.x); s.y = fma(b, v.y, s.y); }
+#pragma unroll
+		for (int q = 0; q < P; ++q) s = csub(s, cmul(L[(long)i * P + q], w[q]));
+#pragma unroll
+		for (int q = P - 1; q > 0; --q) w[q] = w[q - 1];
+		w[0] = s;
+		y[i] = cmul(s, Di[i]);
+	}
+#pragma unroll
+	for (int q = 0; q < P; ++q) w[q] = make_double2(0.0, 0.0);
+	for (int i = N - 1; i >= 0; --i) {
+		double2 x = y[i];
+#pragma unroll
+		for (int q = 0; q < P; ++q)
+			if (i + 1 + q < N) x = csub(x, cmul(L[(long)(i + 1 + q) * P + q], w[q]));
+#pragma unroll
+		for (int q = P - 1; q > 0; --q) w[q] = w[q - 1];
+		w[0] = x;
+		double2 ci = c[i];
+		c[i] = make_double2(2.0 * x.x - ci.x, 2.0 * x.y - ci.y);
+	}
+}
+
+__global__ void k_vg_snorm(const double2* __restrict__ state, const double* __restrict__ S, int N, int P, int nch, double* out)
+{
+	// one block per instance, fixed-order reduction
+	const int b = blockIdx.x;
+	const double2* x = state + (long)b * nch * N;
+	double acc = 0.0;
+	for (long e = threadIdx.x; e < (long)nch * N; e += blockDim.x) {
+		int r = (int)(e % N);
+		double2 t = make_double2(0.0, 0.0);
+		for (int q = 1; q <= P && q <= r; ++q) { double s = S[(long)(r - q) * (P + 1) + q]; double2 v = x[e - q]; t.x = fma(s, v.x, t.x); t.y = fma(s, v.y, t.y); }
+		for (int q = 0; q <= P && r + q < N; ++q) { double s = S[(long)r * (P + 1) + q]; double2 v = x[e + q]; t.x = fma(s, v.x, t.x); t.y = fma(s, v.y, t.y); }
+		acc = fma(x[e].x, t.x, fma(x[e].y, t.y, acc));
+	}
+	__shared__ double sm[256];
+	sm[threadIdx.x] = acc;
+	__syncthreads();
+	for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+		if ((int)threadIdx.x < s) sm[threadIdx.x] += sm[threadIdx.x + s];
+		__syncthreads();
+	}
+	if (threadIdx.x == 0) out[b] = sm[0];
+}
+
+} // namespace
+} // namespace qpc
+
+using namespace qpc;
+
+struct qpc_vgwr {
+	int dev = 0;
+	qpc_dims d{};
+	int N = 0, P = 0, nch = 0, nlh = 0, B = 0;
+	double dt = 0;
+	cudaStream_t st = nullptr;
+	cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+	cublasHandle_t cb = nullptr;
+	double *S = nullptr, *Ri = nullptr, *D = nullptr;
+	double *lam[4] = {nullptr, nullptr, nullptr, nullptr};
+	double *Px1 = nullptr, *Py2 = nullptr;        // real [nch][nch]
+	double2 *M12 = nullptr, *M23 = nullptr, *M34 = nullptr;  // complex [nch][nch]
+	double2 *Lrow = nullptr, *Dinv = nullptr;     // field-free factors
+	double2 *X = nullptr, *W = nullptr, *U = nullptr;
+	double* atab = nullptr;
+	long atab_cap = 0;
+	long long* ntt = nullptr;
+	int* perm = nullptr;
+	double* nrm = nullptr;
+	float last_ms = 0.f;
+	long launches = 0;
+};
+
+namespace {
+
+void vg_free(qpc_vgwr* h)
+{
+	if (!h) return;
+	cudaSetDevice(h->dev);
+	void* ps[] = {h->S, h->Ri, h->D, h->lam[0], h->lam[1], h->lam[2], h->lam[3], h->Px1, h->Py2, h->M12, h->M23, h->M34, h->Lrow,
+		h->Dinv, h->X, h->W, h->U, h->atab, h->ntt, h->perm, h->nrm};
+	for (void* p : ps) if (p) cudaFree(p);
+	if (h->cb) cublasDestroy(h->cb);
+	if (h->ev0) cudaEventDestroy(h->ev0);
+	if (h->ev1) cudaEventDestroy(h->ev1);
+	if (h->st) cudaStreamDestroy(h->st);
+	delete h;
+}
+
+#define QPC_CUBLAS(call) do { cublasStatus_t s_ = (call); if (s_ != CUBLAS_STATUS_SUCCESS) { \
+	set_error("%s failed: cublas status %d (%s:%d)", #call, (int)s_, __FILE__, __LINE__); return QPC_ERR_CUDA; } } while (0)
+
+// out[b] = op(Pm) in[b] for b < nb, state blocks [nch][N] complex.  real: Pm real [nch][nch] on the
+// state viewed as [nch][2N] reals; herm: apply Pm^T (real) or Pm^H (complex).
+int transform(qpc_vgwr* h, const void* Pm, bool real, bool herm, const double2* in, double2* out, int nb)
+{
+	const int nch = h->nch, N = h->N;
+	const long sstate = (long)nch * N;
+	if (real) {
+		const double one = 1.0, zero = 0.0;
+		// column-major: out^T (2N x nch) = in^T (2N x nch) * op(P^T) ; the row-major P buffer is P^T
+		QPC_CUBLAS(cublasDgemmStridedBatched(h->cb, CUBLAS_OP_N, herm ? CUBLAS_OP_T : CUBLAS_OP_N, 2 * N, nch, nch, &one,
+			(const double*)in, 2 * N, 2 * sstate, (const double*)Pm, nch, 0, &zero, (double*)out, 2 * N, 2 * sstate, nb));
+	} else {
+		const cuDoubleComplex one = make_cuDoubleComplex(1.0, 0.0), zero = make_cuDoubleComplex(0.0, 0.0);
+		QPC_CUBLAS(cublasZgemmStridedBatched(h->cb, CUBLAS_OP_N, herm ? CUBLAS_OP_C : CUBLAS_OP_N, N, nch, nch, &one,
+			(const cuDoubleComplex*)in, N, sstate, (const cuDoubleComplex*)Pm, nch, 0, &zero, (cuDoubleComplex*)out, N, sstate, nb));
+	}
+	++h->launches;
+	return QPC_OK;
+}
+
+template <int P>
+int step_t(qpc_vgwr* h, long s, long ld, int nlive, int nff)
+{
+	// first half, live instances (prefix)
+	const int nb = nlive;
+	auto cn = [&](double2* z, int comp, int tofs) {
+		const bool anti = comp == 0 || comp == 2;
+		const double q = h->dt * 0.5 / 2.0;
+		const double2 coef = anti ? make_double2(-q, 0.0) : make_double2(0.0, q);
+		const int axis = comp < 2 ? 0 : 1;
+		const double sgn = comp == 1 ? 1.0 : -1.0;
+		const long nth = (long)nb * h->nch;
+		k_vg_cn<P><<<(unsigned)((nth + VG_THREADS - 1) / VG_THREADS), VG_THREADS, 0, h->st>>>(z, h->U, h->S, anti ? h->D : h->Ri, anti,
+			h->lam[comp], coef, h->atab, ld, s, tofs, axis, sgn, h->perm, h->N, h->nch, nb);
+		++h->launches;
+	};
+	if (nb > 0) {
+		if (int rc = transform(h, h->Px1, true, false, h->X, h->W, nb)) return rc;
+		cn(h->W, 0, 0);
+		if (int rc = transform(h, h->M12, false, false, h->W, h->X, nb)) return rc;
+		cn(h->X, 1, 0);
+		if (int rc = transform(h, h->M23, false, false, h->X, h->W, nb)) return rc;
+		cn(h->W, 2, 0);
+		if (int rc = transform(h, h->M34, false, false, h->W, h->X, nb)) return rc;
+		cn(h->X, 3, 0);
+		if (int rc = transform(h, h->Py2, true, true, h->X, h->W, nb)) return rc;
+		// W holds the live instances' states; the others are still in X
+		QPC_CUDA(cudaMemcpyAsync(h->X, h->W, sizeof(double2) * (size_t)nb * h->nch * h->N, cudaMemcpyDeviceToDevice, h->st));
+	}
+	if (nff > 0) {
+		const long nth = (long)nff * h->nch;
+		k_vg_ff<P><<<(unsigned)((nth + VG_THREADS - 1) / VG_THREADS), VG_THREADS, 0, h->st>>>(h->X, h->U, h->S, h->Lrow, h->Dinv, h->ntt,
+			h->perm, s, h->N, h->d.n_l, h->d.n_m, h->d.m0, h->nlh, nff);
+		++h->launches;
+	}
+	if (nb > 0) {
+		if (int rc = transform(h, h->Py2, true, false, h->X, h->W, nb)) return rc;
+		cn(h->W, 3, 1);
+		if (int rc = transform(h, h->M34, false, true, h->W, h->X, nb)) return rc;
+		cn(h->X, 2, 1);
+		if (int rc = transform(h, h->M23, false, true, h->X, h->W, nb)) return rc;
+		cn(h->W, 1, 1);
+		if (int rc = transform(h, h->M12, false, true, h->W, h->X, nb)) return rc;
+		cn(h->X, 0, 1);
+		if (int rc = transform(h, h->Px1, true, true, h->X, h->W, nb)) return rc;
+		QPC_CUDA(cudaMemcpyAsync(h->X, h->W, sizeof(double2) * (size_t)nb * h->nch * h->N, cudaMemcpyDeviceToDevice, h->st));
+	}
+	return QPC_OK;
+}
+
+int step_dispatch(qpc_vgwr* h, long s, long ld, int nlive, int nff)
+{
+	switch (h->P) {
+	case 1: return step_t<1>(h, s, ld, nlive, nff);
+	case 2: return step_t<2>(h, s, ld, nlive, nff);
+	case 3: return step_t<3>(h, s, ld, nlive, nff);
+	case 4: return step_t<4>(h, s, ld, nlive, nff);
+	case 5: return step_t<5>(h, s, ld, nlive, nff);
+	case 6: return step_t<6>(h, s, ld, nlive, nff);
+	case 7: return step_t<7>(h, s, ld, nlive, nff);
+	default: return step_t<8>(h, s, ld, nlive, nff);
+	}
+}
+
+// reorder instance blocks: X[k] = X[perm[k]] (inverse: X[perm[k]] = X[k]) through W
+int permute(qpc_vgwr* h, const std::vector<int>& perm, bool inverse)
+{
+	const size_t blk = sizeof(double2) * (size_t)h->nch * h->N;
+	for (int k = 0; k < h->B; ++k) {
+		int src = inverse ? k : perm[k], dst = inverse ? perm[k] : k;
+		QPC_CUDA(cudaMemcpyAsync((char*)h->W + dst * blk, (char*)h->X + src * blk, blk, cudaMemcpyDeviceToDevice, h->st));
+	}
+	QPC_CUDA(cudaMemcpyAsync(h->X, h->W, blk * h->B, cudaMemcpyDeviceToDevice, h->st));
+	return QPC_OK;
+}
+
+} // namespace
+
+extern "C" {
+
+int qpc_vgwr_create(const qpc_dims* dims, double dt, const double* S, const double* Rinv, const double* D, const double* H,
+	qpc_vgwr** out)
+{
+	if (!out) { set_error("out is NULL"); return QPC_ERR_ARGS; }
+	*out = nullptr;
+	if (!dims || !S || !Rinv || !D || !H) { set_error("NULL argument"); return QPC_ERR_ARGS; }
+	const qpc_dims d = *dims;
+	if (d.p < 1 || d.p > QPC_MAX_RANK || d.n_r < 2 * d.p + 2 || d.n_l < 1 || d.n_m < 1 || d.n_inst < 1) {
+		set_error("bad dims n_r=%d p=%d n_l=%d n_m=%d n_inst=%d", d.n_r, d.p, d.n_l, d.n_m, d.n_inst);
+		return QPC_ERR_ARGS;
+	}
+	if (!(dt > 0) || !std::isfinite(dt)) { set_error("dt=%g", dt); return QPC_ERR_ARGS; }
+	int dev = 0;
+	if (int rc = check_device(&dev)) return rc;
+	qpc_vgwr* h = new (std::nothrow) qpc_vgwr;
+	if (!h) { set_error("host allocation"); return QPC_ERR_NOMEM; }
+	auto fail = [&](int rc) { vg_free(h); return rc; };
+	h->dev = dev; h->d = d; h->N = d.n_r; h->P = d.p; h->nch = d.n_l * d.n_m; h->B = d.n_inst; h->dt = dt;
+	const int mmax = std::max(std::abs(d.m0), std::abs(d.m0 + d.n_m - 1));
+	h->nlh = mmax + d.n_l;
+	const int N = d.n_r, P = d.p, NE = P + 1, nch = h->nch;
+	// angular eigensystems
+	std::vector<double> lam[4], Pm[4];
+	for (int c = 0; c < 4; ++c) {
+		lam[c].resize(nch);
+		Pm[c].resize((size_t)2 * nch * nch);
+		if (int rc = qpc_vgwr_angular(d.n_l, d.n_m, d.m0, c, lam[c].data(), Pm[c].data())) { set_error("angular eigensystem %d failed", c); return fail(rc); }
+	}
+	std::vector<double> px1((size_t)nch * nch), py2((size_t)nch * nch);
+	for (size_t i = 0; i < px1.size(); ++i) { px1[i] = Pm[0][2 * i]; py2[i] = Pm[3][2 * i]; }
+	// field-free factors
+	std::vector<double> lrow((size_t)h->nlh * N * P * 2), dinv((size_t)h->nlh * N * 2);
+	for (int l = 0; l < h->nlh; ++l) {
+		int bad = qpc_ldlt_csym(N, P, S, H + (size_t)l * N * NE, dt * 0.5, lrow.data() + (size_t)l * N * P * 2, dinv.data() + (size_t)l * N * 2);
+		if (bad < 0) { set_error("ldlt arguments"); return fail(QPC_ERR_ARGS); }
+		if (bad > 0) { set_error("zero pivot factorising S + i dt/2 H_%d", l); return fail(QPC_ERR_SINGULAR); }
+	}
+	QPC_CUDA(cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking));
+	QPC_CUDA(cudaEventCreate(&h->ev0));
+	QPC_CUDA(cudaEventCreate(&h->ev1));
+	if (cublasCreate(&h->cb) != CUBLAS_STATUS_SUCCESS) { set_error("cublasCreate failed"); return fail(QPC_ERR_CUDA); }
+	if (cublasSetStream(h->cb, h->st) != CUBLAS_STATUS_SUCCESS) { set_error("cublasSetStream failed"); return fail(QPC_ERR_CUDA); }
+	const size_t nst = (size_t)h->B * nch * N;
+	int rc;
+	if ((rc = dalloc(&h->S, (size_t)N * NE)) || (rc = dalloc(&h->Ri, (size_t)N * NE)) || (rc = dalloc(&h->D, (size_t)N * NE)) ||
+		(rc = dalloc(&h->lam[0], nch)) || (rc = dalloc(&h->lam[1], nch)) || (rc = dalloc(&h->lam[2], nch)) || (rc = dalloc(&h->lam[3], nch)) ||
+		(rc = dalloc(&h->Px1, (size_t)nch * nch)) || (rc = dalloc(&h->Py2, (size_t)nch * nch)) || (rc = dalloc(&h->M12, (size_t)nch * nch)) ||
+		(rc = dalloc(&h->M23, (size_t)nch * nch)) || (rc = dalloc(&h->M34, (size_t)nch * nch)) ||
+		(rc = dalloc(&h->Lrow, (size_t)h->nlh * N * P)) || (rc = dalloc(&h->Dinv, (size_t)h->nlh * N)) ||
+		(rc = dalloc(&h->X, nst)) || (rc = dalloc(&h->W, nst)) || (rc = dalloc(&h->U, nst * NE)) || (rc = dalloc(&h->ntt, (size_t)h->B)) ||
+		(rc = dalloc(&h->perm, (size_t)h->B)) || (rc = dalloc(&h->nrm, (size_t)h->B)))
+		return fail(rc);
+	// merged transforms P_b P_a^H on the device: row-major C = L R^H; column-major C^T = conj(R) L^T
+	double2 *dP1 = nullptr, *dP2 = nullptr;
+	if ((rc = dalloc(&dP1, (size_t)nch * nch)) || (rc = dalloc(&dP2, (size_t)nch * nch))) {
+		if (dP1) cudaFree(dP1);
+		return fail(rc);
+	}
+	auto merge = [&](const std::vector<double>& Lh, const std::vector<double>& Rh, double2* out) -> int {
+		QPC_CUDA(cudaMemcpy(dP1, Lh.data(), sizeof(double2) * nch * nch, cudaMemcpyHostToDevice));
+		QPC_CUDA(cudaMemcpy(dP2, Rh.data(), sizeof(double2) * nch * nch, cudaMemcpyHostToDevice));
+		const cuDoubleComplex one = make_cuDoubleComplex(1.0, 0.0), zero = make_cuDoubleComplex(0.0, 0.0);
+		// column-major views: A_cm = R^T (buffer R), B_cm = L^T (buffer L); C^T = conj(R) L^T = (A_cm)^H L^T
+		QPC_CUBLAS(cublasZgemm(h->cb, CUBLAS_OP_C, CUBLAS_OP_N, nch, nch, nch, &one, (const cuDoubleComplex*)dP2, nch,
+			(const cuDoubleComplex*)dP1, nch, &zero, (cuDoubleComplex*)out, nch));
+		QPC_CUDA(cudaStreamSynchronize(h->st));
+		return QPC_OK;
+	};
+	int mrc = merge(Pm[1], Pm[0], h->M12);
+	if (!mrc) mrc = merge(Pm[2], Pm[1], h->M23);
+	if (!mrc) mrc = merge(Pm[3], Pm[2], h->M34);
+	cudaFree(dP1);
+	cudaFree(dP2);
+	if (mrc) return fail(mrc);
+	if (cudaMemcpy(h->S, S, sizeof(double) * N * NE, cudaMemcpyHostToDevice) != cudaSuccess ||
+		cudaMemcpy(h->Ri, Rinv, sizeof(double) * N * NE, cudaMemcpyHostToDevice) != cudaSuccess ||
+		cudaMemcpy(h->D, D, sizeof(double) * N * NE, cudaMemcpyHostToDevice) != cudaSuccess ||
+		cudaMemcpy(h->Px1, px1.data(), sizeof(double) * px1.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
+		cudaMemcpy(h->Py2, py2.data(), sizeof(double) * py2.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
+		cudaMemcpy(h->Lrow, lrow.data(), sizeof(double) * lrow.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
+		cudaMemcpy(h->Dinv, dinv.data(), sizeof(double) * dinv.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
+		cudaMemset(h->X, 0, sizeof(double2) * nst) != cudaSuccess) {
+		set_error("device upload failed");
+		return fail(QPC_ERR_CUDA);
+	}
+	for (int c = 0; c < 4; ++c)
+		if (cudaMemcpy(h->lam[c], lam[c].data(), sizeof(double) * nch, cudaMemcpyHostToDevice) != cudaSuccess) { set_error("upload"); return fail(QPC_ERR_CUDA); }
+	*out = h;
+	return QPC_OK;
+}
+
+int qpc_vgwr_destroy(qpc_vgwr* h)
+{
+	vg_free(h);
+	return QPC_OK;
+}
+
+static int vg_copy(qpc_vgwr* h, const double* src, double* dst, cudaMemcpyKind kind)
+{
+	if (!h || (!src && !dst)) { set_error("NULL argument"); return QPC_ERR_ARGS; }
+	cudaSetDevice(h->dev);
+	const size_t bytes = sizeof(double2) * (size_t)h->B * h->nch * h->N;
+	if (src) QPC_CUDA(cudaMemcpyAsync(h->X, src, bytes, kind, h->st));
+	else QPC_CUDA(cudaMemcpyAsync(dst, h->X, bytes, kind, h->st));
+	return wait_on(h->st);
+}
+
+int qpc_vgwr_put(qpc_vgwr* h, const double* coef) { return vg_copy(h, coef, nullptr, cudaMemcpyHostToDevice); }
+int qpc_vgwr_get(qpc_vgwr* h, double* coef) { return vg_copy(h, nullptr, coef, cudaMemcpyDeviceToHost); }
+int qpc_vgwr_put_device(qpc_vgwr* h, const double* c) { return vg_copy(h, c, nullptr, cudaMemcpyDeviceToDevice); }
+int qpc_vgwr_get_device(qpc_vgwr* h, double* c) { return vg_copy(h, nullptr, c, cudaMemcpyDeviceToDevice); }
+
+int qpc_vgwr_run(qpc_vgwr* h, const double* atab, int64_t ld, const int64_t* nt_field, const int64_t* nt_total)
+{
+	if (!h || !nt_field || !nt_total) { set_error("NULL argument"); return QPC_ERR_ARGS; }
+	cudaSetDevice(h->dev);
+	const int B = h->B;
+	long smax = 0;
+	bool anyfield = false;
+	for (int k = 0; k < B; ++k) {
+		if (nt_field[k] < 0 || nt_total[k] < nt_field[k]) { set_error("instance %d: nt_field=%lld nt_total=%lld", k, (long long)nt_field[k], (long long)nt_total[k]); return QPC_ERR_ARGS; }
+		if (nt_field[k] > 0) { anyfield = true; if (ld < nt_field[k] + 1) { set_error("ld=%lld < nt_field+1", (long long)ld); return QPC_ERR_ARGS; } }
+		smax = std::max<long>(smax, nt_total[k]);
+	}
+	if (anyfield && !atab) { set_error("atab is NULL"); return QPC_ERR_ARGS; }
+	if (smax == 0) return QPC_OK;
+	const long cap = anyfield ? (long)B * ld * 2 : 2;
+	if (cap > h->atab_cap) {
+		if (h->atab) cudaFree(h->atab);
+		h->atab = nullptr; h->atab_cap = 0;
+		if (int rc = dalloc(&h->atab, cap)) return rc;
+		h->atab_cap = cap;
+	}
+	if (anyfield) {
+		for (int k = 0; k < B; ++k)
+			for (long i = 0; i <= nt_field[k] && nt_field[k] > 0; ++i)
+				if (!std::isfinite(atab[((size_t)k * ld + i) * 2]) || !std::isfinite(atab[((size_t)k * ld + i) * 2 + 1])) {
+					set_error("non-finite vector potential, instance %d step %ld", k, i);
+					return QPC_ERR_ARGS;
+				}
+		QPC_CUDA(cudaMemcpyAsync(h->atab, atab, sizeof(double) * cap, cudaMemcpyHostToDevice, h->st));
+	}
+	// instances in decreasing nt_field: the ones in their pulse at step s are a prefix
+	std::vector<int> perm(B);
+	std::iota(perm.begin(), perm.end(), 0);
+	std::stable_sort(perm.begin(), perm.end(), [&](int x, int y) { return nt_field[x] > nt_field[y]; });
+	bool ident = true;
+	for (int k = 0; k < B; ++k) ident &= perm[k] == k;
+	std::vector<long long> ntt(nt_total, nt_total + B);
+	QPC_CUDA(cudaMemcpyAsync(h->ntt, ntt.data(), sizeof(long long) * B, cudaMemcpyHostToDevice, h->st));
+	QPC_CUDA(cudaMemcpyAsync(h->perm, perm.data(), sizeof(int) * B, cudaMemcpyHostToDevice, h->st));
+	if (!ident) if (int rc = permute(h, perm, false)) return rc;
+	// instances running (nt_total) at step s: those with nt_total > s; the field-free kernel
+	// checks nt_total per instance, and covers the prefix up to the last running one
+	h->launches = 0;
+	QPC_CUDA(cudaEventRecord(h->ev0, h->st));
+	for (long s = 0; s < smax; ++s) {
+		int nlive = 0, nff = 0;
+		for (int k = 0; k < B; ++k) {
+			if (s < nt_field[perm[k]]) nlive = k + 1;
+			if (s < nt_total[perm[k]]) nff = k + 1;
+		}
+		if (int rc = step_dispatch(h, s, anyfield ? ld : 0, nlive, nff)) return rc;
+	}
+	QPC_CUDA(cudaGetLastError());
+	QPC_CUDA(cudaEventRecord(h->ev1, h->st));
+	if (!ident) if (int rc = permute(h, perm, true)) return rc;
+	if (int rc = wait_on(h->st)) return rc;
+	cudaEventElapsedTime(&h->last_ms, h->ev0, h->ev1);
+	return QPC_OK;
+}
+
+int qpc_vgwr_propagate(qpc_vgwr* h, const double* ax_ti, const double* ax_tf, const double* ay_ti, const double* ay_tf)
+{
+	if (!h || !ax_ti || !ax_tf || !ay_ti || !ay_tf) { set_error("NULL argument"); return QPC_ERR_ARGS; }
+	std::vector<double> tab((size_t)h->B * 4);
+	for (int k = 0; k < h->B; ++k) {
+		tab[(size_t)k * 4 + 0] = ax_ti[k]; tab[(size_t)k * 4 + 1] = ay_ti[k];
+		tab[(size_t)k * 4 + 2] = ax_tf[k]; tab[(size_t)k * 4 + 3] = ay_tf[k];
+	}
+	std::vector<int64_t> one(h->B, 1);
+	return qpc_vgwr_run(h, tab.data(), 2, one.data(), one.data());
+}
+
+int qpc_vgwr_propagate_free(qpc_vgwr* h)
+{
+	if (!h) { set_error("NULL argument"); return QPC_ERR_ARGS; }
+	std::vector<int64_t> zero(h->B, 0), one(h->B, 1);
+	return qpc_vgwr_run(h, nullptr, 1, zero.data(), one.data());
+}
+
+int qpc_vgwr_norm(qpc_vgwr* h, double* norm)
+{
+	if (!h || !norm) { set_error("NULL argument"); return QPC_ERR_ARGS; }
+	cudaSetDevice(h->dev);
+	k_vg_snorm<<<h->B, 256, 0, h->st>>>(h->X, h->S, h->N, h->P, h->nch, h->nrm);
+	QPC_CUDA(cudaGetLastError());
+	QPC_CUDA(cudaMemcpyAsync(norm, h->nrm, sizeof(double) * h->B, cudaMemcpyDeviceToHost, h->st));
+	return wait_on(h->st);
+}
+
+int qpc_vgwr_last_run(qpc_vgwr* h, float* ms, int64_t* launches)
+{
+	if (!h || !ms || !launches) { set_error("NULL argument"); return QPC_ERR_ARGS; }
+	*ms = h->last_ms;
+	*launches = h->launches;
+	return QPC_OK;
+}
+
+} // extern "C"

@@ -146,6 +146,47 @@ class ArnoldiOracle:
         return c, crit, ms
 
 
+class VgwrGrid(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_int32) for n in ("n_r", "p", "n_l", "n_m", "m0", "n_inst")] + [("dt", ctypes.c_double)] + \
+               [(n, ctypes.c_void_p) for n in ("S", "Rinv", "D", "upper", "lower")] + \
+               [("lam", ctypes.c_void_p * 4), ("P", ctypes.c_void_p * 4)]
+
+
+class VgwrOracle:
+    """The CPU oracle of propagator_cn_hc_vgwr (oracle/oracle_cn.cpp), used only as the checker."""
+
+    def __init__(self):
+        self.o = Oracle()
+        self.lib = self.o.lib
+
+    def grid(self, S, Rinv, D, H, dt, n_l, n_m, m0, n_inst=1):
+        q = engine()
+        n_r, ne = S.shape
+        p = ne - 1
+        nlh = max(abs(m0), abs(m0 + n_m - 1)) + n_l
+        up = np.zeros((nlh, n_r, ne), complex)
+        lo = np.zeros((nlh, n_r, ne), complex)
+        assert self.lib.oracle_cn_bands(n_r, p, nlh, _p(np.ascontiguousarray(S)), _p(np.ascontiguousarray(H[:nlh])),
+                                        ctypes.c_double(dt), _p(up), _p(lo)) == 0
+        eig = [q.vgwr_angular(n_l, n_m, m0, c) for c in range(4)]
+        keep = [np.ascontiguousarray(S), np.ascontiguousarray(Rinv), np.ascontiguousarray(D), up, lo] + \
+               [e[0] for e in eig] + [e[1] for e in eig]
+        g = VgwrGrid(n_r, p, n_l, n_m, m0, n_inst, dt, *[_p(a) for a in keep[:5]])
+        for c in range(4):
+            g.lam[c] = keep[5 + c].ctypes.data
+            g.P[c] = keep[9 + c].ctypes.data
+        g._keep = keep
+        return g
+
+    def run(self, g, coef, atab, nt_field, nt_total, threads=1):
+        c = np.ascontiguousarray(coef, dtype=complex).copy()
+        tab = np.ascontiguousarray(atab, dtype=float)
+        nf = np.ascontiguousarray(np.broadcast_to(nt_field, (g.n_inst,)), dtype=np.int64)
+        ntt = np.ascontiguousarray(np.broadcast_to(nt_total, (g.n_inst,)), dtype=np.int64)
+        self.lib.oracle_vgwr_run(ctypes.byref(g), _p(c), _p(tab), ctypes.c_long(tab.shape[-2]), _p(nf), _p(ntt), threads)
+        return c
+
+
 @pytest.fixture(scope="session")
 def q():
     return engine()
@@ -159,6 +200,11 @@ def oracle():
 @pytest.fixture(scope="session")
 def aoracle():
     return ArnoldiOracle()
+
+
+@pytest.fixture(scope="session")
+def voracle():
+    return VgwrOracle()
 
 
 def rel_l2(a, b):

@@ -2,8 +2,8 @@
 propagator (QPC-TDSE headers compiled by oracle/ref/Makefile into oracle/_ref/).
 
 Run on the development machine, where the reference checkout exists:
-    python tests/golden/make_golden.py [/path/to/reference/include] [--arnoldi]
-(--arnoldi regenerates only the Arnoldi fixtures.)
+    python tests/golden/make_golden.py [/path/to/reference/include] [--arnoldi] [--vgwr]
+(--arnoldi / --vgwr regenerate only those fixtures.)
 The fixtures are committed; the tests only read them.
 
 Cases (hydrogen unless stated; r in [0, rmax], uniform knots, m = 0):
@@ -29,6 +29,13 @@ Cases (hydrogen unless stated; r in [0, rmax], uniform knots, m = 0):
                     through 10 field-free steps of dt = 0.1 (Krylov breakdown, "bd")
   arnoldi_mid.npz   the same propagator on the mid grid from the mid_pulse final state:
                     1 and 2 steps of dt = 0.1 at ez = 0.03, kmax = 12
+  vgwr_ep.npz       the velocity-gauge elliptical propagator propagator_cn_hc_vgwr
+  vgwr_ep6.npz      (cn_1e.hpp:812-951) on two multi-m grids: N_r=40, p=5, n_l=4, m=-2..2
+                    (odd n_m: zero-eigenvalue channels) and N_r=48, p=6, n_l=5, m=-3..2,
+                    r in [0, 20], dt = 0.05; seeded random initial state, 20 steps under
+                    A_x = 0.3 sin(0.5 t + 0.1), A_y = 0.2 cos(0.5 t), then 2 field-free
+                    steps: the reference's S, 1/r, D, H_l, the couplings' eigenvalues, the
+                    final coefficients and S-norm
 """
 import json
 import os
@@ -106,12 +113,37 @@ def arnoldi(d):
     np.savez(os.path.join(HERE, "arnoldi_mid.npz"), **out)
 
 
+def vgwr(d):
+    """Velocity-gauge elliptical fixtures (see the module docstring)."""
+    for binary, tag, NR, P, NL, NM, M0 in (("ref_ep", "vgwr_ep", 40, 5, 4, 5, -2), ("ref_ep6", "vgwr_ep6", 48, 6, 5, 6, -3)):
+        RMAX, DT, nt, nfree = 20.0, 0.05, 20, 2
+        run(binary, "setup", d, RMAX, DT, 1, 0, 0)
+        nlh = max(abs(M0), abs(M0 + NM - 1)) + NL
+        out = {"n_r": NR, "p": P, "n_l": NL, "n_m": NM, "m0": M0, "rmax": RMAX, "dt": DT, "nt": nt, "nfree": nfree,
+               "S": load(d, "S", (NR, P + 1)), "RINV": load(d, "RINV", (NR, P + 1)), "D": load(d, "D", (NR, P + 1)),
+               "H": load(d, "H", (nlh, NR, P + 1))}
+        rng = np.random.default_rng(4)
+        n = NR * NL * NM
+        c0 = (rng.standard_normal(n) + 1j * rng.standard_normal(n)) * np.exp(-np.tile(np.arange(NR), NL * NM) / 8.0)
+        c0.tofile(os.path.join(d, "vinit.bin"))
+        t = DT * np.arange(nt + 1)
+        a = np.stack([0.3 * np.sin(0.5 * t + 0.1), 0.2 * np.cos(0.5 * t)], 1)
+        a.tofile(os.path.join(d, "vfield.bin"))
+        run(binary, "vgwr", d, RMAX, DT, 1, 0, 0, os.path.join(d, "vinit.bin"), os.path.join(d, "vfield.bin"), nt, nfree)
+        out.update(init=c0.reshape(NM, NL, NR), atab=a, coef=load(d, "coef", (NM, NL, NR), True), norm=load(d, "norm"),
+                   zeig=np.stack([load(d, "zeig_" + c) for c in ("x1", "x2", "y1", "y2")]))
+        np.savez(os.path.join(HERE, tag + ".npz"), **out)
+
+
 def main():
     ref_include = sys.argv[1] if len(sys.argv) > 1 and not sys.argv[1].startswith("--") else "/root/reference/include"
     build(ref_include)
-    if "--arnoldi" in sys.argv:
+    if "--arnoldi" in sys.argv or "--vgwr" in sys.argv:
         with tempfile.TemporaryDirectory() as d:
-            arnoldi(d)
+            if "--arnoldi" in sys.argv:
+                arnoldi(d)
+            if "--vgwr" in sys.argv:
+                vgwr(d)
         return
     meta = {}
     with tempfile.TemporaryDirectory() as d:
@@ -171,6 +203,7 @@ def main():
                  coef=coef, norm=norm, dipole=dip, proj=load(d, "proj", None, True),
                  proj_nnz=load(d, "proj_nnz").astype(np.int64), proj_energy=load(d, "proj_energy"))
         arnoldi(d)
+        vgwr(d)
     with open(os.path.join(HERE, "make_golden.log.json"), "w") as fh:
         json.dump(meta, fh, indent=1)
 
