@@ -70,7 +70,7 @@ def build_engine(force=False, verbose=False):
     ]
     with cf.ThreadPoolExecutor(7) as ex:
         outs = list(ex.map(_run, jobs))
-    _run([_nvcc()] + NVCC_ARCH + ["-shared", o_cu, o_na, o_ar, o_ml, o_vg, o_cc, o_sp, "-o", LIB + ".tmp", "-lcudart", "-lcublas"])
+    _run([_nvcc()] + NVCC_ARCH + ["-shared", o_cu, o_na, o_ar, o_ml, o_vg, o_cc, o_sp, "-o", LIB + ".tmp", "-lcudart", "-lcublas", "-lcusolver"])
     os.replace(LIB + ".tmp", LIB)
     if verbose:
         print("".join(outs))

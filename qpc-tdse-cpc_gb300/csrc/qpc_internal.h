@@ -7,4 +7,6 @@
 
 namespace qpc {
 void set_error(const char* fmt, ...);
+// real symmetric form D^H Z_c D of a propagator_cn_hc_vgwr coupling (qpc_setup.cpp)
+void vgwr_real_coupling(int n_l, int n_m, int m0, int comp, double* Zr);
 }

@@ -156,6 +156,43 @@ static double potential(const qpc_potential& v, double r)
 	}
 }
 
+// D^H Z_c D (real symmetric, N x N row-major) for coupling component comp of
+// propagator_cn_hc_vgwr, with D = diag(phi_m), phi_m = 1 (mult 1) or i^(m - m0) (mult -i):
+// Z(j, i) = mult * sgn * e(m, l) for j = (m+1, l+-1), e = outer (l+1) or inner (l-1)
+// elements of Y11 (integrate_sinexp1/2) or Q11 (integrate_coslm1/2, sgn = -1 from
+// operator_q11<dims_t,-1>::solve_eigen), basisfunc.hpp:243-299, operators/1e.hpp:336-523.
+// The phase turns mult = -i into a factor conj(phi_{m+1}) (-i) phi_m = -1.
+void vgwr_real_coupling(int n_l, int n_m, int m0, int comp, double* Zr)
+{
+	const int N = n_l * n_m;
+	const bool q11 = comp == 1 || comp == 3;
+	const bool imag = comp == 1 || comp == 2;
+	auto outer = [&](long m, long l) {
+		return q11 ? -std::sqrt(double((l + m + 1) * (l + m + 2)) / double((2 * l + 1) * (2 * l + 3))) * (l + 1)
+			: -std::sqrt(double((l + m + 2) * (l + m + 1)) / double((2 * l + 1) * (2 * l + 3)));
+	};
+	auto inner = [&](long m, long l) {
+		return q11 ? -std::sqrt(double((l - m) * (l - m - 1)) / double((2 * l + 1) * (2 * l - 1))) * l
+			: +std::sqrt(double((l - m) * (l - m - 1)) / double((2 * l + 1) * (2 * l - 1)));
+	};
+	const double fac = (q11 ? -1.0 : 1.0) * (imag ? -1.0 : 1.0);
+	for (size_t i = 0; i < (size_t)N * N; ++i) Zr[i] = 0.0;
+	for (int im = 0; im + 1 < n_m; ++im)
+		for (int il = 0; il < n_l; ++il) {
+			long m = m0 + im, l = il + std::labs(m);
+			long m2 = m + 1;
+			for (int sgn = -1; sgn <= 1; sgn += 2) {
+				long l2 = l + sgn;
+				long il2 = l2 - std::labs(m2);
+				if (l2 < 0 || il2 < 0 || il2 >= n_l) continue;
+				double v = fac * (sgn > 0 ? outer(m, l) : inner(m, l));
+				int i = im * n_l + il, j = (im + 1) * n_l + (int)il2;
+				Zr[(size_t)j * N + i] = v;
+				Zr[(size_t)i * N + j] = v;
+			}
+		}
+}
+
 } // namespace qpc
 
 using namespace qpc;
@@ -553,34 +590,9 @@ int qpc_vgwr_angular(int32_t n_l, int32_t n_m, int32_t m0, int32_t comp, double*
 {
 	if (n_l < 1 || n_m < 1 || comp < 0 || comp > 3 || !lam || !P) return QPC_ERR_ARGS;
 	const int N = n_l * n_m;
-	const bool q11 = comp == 1 || comp == 3;
 	const bool imag = comp == 1 || comp == 2;	// mult = -i
-	auto outer = [&](long m, long l) {
-		return q11 ? -std::sqrt(double((l + m + 1) * (l + m + 2)) / double((2 * l + 1) * (2 * l + 3))) * (l + 1)
-			: -std::sqrt(double((l + m + 2) * (l + m + 1)) / double((2 * l + 1) * (2 * l + 3)));
-	};
-	auto inner = [&](long m, long l) {
-		return q11 ? -std::sqrt(double((l - m) * (l - m - 1)) / double((2 * l + 1) * (2 * l - 1))) * l
-			: +std::sqrt(double((l - m) * (l - m - 1)) / double((2 * l + 1) * (2 * l - 1)));
-	};
-	// real symmetric D^H Z D: Z(j,i) = mult * sgn * e with sgn = -1 for Q11 (operator_q11,
-	// sign < 0); the phase adds a factor conj(phi_{m+1}) (-i) phi_m = -1 when mult = -i
-	const double fac = (q11 ? -1.0 : 1.0) * (imag ? -1.0 : 1.0);
 	std::vector<double> Zr((size_t)N * N, 0.0);
-	for (int im = 0; im + 1 < n_m; ++im)
-		for (int il = 0; il < n_l; ++il) {
-			long m = m0 + im, l = il + std::labs(m);
-			long m2 = m + 1;
-			for (int sgn = -1; sgn <= 1; sgn += 2) {
-				long l2 = l + sgn;
-				long il2 = l2 - std::labs(m2);
-				if (l2 < 0 || il2 < 0 || il2 >= n_l) continue;
-				double v = fac * (sgn > 0 ? outer(m, l) : inner(m, l));
-				int i = im * n_l + il, j = (im + 1) * n_l + (int)il2;
-				Zr[(size_t)j * N + i] = v;
-				Zr[(size_t)i * N + j] = v;
-			}
-		}
+	vgwr_real_coupling(n_l, n_m, m0, comp, Zr.data());
 	// eigenvectors block by block (il parity)
 	std::vector<double> evals;
 	std::vector<std::vector<double>> evecs;	// full-length real vectors

@@ -25,6 +25,8 @@
 #include "qpc_cuda_util.cuh"
 #include <cuda_runtime.h>
 #include <cublas_v2.h>
+#include <cusolverDn.h>
+#include <cstdlib>
 #include <cmath>
 #include <vector>
 #include <algorithm>
@@ -209,6 +211,36 @@ __global__ void __launch_bounds__(VG_THREADS) k_vg_ff(double2* __restrict__ stat
 	}
 }
 
+// P[k][ch] = conj(phi) q_k[ch] from the il-parity blocks' eigenvectors (column-major, as
+// syevd returns them): q_k has block kpar[k], local column kj[k]; channel ch sits in block
+// chpar[ch] at local row chr[ch].  phase: conj(phi_m) = (-i)^(im) when set, else 1.
+__global__ void k_vg_assemble(const double* __restrict__ A0, const double* __restrict__ A1, int nb0, int nb1,
+	const int* __restrict__ kpar, const int* __restrict__ kj, const int* __restrict__ chpar, const int* __restrict__ chr, int N, int nl,
+	bool phase, double2* __restrict__ P)
+{
+	const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+	if (t >= (long)N * N) return;
+	const int k = (int)(t / N), ch = (int)(t - (long)k * N);
+	double v = 0.0;
+	if (kpar[k] == chpar[ch]) v = kpar[k] == 0 ? A0[(long)kj[k] * nb0 + chr[ch]] : A1[(long)kj[k] * nb1 + chr[ch]];
+	double2 out = make_double2(v, 0.0);
+	if (phase) {
+		switch ((ch / nl) & 3) {
+		case 1: out = make_double2(0.0, -v); break;
+		case 2: out = make_double2(-v, 0.0); break;
+		case 3: out = make_double2(0.0, v); break;
+		default: break;
+		}
+	}
+	P[t] = out;
+}
+
+__global__ void k_vg_real_part(const double2* __restrict__ P, long n, double* __restrict__ out)
+{
+	const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+	if (t < n) out[t] = P[t].x;
+}
+
 __global__ void k_vg_snorm(const double2* __restrict__ state, const double* __restrict__ S, int N, int P, int nch, double* out)
 {
 	// one block per instance, fixed-order reduction
@@ -375,6 +407,93 @@ int permute(qpc_vgwr* h, const std::vector<int>& perm, bool inverse)
 	return QPC_OK;
 }
 
+// Angular eigensystems on the device (cuSOLVER syevd per il-parity block) for channel
+// counts where the host solver is slow.  Z_R(y1) = -Z_R(x1) and Z_R(y2) = -Z_R(x2), so two
+// problems give all four: lam_y = -lam_x with the same real eigenvectors.
+int device_angular(qpc_vgwr* h, std::vector<double> lam[4], double2* dP[4])
+{
+	const int nl = h->d.n_l, nm = h->d.n_m, N = h->nch;
+	cusolverDnHandle_t sol = nullptr;
+	if (cusolverDnCreate(&sol) != CUSOLVER_STATUS_SUCCESS) { set_error("cusolverDnCreate failed"); return QPC_ERR_CUDA; }
+	struct guard { cusolverDnHandle_t s; std::vector<void*> p; ~guard() { for (void* q : p) if (q) cudaFree(q); if (s) cusolverDnDestroy(s); } } G{sol, {}};
+	if (cusolverDnSetStream(sol, h->st) != CUSOLVER_STATUS_SUCCESS) { set_error("cusolverDnSetStream failed"); return QPC_ERR_CUDA; }
+	std::vector<int> chpar(N), chr(N), cnt(2, 0);
+	for (int ch = 0; ch < N; ++ch) { chpar[ch] = (ch % nl) % 2; chr[ch] = cnt[chpar[ch]]++; }
+	int *d_kpar = nullptr, *d_kj = nullptr, *d_chpar = nullptr, *d_chr = nullptr, *d_info = nullptr;
+	int rc;
+	if ((rc = dalloc(&d_kpar, N)) || (rc = dalloc(&d_kj, N)) || (rc = dalloc(&d_chpar, N)) || (rc = dalloc(&d_chr, N)) || (rc = dalloc(&d_info, 1))) return rc;
+	G.p.insert(G.p.end(), {d_kpar, d_kj, d_chpar, d_chr, d_info});
+	QPC_CUDA(cudaMemcpy(d_chpar, chpar.data(), sizeof(int) * N, cudaMemcpyHostToDevice));
+	QPC_CUDA(cudaMemcpy(d_chr, chr.data(), sizeof(int) * N, cudaMemcpyHostToDevice));
+	std::vector<double> Zr((size_t)N * N);
+	for (int base = 0; base < 2; ++base) {	// 0: Y11 (x1), 1: Q11 (x2)
+		vgwr_real_coupling(nl, nm, h->d.m0, base, Zr.data());
+		double* A[2] = {nullptr, nullptr};
+		double* W[2] = {nullptr, nullptr};
+		std::vector<double> w[2];
+		for (int par = 0; par < 2; ++par) {
+			const int nb = cnt[par];
+			if (!nb) continue;
+			std::vector<double> blk((size_t)nb * nb);
+			for (int a = 0, ra = 0; a < N; ++a) {
+				if (chpar[a] != par) continue;
+				for (int b = 0, rb = 0; b < N; ++b) {
+					if (chpar[b] != par) continue;
+					blk[(size_t)ra * nb + rb] = Zr[(size_t)a * N + b];
+					++rb;
+				}
+				++ra;
+			}
+			if ((rc = dalloc(&A[par], (size_t)nb * nb)) || (rc = dalloc(&W[par], (size_t)nb))) return rc;
+			G.p.push_back(A[par]); G.p.push_back(W[par]);
+			QPC_CUDA(cudaMemcpy(A[par], blk.data(), sizeof(double) * blk.size(), cudaMemcpyHostToDevice));
+			int lwork = 0;
+			if (cusolverDnDsyevd_bufferSize(sol, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, nb, A[par], nb, W[par], &lwork) != CUSOLVER_STATUS_SUCCESS) {
+				set_error("syevd buffer size failed"); return QPC_ERR_CUDA;
+			}
+			double* work = nullptr;
+			if ((rc = dalloc(&work, (size_t)std::max(lwork, 1)))) return rc;
+			G.p.push_back(work);
+			if (cusolverDnDsyevd(sol, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, nb, A[par], nb, W[par], work, lwork, d_info) != CUSOLVER_STATUS_SUCCESS) {
+				set_error("syevd failed"); return QPC_ERR_CUDA;
+			}
+			int info = 0;
+			QPC_CUDA(cudaMemcpy(&info, d_info, sizeof(int), cudaMemcpyDeviceToHost));
+			if (info) { set_error("syevd info %d", info); return QPC_ERR_NUMERIC; }
+			w[par].resize(nb);
+			QPC_CUDA(cudaMemcpy(w[par].data(), W[par], sizeof(double) * nb, cudaMemcpyDeviceToHost));
+		}
+		// global order: ascending eigenvalue
+		std::vector<std::pair<double, std::pair<int, int>>> ev;
+		for (int par = 0; par < 2; ++par)
+			for (int j = 0; j < cnt[par]; ++j) ev.push_back({w[par][j], {par, j}});
+		std::stable_sort(ev.begin(), ev.end(), [](const auto& x, const auto& y) { return x.first < y.first; });
+		std::vector<int> kpar(N), kj(N);
+		const int cx = base == 0 ? 0 : 1, cy = base == 0 ? 2 : 3;	// x1/y1 from Y11, x2/y2 from Q11
+		lam[cx].resize(N); lam[cy].resize(N);
+		for (int k = 0; k < N; ++k) {
+			kpar[k] = ev[k].second.first; kj[k] = ev[k].second.second;
+			lam[cx][k] = ev[k].first;
+			lam[cy][k] = -ev[k].first;
+		}
+		QPC_CUDA(cudaMemcpy(d_kpar, kpar.data(), sizeof(int) * N, cudaMemcpyHostToDevice));
+		QPC_CUDA(cudaMemcpy(d_kj, kj.data(), sizeof(int) * N, cudaMemcpyHostToDevice));
+		const long nn = (long)N * N;
+		const unsigned nbk = (unsigned)((nn + 255) / 256);
+		// phases: x1 none, y1 (-i)^im ; x2 (-i)^im, y2 none
+		const bool phx = base == 1, phy = base == 0;
+		k_vg_assemble<<<nbk, 256, 0, h->st>>>(A[0], A[1], cnt[0], cnt[1], d_kpar, d_kj, d_chpar, d_chr, N, nl, phx, dP[cx]);
+		k_vg_assemble<<<nbk, 256, 0, h->st>>>(A[0], A[1], cnt[0], cnt[1], d_kpar, d_kj, d_chpar, d_chr, N, nl, phy, dP[cy]);
+		QPC_CUDA(cudaGetLastError());
+		QPC_CUDA(cudaStreamSynchronize(h->st));
+		for (int par = 0; par < 2; ++par) {
+			if (A[par]) { cudaFree(A[par]); std::replace(G.p.begin(), G.p.end(), (void*)A[par], (void*)nullptr); }
+			if (W[par]) { cudaFree(W[par]); std::replace(G.p.begin(), G.p.end(), (void*)W[par], (void*)nullptr); }
+		}
+	}
+	return QPC_OK;
+}
+
 } // namespace
 
 extern "C" {
@@ -400,15 +519,6 @@ int qpc_vgwr_create(const qpc_dims* dims, double dt, const double* S, const doub
 	const int mmax = std::max(std::abs(d.m0), std::abs(d.m0 + d.n_m - 1));
 	h->nlh = mmax + d.n_l;
 	const int N = d.n_r, P = d.p, NE = P + 1, nch = h->nch;
-	// angular eigensystems
-	std::vector<double> lam[4], Pm[4];
-	for (int c = 0; c < 4; ++c) {
-		lam[c].resize(nch);
-		Pm[c].resize((size_t)2 * nch * nch);
-		if (int rc = qpc_vgwr_angular(d.n_l, d.n_m, d.m0, c, lam[c].data(), Pm[c].data())) { set_error("angular eigensystem %d failed", c); return fail(rc); }
-	}
-	std::vector<double> px1((size_t)nch * nch), py2((size_t)nch * nch);
-	for (size_t i = 0; i < px1.size(); ++i) { px1[i] = Pm[0][2 * i]; py2[i] = Pm[3][2 * i]; }
 	// field-free factors
 	std::vector<double> lrow((size_t)h->nlh * N * P * 2), dinv((size_t)h->nlh * N * 2);
 	for (int l = 0; l < h->nlh; ++l) {
@@ -431,33 +541,43 @@ int qpc_vgwr_create(const qpc_dims* dims, double dt, const double* S, const doub
 		(rc = dalloc(&h->X, nst)) || (rc = dalloc(&h->W, nst)) || (rc = dalloc(&h->U, nst * NE)) || (rc = dalloc(&h->ntt, (size_t)h->B)) ||
 		(rc = dalloc(&h->perm, (size_t)h->B)) || (rc = dalloc(&h->nrm, (size_t)h->B)))
 		return fail(rc);
-	// merged transforms P_b P_a^H on the device: row-major C = L R^H; column-major C^T = conj(R) L^T
-	double2 *dP1 = nullptr, *dP2 = nullptr;
-	if ((rc = dalloc(&dP1, (size_t)nch * nch)) || (rc = dalloc(&dP2, (size_t)nch * nch))) {
-		if (dP1) cudaFree(dP1);
-		return fail(rc);
+	// angular eigensystems: complex P_c [nch][nch] on the device, from the host solver or,
+	// for many channels (or QPC_VGWR_DEVICE_EIG=1), from cuSOLVER
+	std::vector<double> lam[4];
+	double2* dP[4] = {nullptr, nullptr, nullptr, nullptr};
+	struct pguard { double2** p; ~pguard() { for (int c = 0; c < 4; ++c) if (p[c]) cudaFree(p[c]); } } PG{dP};
+	for (int c = 0; c < 4; ++c)
+		if ((rc = dalloc(&dP[c], (size_t)nch * nch))) return fail(rc);
+	const char* ev = getenv("QPC_VGWR_DEVICE_EIG");
+	const bool on_device = ev ? atoi(ev) != 0 : nch > 1024;
+	if (on_device) {
+		if ((rc = device_angular(h, lam, dP))) return fail(rc);
+	} else {
+		std::vector<double> Pm((size_t)2 * nch * nch);
+		for (int c = 0; c < 4; ++c) {
+			lam[c].resize(nch);
+			if ((rc = qpc_vgwr_angular(d.n_l, d.n_m, d.m0, c, lam[c].data(), Pm.data()))) { set_error("angular eigensystem %d failed", c); return fail(rc); }
+			if (cudaMemcpy(dP[c], Pm.data(), sizeof(double2) * nch * nch, cudaMemcpyHostToDevice) != cudaSuccess) { set_error("upload"); return fail(QPC_ERR_CUDA); }
+		}
 	}
-	auto merge = [&](const std::vector<double>& Lh, const std::vector<double>& Rh, double2* out) -> int {
-		QPC_CUDA(cudaMemcpy(dP1, Lh.data(), sizeof(double2) * nch * nch, cudaMemcpyHostToDevice));
-		QPC_CUDA(cudaMemcpy(dP2, Rh.data(), sizeof(double2) * nch * nch, cudaMemcpyHostToDevice));
+	// merged transforms P_b P_a^H: row-major C = L R^H; column-major C^T = conj(R) L^T with
+	// A_cm = R^T (buffer R, op C) and B_cm = L^T (buffer L)
+	auto merge = [&](const double2* Ld, const double2* Rd, double2* out) -> int {
 		const cuDoubleComplex one = make_cuDoubleComplex(1.0, 0.0), zero = make_cuDoubleComplex(0.0, 0.0);
-		// column-major views: A_cm = R^T (buffer R), B_cm = L^T (buffer L); C^T = conj(R) L^T = (A_cm)^H L^T
-		QPC_CUBLAS(cublasZgemm(h->cb, CUBLAS_OP_C, CUBLAS_OP_N, nch, nch, nch, &one, (const cuDoubleComplex*)dP2, nch,
-			(const cuDoubleComplex*)dP1, nch, &zero, (cuDoubleComplex*)out, nch));
-		QPC_CUDA(cudaStreamSynchronize(h->st));
+		QPC_CUBLAS(cublasZgemm(h->cb, CUBLAS_OP_C, CUBLAS_OP_N, nch, nch, nch, &one, (const cuDoubleComplex*)Rd, nch,
+			(const cuDoubleComplex*)Ld, nch, &zero, (cuDoubleComplex*)out, nch));
 		return QPC_OK;
 	};
-	int mrc = merge(Pm[1], Pm[0], h->M12);
-	if (!mrc) mrc = merge(Pm[2], Pm[1], h->M23);
-	if (!mrc) mrc = merge(Pm[3], Pm[2], h->M34);
-	cudaFree(dP1);
-	cudaFree(dP2);
-	if (mrc) return fail(mrc);
+	if ((rc = merge(dP[1], dP[0], h->M12)) || (rc = merge(dP[2], dP[1], h->M23)) || (rc = merge(dP[3], dP[2], h->M34))) return fail(rc);
+	{
+		const long nn = (long)nch * nch;
+		k_vg_real_part<<<(unsigned)((nn + 255) / 256), 256, 0, h->st>>>(dP[0], nn, h->Px1);
+		k_vg_real_part<<<(unsigned)((nn + 255) / 256), 256, 0, h->st>>>(dP[3], nn, h->Py2);
+		if (cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(h->st) != cudaSuccess) { set_error("transform setup failed"); return fail(QPC_ERR_CUDA); }
+	}
 	if (cudaMemcpy(h->S, S, sizeof(double) * N * NE, cudaMemcpyHostToDevice) != cudaSuccess ||
 		cudaMemcpy(h->Ri, Rinv, sizeof(double) * N * NE, cudaMemcpyHostToDevice) != cudaSuccess ||
 		cudaMemcpy(h->D, D, sizeof(double) * N * NE, cudaMemcpyHostToDevice) != cudaSuccess ||
-		cudaMemcpy(h->Px1, px1.data(), sizeof(double) * px1.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
-		cudaMemcpy(h->Py2, py2.data(), sizeof(double) * py2.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
 		cudaMemcpy(h->Lrow, lrow.data(), sizeof(double) * lrow.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
 		cudaMemcpy(h->Dinv, dinv.data(), sizeof(double) * dinv.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
 		cudaMemset(h->X, 0, sizeof(double2) * nst) != cudaSuccess) {
