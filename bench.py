@@ -25,6 +25,15 @@ window sits).  Metric: wavefunction-steps/s.
 
 --impl reference times the reference's CPU implementation of the path (the
 oracle port: the reference itself needs x86 and MKL) on all host cores.
+
+--workload c3a times the Arnoldi propagator (k_max = 12, dt = 0.1) on --batch wavefunctions
+with their own screened potentials on the N_r = 800, n_l = 41 grid.
+--workload c1 measures the single large velocity-gauge elliptical instance over a
+window of steps around the pulse peak (a whole 6-cycle pulse at 1800 nm is ~24k steps):
+screened Coulomb V = -(1 + 17 e^{-2r})/r, B-splines order 8 (p = 7), N_r = 2000 on
+[0, 1000] with quadratic-then-linear knots, l <= 60 for |m| <= 60 in the reference's
+rectangular layout (n_m = 121, m0 = -60, n_l = 61: 7381 channels), 1800 nm, ellipticity
+0.5, 8e13 W/cm^2, sin^2 envelope of 6 cycles, dt = 0.05.
 """
 import argparse
 import json
@@ -249,6 +258,116 @@ def run_engine(args):
     return line
 
 
+def c1_knots(n_r, p, rmax, frac=0.1):
+    """Quadratic-then-linear knots (no reference generator): the first `frac` of the
+    n_r + 2 - p intervals grow quadratically, the rest are uniform with the matching slope."""
+    M = n_r + 2 - p
+    Mq = max(1, int(round(frac * M)))
+    rq = rmax / (1.0 + 2.0 * (M - Mq) / Mq)
+    i = np.arange(M + 1, dtype=np.float64)
+    r = np.where(i <= Mq, rq * (i / Mq) ** 2, rq + 2.0 * rq / Mq * (i - Mq))
+    r[-1] = rmax
+    return np.concatenate([np.zeros(p), r, np.full(p, rmax)])
+
+
+def run_c1(args):
+    import importlib
+    q = importlib.import_module("qpc-tdse-cpc_gb300")
+    n_r, p, n_l, n_m, m0, rmax, dt = 2000, 7, 61, 121, -60, 1000.0, 0.05
+    lam_nm, inten, eps, ncyc = 1800.0, 8e13, 0.5, 6
+    kn = c1_knots(n_r, p, rmax)
+    nlh = abs(m0) + n_l
+    t0 = time.perf_counter()
+    S, R, Ri, D, H = q.radial_setup(n_r, p, nlh, kn, (q.POTENTIAL_YUKAWA, 1.0, 17.0, 2.0))
+    c_gs, e_gs = q.ground_state(S, H, n_l, n_m, im=-m0, il=0, ir=0, m0=m0)
+    prop = q.propagator_cn_hc_vgwr().initialize(n_r, p, n_l, n_m, m0, S, Ri, D, H, dt)
+    setup_s = time.perf_counter() - t0
+    w0 = q.wavelength_to_w0(lam_nm)
+    a0 = q.intensity_to_e0(inten) / w0
+    T = ncyc * 2 * np.pi / w0
+    K, W = args.steps, args.warmup
+    s0 = int(T / dt / 2) - W            # window centred on the pulse peak
+    t = dt * (s0 + np.arange(W + K + 1))
+    env = np.sin(np.pi * t / T) ** 2
+    atab = np.stack([a0 / np.sqrt(1 + eps ** 2) * env * np.cos(w0 * t), a0 * eps / np.sqrt(1 + eps ** 2) * env * np.sin(w0 * t)], 1)
+    prop.put(c_gs[None])
+    prop.run(atab[None, :W + 1], [W])
+    n0 = prop.norm()[0]
+    with Clocks() as clk:
+        prop.run(atab[None, W:W + K + 1], [K])
+        dev_ms, launches = prop.last_run()
+    clocks = clk.summary()
+    n1 = prop.norm()[0]
+    nch = n_l * n_m
+    gemm_flops = 4 * 2.0 * (2 * n_r) * nch * nch + 6 * 8.0 * n_r * nch * nch   # 4 real, 6 complex transforms per step
+    tfl = gemm_flops / (dev_ms / K * 1e-3) / 1e12
+    line = {
+        "metric": "wavefunction-steps/s (single large elliptical instance, window at the pulse peak)",
+        "value": K / (dev_ms * 1e-3), "unit": "wf-steps/s", "n_gpus": 1, "steps": K, "warmup": W,
+        "ms_per_step": dev_ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "c128 (complex FP64)", "data": "synthetic (ground state of the screened potential, analytic pulse)",
+        "config": {"workload": "C1: V=-(1+17e^-2r)/r, p=7, N_r=2000 on [0,1000] quadratic-then-linear knots, n_m=121 (m0=-60), "
+                               "n_l=61 (7381 channels), 1800 nm, eps=0.5, 8e13 W/cm^2, 6 cycles, velocity gauge, dt=0.05",
+                   "window_start_step": int(s0 + W), "pulse_steps": int(T / dt), "ground_state_energy": float(e_gs)},
+        "gpu_launches": int(launches),
+        "roofline": {"bound": "fp64", "kernel": "cuBLAS DGEMM/ZGEMM (m,l) transforms", "achieved": tfl, "peak": FP64_PEAK_TFLOPS,
+                     "unit": "TFLOP/s", "frac": tfl / FP64_PEAK_TFLOPS, "flops_per_step": gemm_flops},
+        "norm_drift_over_window": abs(n1 - n0) / n0,
+        "setup_s": setup_s,
+        "clocks": clocks,
+    }
+    return line
+
+
+def arnoldi_flops(n_r, p, n_l, kmax):
+    """FP64 flops per complex element and step of the Arnoldi engine (csrc/qpc_arnoldi.cu):
+    S-norms (kmax launches) 2(2p+1)+2 FMAs, expansion 3(2p+1) FMA pairs + projections 4(k+1)
+    FMAs, S^-1 2(p+1) per real part, Gram-Schmidt 4(k+1), the final combination 4 kmax."""
+    fma = 0.0
+    for k in range(kmax):
+        fma += 2 * (2 * p + 1) + 2                     # S-norm
+        fma += 6 * (2 * p + 1) + 4 * (k + 1) + 6       # expand
+        if k < kmax - 1:
+            fma += 2 * 2 * (p + 1) + 4 * (k + 1)       # S^-1 (re, im) + Gram-Schmidt
+    fma += 4 * kmax
+    return 2.0 * fma * n_r * n_l
+
+
+def run_c3a(args):
+    """Arnoldi propagator on a batch of wavefunctions with their own screened potentials."""
+    import importlib
+    q = importlib.import_module("qpc-tdse-cpc_gb300")
+    B, n_r, p, n_l, dt, kmax = args.batch, 800, 6, 41, 0.1, 12
+    rng = np.random.default_rng(2025)
+    kn = q.linear_knots(n_r, p, 0.0, n_r / 2.0)
+    Hs = []
+    for _ in range(B):
+        S, R, _, _, H = q.radial_setup(n_r, p, n_l, kn, (q.POTENTIAL_YUKAWA, 1.0, rng.uniform(0, 17), rng.uniform(1, 3)))
+        Hs.append(H)
+    c0 = np.stack([q.ground_state(S, H, n_l)[0] for H in Hs])
+    prop = q.propagator_hc_lgwz(kmax, 1e-14, 1e-8).initialize(n_r, p, n_l, S, R, np.stack(Hs), q.y10_coupling(n_l), dt, n_inst=B)
+    K, W = args.steps, args.warmup
+    ez = 0.03 * np.sin(0.057 * dt * np.arange(W + K))[None, :] * np.ones((B, 1))
+    prop.put(c0)
+    prop.run(ez[:, :W])
+    with Clocks() as clk:
+        prop.run(ez[:, W:])
+        dev_ms, launches = prop.last_run()
+    fl = arnoldi_flops(n_r, p, n_l, kmax)
+    tfl = fl * B / (dev_ms / K * 1e-3) / 1e12
+    return {
+        "metric": "wavefunction-steps/s (Arnoldi, k_max = 12, per-instance screened potentials)",
+        "value": B * K / (dev_ms * 1e-3), "unit": "wf-steps/s", "n_gpus": 1, "steps": K, "warmup": W,
+        "ms_per_step": dev_ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "c128 (complex FP64)", "data": "synthetic (seeded screened potentials a in [0,17], b in [1,3])",
+        "config": {"workload": "Arnoldi batch: %d wavefunctions, N_r=800 on [0,400], p=6, n_l=41, dt=0.1, k_max=12" % B},
+        "gpu_launches": int(launches),
+        "roofline": {"bound": "fp64", "kernel": "whole Arnoldi step", "achieved": tfl, "peak": FP64_PEAK_TFLOPS, "unit": "TFLOP/s",
+                     "frac": tfl / FP64_PEAK_TFLOPS, "flops_per_wf_step": fl},
+        "clocks": clk.summary(),
+    }
+
+
 def cpu_baseline(q, S, R, H, c0, ftab, dt, n_l, budget_s=15.0, threads=None):
     """The CPU oracle (port of the reference's propagator_cn_hc_lgwz), one
     wavefunction per host thread, on a bounded number of steps of the same workload."""
@@ -306,7 +425,14 @@ def main():
     ap.add_argument("--batch", type=int, default=256)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--workload", default="c2", choices=["c2", "c1", "c3a"])
     args = ap.parse_args()
+    if args.workload == "c1":
+        print(json.dumps(run_c1(args)))
+        return
+    if args.workload == "c3a":
+        print(json.dumps(run_c3a(args)))
+        return
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     if args.impl == "reference":
