@@ -101,6 +101,11 @@ int qpc_gen_eigen(int32_t n, int32_t p, const double* S, const double* Hl, int32
  * lam[N_ch] ascending and P[N_ch][N_ch] complex with P Z P^H = diag(lam). */
 int qpc_vgwr_angular(int32_t n_l, int32_t n_m, int32_t m0, int32_t comp, double* lam, double* P);
 
+/* absorber_mask::initialize (absorber.hpp:42-49): M[r][k] = <B_r| m |B_{r+k}> with
+ * m(r) = 1 below rmin, 0 above rmax, |cos(pi/2 (r-rmin)/(rmax-rmin))|^index between
+ * (the reference's default index is 1/6). */
+int qpc_mask_band(int32_t n_r, int32_t p, const double* knots, double rmin, double rmax, double index, double* M);
+
 /* lu_dsb (LAPACKE_dpbtrf 'L', algorithm/ed.h:182-193) as operator_sc::initialize uses it
  * (spherical/operators/1e.hpp:1233-1244): S = L L^T with L(r+k, r) at L[r*(p+1)+k], the
  * layout of operator_sc::cholesky(); entries past the last row are zero.  Returns 0, -1 on
@@ -170,6 +175,10 @@ int qpc_lgwz_run_dipole(qpc_lgwz* h, const double* ftab, int64_t ld, const int64
 /* S-norm per instance, sum over (m,l) of c^H S c
  * (operator_rsym::observe, spherical/operators/1e.hpp:69-89); norm[n_inst]. */
 int qpc_lgwz_norm(qpc_lgwz* h, double* norm);
+/* absorber_mask::operator()(coef, prop.s) (absorber.hpp:51-63) on every wavefunction of the
+ * batch: c <- S^-1 (M c) per (m,l) channel, M from qpc_mask_band.  The driver loop applies it
+ * after each propagate (sphTDSE.cpp:807-810). */
+int qpc_lgwz_mask(qpc_lgwz* h, const double* M);
 
 /* <c| f(r) cos(theta) |c> per instance with F = <Bi|f|Bj> ([n_r][p+1])
  * (observable_z::observe, spherical/observable/1e.hpp:26-50); out[2*inst] re, [2*inst+1] im. */

@@ -299,4 +299,18 @@ int oracle_arnoldi_run(const oracle_arnoldi* g, double* coef, const double* ftab
 	return err;
 }
 
+// absorber_mask::operator() (absorber.hpp:51-63): per channel w = S^-1 (M w), the band
+// product by symb_mul_vecd and the Cholesky solves by ltrb_inv_vecd / utrb_inv_vecd.
+void oracle_mask(int n_r, int p, long n_ch, const double* M, const double* chol, double* coef)
+{
+	std::vector<cd> t(n_r);
+	for (long c = 0; c < n_ch; ++c) {
+		cd* w = (cd*)coef + c * n_r;
+		sbmv(n_r, p, M, w, t.data(), 0.0, false);
+		chol_solve(n_r, p, chol, t.data());
+		for (int r = 0; r < n_r; ++r) w[r] = t[r];
+	}
+}
+
 } // extern "C"
+

@@ -36,6 +36,9 @@
 //       (cn_1e.hpp:812-951): FIELD holds NT+1 rows (A_x, A_y) at t_0..t_NT; runs
 //       propagate(coef, ax_i, ax_i+1, ay_i, ay_i+1) for i < NT, then NFREE field-free
 //       steps; writes coef, the S-norm and the eigenvalues of the four couplings.
+//   mask   OUT RMAX DT ZC ZS SG INIT RMIN RMAXM INDEX
+//       absorber_mask (absorber.hpp:40-63) initialised on [RMIN, RMAXM] with exponent INDEX
+//       and applied once to INIT: writes the mask band and the masked coefficients.
 //   proj   OUT RMAX DT ZC ZS SG COEF EMAX
 //       Projection of COEF onto field-free eigenstates with E < EMAX
 //       (eigenstate_sph::initialize + projection, population_1e.hpp:29-118).
@@ -351,6 +354,35 @@ static int cmd_vgwr(int argc, char** argv)
 	return 0;
 }
 
+static int cmd_mask(int argc, char** argv)
+{
+	if (argc < 12) return 1;
+	std::string out = argv[2];
+	double rmax = atof(argv[3]), dt = atof(argv[4]);
+	potn_any potn{atof(argv[5]), atof(argv[6]), atof(argv[7])};
+	const char* init = argv[8];
+	double r0 = atof(argv[9]), r1 = atof(argv[10]), index = atof(argv[11]);
+	omp_set_num_threads(1);
+	auto radi = integrator_radi<dims_t>();
+	auto angu = integrator_angu<dims_t>();
+	auto prop = propagator_cn_hc_lgwz<dims_t>();
+	init_prop(prop, radi, angu, rmax, dt, potn, 1);
+	auto coef = coefficient<dims_t>();
+	auto v = slurp(init, 2 * dims_t::n_leng);
+	std::memcpy((double*)coef.data, v.data(), sizeof(double) * v.size());
+	struct probe : absorber_mask<dims_t> {
+		using absorber_mask<dims_t>::absorber_mask;
+		const double* band() const { return this->data; }
+	};
+	auto mask = probe(1);
+	mask.initialize(radi, r0, r1, index);
+	coefficient_view<dims_t> view{coef.data};
+	mask(view, prop.s);
+	dump(out, "maskband", mask.band(), dims_t::n_rsub);
+	dump(out, "coef", coef.data, 2 * dims_t::n_leng);
+	return 0;
+}
+
 int main(int argc, char** argv)
 {
 	if (argc < 2) { std::fprintf(stderr, "usage: setup|field|propagate|proj|arnoldi ...\n"); return 1; }
@@ -363,6 +395,7 @@ int main(int argc, char** argv)
 		else if (c == "proj") rc = cmd_proj(argc, argv);
 		else if (c == "arnoldi") rc = cmd_arnoldi(argc, argv);
 		else if (c == "vgwr") rc = cmd_vgwr(argc, argv);
+		else if (c == "mask") rc = cmd_mask(argc, argv);
 		if (rc) std::fprintf(stderr, "bad arguments for %s\n", argv[1]);
 		return rc;
 	} catch (std::exception& e) {

@@ -40,6 +40,7 @@ EXPORTS = (
     "qpc_mlp_loss_grad", "qpc_mlp_train", "qpc_mlp_predict", "qpc_vgwr_angular", "qpc_vgwr_create",
     "qpc_vgwr_destroy", "qpc_vgwr_put", "qpc_vgwr_get", "qpc_vgwr_put_device", "qpc_vgwr_get_device",
     "qpc_vgwr_propagate", "qpc_vgwr_propagate_free", "qpc_vgwr_run", "qpc_vgwr_norm", "qpc_vgwr_last_run",
+    "qpc_mask_band", "qpc_lgwz_mask",
 )
 NOALLOC_MAX_ELEMS = 1 << 20
 KERNELS = ("factor", "transform_fwd", "sweep", "transform_bwd", "fieldfree")
@@ -111,6 +112,8 @@ def load(path=None):
         "qpc_lgwz_run_many": (ctypes.c_int, [i32, P, P, P, P, P, P]),
         "qpc_mlp_create": (ctypes.c_int, [i32, i32, i32, i32, i32, ctypes.c_uint64, P]),
         "qpc_vgwr_angular": (ctypes.c_int, [i32, i32, i32, i32, P, P]),
+        "qpc_mask_band": (ctypes.c_int, [i32, i32, P, d, d, d, P]),
+        "qpc_lgwz_mask": (ctypes.c_int, [P, P]),
         "qpc_vgwr_create": (ctypes.c_int, [P, d, P, P, P, P, P]),
         "qpc_vgwr_destroy": (ctypes.c_int, [P]),
         "qpc_vgwr_put": (ctypes.c_int, [P, P]),
@@ -436,6 +439,10 @@ class propagator_cn_hc_lgwz:
         _check(load().qpc_lgwz_norm(self._h, _ptr(out)))
         return out
 
+    def mask(self, M):
+        """absorber_mask::operator()(coef, s) on every wavefunction: c <- S^-1 (M c) per channel."""
+        _check(load().qpc_lgwz_mask(self._h, _ptr(_f64(M))))
+
     def dipole(self, F):
         out = np.zeros(2 * self.shape[0])
         _check(load().qpc_lgwz_dipole(self._h, _ptr(_f64(F)), _ptr(out)))
@@ -493,6 +500,14 @@ def vgwr_angular(n_l, n_m, m0, comp):
     P = np.zeros((N, N), complex)
     _check(load().qpc_vgwr_angular(n_l, n_m, m0, comp, _ptr(lam), _ptr(P)))
     return lam, P
+
+
+def mask_band(n_r, p, knots, rmin, rmax, index=1.0 / 6.0):
+    """absorber_mask::initialize (absorber.hpp:42-49): <B_i|m(r)|B_j>, m = |cos(pi/2 (r-rmin)/(rmax-rmin))|^index."""
+    kn = _f64(knots)
+    M = np.zeros((n_r, p + 1))
+    _check(load().qpc_mask_band(n_r, p, _ptr(kn), rmin, rmax, index, _ptr(M)))
+    return M
 
 
 def cholesky_band(S, p):

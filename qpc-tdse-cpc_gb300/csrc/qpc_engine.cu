@@ -401,6 +401,8 @@ struct qpc_lgwz {
 	int K = 1;
 	int* status = nullptr;
 	double2* red = nullptr;   // reduction scratch [2*B*M*L]
+	// absorbing mask: the mask band and the Cholesky factor of S (set by qpc_lgwz_mask)
+	double *mM = nullptr, *mLrow = nullptr, *mLcol = nullptr, *mdinv = nullptr;
 	// in-loop dipole (qpc_lgwz_run_dipole)
 	double* obsF = nullptr;   // device band of <B|f|B> [N][P+1]
 	double* obs = nullptr;    // per coupling chain [B][M][npair][2]
@@ -430,6 +432,70 @@ struct qpc_lgwz {
 	std::vector<double> h_lam;   // [M][L]
 	std::vector<double> h_P;     // [M][L][L]
 };
+
+// ---------------------------------------------------------------- absorbing mask
+// absorber_mask::operator() (absorber.hpp:51-63) on the engine's r-major state [B][M][N][L]:
+// t = M c per channel (all lanes, one element each), then c = (L L^T)^-1 t with one lane per
+// real recurrence (channel, real or imaginary part); Lrow[r][j-1] = L(r, r-j),
+// Lcol[r][k-1] = L(r+k, r), dinv[r] = 1/L(r, r).
+__global__ void k_mask_band(const double2* __restrict__ st, double2* __restrict__ t, const double* __restrict__ Mb, int N, int P, int L,
+	long total)
+{
+	const long e = (long)blockIdx.x * blockDim.x + threadIdx.x;
+	if (e >= total) return;
+	const long row = e / L;
+	const int r = (int)(row % N);
+	double2 acc = make_double2(0.0, 0.0);
+	for (int q = 1; q <= P && q <= r; ++q) {
+		double m = Mb[(long)(r - q) * (P + 1) + q];
+		double2 v = st[e - (long)q * L];
+		acc.x = fma(m, v.x, acc.x); acc.y = fma(m, v.y, acc.y);
+	}
+	for (int q = 0; q <= P && r + q < N; ++q) {
+		double m = Mb[(long)r * (P + 1) + q];
+		double2 v = st[e + (long)q * L];
+		acc.x = fma(m, v.x, acc.x); acc.y = fma(m, v.y, acc.y);
+	}
+	t[e] = acc;
+}
+
+template <int P>
+__global__ void k_mask_solve(double2* __restrict__ st, double2* __restrict__ tb, const double* __restrict__ Lrow,
+	const double* __restrict__ Lcol, const double* __restrict__ dinv, int N, int L, long nchain)
+{
+	const long c = (long)blockIdx.x * blockDim.x + threadIdx.x;
+	if (c >= nchain) return;
+	const long bm = c / (2L * L);
+	const int rest = (int)(c - bm * 2L * L);	// l * 2 + part
+	const long stride = 2L * L;
+	double* t = reinterpret_cast<double*>(tb) + bm * N * stride + rest;
+	double* x = reinterpret_cast<double*>(st) + bm * N * stride + rest;
+	double w[P];
+#pragma unroll
+	for (int j = 0; j < P; ++j) w[j] = 0.0;
+	for (int r = 0; r < N; ++r) {
+		double v = t[(long)r * stride];
+#pragma unroll
+		for (int j = 0; j < P; ++j) v = fma(-w[j], Lrow[(long)r * P + j], v);
+		v *= dinv[r];
+#pragma unroll
+		for (int j = P - 1; j > 0; --j) w[j] = w[j - 1];
+		w[0] = v;
+		t[(long)r * stride] = v;
+	}
+#pragma unroll
+	for (int j = 0; j < P; ++j) w[j] = 0.0;
+	for (int r = N - 1; r >= 0; --r) {
+		double v = t[(long)r * stride];
+#pragma unroll
+		for (int j = 0; j < P; ++j) v = fma(-w[j], Lcol[(long)r * P + j], v);
+		v *= dinv[r];
+#pragma unroll
+		for (int j = P - 1; j > 0; --j) w[j] = w[j - 1];
+		w[0] = v;
+		x[(long)r * stride] = v;
+	}
+}
 
 namespace {
 
@@ -803,6 +869,7 @@ int qpc_lgwz_destroy(qpc_lgwz* h)
 	cudaFree(h->st); cudaFree(h->eo); cudaFree(h->wk); cudaFree(h->hostlay); cudaFree(h->fac);
 	cudaFree(h->status); cudaFree(h->red); cudaFree(h->ntf); cudaFree(h->ntt); cudaFree(h->ftab);
 	cudaFree(h->obsF); cudaFree(h->obs); cudaFree(h->dl); cudaFree(h->y10d); cudaFree(h->zdev);
+	cudaFree(h->mM); cudaFree(h->mLrow); cudaFree(h->mLcol); cudaFree(h->mdinv);
 	for (auto e : h->evpool) cudaEventDestroy(e);
 	for (int g = 0; g < qpc_lgwz::MAXNS; ++g) {
 		if (h->gs[g]) { cudaStreamSynchronize(h->gs[g]); cudaStreamDestroy(h->gs[g]); }
@@ -1071,6 +1138,52 @@ int qpc_lgwz_norm(qpc_lgwz* h, double* norm)
 		norm[k] = s;
 	}
 	return QPC_OK;
+}
+
+int qpc_lgwz_mask(qpc_lgwz* h, const double* M)
+{
+	if (!h || !M) { set_error("NULL argument"); return QPC_ERR_ARGS; }
+	const int N = h->N, P = h->P, NE = P + 1;
+	if (!h->mLrow) {
+		std::vector<double> S((size_t)N * NE), Lc((size_t)N * NE);
+		QPC_CUDA(cudaMemcpy(S.data(), h->S, sizeof(double) * S.size(), cudaMemcpyDeviceToHost));
+		int bad = qpc_cholesky_band(N, P, S.data(), Lc.data());
+		if (bad) { set_error("S is not positive definite (pivot %d)", bad); return QPC_ERR_SINGULAR; }
+		std::vector<double> lrow((size_t)N * P, 0.0), lcol((size_t)N * P, 0.0), di(N);
+		for (int r = 0; r < N; ++r) {
+			di[r] = 1.0 / Lc[(size_t)r * NE];
+			for (int j = 1; j <= P; ++j) {
+				if (r - j >= 0) lrow[(size_t)r * P + j - 1] = Lc[(size_t)(r - j) * NE + j];
+				if (r + j < N) lcol[(size_t)r * P + j - 1] = Lc[(size_t)r * NE + j];
+			}
+		}
+		int rc;
+		if ((rc = dalloc(&h->mM, (size_t)N * NE)) || (rc = dalloc(&h->mLrow, (size_t)N * P)) || (rc = dalloc(&h->mLcol, (size_t)N * P)) ||
+			(rc = dalloc(&h->mdinv, (size_t)N)))
+			return rc;
+		QPC_CUDA(cudaMemcpy(h->mLrow, lrow.data(), sizeof(double) * lrow.size(), cudaMemcpyHostToDevice));
+		QPC_CUDA(cudaMemcpy(h->mLcol, lcol.data(), sizeof(double) * lcol.size(), cudaMemcpyHostToDevice));
+		QPC_CUDA(cudaMemcpy(h->mdinv, di.data(), sizeof(double) * N, cudaMemcpyHostToDevice));
+	}
+	QPC_CUDA(cudaMemcpyAsync(h->mM, M, sizeof(double) * N * NE, cudaMemcpyHostToDevice, h->stream));
+	const long total = state_len(h);
+	k_mask_band<<<(unsigned)((total + 255) / 256), 256, 0, h->stream>>>(h->st, h->wk, h->mM, N, P, h->L, total);
+	LAUNCH(h);
+	const long nchain = 2L * h->B * h->M * h->L;
+	const unsigned nb = (unsigned)((nchain + 63) / 64);
+	switch (P) {
+	case 1: k_mask_solve<1><<<nb, 64, 0, h->stream>>>(h->st, h->wk, h->mLrow, h->mLcol, h->mdinv, N, h->L, nchain); break;
+	case 2: k_mask_solve<2><<<nb, 64, 0, h->stream>>>(h->st, h->wk, h->mLrow, h->mLcol, h->mdinv, N, h->L, nchain); break;
+	case 3: k_mask_solve<3><<<nb, 64, 0, h->stream>>>(h->st, h->wk, h->mLrow, h->mLcol, h->mdinv, N, h->L, nchain); break;
+	case 4: k_mask_solve<4><<<nb, 64, 0, h->stream>>>(h->st, h->wk, h->mLrow, h->mLcol, h->mdinv, N, h->L, nchain); break;
+	case 5: k_mask_solve<5><<<nb, 64, 0, h->stream>>>(h->st, h->wk, h->mLrow, h->mLcol, h->mdinv, N, h->L, nchain); break;
+	case 6: k_mask_solve<6><<<nb, 64, 0, h->stream>>>(h->st, h->wk, h->mLrow, h->mLcol, h->mdinv, N, h->L, nchain); break;
+	case 7: k_mask_solve<7><<<nb, 64, 0, h->stream>>>(h->st, h->wk, h->mLrow, h->mLcol, h->mdinv, N, h->L, nchain); break;
+	default: k_mask_solve<8><<<nb, 64, 0, h->stream>>>(h->st, h->wk, h->mLrow, h->mLcol, h->mdinv, N, h->L, nchain); break;
+	}
+	LAUNCH(h);
+	QPC_CUDA(cudaGetLastError());
+	return wait_stream(h);
 }
 
 int qpc_lgwz_dipole(qpc_lgwz* h, const double* F, double* out)

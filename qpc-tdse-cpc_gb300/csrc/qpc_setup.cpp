@@ -556,6 +556,25 @@ int qpc_gen_eigen(int32_t n, int32_t p, const double* S, const double* Hl, int32
 	return QPC_OK;
 }
 
+// absorber_mask::initialize (absorber.hpp:42-49): M = <B_i| m(r) |B_j> with m(r) = 1 for
+// r < rmin, 0 for r > rmax, |cos(pi/2 (r - rmin)/(rmax - rmin))|^index between, by the same
+// quadrature as the other radial matrices (integrate_0r0).
+int qpc_mask_band(int32_t n_r, int32_t p, const double* knots, double rmin, double rmax, double index, double* M)
+{
+	if (n_r < 2 * p + 2 || p < 1 || p > QPC_MAX_RANK || !knots || !M || !(rmax > rmin)) return QPC_ERR_ARGS;
+	radial_basis B;
+	B.n = n_r; B.p = p; B.nq = 2 * p + 2;
+	B.t.assign(knots, knots + n_r + p + 3);
+	for (size_t i = 1; i < B.t.size(); ++i) if (B.t[i] < B.t[i - 1]) return QPC_ERR_ARGS;
+	build_basis(B);
+	const double pi = 3.14159265358979323846;
+	auto f = [&](double r) { return r < rmin ? 1.0 : r > rmax ? 0.0 : std::pow(std::fabs(std::cos(0.5 * pi * (r - rmin) / (rmax - rmin))), index); };
+	const int ne = p + 1;
+	for (int i = 0; i < n_r; ++i)
+		for (int k = 0; k < ne; ++k) M[(size_t)i * ne + k] = i + k < n_r ? integrate(B, 0, 0, i, i + k, f) : 0.0;
+	return QPC_OK;
+}
+
 // lu_dsb (LAPACKE_dpbtrf 'L', algorithm/ed.h:182-193) in operator_sc's layout
 // (operators/1e.hpp:1233-1244): L(r+k, r) at L[r*(p+1)+k], zero past the last row
 int qpc_cholesky_band(int32_t n, int32_t p, const double* S, double* L)

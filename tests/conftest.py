@@ -133,6 +133,13 @@ class ArnoldiOracle:
         g._keep = keep
         return g
 
+    def mask(self, M, chol, coef, n_ch):
+        """absorber_mask::operator() restated: c <- S^-1 (M c) per channel."""
+        c = np.ascontiguousarray(coef, dtype=complex).copy()
+        M = np.ascontiguousarray(M, dtype=float)
+        self.lib.oracle_mask(M.shape[0], M.shape[1] - 1, ctypes.c_long(n_ch), _p(M), _p(np.ascontiguousarray(chol, dtype=float)), _p(c))
+        return c
+
     def run(self, g, coef, eztab, nt=None, threads=1):
         """Returns (coef, crit[inst, s], msub[inst, s])."""
         c = np.ascontiguousarray(coef, dtype=complex).copy()

@@ -2,8 +2,8 @@
 propagator (QPC-TDSE headers compiled by oracle/ref/Makefile into oracle/_ref/).
 
 Run on the development machine, where the reference checkout exists:
-    python tests/golden/make_golden.py [/path/to/reference/include] [--arnoldi] [--vgwr]
-(--arnoldi / --vgwr regenerate only those fixtures.)
+    python tests/golden/make_golden.py [/path/to/reference/include] [--arnoldi] [--vgwr] [--mask]
+(--arnoldi / --vgwr / --mask regenerate only those fixtures.)
 The fixtures are committed; the tests only read them.
 
 Cases (hydrogen unless stated; r in [0, rmax], uniform knots, m = 0):
@@ -29,6 +29,8 @@ Cases (hydrogen unless stated; r in [0, rmax], uniform knots, m = 0):
                     through 10 field-free steps of dt = 0.1 (Krylov breakdown, "bd")
   arnoldi_mid.npz   the same propagator on the mid grid from the mid_pulse final state:
                     1 and 2 steps of dt = 0.1 at ez = 0.03, kmax = 12
+  small_mask.npz    absorber_mask (absorber.hpp:40-63) on the small grid, [20, 30] with index 1/6,
+                    applied once to a seeded random state: the mask band and the result
   vgwr_ep.npz       the velocity-gauge elliptical propagator propagator_cn_hc_vgwr
   vgwr_ep6.npz      (cn_1e.hpp:812-951) on two multi-m grids: N_r=40, p=5, n_l=4, m=-2..2
                     (odd n_m: zero-eigenvalue channels) and N_r=48, p=6, n_l=5, m=-3..2,
@@ -113,6 +115,16 @@ def arnoldi(d):
     np.savez(os.path.join(HERE, "arnoldi_mid.npz"), **out)
 
 
+def mask(d):
+    NR, P, NL, RMAX = 64, 6, 6, 30.0
+    rng = np.random.default_rng(8)
+    c0 = rng.standard_normal(NL * NR) + 1j * rng.standard_normal(NL * NR)
+    c0.tofile(os.path.join(d, "minit.bin"))
+    run("ref_small", "mask", d, RMAX, 0.05, 1, 0, 0, os.path.join(d, "minit.bin"), 20.0, 30.0, 1.0 / 6.0)
+    np.savez(os.path.join(HERE, "small_mask.npz"), rmin=20.0, rmax_mask=30.0, index=1.0 / 6.0, init=c0.reshape(NL, NR),
+             band=load(d, "maskband", (NR, P + 1)), coef=load(d, "coef", (NL, NR), True))
+
+
 def vgwr(d):
     """Velocity-gauge elliptical fixtures (see the module docstring)."""
     for binary, tag, NR, P, NL, NM, M0 in (("ref_ep", "vgwr_ep", 40, 5, 4, 5, -2), ("ref_ep6", "vgwr_ep6", 48, 6, 5, 6, -3)):
@@ -138,12 +150,14 @@ def vgwr(d):
 def main():
     ref_include = sys.argv[1] if len(sys.argv) > 1 and not sys.argv[1].startswith("--") else "/root/reference/include"
     build(ref_include)
-    if "--arnoldi" in sys.argv or "--vgwr" in sys.argv:
+    if "--arnoldi" in sys.argv or "--vgwr" in sys.argv or "--mask" in sys.argv:
         with tempfile.TemporaryDirectory() as d:
             if "--arnoldi" in sys.argv:
                 arnoldi(d)
             if "--vgwr" in sys.argv:
                 vgwr(d)
+            if "--mask" in sys.argv:
+                mask(d)
         return
     meta = {}
     with tempfile.TemporaryDirectory() as d:
@@ -204,6 +218,7 @@ def main():
                  proj_nnz=load(d, "proj_nnz").astype(np.int64), proj_energy=load(d, "proj_energy"))
         arnoldi(d)
         vgwr(d)
+        mask(d)
     with open(os.path.join(HERE, "make_golden.log.json"), "w") as fh:
         json.dump(meta, fh, indent=1)
 
