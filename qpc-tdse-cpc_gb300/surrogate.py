@@ -13,11 +13,13 @@ No counterpart in the reference.  Pieces:
                      state through each pulse, recording <z>(t) in the loop, then projects
                      on the field-free eigenstates.  Labels:
                        PES  256 bins on [0, 3.17 U_p): sum |<E_n|psi>|^2 g(E - E_n) with a
-                            Gaussian g of width 3.17 U_p / 128 (the box's discrete
-                            continuum broadened), times U_p, as log10(max(., 1e-10));
+                            Gaussian g of width max(3.17 U_p / 32, 0.003 a.u.) (the box's
+                            discrete continuum broadened beyond its level spacing), times
+                            U_p, log10, floored 6 decades below the spectrum's maximum;
                        HHG  harmonic orders 1..128: mean of S(w) (plot_hhs.m restated,
                             sin^2 window over the pulse) over w / w0 in [q - 1/2, q + 1/2),
-                            as log10(max(., 1e-30)).
+                            log10, floored 8 decades below the maximum (a detector's
+                            dynamic range; below it the spectrum is window leakage).
   * Surrogate        a 5-member ensemble of 6 -> 4 x 256 GELU -> 384 MLPs trained on the GPU
                      (qpc_mlp: bfloat16 operands, fp32 accumulation, Adam) on standardised
                      targets; query() answers from the ensemble mean when the members agree
@@ -32,6 +34,7 @@ import numpy as np
 
 C2_GRID = dict(n_r=800, p=6, n_l=41, rmax=400.0, dt=0.05)
 N_PES, N_HHG = 256, 128
+PES_DECADES, HHG_DECADES = 6.0, 8.0
 
 
 def _q():
@@ -77,16 +80,17 @@ class _Setup:
 
 
 def _pes_label(proj, energy, u):
-    """Gaussian-broadened PES on [0, 3.17 U_p), 256 bins, in units of 1/U_p, log10."""
+    """Gaussian-broadened PES on [0, 3.17 U_p), 256 bins, in units of 1/U_p, log10, floored."""
     emax = 3.17 * u
     edges = np.linspace(0.0, emax, N_PES + 1)
     centres = 0.5 * (edges[1:] + edges[:-1])
     w = np.abs(proj) ** 2
-    keep = (energy > -0.5 * emax) & (energy < 1.5 * emax)
-    sig = emax / 128.0
+    sig = max(emax / 32.0, 0.003)
+    keep = (energy > -6 * sig) & (energy < emax + 6 * sig)
     d = (centres[:, None] - energy[keep][None, :]) / sig
     dens = (np.exp(-0.5 * d * d) / (sig * np.sqrt(2 * np.pi))) @ w[keep]
-    return np.log10(np.maximum(dens * u, 1e-10))
+    y = np.log10(np.maximum(dens * u, 1e-300))
+    return np.maximum(y, y.max() - PES_DECADES)
 
 
 def _hhg_label(z, dt, w0):
@@ -94,12 +98,13 @@ def _hhg_label(z, dt, w0):
     n = z.size
     om, s = q.hhg_spectrum(z, dt, 0.0, 0.0, dt * (n - 1))
     h = om / w0
-    out = np.full(N_HHG, 1e-30)
+    out = np.full(N_HHG, 1e-300)
     for k in range(N_HHG):
         sel = (h >= k + 0.5) & (h < k + 1.5)
         if sel.any():
-            out[k] = max(float(s[sel].mean()), 1e-30)
-    return np.log10(out)
+            out[k] = max(float(s[sel].mean()), 1e-300)
+    y = np.log10(out)
+    return np.maximum(y, y.max() - HHG_DECADES)
 
 
 def tdse_spectra(p, grid=C2_GRID, batch=256, setup=None, log=None):
