@@ -68,10 +68,10 @@ __global__ void __launch_bounds__(VG_THREADS) k_vg_cn(double2* __restrict__ stat
 	constexpr int NE = P + 1;
 	// window: U rows of the previous P rows (row i-1-q at slot q), entries c = 0..P for column row+c
 	double2 Uw[P][NE];
-	double2 yw[P];
+	double2 yw[P], zw[P];	// y and the input z of the previous P rows (z is overwritten by y)
 #pragma unroll
 	for (int q = 0; q < P; ++q) {
-		yw[q] = make_double2(0.0, 0.0);
+		yw[q] = zw[q] = make_double2(0.0, 0.0);
 #pragma unroll
 		for (int c = 0; c < NE; ++c) Uw[q][c] = make_double2(0.0, 0.0);
 	}
@@ -89,7 +89,7 @@ __global__ void __launch_bounds__(VG_THREADS) k_vg_cn(double2* __restrict__ stat
 				double2 fo = make_double2(ifet.x * ol, ifet.y * ol);
 				lo[q] = make_double2(s + fo.x, fo.y);
 				double2 am = make_double2(s - fo.x, -fo.y);
-				double2 pr = cmul(am, z[i - j]);
+				double2 pr = cmul(am, zw[q]);
 				rhs.x += pr.x; rhs.y += pr.y;
 			}
 		}
@@ -128,13 +128,16 @@ __global__ void __launch_bounds__(VG_THREADS) k_vg_cn(double2* __restrict__ stat
 #pragma unroll
 		for (int q = 0; q < P; ++q) y = csub(y, cmul(lq[q], yw[q]));
 		// shift the windows, store U row i and y_i
+		const double2 zi = z[i];
 #pragma unroll
 		for (int q = P - 1; q > 0; --q) {
 			yw[q] = yw[q - 1];
+			zw[q] = zw[q - 1];
 #pragma unroll
 			for (int c = 0; c < NE; ++c) Uw[q][c] = Uw[q - 1][c];
 		}
 		yw[0] = y;
+		zw[0] = zi;
 #pragma unroll
 		for (int c = 0; c < NE; ++c) {
 			Uw[0][c] = up[c];
