@@ -386,6 +386,92 @@ __global__ void __launch_bounds__(CH_THREADS) k_ar_sinv(ar_args g, double2* __re
 	sinv_sweep<P, false>(g, v, stride, act, Lt);
 }
 
+// The same solve with P lanes per real recurrence, column-oriented (for batches too small
+// to occupy the GPU one lane per recurrence): lane j of a recurrence holds the pending sum
+// of one of the next P rows; when row r is complete its owner's sum is broadcast, every lane
+// computes x_r, and each lane adds L(row_j, r) x_r to its own row's sum.  Three FP64
+// instructions per row instead of P + 1, on P times as many warps.
+template <int P>
+__global__ void __launch_bounds__(128) k_ar_sinv_sys(ar_args g, double2* __restrict__ vbuf)
+{
+	const int b = g.b0 + blockIdx.y;
+	if (g.flag[b] != AR_LIVE) return;
+	constexpr int CPW = 32 / P;
+	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+	const int cs = lane / P, j = lane - cs * P;
+	const int c = (blockIdx.x * (int)(blockDim.x >> 5) + warp) * CPW + cs;
+	const bool act = cs < CPW && c < 2 * g.nch;
+	const int base = (cs < CPW ? cs : 0) * P;
+	const long stride = 2L * g.nch;
+	const int N = g.N;
+	double* v = reinterpret_cast<double*>(vbuf + (long)b * g.n) + (act ? c : 0);
+	const double* __restrict__ Lcol = g.Lcol;
+	const double* __restrict__ Lrow = g.Lrow;
+	const double* __restrict__ dinv = g.dinv;
+	// forward: rows r ascending, owner o = r mod P
+	{
+		double acc = 0.0, cur[SV_D], nxt[SV_D];
+		const int ntile = (N + SV_D - 1) / SV_D;
+#pragma unroll
+		for (int q = 0; q < SV_D; ++q) cur[q] = (act && q < N) ? v[(long)q * stride] : 0.0;
+		int o = 0;
+		for (int t = 0; t < ntile; ++t) {
+#pragma unroll
+			for (int q = 0; q < SV_D; ++q) {
+				int r = (t + 1) * SV_D + q;
+				nxt[q] = (act && r < N) ? v[(long)r * stride] : 0.0;
+			}
+#pragma unroll
+			for (int q = 0; q < SV_D; ++q) {
+				const int r = t * SV_D + q;
+				if (r < N) {
+					double ao = __shfl_sync(0xffffffffu, acc, base + o);
+					double x = (cur[q] - ao) * dinv[r];
+					if (j == o) acc = 0.0;
+					int k = (j - o - 1 + P) % P + 1;
+					acc = fma(Lcol[(long)r * P + k - 1], x, acc);
+					if (act && j == o) v[(long)r * stride] = x;
+					o = (o + 1 == P) ? 0 : o + 1;
+				}
+			}
+#pragma unroll
+			for (int q = 0; q < SV_D; ++q) cur[q] = nxt[q];
+		}
+	}
+	__syncwarp();
+	// backward: rows s = N-1-i descending, owner o = i mod P
+	{
+		double acc = 0.0, cur[SV_D], nxt[SV_D];
+		const int ntile = (N + SV_D - 1) / SV_D;
+#pragma unroll
+		for (int q = 0; q < SV_D; ++q) cur[q] = (act && q < N) ? v[(long)(N - 1 - q) * stride] : 0.0;
+		int o = 0;
+		for (int t = 0; t < ntile; ++t) {
+#pragma unroll
+			for (int q = 0; q < SV_D; ++q) {
+				int i = (t + 1) * SV_D + q;
+				nxt[q] = (act && i < N) ? v[(long)(N - 1 - i) * stride] : 0.0;
+			}
+#pragma unroll
+			for (int q = 0; q < SV_D; ++q) {
+				const int i = t * SV_D + q;
+				if (i < N) {
+					const int sr = N - 1 - i;
+					double ao = __shfl_sync(0xffffffffu, acc, base + o);
+					double x = (cur[q] - ao) * dinv[sr];
+					if (j == o) acc = 0.0;
+					int k = (j - o - 1 + P) % P + 1;
+					acc = fma(Lrow[(long)sr * P + k - 1], x, acc);
+					if (act && j == o) v[(long)sr * stride] = x;
+					o = (o + 1 == P) ? 0 : o + 1;
+				}
+			}
+#pragma unroll
+			for (int q = 0; q < SV_D; ++q) cur[q] = nxt[q];
+		}
+	}
+}
+
 // ---------------------------------------------------------------- Gram-Schmidt
 // v -= u_i x_i for i <= k with i == k or |x_i|^2 > 4e-27, i ascending (la_1e.hpp:212-219)
 __global__ void __launch_bounds__(AR_THREADS) k_ar_orth(ar_args g, double2* __restrict__ vbuf, int k)
@@ -588,6 +674,23 @@ ar_args make_args(qpc_arnoldi* h)
 
 void launch_sinv(const ar_args& g, int Bg, double2* v, cudaStream_t st)
 {
+	// one lane per recurrence when that fills the GPU, else P lanes per recurrence
+	const long chains = 2L * g.nch * Bg;
+	const char* e = getenv("QPC_AR_SINV");
+	const bool sys = e ? atoi(e) == 2 : chains < 32L * 304;
+	if (sys && g.P >= 2) {
+		const int cpw = 32 / g.P;
+		dim3 gs((unsigned)((2 * g.nch + 4 * cpw - 1) / (4 * cpw)), Bg);
+		switch (g.P) {
+		case 2: k_ar_sinv_sys<2><<<gs, 128, 0, st>>>(g, v); return;
+		case 3: k_ar_sinv_sys<3><<<gs, 128, 0, st>>>(g, v); return;
+		case 4: k_ar_sinv_sys<4><<<gs, 128, 0, st>>>(g, v); return;
+		case 5: k_ar_sinv_sys<5><<<gs, 128, 0, st>>>(g, v); return;
+		case 6: k_ar_sinv_sys<6><<<gs, 128, 0, st>>>(g, v); return;
+		case 7: k_ar_sinv_sys<7><<<gs, 128, 0, st>>>(g, v); return;
+		default: k_ar_sinv_sys<8><<<gs, 128, 0, st>>>(g, v); return;
+		}
+	}
 	dim3 grid((2 * g.nch + CH_THREADS - 1) / CH_THREADS, Bg);
 	switch (g.P) {
 	case 1: k_ar_sinv<1><<<grid, CH_THREADS, 0, st>>>(g, v); break;

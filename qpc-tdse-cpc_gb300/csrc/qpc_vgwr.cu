@@ -460,6 +460,9 @@ int device_angular(qpc_vgwr* h, std::vector<double> lam[4], double2* dP[4])
 			if (cusolverDnDsyevd(sol, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, nb, A[par], nb, W[par], work, lwork, d_info) != CUSOLVER_STATUS_SUCCESS) {
 				set_error("syevd failed"); return QPC_ERR_CUDA;
 			}
+			// syevd runs on the handle's stream, which does not synchronise with the legacy
+			// stream the copies below use
+			QPC_CUDA(cudaStreamSynchronize(h->st));
 			int info = 0;
 			QPC_CUDA(cudaMemcpy(&info, d_info, sizeof(int), cudaMemcpyDeviceToHost));
 			if (info) { set_error("syevd info %d", info); return QPC_ERR_NUMERIC; }
