@@ -26,6 +26,9 @@ window sits).  Metric: wavefunction-steps/s.
 --impl reference times the reference's CPU implementation of the path (the
 oracle port: the reference itself needs x86 and MKL) on all host cores.
 
+--workload c0 times the reference's own CPU case (one hydrogen atom, N_r = 400, l_max = 20, the whole
+4-cycle 800 nm pulse) on the GPU, with the CPU oracle beside it.
+--workload c3 runs 64 wavefunctions on mixed grids (one handle each, qpc_lgwz_run_many) for a window.
 --workload c3a times the Arnoldi propagator (k_max = 12, dt = 0.1) on --batch wavefunctions
 with their own screened potentials on the N_r = 800, n_l = 41 grid.
 --workload c1 measures the single large velocity-gauge elliptical instance over a
@@ -368,6 +371,86 @@ def run_c3a(args):
     }
 
 
+def run_c0(args):
+    """The single hydrogen atom of the reference's CPU case: N_r = 400 on [0, 200], p = 6, l_max = 20,
+    800 nm, 1e14 W/cm^2, sin^2 4 cycles, dt = 0.05 (8826 steps), one wavefunction, the whole pulse."""
+    import importlib
+    q = importlib.import_module("qpc-tdse-cpc_gb300")
+    n_r, p, n_l, dt = 400, 6, 21, 0.05
+    S, R, H, c0 = setup_grid(q, n_r, p, n_l, 200.0)
+    f = q.field_sinen(q.intensity_to_e0(1e14), q.wavelength_to_w0(800.0), 4.0, 0.0, 0.0, dt)
+    nt = f.size - 1
+    prop = q.propagator_cn_hc_lgwz().initialize(n_r, p, n_l, S, R, H, dt)
+    prop.put(c0[None])
+    prop.run(f[None, :11], [10])                  # warm-up (autotuner)
+    prop.put(c0[None])
+    with Clocks() as clk:
+        l0 = prop.launch_count()
+        t0 = time.perf_counter()
+        prop.put(c0[None])
+        prop.run(f[None, :], [nt])
+        out = prop.get()
+        e2e_s = time.perf_counter() - t0
+        dev_ms = prop.last_run_ms()
+        launches = prop.launch_count() - l0
+    norm = prop.norm()[0]
+    cpu = cpu_baseline(q, S, R, H, c0, f[None, :], dt, n_l, budget_s=args.cpu_seconds) if not args.no_cpu else None
+    return {
+        "metric": "wavefunction-steps/s (one hydrogen atom, whole 4-cycle pulse)",
+        "value": nt / (dev_ms * 1e-3), "unit": "wf-steps/s", "n_gpus": 1, "steps": nt, "warmup": 10,
+        "ms_per_step": dev_ms / nt, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "c128 (complex FP64)", "data": "the reference's C0 case (analytic pulse)",
+        "config": {"workload": "C0: H atom, N_r=400 on [0,200], p=6, l_max=20, 800 nm, 1e14 W/cm^2, 4 cycles, dt=0.05"},
+        "e2e": {"value": nt / e2e_s, "unit": "wf-steps/s", "h2d_bytes_per_step": (c0.nbytes + f.nbytes) / nt,
+                "d2h_bytes_per_step": out.nbytes / nt},
+        "gpu_launches": int(launches), "final_norm": float(norm),
+        "cpu_baseline": cpu, "clocks": clk.summary(),
+    }
+
+
+def run_c3(args):
+    """Mixed grids: 64 wavefunctions with N_r in {400,...,2000}, l_max in {20,40,60,80} and their own
+    screened potential, one length-gauge handle each, run together (qpc_lgwz_run_many) for a window of
+    steps inside their pulses (fields drawn like the batched scan).  The initial state is a normalised
+    Gaussian in the l = 0 channel: the throughput does not depend on it."""
+    import importlib
+    q = importlib.import_module("qpc-tdse-cpc_gb300")
+    rng = np.random.default_rng(2025)
+    n_inst, p, dt = args.batch if args.batch != 256 else 64, 6, 0.05
+    K, W = args.steps, args.warmup
+    props, tabs, work = [], [], 0
+    inten, lam_nm, cep, cyc = c2_workload(n_inst, seed=7)
+    ft, nt = field_tables(q, inten, lam_nm, cep, cyc, dt)
+    for k in range(n_inst):
+        n_r = int(rng.choice([400, 800, 1200, 1600, 2000]))
+        n_l = int(rng.choice([21, 41, 61, 81]))
+        a, b = rng.uniform(0, 17), rng.uniform(1, 3)
+        S, R, _, _, H = q.radial_setup(n_r, p, n_l, q.linear_knots(n_r, p, 0.0, n_r / 2.0), (q.POTENTIAL_YUKAWA, 1.0, a, b))
+        c0 = np.zeros((1, n_l, n_r), complex)
+        r = np.arange(n_r) * 0.5
+        c0[0, 0] = np.exp(-((r - 3.0) / 1.5) ** 2)
+        pr = q.propagator_cn_hc_lgwz().initialize(n_r, p, n_l, S, R, H, dt)
+        pr.put(c0[None])
+        props.append(pr)
+        tabs.append(ft[k][None, :W + K + 1])
+        work += n_r * n_l
+    q.run_many(props, [t[:, :W + 1] for t in tabs], [W] * n_inst)
+    with Clocks() as clk:
+        t0 = time.perf_counter()
+        q.run_many(props, [t[:, W:] for t in tabs], [K] * n_inst)
+        wall = time.perf_counter() - t0
+    return {
+        "metric": "wavefunction-steps/s (mixed grids, one handle per wavefunction, run together)",
+        "value": n_inst * K / wall, "unit": "wf-steps/s", "n_gpus": 1, "steps": K, "warmup": W,
+        "ms_per_step": wall / K * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "c128 (complex FP64)", "data": "synthetic (seeded grids, potentials and fields)",
+        "config": {"workload": "C3 (CN): %d wavefunctions, N_r in {400..2000}, l_max in {20,40,60,80}, "
+                               "V=-(1+a e^-br)/r, dt=0.05" % n_inst, "channel_rows": int(work)},
+        "timing": "host wall clock around qpc_lgwz_run_many (64 concurrent handles)",
+        "clocks": clk.summary(),
+    }
+
+
 def cpu_baseline(q, S, R, H, c0, ftab, dt, n_l, budget_s=15.0, threads=None):
     """The CPU oracle (port of the reference's propagator_cn_hc_lgwz), one
     wavefunction per host thread, on a bounded number of steps of the same workload."""
@@ -425,8 +508,14 @@ def main():
     ap.add_argument("--batch", type=int, default=256)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", default="c2", choices=["c2", "c1", "c3a"])
+    ap.add_argument("--workload", default="c2", choices=["c2", "c0", "c1", "c3", "c3a"])
     args = ap.parse_args()
+    if args.workload == "c0":
+        print(json.dumps(run_c0(args)))
+        return
+    if args.workload == "c3":
+        print(json.dumps(run_c3(args)))
+        return
     if args.workload == "c1":
         print(json.dumps(run_c1(args)))
         return
