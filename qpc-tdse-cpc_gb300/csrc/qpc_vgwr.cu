@@ -12,10 +12,13 @@
 // transforms are merged, P_x2 P_x1^H etc. (cn_1e.hpp:884-889).  F is the field-free CN of
 // every (m,l) channel.
 //
-// GB300 mapping: the transforms are dense GEMMs, N_ch x N_ch times N_ch x N_r per
-// wavefunction (N_ch = n_m n_l up to 7381): they run as cuBLAS DGEMM (real P_x1, P_y2, on
-// the state viewed as 2 N_r reals) and ZGEMM (merged, complex), strided over the live
-// wavefunctions.  The banded CN of each eigen-channel runs one chain per thread: the LU of
+// GB300 mapping: Z couples (m, l) only to (m +- 1, l +- 1), so it keeps il mod 2 and every
+// transform is block-diagonal once the channels are ordered il-even first (the engine's
+// internal order; put/get convert): two dense GEMMs of n_e and n_o = N_ch/2 rows per
+// transform instead of one of N_ch, half the FP64 work.  They run as cuBLAS DGEMM (real
+// P_x1, P_y2, on the state viewed as 2 N_r reals) and ZGEMM (merged, complex), strided
+// over the live wavefunctions.  The angular eigensystems come from cuSOLVER syevd, block by
+// block, on the real symmetric form of each coupling.  The banded CN of each eigen-channel runs one chain per thread: the LU of
 // S + ifet O is formed row by row with the previous p rows of U in registers, the forward
 // substitution fused, U rows kept in a scratch buffer for the backward substitution.
 // The field-free step uses the LDL^T factors of S + i dt/2 H_l (qpc_ldlt_csym) as
@@ -167,14 +170,15 @@ __global__ void __launch_bounds__(VG_THREADS) k_vg_cn(double2* __restrict__ stat
 template <int P>
 __global__ void __launch_bounds__(VG_THREADS) k_vg_ff(double2* __restrict__ state, double2* __restrict__ ybuf, const double* __restrict__ S,
 	const double2* __restrict__ Lrow, const double2* __restrict__ Dinv, const long long* __restrict__ ntt, const int* __restrict__ perm,
-	long step, int N, int nl, int nm, int m0, int nlh, int B)
+	const int* __restrict__ chmap, long step, int N, int nl, int nm, int m0, int nlh, int B)
 {
 	const long t = (long)blockIdx.x * VG_THREADS + threadIdx.x;
 	const int nch = nl * nm;
 	if (t >= (long)B * nch) return;
 	const int k = (int)(t / nch), ch = (int)(t - (long)k * nch);
 	if (step >= ntt[perm[k]]) return;
-	const int im = ch / nl, il = ch - im * nl;
+	const int och = chmap[ch];
+	const int im = och / nl, il = och - im * nl;
 	const int l = il + abs(m0 + im);
 	constexpr int NE = P + 1;
 	double2* c = state + t * N;
@@ -214,21 +218,19 @@ __global__ void __launch_bounds__(VG_THREADS) k_vg_ff(double2* __restrict__ stat
 	}
 }
 
-// P[k][ch] = conj(phi) q_k[ch] from the il-parity blocks' eigenvectors (column-major, as
-// syevd returns them): q_k has block kpar[k], local column kj[k]; channel ch sits in block
-// chpar[ch] at local row chr[ch].  phase: conj(phi_m) = (-i)^(im) when set, else 1.
-__global__ void k_vg_assemble(const double* __restrict__ A0, const double* __restrict__ A1, int nb0, int nb1,
-	const int* __restrict__ kpar, const int* __restrict__ kj, const int* __restrict__ chpar, const int* __restrict__ chr, int N, int nl,
-	bool phase, double2* __restrict__ P)
+// One il-parity block of a transform: P[k][j] = conj(phi(ch_j)) q_k[j] from the block's
+// eigenvectors (column-major, as syevd returns them), ch_j the block's j-th channel;
+// conj(phi_m) = (-i)^(im) when phase is set, else 1.
+__global__ void k_vg_pblock(const double* __restrict__ Q, int nb, const int* __restrict__ chl, int nl, bool phase,
+	double2* __restrict__ P)
 {
 	const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
-	if (t >= (long)N * N) return;
-	const int k = (int)(t / N), ch = (int)(t - (long)k * N);
-	double v = 0.0;
-	if (kpar[k] == chpar[ch]) v = kpar[k] == 0 ? A0[(long)kj[k] * nb0 + chr[ch]] : A1[(long)kj[k] * nb1 + chr[ch]];
+	if (t >= (long)nb * nb) return;
+	const int k = (int)(t / nb), j = (int)(t - (long)k * nb);
+	const double v = Q[(long)k * nb + j];
 	double2 out = make_double2(v, 0.0);
 	if (phase) {
-		switch ((ch / nl) & 3) {
+		switch ((chl[j] / nl) & 3) {
 		case 1: out = make_double2(0.0, -v); break;
 		case 2: out = make_double2(-v, 0.0); break;
 		case 3: out = make_double2(0.0, v); break;
@@ -236,6 +238,20 @@ __global__ void k_vg_assemble(const double* __restrict__ A0, const double* __res
 		}
 	}
 	P[t] = out;
+}
+
+// engine channel order (il-even channels first) <-> the reference's [m][l] order
+__global__ void k_vg_permute(const double2* __restrict__ src, double2* __restrict__ dst, const int* __restrict__ chmap, int N, int nch,
+	long total, bool to_engine)
+{
+	const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= total) return;
+	const long per = (long)nch * N;
+	const long k = i / per, e = i - k * per;
+	const int t = (int)(e / N), r = (int)(e - (long)t * N);
+	const long o = k * per + (long)chmap[t] * N + r;
+	if (to_engine) dst[i] = src[o];
+	else dst[o] = src[i];
 }
 
 __global__ void k_vg_real_part(const double2* __restrict__ P, long n, double* __restrict__ out)
@@ -282,8 +298,14 @@ struct qpc_vgwr {
 	cublasHandle_t cb = nullptr;
 	double *S = nullptr, *Ri = nullptr, *D = nullptr;
 	double *lam[4] = {nullptr, nullptr, nullptr, nullptr};
-	double *Px1 = nullptr, *Py2 = nullptr;        // real [nch][nch]
-	double2 *M12 = nullptr, *M23 = nullptr, *M34 = nullptr;  // complex [nch][nch]
+	// transforms, block-diagonal in the engine's channel order (il-even channels first):
+	// block b (b = 0 even, 1 odd) has nb[b] rows at channel offset off[b] and is stored at
+	// element offset boff[b]
+	int nb[2] = {0, 0}, off[2] = {0, 0};
+	long boff[2] = {0, 0}, bsz = 0;
+	int* chmap = nullptr;                          // engine channel -> reference channel im*n_l+il
+	double *Px1 = nullptr, *Py2 = nullptr;        // real blocks
+	double2 *M12 = nullptr, *M23 = nullptr, *M34 = nullptr;  // complex blocks
 	double2 *Lrow = nullptr, *Dinv = nullptr;     // field-free factors
 	double2 *X = nullptr, *W = nullptr, *U = nullptr;
 	double* atab = nullptr;
@@ -302,7 +324,7 @@ void vg_free(qpc_vgwr* h)
 	if (!h) return;
 	cudaSetDevice(h->dev);
 	void* ps[] = {h->S, h->Ri, h->D, h->lam[0], h->lam[1], h->lam[2], h->lam[3], h->Px1, h->Py2, h->M12, h->M23, h->M34, h->Lrow,
-		h->Dinv, h->X, h->W, h->U, h->atab, h->ntt, h->perm, h->nrm};
+		h->Dinv, h->X, h->W, h->U, h->atab, h->ntt, h->perm, h->nrm, h->chmap};
 	for (void* p : ps) if (p) cudaFree(p);
 	if (h->cb) cublasDestroy(h->cb);
 	if (h->ev0) cudaEventDestroy(h->ev0);
@@ -320,17 +342,24 @@ int transform(qpc_vgwr* h, const void* Pm, bool real, bool herm, const double2* 
 {
 	const int nch = h->nch, N = h->N;
 	const long sstate = (long)nch * N;
-	if (real) {
-		const double one = 1.0, zero = 0.0;
-		// column-major: out^T (2N x nch) = in^T (2N x nch) * op(P^T) ; the row-major P buffer is P^T
-		QPC_CUBLAS(cublasDgemmStridedBatched(h->cb, CUBLAS_OP_N, herm ? CUBLAS_OP_T : CUBLAS_OP_N, 2 * N, nch, nch, &one,
-			(const double*)in, 2 * N, 2 * sstate, (const double*)Pm, nch, 0, &zero, (double*)out, 2 * N, 2 * sstate, nb));
-	} else {
-		const cuDoubleComplex one = make_cuDoubleComplex(1.0, 0.0), zero = make_cuDoubleComplex(0.0, 0.0);
-		QPC_CUBLAS(cublasZgemmStridedBatched(h->cb, CUBLAS_OP_N, herm ? CUBLAS_OP_C : CUBLAS_OP_N, N, nch, nch, &one,
-			(const cuDoubleComplex*)in, N, sstate, (const cuDoubleComplex*)Pm, nch, 0, &zero, (cuDoubleComplex*)out, N, sstate, nb));
+	for (int bl = 0; bl < 2; ++bl) {
+		const int n = h->nb[bl];
+		if (!n) continue;
+		const long o = (long)h->off[bl] * N;
+		if (real) {
+			const double one = 1.0, zero = 0.0;
+			// column-major: out^T (2N x n) = in^T (2N x n) * op(P^T); the row-major block buffer is P^T
+			QPC_CUBLAS(cublasDgemmStridedBatched(h->cb, CUBLAS_OP_N, herm ? CUBLAS_OP_T : CUBLAS_OP_N, 2 * N, n, n, &one,
+				(const double*)(in + o), 2 * N, 2 * sstate, (const double*)Pm + h->boff[bl], n, 0, &zero, (double*)(out + o), 2 * N,
+				2 * sstate, nb));
+		} else {
+			const cuDoubleComplex one = make_cuDoubleComplex(1.0, 0.0), zero = make_cuDoubleComplex(0.0, 0.0);
+			QPC_CUBLAS(cublasZgemmStridedBatched(h->cb, CUBLAS_OP_N, herm ? CUBLAS_OP_C : CUBLAS_OP_N, N, n, n, &one,
+				(const cuDoubleComplex*)(in + o), N, sstate, (const cuDoubleComplex*)Pm + h->boff[bl], n, 0, &zero,
+				(cuDoubleComplex*)(out + o), N, sstate, nb));
+		}
+		++h->launches;
 	}
-	++h->launches;
 	return QPC_OK;
 }
 
@@ -366,7 +395,7 @@ int step_t(qpc_vgwr* h, long s, long ld, int nlive, int nff)
 	if (nff > 0) {
 		const long nth = (long)nff * h->nch;
 		k_vg_ff<P><<<(unsigned)((nth + VG_THREADS - 1) / VG_THREADS), VG_THREADS, 0, h->st>>>(h->X, h->U, h->S, h->Lrow, h->Dinv, h->ntt,
-			h->perm, s, h->N, h->d.n_l, h->d.n_m, h->d.m0, h->nlh, nff);
+			h->perm, h->chmap, s, h->N, h->d.n_l, h->d.n_m, h->d.m0, h->nlh, nff);
 		++h->launches;
 	}
 	if (nb > 0) {
@@ -410,9 +439,12 @@ int permute(qpc_vgwr* h, const std::vector<int>& perm, bool inverse)
 	return QPC_OK;
 }
 
-// Angular eigensystems on the device (cuSOLVER syevd per il-parity block) for channel
-// counts where the host solver is slow.  Z_R(y1) = -Z_R(x1) and Z_R(y2) = -Z_R(x2), so two
-// problems give all four: lam_y = -lam_x with the same real eigenvectors.
+// Angular eigensystems on the device, block by block (cuSOLVER syevd): Z couples (m, l) to
+// (m +- 1, l +- 1) only, so it keeps il mod 2 and every transform is block-diagonal in the
+// engine's channel order.  With D = diag(i^(m - m0)) the -i couplings are real symmetric,
+// Z_R(y1) = -Z_R(x1) and Z_R(y2) = -Z_R(x2): two problems per block give all four couplings
+// (lam_y = -lam_x, same real eigenvectors).  Writes lam[c] in the engine's eigen order (even
+// block's ascending eigenvalues, then the odd block's) and the complex blocks dP[c].
 int device_angular(qpc_vgwr* h, std::vector<double> lam[4], double2* dP[4])
 {
 	const int nl = h->d.n_l, nm = h->d.n_m, N = h->nch;
@@ -420,44 +452,39 @@ int device_angular(qpc_vgwr* h, std::vector<double> lam[4], double2* dP[4])
 	if (cusolverDnCreate(&sol) != CUSOLVER_STATUS_SUCCESS) { set_error("cusolverDnCreate failed"); return QPC_ERR_CUDA; }
 	struct guard { cusolverDnHandle_t s; std::vector<void*> p; ~guard() { for (void* q : p) if (q) cudaFree(q); if (s) cusolverDnDestroy(s); } } G{sol, {}};
 	if (cusolverDnSetStream(sol, h->st) != CUSOLVER_STATUS_SUCCESS) { set_error("cusolverDnSetStream failed"); return QPC_ERR_CUDA; }
-	std::vector<int> chpar(N), chr(N), cnt(2, 0);
-	for (int ch = 0; ch < N; ++ch) { chpar[ch] = (ch % nl) % 2; chr[ch] = cnt[chpar[ch]]++; }
-	int *d_kpar = nullptr, *d_kj = nullptr, *d_chpar = nullptr, *d_chr = nullptr, *d_info = nullptr;
+	std::vector<int> chl[2];
+	for (int ch = 0; ch < N; ++ch) chl[(ch % nl) % 2].push_back(ch);
+	int* d_info = nullptr;
 	int rc;
-	if ((rc = dalloc(&d_kpar, N)) || (rc = dalloc(&d_kj, N)) || (rc = dalloc(&d_chpar, N)) || (rc = dalloc(&d_chr, N)) || (rc = dalloc(&d_info, 1))) return rc;
-	G.p.insert(G.p.end(), {d_kpar, d_kj, d_chpar, d_chr, d_info});
-	QPC_CUDA(cudaMemcpy(d_chpar, chpar.data(), sizeof(int) * N, cudaMemcpyHostToDevice));
-	QPC_CUDA(cudaMemcpy(d_chr, chr.data(), sizeof(int) * N, cudaMemcpyHostToDevice));
+	if ((rc = dalloc(&d_info, 1))) return rc;
+	G.p.push_back(d_info);
+	for (int c = 0; c < 4; ++c) lam[c].assign(N, 0.0);
 	std::vector<double> Zr((size_t)N * N);
-	for (int base = 0; base < 2; ++base) {	// 0: Y11 (x1), 1: Q11 (x2)
+	for (int base = 0; base < 2; ++base) {	// 0: Y11 (x1, y1), 1: Q11 (x2, y2)
 		vgwr_real_coupling(nl, nm, h->d.m0, base, Zr.data());
-		double* A[2] = {nullptr, nullptr};
-		double* W[2] = {nullptr, nullptr};
-		std::vector<double> w[2];
-		for (int par = 0; par < 2; ++par) {
-			const int nb = cnt[par];
+		const int cx = base == 0 ? 0 : 1, cy = base == 0 ? 2 : 3;
+		for (int bl = 0; bl < 2; ++bl) {
+			const int nb = (int)chl[bl].size();
 			if (!nb) continue;
 			std::vector<double> blk((size_t)nb * nb);
-			for (int a = 0, ra = 0; a < N; ++a) {
-				if (chpar[a] != par) continue;
-				for (int b = 0, rb = 0; b < N; ++b) {
-					if (chpar[b] != par) continue;
-					blk[(size_t)ra * nb + rb] = Zr[(size_t)a * N + b];
-					++rb;
-				}
-				++ra;
+			for (int a = 0; a < nb; ++a)
+				for (int b = 0; b < nb; ++b) blk[(size_t)a * nb + b] = Zr[(size_t)chl[bl][a] * N + chl[bl][b]];
+			double *A = nullptr, *W = nullptr, *work = nullptr;
+			int* dch = nullptr;
+			if ((rc = dalloc(&A, (size_t)nb * nb)) || (rc = dalloc(&W, (size_t)nb)) || (rc = dalloc(&dch, (size_t)nb))) {
+				G.p.push_back(A); G.p.push_back(W); G.p.push_back(dch);
+				return rc;
 			}
-			if ((rc = dalloc(&A[par], (size_t)nb * nb)) || (rc = dalloc(&W[par], (size_t)nb))) return rc;
-			G.p.push_back(A[par]); G.p.push_back(W[par]);
-			QPC_CUDA(cudaMemcpy(A[par], blk.data(), sizeof(double) * blk.size(), cudaMemcpyHostToDevice));
+			G.p.push_back(A); G.p.push_back(W); G.p.push_back(dch);
+			QPC_CUDA(cudaMemcpy(A, blk.data(), sizeof(double) * blk.size(), cudaMemcpyHostToDevice));
+			QPC_CUDA(cudaMemcpy(dch, chl[bl].data(), sizeof(int) * nb, cudaMemcpyHostToDevice));
 			int lwork = 0;
-			if (cusolverDnDsyevd_bufferSize(sol, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, nb, A[par], nb, W[par], &lwork) != CUSOLVER_STATUS_SUCCESS) {
+			if (cusolverDnDsyevd_bufferSize(sol, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, nb, A, nb, W, &lwork) != CUSOLVER_STATUS_SUCCESS) {
 				set_error("syevd buffer size failed"); return QPC_ERR_CUDA;
 			}
-			double* work = nullptr;
 			if ((rc = dalloc(&work, (size_t)std::max(lwork, 1)))) return rc;
 			G.p.push_back(work);
-			if (cusolverDnDsyevd(sol, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, nb, A[par], nb, W[par], work, lwork, d_info) != CUSOLVER_STATUS_SUCCESS) {
+			if (cusolverDnDsyevd(sol, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, nb, A, nb, W, work, lwork, d_info) != CUSOLVER_STATUS_SUCCESS) {
 				set_error("syevd failed"); return QPC_ERR_CUDA;
 			}
 			// syevd runs on the handle's stream, which does not synchronise with the legacy
@@ -466,35 +493,18 @@ int device_angular(qpc_vgwr* h, std::vector<double> lam[4], double2* dP[4])
 			int info = 0;
 			QPC_CUDA(cudaMemcpy(&info, d_info, sizeof(int), cudaMemcpyDeviceToHost));
 			if (info) { set_error("syevd info %d", info); return QPC_ERR_NUMERIC; }
-			w[par].resize(nb);
-			QPC_CUDA(cudaMemcpy(w[par].data(), W[par], sizeof(double) * nb, cudaMemcpyDeviceToHost));
-		}
-		// global order: ascending eigenvalue
-		std::vector<std::pair<double, std::pair<int, int>>> ev;
-		for (int par = 0; par < 2; ++par)
-			for (int j = 0; j < cnt[par]; ++j) ev.push_back({w[par][j], {par, j}});
-		std::stable_sort(ev.begin(), ev.end(), [](const auto& x, const auto& y) { return x.first < y.first; });
-		std::vector<int> kpar(N), kj(N);
-		const int cx = base == 0 ? 0 : 1, cy = base == 0 ? 2 : 3;	// x1/y1 from Y11, x2/y2 from Q11
-		lam[cx].resize(N); lam[cy].resize(N);
-		for (int k = 0; k < N; ++k) {
-			kpar[k] = ev[k].second.first; kj[k] = ev[k].second.second;
-			lam[cx][k] = ev[k].first;
-			lam[cy][k] = -ev[k].first;
-		}
-		QPC_CUDA(cudaMemcpy(d_kpar, kpar.data(), sizeof(int) * N, cudaMemcpyHostToDevice));
-		QPC_CUDA(cudaMemcpy(d_kj, kj.data(), sizeof(int) * N, cudaMemcpyHostToDevice));
-		const long nn = (long)N * N;
-		const unsigned nbk = (unsigned)((nn + 255) / 256);
-		// phases: x1 none, y1 (-i)^im ; x2 (-i)^im, y2 none
-		const bool phx = base == 1, phy = base == 0;
-		k_vg_assemble<<<nbk, 256, 0, h->st>>>(A[0], A[1], cnt[0], cnt[1], d_kpar, d_kj, d_chpar, d_chr, N, nl, phx, dP[cx]);
-		k_vg_assemble<<<nbk, 256, 0, h->st>>>(A[0], A[1], cnt[0], cnt[1], d_kpar, d_kj, d_chpar, d_chr, N, nl, phy, dP[cy]);
-		QPC_CUDA(cudaGetLastError());
-		QPC_CUDA(cudaStreamSynchronize(h->st));
-		for (int par = 0; par < 2; ++par) {
-			if (A[par]) { cudaFree(A[par]); std::replace(G.p.begin(), G.p.end(), (void*)A[par], (void*)nullptr); }
-			if (W[par]) { cudaFree(W[par]); std::replace(G.p.begin(), G.p.end(), (void*)W[par], (void*)nullptr); }
+			std::vector<double> w(nb);
+			QPC_CUDA(cudaMemcpy(w.data(), W, sizeof(double) * nb, cudaMemcpyDeviceToHost));
+			for (int k = 0; k < nb; ++k) {
+				lam[cx][h->off[bl] + k] = w[k];
+				lam[cy][h->off[bl] + k] = -w[k];
+			}
+			// phases: x1 none, y1 (-i)^im; x2 (-i)^im, y2 none
+			const unsigned nbk = (unsigned)(((long)nb * nb + 255) / 256);
+			k_vg_pblock<<<nbk, 256, 0, h->st>>>(A, nb, dch, nl, base == 1, dP[cx] + h->boff[bl]);
+			k_vg_pblock<<<nbk, 256, 0, h->st>>>(A, nb, dch, nl, base == 0, dP[cy] + h->boff[bl]);
+			QPC_CUDA(cudaGetLastError());
+			QPC_CUDA(cudaStreamSynchronize(h->st));
 		}
 	}
 	return QPC_OK;
@@ -538,45 +548,48 @@ int qpc_vgwr_create(const qpc_dims* dims, double dt, const double* S, const doub
 	if (cublasCreate(&h->cb) != CUBLAS_STATUS_SUCCESS) { set_error("cublasCreate failed"); return fail(QPC_ERR_CUDA); }
 	if (cublasSetStream(h->cb, h->st) != CUBLAS_STATUS_SUCCESS) { set_error("cublasSetStream failed"); return fail(QPC_ERR_CUDA); }
 	const size_t nst = (size_t)h->B * nch * N;
+	// engine channel order: il-even channels first, then il-odd
+	std::vector<int> chmap;
+	for (int par = 0; par < 2; ++par) {
+		h->off[par] = (int)chmap.size();
+		for (int ch = 0; ch < nch; ++ch) if ((ch % d.n_l) % 2 == par) chmap.push_back(ch);
+		h->nb[par] = (int)chmap.size() - h->off[par];
+	}
+	h->boff[0] = 0;
+	h->boff[1] = (long)h->nb[0] * h->nb[0];
+	h->bsz = h->boff[1] + (long)h->nb[1] * h->nb[1];
 	int rc;
 	if ((rc = dalloc(&h->S, (size_t)N * NE)) || (rc = dalloc(&h->Ri, (size_t)N * NE)) || (rc = dalloc(&h->D, (size_t)N * NE)) ||
 		(rc = dalloc(&h->lam[0], nch)) || (rc = dalloc(&h->lam[1], nch)) || (rc = dalloc(&h->lam[2], nch)) || (rc = dalloc(&h->lam[3], nch)) ||
-		(rc = dalloc(&h->Px1, (size_t)nch * nch)) || (rc = dalloc(&h->Py2, (size_t)nch * nch)) || (rc = dalloc(&h->M12, (size_t)nch * nch)) ||
-		(rc = dalloc(&h->M23, (size_t)nch * nch)) || (rc = dalloc(&h->M34, (size_t)nch * nch)) ||
+		(rc = dalloc(&h->Px1, (size_t)h->bsz)) || (rc = dalloc(&h->Py2, (size_t)h->bsz)) || (rc = dalloc(&h->M12, (size_t)h->bsz)) ||
+		(rc = dalloc(&h->M23, (size_t)h->bsz)) || (rc = dalloc(&h->M34, (size_t)h->bsz)) || (rc = dalloc(&h->chmap, (size_t)nch)) ||
 		(rc = dalloc(&h->Lrow, (size_t)h->nlh * N * P)) || (rc = dalloc(&h->Dinv, (size_t)h->nlh * N)) ||
 		(rc = dalloc(&h->X, nst)) || (rc = dalloc(&h->W, nst)) || (rc = dalloc(&h->U, nst * NE)) || (rc = dalloc(&h->ntt, (size_t)h->B)) ||
 		(rc = dalloc(&h->perm, (size_t)h->B)) || (rc = dalloc(&h->nrm, (size_t)h->B)))
 		return fail(rc);
-	// angular eigensystems: complex P_c [nch][nch] on the device, from the host solver or,
-	// for many channels (or QPC_VGWR_DEVICE_EIG=1), from cuSOLVER
+	if (cudaMemcpy(h->chmap, chmap.data(), sizeof(int) * nch, cudaMemcpyHostToDevice) != cudaSuccess) { set_error("upload"); return fail(QPC_ERR_CUDA); }
+	// angular eigensystems, block by block on the device; complex blocks P_c
 	std::vector<double> lam[4];
 	double2* dP[4] = {nullptr, nullptr, nullptr, nullptr};
 	struct pguard { double2** p; ~pguard() { for (int c = 0; c < 4; ++c) if (p[c]) cudaFree(p[c]); } } PG{dP};
 	for (int c = 0; c < 4; ++c)
-		if ((rc = dalloc(&dP[c], (size_t)nch * nch))) return fail(rc);
-	const char* ev = getenv("QPC_VGWR_DEVICE_EIG");
-	const bool on_device = ev ? atoi(ev) != 0 : nch > 1024;
-	if (on_device) {
-		if ((rc = device_angular(h, lam, dP))) return fail(rc);
-	} else {
-		std::vector<double> Pm((size_t)2 * nch * nch);
-		for (int c = 0; c < 4; ++c) {
-			lam[c].resize(nch);
-			if ((rc = qpc_vgwr_angular(d.n_l, d.n_m, d.m0, c, lam[c].data(), Pm.data()))) { set_error("angular eigensystem %d failed", c); return fail(rc); }
-			if (cudaMemcpy(dP[c], Pm.data(), sizeof(double2) * nch * nch, cudaMemcpyHostToDevice) != cudaSuccess) { set_error("upload"); return fail(QPC_ERR_CUDA); }
-		}
-	}
-	// merged transforms P_b P_a^H: row-major C = L R^H; column-major C^T = conj(R) L^T with
-	// A_cm = R^T (buffer R, op C) and B_cm = L^T (buffer L)
+		if ((rc = dalloc(&dP[c], (size_t)h->bsz))) return fail(rc);
+	if ((rc = device_angular(h, lam, dP))) return fail(rc);
+	// merged transforms P_b P_a^H per block: row-major C = L R^H; column-major C^T = conj(R) L^T
+	// with A_cm = R^T (buffer R, op C) and B_cm = L^T (buffer L)
 	auto merge = [&](const double2* Ld, const double2* Rd, double2* out) -> int {
 		const cuDoubleComplex one = make_cuDoubleComplex(1.0, 0.0), zero = make_cuDoubleComplex(0.0, 0.0);
-		QPC_CUBLAS(cublasZgemm(h->cb, CUBLAS_OP_C, CUBLAS_OP_N, nch, nch, nch, &one, (const cuDoubleComplex*)Rd, nch,
-			(const cuDoubleComplex*)Ld, nch, &zero, (cuDoubleComplex*)out, nch));
+		for (int bl = 0; bl < 2; ++bl) {
+			const int n = h->nb[bl];
+			if (!n) continue;
+			QPC_CUBLAS(cublasZgemm(h->cb, CUBLAS_OP_C, CUBLAS_OP_N, n, n, n, &one, (const cuDoubleComplex*)(Rd + h->boff[bl]), n,
+				(const cuDoubleComplex*)(Ld + h->boff[bl]), n, &zero, (cuDoubleComplex*)(out + h->boff[bl]), n));
+		}
 		return QPC_OK;
 	};
 	if ((rc = merge(dP[1], dP[0], h->M12)) || (rc = merge(dP[2], dP[1], h->M23)) || (rc = merge(dP[3], dP[2], h->M34))) return fail(rc);
 	{
-		const long nn = (long)nch * nch;
+		const long nn = h->bsz;
 		k_vg_real_part<<<(unsigned)((nn + 255) / 256), 256, 0, h->st>>>(dP[0], nn, h->Px1);
 		k_vg_real_part<<<(unsigned)((nn + 255) / 256), 256, 0, h->st>>>(dP[3], nn, h->Py2);
 		if (cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(h->st) != cudaSuccess) { set_error("transform setup failed"); return fail(QPC_ERR_CUDA); }
@@ -606,9 +619,17 @@ static int vg_copy(qpc_vgwr* h, const double* src, double* dst, cudaMemcpyKind k
 {
 	if (!h || (!src && !dst)) { set_error("NULL argument"); return QPC_ERR_ARGS; }
 	cudaSetDevice(h->dev);
-	const size_t bytes = sizeof(double2) * (size_t)h->B * h->nch * h->N;
-	if (src) QPC_CUDA(cudaMemcpyAsync(h->X, src, bytes, kind, h->st));
-	else QPC_CUDA(cudaMemcpyAsync(dst, h->X, bytes, kind, h->st));
+	const long total = (long)h->B * h->nch * h->N;
+	const size_t bytes = sizeof(double2) * (size_t)total;
+	const unsigned nb = (unsigned)((total + 255) / 256);
+	if (src) {
+		QPC_CUDA(cudaMemcpyAsync(h->W, src, bytes, kind, h->st));
+		k_vg_permute<<<nb, 256, 0, h->st>>>(h->W, h->X, h->chmap, h->N, h->nch, total, true);
+	} else {
+		k_vg_permute<<<nb, 256, 0, h->st>>>(h->X, h->W, h->chmap, h->N, h->nch, total, false);
+		QPC_CUDA(cudaMemcpyAsync(dst, h->W, bytes, kind, h->st));
+	}
+	QPC_CUDA(cudaGetLastError());
 	return wait_on(h->st);
 }
 

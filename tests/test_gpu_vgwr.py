@@ -28,19 +28,6 @@ def test_golden_run(q, tag):
 
 
 @pytest.mark.parametrize("tag", CASES)
-def test_golden_run_device_eigensolver(q, tag, monkeypatch):
-    """The same run with the couplings' eigensystems from cuSOLVER (the path taken for
-    more than 1024 channels)."""
-    monkeypatch.setenv("QPC_VGWR_DEVICE_EIG", "1")
-    g = golden(tag)
-    pr = make(q, g)
-    pr.put(g["init"][None])
-    nt, nf = int(g["nt"]), int(g["nfree"])
-    pr.run(g["atab"][None], [nt], [nt + nf])
-    assert rel_l2(pr.get()[0], g["coef"]) < 1e-12
-
-
-@pytest.mark.parametrize("tag", CASES)
 def test_stepwise_equals_run(q, tag):
     g = golden(tag)
     pr = make(q, g)
