@@ -154,7 +154,10 @@ class Surrogate:
         self.n_members, self.n_hidden, self.n_layers, self.seed = n_members, n_hidden, n_layers, seed
         self.net = None
 
-    def fit(self, p, pes, hhg, epochs=400, batch=256, lr=1e-3):
+    def fit(self, p, pes, hhg, epochs=400, batch=256, lr=1e-3, stages=1):
+        """Adam on standardised targets; with stages > 1 the epochs are split into stages whose
+        learning rate falls by 3x each (the optimiser state carries over).  Returns the loss
+        history [epochs][members]."""
         q = _q()
         X = features(p)
         Y = np.concatenate([pes, hhg], axis=1).astype(np.float64)
@@ -162,7 +165,12 @@ class Surrogate:
         self.sd = np.maximum(Y.std(axis=0), 1e-3)
         Yn = ((Y - self.mu) / self.sd).astype(np.float32)
         self.net = q.mlp_ensemble(X.shape[1], Y.shape[1], self.n_hidden, self.n_layers, self.n_members, self.seed)
-        return self.net.train(X, Yn, epochs, batch, lr, seed=self.seed + 1)
+        hist = []
+        per = max(1, epochs // stages)
+        for st in range(stages):
+            ep = per if st < stages - 1 else epochs - per * (stages - 1)
+            hist.append(self.net.train(X, Yn, ep, batch, lr / 3.0 ** st, seed=self.seed + 1 + st))
+        return np.concatenate(hist, axis=0)
 
     def predict(self, p):
         """(mean [n][384], disagreement [n]) in label units; disagreement is the mean over

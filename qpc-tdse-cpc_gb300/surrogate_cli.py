@@ -48,7 +48,7 @@ def fit(a):
     te = {k: v[ntr:] for k, v in p.items()}
     s = sg.Surrogate(seed=a.seed)
     t0 = time.time()
-    hist = s.fit(tr, pes[:ntr], hhg[:ntr], epochs=a.epochs, batch=a.batch, lr=a.lr)
+    hist = s.fit(tr, pes[:ntr], hhg[:ntr], epochs=a.epochs, batch=a.batch, lr=a.lr, stages=a.stages)
     train_s = time.time() - t0
     # threshold from the training rows' disagreement
     thr = s.calibrate(tr, None, a.quantile)
@@ -69,7 +69,7 @@ def fit(a):
     qps = 65536 / (time.time() - t0)
     rep = {
         "files": [os.path.basename(f) for f in files], "n_train": int(ntr), "n_holdout": int(a.holdout),
-        "epochs": a.epochs, "batch": a.batch, "lr": a.lr, "train_s": train_s,
+        "epochs": a.epochs, "batch": a.batch, "lr": a.lr, "lr_stages": a.stages, "train_s": train_s,
         "final_train_loss": [float(x) for x in hist[-1]],
         "holdout_rel_l2_mean": float(e_all.mean()), "holdout_rel_l2_median": float(np.median(e_all)),
         "holdout_rel_l2_pes_mean": float(e_pes.mean()), "holdout_rel_l2_hhg_mean": float(e_hhg.mean()),
@@ -100,6 +100,7 @@ def main():
     f.add_argument("--epochs", type=int, default=400)
     f.add_argument("--batch", type=int, default=256)
     f.add_argument("--lr", type=float, default=1e-3)
+    f.add_argument("--stages", type=int, default=3)
     f.add_argument("--quantile", type=float, default=0.9)
     f.add_argument("--seed", type=int, default=0)
     f.add_argument("--out", default=None)
