@@ -3,6 +3,7 @@ engine, GPU training of the ensemble, and the trust gate that routes queries to 
 TDSE fallback (fallback answers equal the TDSE labels; ellipticity != 0 is refused
 by the z-linear engine)."""
 import importlib
+import time
 
 import numpy as np
 import pytest
@@ -27,7 +28,9 @@ def small_params(sg, n, seed):
 def test_surrogate_pipeline(sg):
     p = small_params(sg, 48, 1)
     setup = sg._Setup(GRID, emax=max(3.17 * float(sg.up(p).max()) * 1.5, 1.0))
+    t0 = time.perf_counter()
     pes, hhg, info = sg.tdse_spectra(p, grid=GRID, batch=24, setup=setup)
+    tdse_s = time.perf_counter() - t0
     assert pes.shape == (48, sg.N_PES) and hhg.shape == (48, sg.N_HHG)
     assert np.all(np.isfinite(pes)) and np.all(np.isfinite(hhg))
     assert info["wf_steps"] > 0
@@ -39,6 +42,11 @@ def test_surrogate_pipeline(sg):
     assert np.all(hist[-1] < hist[0])
     mean, dis = s.predict(p)
     assert mean.shape == (48, sg.N_PES + sg.N_HHG) and np.all(dis >= 0)
+    # what the network gains: the same 48 answers in a small fraction of the TDSE time
+    t0 = time.perf_counter()
+    s.predict(p)
+    net_s = time.perf_counter() - t0
+    assert net_s * 20 < tdse_s, (net_s, tdse_s)
     # trust everything: no fallback
     out, fall = s.query({k: v[:6] for k, v in p.items()}, threshold=np.inf, setup=setup)
     assert not fall.any()
