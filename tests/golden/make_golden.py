@@ -2,8 +2,8 @@
 propagator (QPC-TDSE headers compiled by oracle/ref/Makefile into oracle/_ref/).
 
 Run on the development machine, where the reference checkout exists:
-    python tests/golden/make_golden.py [/path/to/reference/include] [--arnoldi] [--vgwr] [--mask]
-(--arnoldi / --vgwr / --mask regenerate only those fixtures.)
+    python tests/golden/make_golden.py [/path/to/reference/include] [--arnoldi] [--vgwr] [--mask] [--multim]
+(those flags regenerate only the named fixtures.)
 The fixtures are committed; the tests only read them.
 
 Cases (hydrogen unless stated; r in [0, rmax], uniform knots, m = 0):
@@ -29,6 +29,10 @@ Cases (hydrogen unless stated; r in [0, rmax], uniform knots, m = 0):
                     through 10 field-free steps of dt = 0.1 (Krylov breakdown, "bd")
   arnoldi_mid.npz   the same propagator on the mid grid from the mid_pulse final state:
                     1 and 2 steps of dt = 0.1 at ez = 0.03, kmax = 12
+  ep_prop.npz       the length-gauge propagator on a multi-m grid (N_r=40, p=5, n_l=4,
+                    m = -2..2, r in [0, 20], dt = 0.05): the reference's S, R, H_l,
+                    a seeded random state through 20 field steps f_i = 0.04 sin(0.2 i + 0.3)
+                    and 2 field-free steps
   small_mask.npz    absorber_mask (absorber.hpp:40-63) on the small grid, [20, 30] with index 1/6,
                     applied once to a seeded random state: the mask band and the result
   vgwr_ep.npz       the velocity-gauge elliptical propagator propagator_cn_hc_vgwr
@@ -115,6 +119,23 @@ def arnoldi(d):
     np.savez(os.path.join(HERE, "arnoldi_mid.npz"), **out)
 
 
+def multi_m(d):
+    NR, P, NL, NM, M0, RMAX, DT = 40, 5, 4, 5, -2, 20.0, 0.05
+    run("ref_ep", "setup", d, RMAX, DT, 1, 0, 0)
+    nlh = abs(M0) + NL
+    rng = np.random.default_rng(12)
+    n = NR * NL * NM
+    c0 = (rng.standard_normal(n) + 1j * rng.standard_normal(n)) * np.exp(-np.tile(np.arange(NR), NL * NM) / 8.0)
+    c0.tofile(os.path.join(d, "einit.bin"))
+    nt, nfree = 20, 2
+    f = 0.04 * np.sin(0.2 * np.arange(nt + 1) + 0.3)
+    f.tofile(os.path.join(d, "efield.bin"))
+    S, R, H = load(d, "S", (NR, P + 1)), load(d, "R", (NR, P + 1)), load(d, "H", (nlh, NR, P + 1))
+    run("ref_ep", "propagate", d, RMAX, DT, 1, 0, 0, os.path.join(d, "einit.bin"), os.path.join(d, "efield.bin"), nt, nfree, 1)
+    np.savez(os.path.join(HERE, "ep_prop.npz"), n_r=NR, p=P, n_l=NL, n_m=NM, m0=M0, dt=DT, S=S, R=R, H=H,
+             init=c0.reshape(NM, NL, NR), f=f, nt=nt, nfree=nfree, coef=load(d, "coef", (NM, NL, NR), True), norm=load(d, "norm"))
+
+
 def mask(d):
     NR, P, NL, RMAX = 64, 6, 6, 30.0
     rng = np.random.default_rng(8)
@@ -150,7 +171,7 @@ def vgwr(d):
 def main():
     ref_include = sys.argv[1] if len(sys.argv) > 1 and not sys.argv[1].startswith("--") else "/root/reference/include"
     build(ref_include)
-    if "--arnoldi" in sys.argv or "--vgwr" in sys.argv or "--mask" in sys.argv:
+    if any(a in sys.argv for a in ("--arnoldi", "--vgwr", "--mask", "--multim")):
         with tempfile.TemporaryDirectory() as d:
             if "--arnoldi" in sys.argv:
                 arnoldi(d)
@@ -158,6 +179,8 @@ def main():
                 vgwr(d)
             if "--mask" in sys.argv:
                 mask(d)
+            if "--multim" in sys.argv:
+                multi_m(d)
         return
     meta = {}
     with tempfile.TemporaryDirectory() as d:
@@ -219,6 +242,7 @@ def main():
         arnoldi(d)
         vgwr(d)
         mask(d)
+        multi_m(d)
     with open(os.path.join(HERE, "make_golden.log.json"), "w") as fh:
         json.dump(meta, fh, indent=1)
 

@@ -306,3 +306,15 @@ def test_masked_driver_loop_matches_oracle(q, oracle, aoracle):
         c = oracle.step(og, c, f[i], f[i + 1])
         c = aoracle.mask(m["band"], chol, c.reshape(-1), n_l).reshape(1, -1)
     assert rel_l2(prop.get().reshape(-1), c[0]) < 1e-12
+
+
+def test_golden_multi_m(q):
+    """Several m (m = -2..2) against the reference's own propagator (tests/golden/ep_prop)."""
+    g = golden("ep_prop")
+    n_r, p, n_l, n_m, m0 = int(g["n_r"]), int(g["p"]), int(g["n_l"]), int(g["n_m"]), int(g["m0"])
+    prop = q.propagator_cn_hc_lgwz().initialize(n_r, p, n_l, g["S"], g["R"], g["H"], float(g["dt"]), n_m=n_m, m0=m0)
+    prop.put(g["init"][None])
+    nt, nf = int(g["nt"]), int(g["nfree"])
+    prop.run(g["f"][None, :], [nt], [nt + nf])
+    assert rel_l2(prop.get()[0], g["coef"]) < 1e-12
+    assert abs(prop.norm()[0] - g["norm"][0]) < 1e-12 * g["norm"][0]

@@ -85,3 +85,13 @@ def test_c0_full_pulse(oracle):
     assert rel_l2(sgn * c, ref) < 1e-10
     # S-norm drift over 8826 steps is rounding only (Crank-Nicolson is S-unitary)
     assert abs(oracle.norm(grid, c)[0] - g["norm"][0]) < 1e-10
+
+
+def test_multi_m_propagation(oracle):
+    """Several m (m = -2..2): per-m Y10 couplings and H_{|m|+il}, against the reference."""
+    g = golden("ep_prop")
+    n_l, n_m, m0 = int(g["n_l"]), int(g["n_m"]), int(g["m0"])
+    og = oracle.grid(g["S"], g["R"], g["H"], float(g["dt"]), n_l, n_m=n_m, m0=m0)
+    nt, nf = int(g["nt"]), int(g["nfree"])
+    c = oracle.run(og, g["init"].reshape(1, -1), g["f"][None, :], [nt], [nt + nf])
+    assert rel_l2(c.reshape(g["coef"].shape), g["coef"]) < 1e-12
