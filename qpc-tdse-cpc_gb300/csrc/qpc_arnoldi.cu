@@ -797,12 +797,12 @@ int qpc_arnoldi_create(const qpc_dims* dims, const double* S, const double* R, c
 					Hr[(((size_t)hs * N + r) * NE + k) * h->nlh + l] = v;
 				}
 	int rc = 0;
-	QPC_CUDA(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
-	QPC_CUDA(cudaEventCreate(&h->ev0));
-	QPC_CUDA(cudaEventCreate(&h->ev1));
-	QPC_CUDA(cudaEventCreateWithFlags(&h->ev2, cudaEventDisableTiming));
+	if ((cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking)) != cudaSuccess) { set_error("cudaStreamCreateWithFlags failed"); return fail(QPC_ERR_CUDA); }
+	if ((cudaEventCreate(&h->ev0)) != cudaSuccess) { set_error("cudaEventCreate failed"); return fail(QPC_ERR_CUDA); }
+	if ((cudaEventCreate(&h->ev1)) != cudaSuccess) { set_error("cudaEventCreate failed"); return fail(QPC_ERR_CUDA); }
+	if ((cudaEventCreateWithFlags(&h->ev2, cudaEventDisableTiming)) != cudaSuccess) { set_error("cudaEventCreateWithFlags failed"); return fail(QPC_ERR_CUDA); }
 	if (B >= 2 && !(getenv("QPC_STREAMS") && atoi(getenv("QPC_STREAMS")) == 1))
-		QPC_CUDA(cudaStreamCreateWithFlags(&h->stream2, cudaStreamNonBlocking));
+		if ((cudaStreamCreateWithFlags(&h->stream2, cudaStreamNonBlocking)) != cudaSuccess) { set_error("cudaStreamCreateWithFlags failed"); return fail(QPC_ERR_CUDA); }
 	const long nst = (long)B * h->n;
 	if ((rc = dalloc(&h->S, (size_t)N * NE)) || (rc = dalloc(&h->R, (size_t)N * NE)) || (rc = dalloc(&h->Lrow, (size_t)N * P)) ||
 		(rc = dalloc(&h->Lcol, (size_t)N * P)) || (rc = dalloc(&h->dinv, (size_t)N)) || (rc = dalloc(&h->H, Hr.size())) ||

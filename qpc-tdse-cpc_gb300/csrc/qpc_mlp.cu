@@ -469,7 +469,7 @@ int qpc_mlp_create(int32_t n_in, int32_t n_hidden, int32_t n_layers, int32_t n_o
 		h->nW += (long)h->Ns[j] * h->Ks[j];
 		h->nb += h->Ns[j];
 	}
-	QPC_CUDA(cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking));
+	if ((cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking)) != cudaSuccess) { set_error("cudaStreamCreateWithFlags failed"); return fail(QPC_ERR_CUDA); }
 	const size_t tw = (size_t)h->E * h->nW, tb = (size_t)h->E * h->nb;
 	int rc;
 	if ((rc = dalloc(&h->W, tw)) || (rc = dalloc(&h->b, tb)) || (rc = dalloc(&h->gW, tw)) || (rc = dalloc(&h->gb, tb)) ||

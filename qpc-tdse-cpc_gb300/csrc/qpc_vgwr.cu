@@ -542,9 +542,9 @@ int qpc_vgwr_create(const qpc_dims* dims, double dt, const double* S, const doub
 		if (bad < 0) { set_error("ldlt arguments"); return fail(QPC_ERR_ARGS); }
 		if (bad > 0) { set_error("zero pivot factorising S + i dt/2 H_%d", l); return fail(QPC_ERR_SINGULAR); }
 	}
-	QPC_CUDA(cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking));
-	QPC_CUDA(cudaEventCreate(&h->ev0));
-	QPC_CUDA(cudaEventCreate(&h->ev1));
+	if ((cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking)) != cudaSuccess) { set_error("cudaStreamCreateWithFlags failed"); return fail(QPC_ERR_CUDA); }
+	if ((cudaEventCreate(&h->ev0)) != cudaSuccess) { set_error("cudaEventCreate failed"); return fail(QPC_ERR_CUDA); }
+	if ((cudaEventCreate(&h->ev1)) != cudaSuccess) { set_error("cudaEventCreate failed"); return fail(QPC_ERR_CUDA); }
 	if (cublasCreate(&h->cb) != CUBLAS_STATUS_SUCCESS) { set_error("cublasCreate failed"); return fail(QPC_ERR_CUDA); }
 	if (cublasSetStream(h->cb, h->st) != CUBLAS_STATUS_SUCCESS) { set_error("cublasSetStream failed"); return fail(QPC_ERR_CUDA); }
 	const size_t nst = (size_t)h->B * nch * N;
