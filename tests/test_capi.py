@@ -60,3 +60,32 @@ def test_field_and_setup_errors(q):
         q.field_sinen(0.05, -1.0, 4, 0, 0, 0.05)
     with pytest.raises(q.QpcError):
         q.radial_setup(8, 6, 1, np.zeros(17))
+
+
+def test_other_engines_check_arguments_and_device(q):
+    """Arnoldi, velocity-gauge and surrogate handles: argument errors before any device use,
+    QPC_ERR_NODEVICE (not a CPU path) without a GPU."""
+    torch = pytest.importorskip("torch")
+    lib = q.load()
+    t = q.linear_knots(32, 6, 0.0, 20.0)
+    S, R, Ri, D, H = q.radial_setup(32, 6, 6, t)
+    y10 = q.y10_coupling(4)
+    h = ctypes.c_void_p()
+    d = q.qpc_dims(32, 6, 4, 1, 0, 1)
+    P = lambda a: a.ctypes.data
+    # emin > emax: rejected as the reference's arnoldi_workspace constructor does
+    assert lib.qpc_arnoldi_create(ctypes.byref(d), P(S), P(R), P(H), 0, P(y10), 0.1, 12, 1e-8, 1e-14, ctypes.byref(h)) == 1
+    assert lib.qpc_arnoldi_create(ctypes.byref(d), P(S), P(R), P(H), 0, P(y10), 0.1, 0, 1e-14, 1e-8, ctypes.byref(h)) == 1
+    assert lib.qpc_vgwr_create(ctypes.byref(d), -0.05, P(S), P(Ri), P(D), P(H), ctypes.byref(h)) == 1
+    assert lib.qpc_mlp_create(6, 250, 4, 384, 5, 0, ctypes.byref(h)) == 1       # n_hidden not a multiple of 16
+    if torch.cuda.is_available():
+        return
+    with pytest.raises(q.QpcError) as e:
+        q.propagator_hc_lgwz(12, 1e-14, 1e-8).initialize(32, 6, 4, S, R, H, y10, 0.1)
+    assert e.value.code == 8
+    with pytest.raises(q.QpcError) as e:
+        q.propagator_cn_hc_vgwr().initialize(32, 6, 2, 3, -1, S, Ri, D, H, 0.05)
+    assert e.value.code == 8
+    with pytest.raises(q.QpcError) as e:
+        q.mlp_ensemble(6, 384)
+    assert e.value.code == 8
