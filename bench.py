@@ -28,7 +28,8 @@ oracle port: the reference itself needs x86 and MKL) on all host cores.
 
 --workload c0 times the reference's own CPU case (one hydrogen atom, N_r = 400, l_max = 20, the whole
 4-cycle 800 nm pulse) on the GPU, with the CPU oracle beside it.
---workload c3 runs 64 wavefunctions on mixed grids (one handle each, qpc_lgwz_run_many) for a window.
+--workload c3 runs 64 wavefunctions on mixed grids (one handle each, qpc_lgwz_run_many) for a window;
+--workload c3arn the same grids with the Arnoldi propagator (one handle and host thread each).
 --workload c3a times the Arnoldi propagator (k_max = 12, dt = 0.1) on --batch wavefunctions
 with their own screened potentials on the N_r = 800, n_l = 41 grid.
 --workload c1 measures the single large velocity-gauge elliptical instance over a
@@ -338,6 +339,56 @@ def arnoldi_flops(n_r, p, n_l, kmax):
     return 2.0 * fma * n_r * n_l
 
 
+def run_c3arn(args):
+    """Arnoldi propagator (k_max = 12, dt = 0.1) on the mixed grids of run_c3: one handle per
+    wavefunction, each driven from its own host thread, all on the GPU together."""
+    import importlib
+    import threading
+    q = importlib.import_module("qpc-tdse-cpc_gb300")
+    rng = np.random.default_rng(2025)
+    n_inst, p, dt = args.batch if args.batch != 256 else 64, 6, 0.1
+    K, W = args.steps, args.warmup
+    props, flops = [], 0.0
+    for k in range(n_inst):
+        n_r = int(rng.choice([400, 800, 1200, 1600, 2000]))
+        n_l = int(rng.choice([21, 41, 61, 81]))
+        a, b = rng.uniform(0, 17), rng.uniform(1, 3)
+        S, R, _, _, H = q.radial_setup(n_r, p, n_l, q.linear_knots(n_r, p, 0.0, n_r / 2.0), (q.POTENTIAL_YUKAWA, 1.0, a, b))
+        c0 = np.zeros((1, n_l, n_r), complex)
+        r = np.arange(n_r) * 0.5
+        c0[0, 0] = np.exp(-((r - 3.0) / 1.5) ** 2)
+        pr = q.propagator_hc_lgwz(12, 1e-14, 1e-8).initialize(n_r, p, n_l, S, R, H, q.y10_coupling(n_l), dt)
+        pr.put(c0[None])
+        props.append(pr)
+        flops += arnoldi_flops(n_r, p, n_l, 12)
+    ez = 0.03 * np.sin(0.057 * dt * np.arange(W + K))
+
+    def go(tab):
+        th = [threading.Thread(target=pr.run, args=(tab[None, :],)) for pr in props]
+        for t in th:
+            t.start()
+        for t in th:
+            t.join()
+    go(ez[:W])
+    with Clocks() as clk:
+        t0 = time.perf_counter()
+        go(ez[W:])
+        wall = time.perf_counter() - t0
+    tfl = flops * K / wall / 1e12
+    return {
+        "metric": "wavefunction-steps/s (Arnoldi, mixed grids, one handle per wavefunction, run together)",
+        "value": n_inst * K / wall, "unit": "wf-steps/s", "n_gpus": 1, "steps": K, "warmup": W,
+        "ms_per_step": wall / K * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "c128 (complex FP64)", "data": "synthetic (seeded grids and potentials)",
+        "config": {"workload": "C3 (Arnoldi): %d wavefunctions, N_r in {400..2000}, l_max in {20,40,60,80}, "
+                               "V=-(1+a e^-br)/r, k_max=12, dt=0.1" % n_inst},
+        "timing": "host wall clock around the concurrent runs",
+        "roofline": {"bound": "fp64", "kernel": "whole Arnoldi step", "achieved": tfl, "peak": FP64_PEAK_TFLOPS, "unit": "TFLOP/s",
+                     "frac": tfl / FP64_PEAK_TFLOPS},
+        "clocks": clk.summary(),
+    }
+
+
 def run_c3a(args):
     """Arnoldi propagator on a batch of wavefunctions with their own screened potentials."""
     import importlib
@@ -510,7 +561,7 @@ def main():
     ap.add_argument("--batch", type=int, default=256)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", default="c2", choices=["c2", "c0", "c1", "c3", "c3a"])
+    ap.add_argument("--workload", default="c2", choices=["c2", "c0", "c1", "c3", "c3a", "c3arn"])
     args = ap.parse_args()
     if args.workload == "c0":
         print(json.dumps(run_c0(args)))
@@ -523,6 +574,9 @@ def main():
         return
     if args.workload == "c3a":
         print(json.dumps(run_c3a(args)))
+        return
+    if args.workload == "c3arn":
+        print(json.dumps(run_c3arn(args)))
         return
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
