@@ -142,6 +142,8 @@ int qpc_lgwz_get(qpc_lgwz* h, double* coef);
 /* Same, with device-resident buffers in the host layout (no host copy). */
 int qpc_lgwz_put_device(qpc_lgwz* h, const double* dev_coef);
 int qpc_lgwz_get_device(qpc_lgwz* h, double* dev_coef);
+/* The grid and batch size the handle was created with. */
+int qpc_lgwz_dims(qpc_lgwz* h, qpc_dims* dims);
 
 /* One call of propagate(coef, ez_ti, ez_tf) (cn_1e.hpp:595-613) for every
  * instance: f_ti[inst], f_tf[inst] are the field at t_i and t_{i+1}. */
@@ -242,6 +244,7 @@ int qpc_vgwr_put(qpc_vgwr* h, const double* coef);
 int qpc_vgwr_get(qpc_vgwr* h, double* coef);
 int qpc_vgwr_put_device(qpc_vgwr* h, const double* dev_coef);
 int qpc_vgwr_get_device(qpc_vgwr* h, double* dev_coef);
+int qpc_vgwr_dims(qpc_vgwr* h, qpc_dims* dims);
 int qpc_vgwr_propagate(qpc_vgwr* h, const double* ax_ti, const double* ax_tf, const double* ay_ti, const double* ay_tf);
 int qpc_vgwr_propagate_free(qpc_vgwr* h);
 int qpc_vgwr_run(qpc_vgwr* h, const double* atab, int64_t ld, const int64_t* nt_field, const int64_t* nt_total);
@@ -338,6 +341,85 @@ int qpc_mlp_predict(qpc_mlp* h, const float* X, int32_t n, float* out);
  * it later reads. */
 #define QPC_NOALLOC_MAX_ELEMS (1L << 20)
 int qpc_fieldfree_noalloc(const qpc_dims* dims, const double* S, const double* ffac, double* coef, void* stream);
+
+/* ---------------------------------------------------------------- momentum spectra
+ * Photoelectron momentum distributions of spherical/spectrum/momentum_1e.hpp: the
+ * projection of the final state onto Coulomb (or plane) partial waves of
+ * spectrum_c_pcs (443-514, measure_* 337-403), and the t-SURFF flux integral of
+ * spectrum_c_tsf (516-1072), accumulated after every step (binsrc/sphTDSE.cpp:800,
+ * 804, 940, 944).  Tables are built on the host; the contractions run on the GPU.
+ * Angles: kt = polar angle theta_k, kp = azimuth phi_k. */
+typedef struct qpc_kgrid {
+	int32_t nkr, nkt, nkp;   /* points in |k|, theta_k, phi_k (spec_nkr/nkt/nkp) */
+	double krmin, krmax;     /* |k| range; must give |k| > 0 everywhere */
+	double ktmin, ktmax;     /* theta_k range (uniform, set_sequence_lin) */
+	double kpmin, kpmax;     /* phi_k range (uniform) */
+	int32_t flag;            /* 0: |k| uniform; 1: k^2/2 uniform (set_sequence_sqr), spectrum/inventory.h:15-39 */
+} qpc_kgrid;
+
+/* Building blocks of the tables (functions/coulomb.h, functions/basis_legendre.h):
+ * F[l] = F_l(eta, rho), Fp[l] = dF_l/drho for l = 0..lmax, rho > 0 (Abramowitz-Stegun
+ * normalisation); sigma[l] = arg Gamma(l + 1 + i eta); out[l(l+1)/2 + m] = Y_lm(theta, 0)
+ * at x = cos(theta) with the Condon-Shortley phase, 0 <= m <= l <= lmax. */
+int qpc_coulomb_f(double eta, double rho, int32_t lmax, double* F, double* Fp);
+int qpc_coulomb_sigma(double eta, int32_t lmax, double* sigma);
+int qpc_sph_legendre(int32_t lmax, double x, double* out);
+
+/* spectrum_c_pcs::initialize with the analytic Coulomb waves of charge zc
+ * (momentum_1e.hpp:453-485; initialize_kr 119-148, initialize_th/ph 11-50): kr[nkr],
+ * kt[nkt], kp[nkp]; ijl[kr][l][r] = int B_r F_l(-zc/k, k r) w(r) dr / k with
+ * w = 1/(1 + e^{-5 (r - rb)}) for rb > 0 (plane waves with zc = 0) else 1;
+ * plm[kt][im][il] = Y_lm(kt, 0); exm[kp][im] = e^{i m kp}; cps[kr][l] = e^{i (sigma_l - l pi/2)},
+ * complex arrays as (re, im); l = 0..lmax, lmax = max|m| + n_l - 1. */
+int qpc_pcs_tables(const qpc_dims* dims, const double* knots, const qpc_kgrid* grid, double zc, double rb,
+	double* kr, double* kt, double* kp, double* ijl, double* plm, double* exm, double* cps);
+
+/* spectrum_c_tsf::initialize (momentum_1e.hpp:778-866) at the surface r0 with Coulomb
+ * correction zc: axes as above; the nb <= p+1 splines non-zero at r0 (ib active index,
+ * b0 value, br derivative); j0[kr][l] = F_l(-zc/k, k r0)/k, jr[kr][l] = F'_l(-zc/k, k r0);
+ * y0[kt][im][il] = Y_lm(kt, 0); e0[kp][im] = e^{i m kp}; pmat[3][im][il] = <l m|cos|l+1 m>,
+ * <l m|sin e^{-i phi}|l+1 m+1>, <l m|sin e^{-i phi}|l-1 m+1> (basisfunc.hpp:222-259). */
+int qpc_tsurff_tables(const qpc_dims* dims, const double* knots, const qpc_kgrid* grid, double r0, double zc,
+	double* kr, double* kt, double* kp, int32_t* nb, int32_t* ib, double* b0, double* br, double* j0, double* jr,
+	double* y0, double* e0, double* pmat);
+
+enum { QPC_SPEC_LMD = 0, QPC_SPEC_PMD = 1, QPC_SPEC_PAD = 2 };
+
+/* PCS projector on the GPU: the tables of qpc_pcs_tables (or the caller's own, same layouts),
+ * for wavefunctions of dims (dims->n_inst is ignored). */
+typedef struct qpc_pcs qpc_pcs;
+int qpc_pcs_create(const qpc_dims* dims, const qpc_kgrid* grid, const double* kr, const double* ijl, const double* plm,
+	const double* exm, const double* cps, qpc_pcs** out);
+int qpc_pcs_destroy(qpc_pcs* h);
+/* measure_lmd (kind QPC_SPEC_LMD), measure_prj (PMD) or measure_pad (PAD) of
+ * momentum_1e.hpp:337-403 for n_inst wavefunctions c[inst][m][l][r] (device memory when
+ * on_device != 0, else host).  out (host, complex128): LMD [inst][kr][im][il] =
+ * sqrt(2/pi) cps <ijl|c>; PMD [inst][kr][kt][kp] = sqrt(2/pi) sum plm exm cps <ijl|c>;
+ * PAD [inst][kr][kt] = 2 sqrt(k) sum plm cps <ijl|c>. */
+int qpc_pcs_measure(qpc_pcs* h, int32_t kind, const double* coef, int32_t on_device, int32_t n_inst, double* out);
+/* the same on the resident state of a propagator handle (every instance) */
+int qpc_lgwz_pcs(qpc_lgwz* prop, qpc_pcs* h, int32_t kind, double* out);
+
+/* t-SURFF accumulator on the GPU for dims->n_inst wavefunctions: the tables of
+ * qpc_tsurff_tables; the spectrum work[inst][kr][kt][kp] and the clock (time and the
+ * displacements int A dt per instance) start at zero (clearwork). */
+typedef struct qpc_tsurff qpc_tsurff;
+int qpc_tsurff_create(const qpc_dims* dims, const qpc_kgrid* grid, const double* kr, const double* kt, const double* kp,
+	int32_t nb, const int32_t* ib, const double* b0, const double* br, const double* j0, const double* jr, const double* y0,
+	const double* e0, const double* pmat, qpc_tsurff** out);
+int qpc_tsurff_destroy(qpc_tsurff* h);
+int qpc_tsurff_clear(qpc_tsurff* h);
+enum { QPC_TSURFF_FREE = 0, QPC_TSURFF_Z = 1, QPC_TSURFF_XY = 2 };
+/* spectrum_c_tsf::accumulate (momentum_1e.hpp:627-777) for every instance after a step of
+ * length dt: mode QPC_TSURFF_FREE (a unused), QPC_TSURFF_Z with a[inst][2] = (A_z(t_i), A_z(t_i+1)),
+ * QPC_TSURFF_XY with a[inst][4] = (A_x(t_i), A_x(t_i+1), A_y(t_i), A_y(t_i+1)); a is host memory.
+ * coef: the wavefunctions c[inst][m][l][r] after the step (device when on_device != 0). */
+int qpc_tsurff_accumulate(qpc_tsurff* h, int32_t mode, const double* a, double dt, const double* coef, int32_t on_device);
+/* the same on the resident state of a propagator handle */
+int qpc_lgwz_tsurff(qpc_lgwz* prop, qpc_tsurff* h, int32_t mode, const double* a, double dt);
+int qpc_vgwr_tsurff(qpc_vgwr* prop, qpc_tsurff* h, int32_t mode, const double* a, double dt);
+/* work[inst][kr][kt][kp] complex128 (host); clock[inst][4] = (time, disx, disy, disz) when not NULL */
+int qpc_tsurff_get(qpc_tsurff* h, double* work, double* clock);
 
 #ifdef __cplusplus
 }

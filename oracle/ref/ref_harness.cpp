@@ -42,6 +42,9 @@
 //   proj   OUT RMAX DT ZC ZS SG COEF EMAX
 //       Projection of COEF onto field-free eigenstates with E < EMAX
 //       (eigenstate_sph::initialize + projection, population_1e.hpp:29-118).
+//   pcs    OUT RMAX DT ZC ZS SG COEF KRMIN KRMAX THMIN THMAX PHMIN PHMAX PZC RB FLAG
+//   tsurff OUT RMAX DT ZC ZS SG INIT FIELD NT NFREE MODE R0 TZC KRMIN KRMAX THMIN THMAX PHMIN PHMAX FLAG
+//       momentum spectra (spectrum/momentum_1e.hpp); see cmd_pcs and cmd_tsurff.
 #include <spherical/inventory.h>
 #include <omp.h>
 #include <string>
@@ -383,6 +386,130 @@ static int cmd_mask(int argc, char** argv)
 	return 0;
 }
 
+// ---------------------------------------------------------------- momentum spectra (momentum_1e.hpp)
+// Momentum grids are compile-time in the reference (spectrum_c_pcs<dims_t, nkr, nkt, nkp>):
+// -DHNKR, -DHNKT, -DHNKP.
+#ifndef HNKR
+#define HNKR 24
+#endif
+#ifndef HNKT
+#define HNKT 5
+#endif
+#ifndef HNKP
+#define HNKP 4
+#endif
+
+//   pcs OUT RMAX DT ZC ZS SG COEF KRMIN KRMAX THMIN THMAX PHMIN PHMAX PZC RB FLAG
+//       spectrum_c_pcs::initialize with the analytic Coulomb waves of charge PZC and cut-off RB
+//       (momentum_1e.hpp:453-485) on the grid of RMAX, then measure_lmd, measure_prj and
+//       measure_pad of COEF (337-403); writes the axes, the tables and the three spectra.
+static int cmd_pcs(int argc, char** argv)
+{
+	if (argc < 18) return 1;
+	std::string out = argv[2];
+	double rmax = atof(argv[3]);
+	const char* cf = argv[8];
+	double krmin = atof(argv[9]), krmax = atof(argv[10]), thmin = atof(argv[11]), thmax = atof(argv[12]);
+	double phmin = atof(argv[13]), phmax = atof(argv[14]), pzc = atof(argv[15]), rb = atof(argv[16]);
+	int flag = atoi(argv[17]);
+	omp_set_num_threads(1);
+	auto radi = integrator_radi<dims_t>();
+	radi.initialize(0.0, rmax);
+	auto coef = coefficient<dims_t>();
+	auto v = slurp(cf, 2 * dims_t::n_leng);
+	std::memcpy((double*)coef.data, v.data(), sizeof(double) * v.size());
+	coefficient_view<dims_t> view{coef.data};
+	auto* pcs = new spectrum_c_pcs<dims_t, HNKR, HNKT, HNKP>();
+	pcs->initialize(radi, krmin, krmax, thmin, thmax, phmin, phmax, pzc, rb, flag);
+	dump(out, "kr", pcs->kr, HNKR);
+	dump(out, "kt", pcs->kt, HNKT);
+	dump(out, "kp", pcs->kp, HNKP);
+	dump(out, "ijl", pcs->ijl.data, pcs->ijl.dim.n_leng);
+	dump(out, "plm", pcs->plm.data, pcs->plm.dim.n_leng);
+	dump(out, "exm", pcs->exm.data, 2 * pcs->exm.dim.n_leng);
+	dump(out, "cps", pcs->cps.data, 2 * pcs->cps.dim.n_leng);
+	pcs->measure_lmd(view, 1);
+	dump(out, "lmd", pcs->dptr(), 2 * pcs->size());
+	pcs->measure_prj(view, 1);
+	dump(out, "pmd", pcs->dptr(), 2 * pcs->size());
+	pcs->measure_pad(view, 1);
+	dump(out, "pad", pcs->dptr(), 2 * pcs->size());
+	delete pcs;
+	return 0;
+}
+
+//   tsurff OUT RMAX DT ZC ZS SG INIT FIELD NT NFREE MODE R0 TZC KRMIN KRMAX THMIN THMAX PHMIN PHMAX FLAG
+//       spectrum_c_tsf::initialize at R0 with Coulomb correction TZC (momentum_1e.hpp:778-866), then the
+//       driver loop with t-SURFF (binsrc/sphTDSE.cpp:786-831, 936-945): MODE "z" propagates with
+//       propagator_cn_hc_lgwz and FIELD = NT+1 values f_i, calling accumulate(f_i, f_i+1, dt, coef)
+//       after each field step; MODE "xy" with propagator_cn_hc_vgwr and FIELD = NT+1 rows (A_x, A_y),
+//       calling accumulate(ax_i, ax_i+1, ay_i, ay_i+1, dt, coef); both call accumulate(dt, coef) after
+//       each of the NFREE field-free steps.  Writes the tables, the spectrum work and the final coef.
+static int cmd_tsurff(int argc, char** argv)
+{
+	if (argc < 21) return 1;
+	std::string out = argv[2];
+	double rmax = atof(argv[3]), dt = atof(argv[4]);
+	potn_any potn{atof(argv[5]), atof(argv[6]), atof(argv[7])};
+	const char* init = argv[8];
+	const char* field = argv[9];
+	size_t nt = strtoul(argv[10], 0, 10), nfree = strtoul(argv[11], 0, 10);
+	std::string mode = argv[12];
+	double r0 = atof(argv[13]), tzc = atof(argv[14]);
+	double krmin = atof(argv[15]), krmax = atof(argv[16]), thmin = atof(argv[17]), thmax = atof(argv[18]);
+	double phmin = atof(argv[19]), phmax = atof(argv[20]);
+	int flag = argc > 21 ? atoi(argv[21]) : 0;
+	if (mode != "z" && mode != "xy") return 1;
+	omp_set_num_threads(1);
+	auto radi = integrator_radi<dims_t>();
+	auto angu = integrator_angu<dims_t>();
+	auto coef = coefficient<dims_t>();
+	auto v = slurp(init, 2 * dims_t::n_leng);
+	std::memcpy((double*)coef.data, v.data(), sizeof(double) * v.size());
+	auto* tsf = new spectrum_c_tsf<dims_t, HNKR, HNKT, HNKP>();
+	radi.initialize(0.0, rmax);
+	tsf->initialize(radi, angu, r0, tzc, krmin, krmax, thmin, thmax, phmin, phmax, flag);
+	if (mode == "z") {
+		auto prop = propagator_cn_hc_lgwz<dims_t>();
+		prop.initialize(1, radi, angu, 1.0, potn, dt);
+		std::vector<double> f = nt ? slurp(field, nt + 1) : std::vector<double>{};
+		for (size_t it = 0; it < nt + nfree; ++it) {
+			if (it < nt) { prop.propagate(coef, f[it], f[it + 1]); tsf->accumulate(f[it], f[it + 1], dt, coef.data); }
+			else { prop.propagate(coef); tsf->accumulate(dt, coef.data); }
+		}
+	} else {
+		auto prop = propagator_cn_hc_vgwr<dims_t>();
+		prop.initialize(1, radi, angu, 1.0, potn, dt);
+		std::vector<double> f = nt ? slurp(field, 2 * (nt + 1)) : std::vector<double>{};
+		for (size_t it = 0; it < nt + nfree; ++it) {
+			if (it < nt) {
+				prop.propagate(coef, f[2 * it], f[2 * it + 2], f[2 * it + 1], f[2 * it + 3]);
+				tsf->accumulate(f[2 * it], f[2 * it + 2], f[2 * it + 1], f[2 * it + 3], dt, coef.data);
+			} else { prop.propagate(coef); tsf->accumulate(dt, coef.data); }
+		}
+	}
+	dump(out, "kr", tsf->kr, HNKR);
+	dump(out, "kt", tsf->kt, HNKT);
+	dump(out, "kp", tsf->kp, HNKP);
+	std::vector<double> ibd(tsf->ib, tsf->ib + tsf->nb);
+	dump(out, "ib", ibd.data(), ibd.size());
+	dump(out, "b0", tsf->b0, tsf->nb);
+	dump(out, "br", tsf->br, tsf->nb);
+	dump(out, "j0", tsf->j0.data, tsf->j0.dim.n_leng);
+	dump(out, "jr", tsf->jr.data, tsf->jr.dim.n_leng);
+	dump(out, "y0", tsf->y0.data, tsf->y0.dim.n_leng);
+	dump(out, "e0", tsf->e0.data, 2 * tsf->e0.dim.n_leng);
+	dump(out, "pmat0", tsf->pmat0.data, tsf->pmat0.dim.n_leng);
+	dump(out, "pmat1", tsf->pmat1.data, tsf->pmat1.dim.n_leng);
+	dump(out, "pmat2", tsf->pmat2.data, tsf->pmat2.dim.n_leng);
+	dump(out, "work", tsf->dptr(), 2 * tsf->size());
+	double clk[4] = {tsf->time, tsf->disx, tsf->disy, tsf->disz};
+	dump(out, "clock", clk, 4);
+	dump(out, "coef", coef.data, 2 * dims_t::n_leng);
+	delete tsf;
+	return 0;
+}
+
 int main(int argc, char** argv)
 {
 	if (argc < 2) { std::fprintf(stderr, "usage: setup|field|propagate|proj|arnoldi ...\n"); return 1; }
@@ -396,6 +523,8 @@ int main(int argc, char** argv)
 		else if (c == "arnoldi") rc = cmd_arnoldi(argc, argv);
 		else if (c == "vgwr") rc = cmd_vgwr(argc, argv);
 		else if (c == "mask") rc = cmd_mask(argc, argv);
+		else if (c == "pcs") rc = cmd_pcs(argc, argv);
+		else if (c == "tsurff") rc = cmd_tsurff(argc, argv);
 		if (rc) std::fprintf(stderr, "bad arguments for %s\n", argv[1]);
 		return rc;
 	} catch (std::exception& e) {

@@ -40,8 +40,13 @@ EXPORTS = (
     "qpc_mlp_loss_grad", "qpc_mlp_train", "qpc_mlp_predict", "qpc_vgwr_angular", "qpc_vgwr_create",
     "qpc_vgwr_destroy", "qpc_vgwr_put", "qpc_vgwr_get", "qpc_vgwr_put_device", "qpc_vgwr_get_device",
     "qpc_vgwr_propagate", "qpc_vgwr_propagate_free", "qpc_vgwr_run", "qpc_vgwr_norm", "qpc_vgwr_last_run",
-    "qpc_mask_band", "qpc_lgwz_mask",
+    "qpc_mask_band", "qpc_lgwz_mask", "qpc_lgwz_dims", "qpc_vgwr_dims", "qpc_coulomb_f", "qpc_coulomb_sigma",
+    "qpc_sph_legendre", "qpc_pcs_tables", "qpc_tsurff_tables", "qpc_pcs_create", "qpc_pcs_destroy", "qpc_pcs_measure",
+    "qpc_lgwz_pcs", "qpc_tsurff_create", "qpc_tsurff_destroy", "qpc_tsurff_clear", "qpc_tsurff_accumulate",
+    "qpc_lgwz_tsurff", "qpc_vgwr_tsurff", "qpc_tsurff_get",
 )
+SPEC_LMD, SPEC_PMD, SPEC_PAD = 0, 1, 2
+TSURFF_FREE, TSURFF_Z, TSURFF_XY = 0, 1, 2
 NOALLOC_MAX_ELEMS = 1 << 20
 KERNELS = ("factor", "transform_fwd", "sweep", "transform_bwd", "fieldfree")
 
@@ -59,6 +64,12 @@ class qpc_potential(ctypes.Structure):
 class qpc_dims(ctypes.Structure):
     _fields_ = [("n_r", ctypes.c_int32), ("p", ctypes.c_int32), ("n_l", ctypes.c_int32),
                 ("n_m", ctypes.c_int32), ("m0", ctypes.c_int32), ("n_inst", ctypes.c_int32)]
+
+
+class qpc_kgrid(ctypes.Structure):
+    _fields_ = [("nkr", ctypes.c_int32), ("nkt", ctypes.c_int32), ("nkp", ctypes.c_int32),
+                ("krmin", ctypes.c_double), ("krmax", ctypes.c_double), ("ktmin", ctypes.c_double),
+                ("ktmax", ctypes.c_double), ("kpmin", ctypes.c_double), ("kpmax", ctypes.c_double), ("flag", ctypes.c_int32)]
 
 
 _lib = None
@@ -142,6 +153,24 @@ def load(path=None):
         "qpc_arnoldi_propagate": (ctypes.c_int, [P, P, P]),
         "qpc_arnoldi_norm": (ctypes.c_int, [P, P]),
         "qpc_arnoldi_last_run": (ctypes.c_int, [P, P, P]),
+        "qpc_lgwz_dims": (ctypes.c_int, [P, P]),
+        "qpc_vgwr_dims": (ctypes.c_int, [P, P]),
+        "qpc_coulomb_f": (ctypes.c_int, [d, d, i32, P, P]),
+        "qpc_coulomb_sigma": (ctypes.c_int, [d, i32, P]),
+        "qpc_sph_legendre": (ctypes.c_int, [i32, d, P]),
+        "qpc_pcs_tables": (ctypes.c_int, [P, P, P, d, d, P, P, P, P, P, P, P]),
+        "qpc_tsurff_tables": (ctypes.c_int, [P, P, P, d, d, P, P, P, P, P, P, P, P, P, P, P, P]),
+        "qpc_pcs_create": (ctypes.c_int, [P, P, P, P, P, P, P, P]),
+        "qpc_pcs_destroy": (ctypes.c_int, [P]),
+        "qpc_pcs_measure": (ctypes.c_int, [P, i32, P, i32, i32, P]),
+        "qpc_lgwz_pcs": (ctypes.c_int, [P, P, i32, P]),
+        "qpc_tsurff_create": (ctypes.c_int, [P, P, P, P, P, i32, P, P, P, P, P, P, P, P, P]),
+        "qpc_tsurff_destroy": (ctypes.c_int, [P]),
+        "qpc_tsurff_clear": (ctypes.c_int, [P]),
+        "qpc_tsurff_accumulate": (ctypes.c_int, [P, i32, P, d, P, i32]),
+        "qpc_lgwz_tsurff": (ctypes.c_int, [P, P, i32, P, d]),
+        "qpc_vgwr_tsurff": (ctypes.c_int, [P, P, i32, P, d]),
+        "qpc_tsurff_get": (ctypes.c_int, [P, P, P]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -753,3 +782,198 @@ class propagator_cn_hc_vgwr:
         _check(load().qpc_vgwr_last_run(self._h, ctypes.byref(ms), ctypes.byref(n)))
         return ms.value, n.value
 
+
+
+# ------------------------------------------------------------------ momentum spectra
+
+def coulomb_f(eta, rho, lmax):
+    """F_l(eta, rho) and dF_l/drho for l = 0..lmax (functions/coulomb.h, coulombfg)."""
+    F, Fp = np.zeros(lmax + 1), np.zeros(lmax + 1)
+    _check(load().qpc_coulomb_f(eta, rho, lmax, _ptr(F), _ptr(Fp)))
+    return F, Fp
+
+
+def coulomb_sigma(eta, lmax):
+    """arg Gamma(l + 1 + i eta), l = 0..lmax (coulomb_sig_real)."""
+    out = np.zeros(lmax + 1)
+    _check(load().qpc_coulomb_sigma(eta, lmax, _ptr(out)))
+    return out
+
+
+def sph_legendre(lmax, x):
+    """Y_lm(theta, 0) at x = cos(theta), array index l(l+1)/2 + m (legendre::cal, functions/basis_legendre.h)."""
+    out = np.zeros((lmax + 1) * (lmax + 2) // 2)
+    _check(load().qpc_sph_legendre(lmax, x, _ptr(out)))
+    return out
+
+
+def _kgrid(nkr, nkt, nkp, krmin, krmax, ktmin, ktmax, kpmin, kpmax, flag):
+    return qpc_kgrid(nkr, nkt, nkp, krmin, krmax, ktmin, ktmax, kpmin, kpmax, flag)
+
+
+def _lmax(n_l, n_m, m0):
+    return max(abs(m0), abs(m0 + n_m - 1)) + n_l - 1
+
+
+def pcs_tables(n_r, p, n_l, knots, nkr, nkt, nkp, krmin, krmax, ktmin, ktmax, kpmin, kpmax, zc, rb=0.0, flag=0, n_m=1, m0=0):
+    """spectrum_c_pcs::initialize (analytic Coulomb waves; spherical/spectrum/momentum_1e.hpp:453-485):
+    dict of kr, kt, kp, ijl [nkr][lmax+1][n_r], plm [nkt][n_m][n_l], exm [nkp][n_m], cps [nkr][lmax+1]."""
+    d = qpc_dims(n_r, p, n_l, n_m, m0, 1)
+    g = _kgrid(nkr, nkt, nkp, krmin, krmax, ktmin, ktmax, kpmin, kpmax, flag)
+    nl = _lmax(n_l, n_m, m0) + 1
+    t = {"kr": np.zeros(nkr), "kt": np.zeros(nkt), "kp": np.zeros(nkp), "ijl": np.zeros((nkr, nl, n_r)),
+         "plm": np.zeros((nkt, n_m, n_l)), "exm": np.zeros((nkp, n_m), complex), "cps": np.zeros((nkr, nl), complex)}
+    _check(load().qpc_pcs_tables(ctypes.byref(d), _ptr(_f64(knots)), ctypes.byref(g), zc, rb, *[_ptr(t[k]) for k in
+                                 ("kr", "kt", "kp", "ijl", "plm", "exm", "cps")]))
+    return t
+
+
+def tsurff_tables(n_r, p, n_l, knots, r0, zc, nkr, nkt, nkp, krmin, krmax, ktmin, ktmax, kpmin, kpmax, flag=0, n_m=1, m0=0):
+    """spectrum_c_tsf::initialize (spherical/spectrum/momentum_1e.hpp:778-866): dict of kr, kt, kp,
+    ib, b0, br (splines non-zero at r0), j0, jr [nkr][lmax+1], y0 [nkt][n_m][n_l], e0 [nkp][n_m],
+    pmat [3][n_m][n_l]."""
+    d = qpc_dims(n_r, p, n_l, n_m, m0, 1)
+    g = _kgrid(nkr, nkt, nkp, krmin, krmax, ktmin, ktmax, kpmin, kpmax, flag)
+    nl = _lmax(n_l, n_m, m0) + 1
+    t = {"kr": np.zeros(nkr), "kt": np.zeros(nkt), "kp": np.zeros(nkp), "ib": np.zeros(p + 1, np.int32),
+         "b0": np.zeros(p + 1), "br": np.zeros(p + 1), "j0": np.zeros((nkr, nl)), "jr": np.zeros((nkr, nl)),
+         "y0": np.zeros((nkt, n_m, n_l)), "e0": np.zeros((nkp, n_m), complex), "pmat": np.zeros((3, n_m, n_l))}
+    nb = ctypes.c_int32(0)
+    _check(load().qpc_tsurff_tables(ctypes.byref(d), _ptr(_f64(knots)), ctypes.byref(g), r0, zc, _ptr(t["kr"]), _ptr(t["kt"]),
+                                    _ptr(t["kp"]), ctypes.byref(nb), _ptr(t["ib"]), _ptr(t["b0"]), _ptr(t["br"]), _ptr(t["j0"]),
+                                    _ptr(t["jr"]), _ptr(t["y0"]), _ptr(t["e0"]), _ptr(t["pmat"])))
+    for k in ("ib", "b0", "br"):
+        t[k] = t[k][:nb.value].copy()
+    return t
+
+
+class spectrum_c_pcs:
+    """Photoelectron momentum spectra by projection onto Coulomb partial waves on the GPU
+    (spectrum_c_pcs<dims_t, nkr, nkt, nkp>, spherical/spectrum/momentum_1e.hpp:443-514).
+
+    initialize(...) builds the tables (pcs_tables; the grid is given by its knots instead of an
+    integrator_radi) and uploads them; measure_lmd / measure_prj / measure_pad(coef) mirror the
+    reference's members for a batch coef[inst][m][l][r] (host array, or a propagator_cn_hc_lgwz
+    whose resident state is measured)."""
+
+    def __init__(self, nkr, nkt, nkp):
+        self.nkr, self.nkt, self.nkp = nkr, nkt, nkp
+        self._h = None
+
+    def initialize(self, n_r, p, n_l, knots, krmin, krmax, thmin, thmax, phmin, phmax, zc, rb=0.0, flag=0, n_m=1, m0=0, tables=None):
+        lib = load()
+        self.close()
+        t = tables or pcs_tables(n_r, p, n_l, knots, self.nkr, self.nkt, self.nkp, krmin, krmax, thmin, thmax, phmin, phmax, zc, rb,
+                                 flag, n_m, m0)
+        d = qpc_dims(n_r, p, n_l, n_m, m0, 1)
+        g = _kgrid(self.nkr, self.nkt, self.nkp, krmin, krmax, thmin, thmax, phmin, phmax, flag)
+        h = ctypes.c_void_p()
+        _check(lib.qpc_pcs_create(ctypes.byref(d), ctypes.byref(g), _ptr(_f64(t["kr"])), _ptr(_f64(t["ijl"])), _ptr(_f64(t["plm"])),
+                                  _ptr(np.ascontiguousarray(t["exm"], np.complex128)), _ptr(np.ascontiguousarray(t["cps"], np.complex128)),
+                                  ctypes.byref(h)))
+        self._h, self.tables, self.shape = h, t, (n_m, n_l, n_r)
+        self.kr, self.kt, self.kp = t["kr"], t["kt"], t["kp"]
+        return self
+
+    def close(self):
+        if self._h is not None:
+            load().qpc_pcs_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _measure(self, kind, coef):
+        n_m, n_l, _ = self.shape
+        shapes = {SPEC_LMD: (self.nkr, n_m, n_l), SPEC_PMD: (self.nkr, self.nkt, self.nkp), SPEC_PAD: (self.nkr, self.nkt)}
+        if isinstance(coef, propagator_cn_hc_lgwz):
+            out = np.zeros((coef.shape[0],) + shapes[kind], np.complex128)
+            _check(load().qpc_lgwz_pcs(coef._h, self._h, kind, _ptr(out)))
+            return out
+        c = np.ascontiguousarray(coef, dtype=np.complex128).reshape((-1,) + self.shape)
+        out = np.zeros((c.shape[0],) + shapes[kind], np.complex128)
+        _check(load().qpc_pcs_measure(self._h, kind, _ptr(c), 0, c.shape[0], _ptr(out)))
+        return out
+
+    def measure_lmd(self, coef):
+        """[inst][kr][m][l] partial-wave amplitudes (measure_lmd, momentum_1e.hpp:386-403)"""
+        return self._measure(SPEC_LMD, coef)
+
+    def measure_prj(self, coef):
+        """[inst][kr][kt][kp] momentum amplitudes (measure_prj, momentum_1e.hpp:337-355)"""
+        return self._measure(SPEC_PMD, coef)
+
+    def measure_pad(self, coef):
+        """[inst][kr][kt] (measure_pad, momentum_1e.hpp:358-383)"""
+        return self._measure(SPEC_PAD, coef)
+
+
+class spectrum_c_tsf:
+    """t-SURFF momentum spectra on the GPU (spectrum_c_tsf, spherical/spectrum/momentum_1e.hpp:516-1072)
+    for n_inst wavefunctions: initialize(...) at the surface r0; accumulate(coef, dt, a) after every
+    step with a = None (field-free), a[inst][2] = (A_z(t_i), A_z(t_i+1)) or a[inst][4] =
+    (A_x(t_i), A_x(t_i+1), A_y(t_i), A_y(t_i+1)); coef is a host array [inst][m][l][r] or a
+    propagator handle (propagator_cn_hc_lgwz, propagator_cn_hc_vgwr) whose resident state is used."""
+
+    def __init__(self, nkr, nkt, nkp):
+        self.nkr, self.nkt, self.nkp = nkr, nkt, nkp
+        self._h = None
+
+    def initialize(self, n_r, p, n_l, knots, r0, zc, krmin, krmax, thmin, thmax, phmin, phmax, flag=0, n_m=1, m0=0, n_inst=1, tables=None):
+        lib = load()
+        self.close()
+        t = tables or tsurff_tables(n_r, p, n_l, knots, r0, zc, self.nkr, self.nkt, self.nkp, krmin, krmax, thmin, thmax, phmin, phmax,
+                                    flag, n_m, m0)
+        d = qpc_dims(n_r, p, n_l, n_m, m0, n_inst)
+        g = _kgrid(self.nkr, self.nkt, self.nkp, krmin, krmax, thmin, thmax, phmin, phmax, flag)
+        h = ctypes.c_void_p()
+        ib = np.ascontiguousarray(t["ib"], np.int32)
+        _check(lib.qpc_tsurff_create(ctypes.byref(d), ctypes.byref(g), _ptr(_f64(t["kr"])), _ptr(_f64(t["kt"])), _ptr(_f64(t["kp"])),
+                                     len(ib), _ptr(ib), _ptr(_f64(t["b0"])), _ptr(_f64(t["br"])), _ptr(_f64(t["j0"])), _ptr(_f64(t["jr"])),
+                                     _ptr(_f64(t["y0"])), _ptr(np.ascontiguousarray(t["e0"], np.complex128)), _ptr(_f64(t["pmat"])),
+                                     ctypes.byref(h)))
+        self._h, self.tables, self.shape = h, t, (n_inst, n_m, n_l, n_r)
+        self.kr, self.kt, self.kp = t["kr"], t["kt"], t["kp"]
+        return self
+
+    def close(self):
+        if self._h is not None:
+            load().qpc_tsurff_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def clearwork(self):
+        _check(load().qpc_tsurff_clear(self._h))
+
+    def accumulate(self, coef, dt, a=None):
+        B = self.shape[0]
+        if a is None:
+            mode, av = TSURFF_FREE, None
+        else:
+            av = _f64(np.asarray(a, np.float64).reshape(B, -1) if np.ndim(a) > 1 else np.broadcast_to(np.asarray(a, np.float64), (B, len(a))))
+            if av.shape[1] not in (2, 4):
+                raise QpcError(1, "a needs 2 (z) or 4 (xy) values per instance")
+            mode = TSURFF_Z if av.shape[1] == 2 else TSURFF_XY
+        lib = load()
+        if isinstance(coef, propagator_cn_hc_lgwz):
+            _check(lib.qpc_lgwz_tsurff(coef._h, self._h, mode, _ptr(av), dt))
+        elif isinstance(coef, propagator_cn_hc_vgwr):
+            _check(lib.qpc_vgwr_tsurff(coef._h, self._h, mode, _ptr(av), dt))
+        else:
+            c = np.ascontiguousarray(coef, dtype=np.complex128).reshape(self.shape)
+            _check(lib.qpc_tsurff_accumulate(self._h, mode, _ptr(av), dt, _ptr(c), 0))
+
+    def get(self):
+        """(work [inst][kr][kt][kp] complex, clock [inst][4] = time, disx, disy, disz)"""
+        w = np.zeros((self.shape[0], self.nkr, self.nkt, self.nkp), np.complex128)
+        ck = np.zeros((self.shape[0], 4))
+        _check(load().qpc_tsurff_get(self._h, _ptr(w), _ptr(ck)))
+        return w, ck

@@ -925,6 +925,12 @@ int qpc_lgwz_get_device(qpc_lgwz* h, double* dev_coef)
 	if (!h || !dev_coef) { set_error("NULL argument"); return QPC_ERR_ARGS; }
 	return get_common(h, dev_coef, cudaMemcpyDeviceToDevice);
 }
+int qpc_lgwz_dims(qpc_lgwz* h, qpc_dims* dims)
+{
+	if (!h || !dims) { set_error("NULL argument"); return QPC_ERR_ARGS; }
+	*dims = h->d;
+	return QPC_OK;
+}
 
 static int run_impl(qpc_lgwz* h, const double* ftab, int64_t ld, const int64_t* nt_field, const int64_t* nt_total,
 	const double* F, double* zlist, int64_t ldz)

@@ -4,8 +4,22 @@
 #include "../../include/qpc_gb300.h"
 #include <cstddef>
 #include <cstdint>
+#include <vector>
 
 namespace qpc {
+// B-spline basis of one radial grid with its Gauss-Legendre quadrature (nq points per knot
+// interval, absolute interval index s over the knot vector t); built by build_basis.
+struct radial_basis {
+	int n, p, nq;
+	std::vector<double> t;               // absolute knots t_0 .. t_{n+p+2}
+	std::vector<double> xq, wq;          // [interval][nq]
+	std::vector<double> b0, b1;          // [interval][p+1][nq], spline s-p+j at interval s
+	int nint() const { return (int)t.size() - 1; }
+};
+void build_basis(radial_basis& B);
+// values and first derivatives of the p+1 splines non-zero on interval [t_s, t_s+1) at x
+void bspline_eval(const std::vector<double>& t, int s, int p, double x, double* out0, double* out1);
+
 void set_error(const char* fmt, ...);
 // real symmetric form D^H Z_c D of a propagator_cn_hc_vgwr coupling (qpc_setup.cpp)
 void vgwr_real_coupling(int n_l, int n_m, int m0, int comp, double* Zr);

@@ -47,7 +47,7 @@ static void gauss_legendre(int n, std::vector<double>& x, std::vector<double>& w
 // Values and first derivatives of the p+1 B-splines of degree p that are
 // non-zero on knot interval [t_s, t_{s+1}) at point x, by the Cox-de Boor
 // triangular recursion.  out0[j], out1[j] belong to absolute spline s-p+j.
-static void bspline_eval(const std::vector<double>& t, int s, int p, double x, double* out0, double* out1)
+void bspline_eval(const std::vector<double>& t, int s, int p, double x, double* out0, double* out1)
 {
 	std::vector<double> N(p + 1, 0.0), left(p + 1), right(p + 1), Nm1(p + 1, 0.0);
 	N[0] = 1.0;
@@ -77,14 +77,6 @@ static void bspline_eval(const std::vector<double>& t, int s, int p, double x, d
 	}
 }
 
-struct radial_basis {
-	int n, p, nq;
-	std::vector<double> t;               // absolute knots t_0 .. t_{n+p+2}
-	std::vector<double> xq, wq;          // [interval][nq]
-	std::vector<double> b0, b1;          // [interval][p+1][nq], spline s-p+j at interval s
-	int nint() const { return (int)t.size() - 1; }
-};
-
 // Knot vector of the reference's initialize_axis_linear_step
 // (functions/basis_bsplines.h:450-459): p+1 copies of rmin, uniform interior
 // step (rmax-rmin)/(n+2-p), p+1 copies of rmax; spline 0 and spline n+1 (the
@@ -101,7 +93,7 @@ static std::vector<double> linear_knots(int n, int p, double rmin, double rmax)
 	return t;
 }
 
-static void build_basis(radial_basis& B)
+void build_basis(radial_basis& B)
 {
 	int ni = B.nint();
 	B.xq.assign((size_t)ni * B.nq, 0.0); B.wq.assign((size_t)ni * B.nq, 0.0);

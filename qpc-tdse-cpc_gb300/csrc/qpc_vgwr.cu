@@ -637,6 +637,12 @@ int qpc_vgwr_put(qpc_vgwr* h, const double* coef) { return vg_copy(h, coef, null
 int qpc_vgwr_get(qpc_vgwr* h, double* coef) { return vg_copy(h, nullptr, coef, cudaMemcpyDeviceToHost); }
 int qpc_vgwr_put_device(qpc_vgwr* h, const double* c) { return vg_copy(h, c, nullptr, cudaMemcpyDeviceToDevice); }
 int qpc_vgwr_get_device(qpc_vgwr* h, double* c) { return vg_copy(h, nullptr, c, cudaMemcpyDeviceToDevice); }
+int qpc_vgwr_dims(qpc_vgwr* h, qpc_dims* dims)
+{
+	if (!h || !dims) { set_error("NULL argument"); return QPC_ERR_ARGS; }
+	*dims = h->d;
+	return QPC_OK;
+}
 
 int qpc_vgwr_run(qpc_vgwr* h, const double* atab, int64_t ld, const int64_t* nt_field, const int64_t* nt_total)
 {

@@ -2,7 +2,7 @@
 propagator (QPC-TDSE headers compiled by oracle/ref/Makefile into oracle/_ref/).
 
 Run on the development machine, where the reference checkout exists:
-    python tests/golden/make_golden.py [/path/to/reference/include] [--arnoldi] [--vgwr] [--mask] [--multim]
+    python tests/golden/make_golden.py [/path/to/reference/include] [--arnoldi] [--vgwr] [--mask] [--multim] [--momentum]
 (those flags regenerate only the named fixtures.)
 The fixtures are committed; the tests only read them.
 
@@ -42,6 +42,21 @@ Cases (hydrogen unless stated; r in [0, rmax], uniform knots, m = 0):
                     A_x = 0.3 sin(0.5 t + 0.1), A_y = 0.2 cos(0.5 t), then 2 field-free
                     steps: the reference's S, 1/r, D, H_l, the couplings' eigenvalues, the
                     final coefficients and S-norm
+  pcs_small.npz     spectrum_c_pcs (spectrum/momentum_1e.hpp:443-514) on the small grid (rmax = 30)
+  pcs_ep.npz        and on the multi-m grid (N_r=40, p=5, n_l=4, m=-2..2, rmax = 20): a seeded
+                    random state, nkr = 24, nkt = 5, nkp = 4, theta in [0, 3], phi in [0, 6];
+                    "coul": Coulomb waves zc = 1, |k| uniform in [0.1, 2]; "plane": plane waves
+                    with the cut-off at rb = 10, k^2/2 uniform for |k| in [0.2, 1.5]; the tables
+                    (kr, kt, kp, ijl, plm, exm, cps) and measure_lmd / measure_prj / measure_pad
+  tsurff_small.npz  spectrum_c_tsf (momentum_1e.hpp:516-1072) in the driver loop of the
+                    length-gauge propagator on the small grid: a seeded random state, 60 steps
+                    with f_i = 0.3 sin(0.4 t_i) sin^2(pi t_i / t_60) passed to accumulate(f_i,
+                    f_i+1, dt, coef), then 20 field-free steps with accumulate(dt, coef);
+                    surface r0 = 20, zc = 0, nkr = 24 (|k| in [0.2, 1.6]), nkt = 5 (theta in
+                    [0.1, 3]), nkp = 4 (phi in [0, 4.5]): tables, work, clock, final state
+  tsurff_ep.npz     the same with the velocity-gauge elliptical propagator on the multi-m grid
+                    and accumulate(ax_i, ax_i+1, ay_i, ay_i+1, dt, coef) under the vgwr_ep
+                    field, surface r0 = 12, zc = 1
 """
 import json
 import os
@@ -168,10 +183,66 @@ def vgwr(d):
         np.savez(os.path.join(HERE, tag + ".npz"), **out)
 
 
+def momentum(d):
+    """Momentum-spectrum fixtures (see the module docstring); the harness's momentum grids are
+    compile-time: nkr = 24, nkt = 5, nkp = 4."""
+    nk = (24, 5, 4)
+    # ---- PCS on the small grid (m = 0) and on the multi-m grid
+    for binary, tag, NR, P, NL, NM, M0, RMAX in (("ref_small", "pcs_small", 64, 6, 6, 1, 0, 30.0), ("ref_ep", "pcs_ep", 40, 5, 4, 5, -2, 20.0)):
+        rng = np.random.default_rng(21)
+        n = NR * NL * NM
+        c = (rng.standard_normal(n) + 1j * rng.standard_normal(n)) * np.exp(-np.tile(np.arange(NR), NL * NM) / 12.0)
+        c.tofile(os.path.join(d, "pcoef.bin"))
+        out = {"n_r": NR, "p": P, "n_l": NL, "n_m": NM, "m0": M0, "rmax": RMAX, "nkr": nk[0], "nkt": nk[1], "nkp": nk[2],
+               "coef": c.reshape(NM, NL, NR)}
+        lmax = max(abs(M0), abs(M0 + NM - 1)) + NL - 1
+        for case, krng, pzc, rb, flag in (("coul", (0.1, 2.0), 1.0, 0.0, 0), ("plane", (0.2, 1.5), 0.0, 10.0, 1)):
+            ang = (0.0, 3.0, 0.0, 6.0)
+            run(binary, "pcs", d, RMAX, 0.05, 1, 0, 0, os.path.join(d, "pcoef.bin"), krng[0], krng[1], *ang, pzc, rb, flag)
+            out.update({case + "_grid": np.array([krng[0], krng[1], *ang, pzc, rb, flag]),
+                        case + "_kr": load(d, "kr"), case + "_kt": load(d, "kt"), case + "_kp": load(d, "kp"),
+                        case + "_ijl": load(d, "ijl", (nk[0], lmax + 1, NR)), case + "_plm": load(d, "plm", (nk[1], NM, NL)),
+                        case + "_exm": load(d, "exm", (nk[2], NM), True), case + "_cps": load(d, "cps", (nk[0], lmax + 1), True),
+                        case + "_lmd": load(d, "lmd", (nk[0], NM, NL), True), case + "_pmd": load(d, "pmd", nk, True),
+                        case + "_pad": load(d, "pad", None, True)[:nk[0] * nk[1]].reshape(nk[0], nk[1])})
+        np.savez(os.path.join(HERE, tag + ".npz"), **out)
+    # ---- t-SURFF in the driver loops
+    for binary, tag, NR, P, NL, NM, M0, RMAX, mode, r0, tzc in (("ref_small", "tsurff_small", 64, 6, 6, 1, 0, 30.0, "z", 20.0, 0.0),
+                                                                 ("ref_ep", "tsurff_ep", 40, 5, 4, 5, -2, 20.0, "xy", 12.0, 1.0)):
+        DT, nt, nfree = 0.05, 60, 20
+        run(binary, "setup", d, RMAX, DT, 1, 0, 0)
+        nlh = max(abs(M0), abs(M0 + NM - 1)) + NL
+        rng = np.random.default_rng(22)
+        n = NR * NL * NM
+        c0 = (rng.standard_normal(n) + 1j * rng.standard_normal(n)) * np.exp(-np.tile(np.arange(NR), NL * NM) / 10.0)
+        c0.tofile(os.path.join(d, "tinit.bin"))
+        t = DT * np.arange(nt + 1)
+        if mode == "z":
+            f = 0.3 * np.sin(0.4 * t) * np.sin(np.pi * t / t[-1]) ** 2
+        else:
+            f = np.stack([0.3 * np.sin(0.5 * t + 0.1), 0.2 * np.cos(0.5 * t)], 1)
+        f.tofile(os.path.join(d, "tfield.bin"))
+        krng, ang = (0.2, 1.6), (0.1, 3.0, 0.0, 4.5)
+        run(binary, "tsurff", d, RMAX, DT, 1, 0, 0, os.path.join(d, "tinit.bin"), os.path.join(d, "tfield.bin"), nt, nfree, mode, r0, tzc,
+            krng[0], krng[1], *ang, 0)
+        lmax = nlh - 1
+        out = {"n_r": NR, "p": P, "n_l": NL, "n_m": NM, "m0": M0, "rmax": RMAX, "dt": DT, "nt": nt, "nfree": nfree, "mode": mode,
+               "r0": r0, "tzc": tzc, "grid": np.array([krng[0], krng[1], *ang, 0]), "nkr": nk[0], "nkt": nk[1], "nkp": nk[2],
+               "S": load(d, "S", (NR, P + 1)), "R": load(d, "R", (NR, P + 1)), "RINV": load(d, "RINV", (NR, P + 1)),
+               "D": load(d, "D", (NR, P + 1)), "H": load(d, "H", (nlh, NR, P + 1)), "knots": load(d, "knots"),
+               "init": c0.reshape(NM, NL, NR), "field": f,
+               "kr": load(d, "kr"), "kt": load(d, "kt"), "kp": load(d, "kp"), "ib": load(d, "ib").astype(np.int32),
+               "b0": load(d, "b0"), "br": load(d, "br"), "j0": load(d, "j0", (nk[0], lmax + 1)), "jr": load(d, "jr", (nk[0], lmax + 1)),
+               "y0": load(d, "y0", (nk[1], NM, NL)), "e0": load(d, "e0", (nk[2], NM), True),
+               "pmat": np.stack([load(d, "pmat%d" % i, (NM, NL)) for i in range(3)]),
+               "work": load(d, "work", nk, True), "clock": load(d, "clock"), "coef": load(d, "coef", (NM, NL, NR), True)}
+        np.savez(os.path.join(HERE, tag + ".npz"), **out)
+
+
 def main():
     ref_include = sys.argv[1] if len(sys.argv) > 1 and not sys.argv[1].startswith("--") else "/root/reference/include"
     build(ref_include)
-    if any(a in sys.argv for a in ("--arnoldi", "--vgwr", "--mask", "--multim")):
+    if any(a in sys.argv for a in ("--arnoldi", "--vgwr", "--mask", "--multim", "--momentum")):
         with tempfile.TemporaryDirectory() as d:
             if "--arnoldi" in sys.argv:
                 arnoldi(d)
@@ -181,6 +252,8 @@ def main():
                 mask(d)
             if "--multim" in sys.argv:
                 multi_m(d)
+            if "--momentum" in sys.argv:
+                momentum(d)
         return
     meta = {}
     with tempfile.TemporaryDirectory() as d:
@@ -243,6 +316,7 @@ def main():
         vgwr(d)
         mask(d)
         multi_m(d)
+        momentum(d)
     with open(os.path.join(HERE, "make_golden.log.json"), "w") as fh:
         json.dump(meta, fh, indent=1)
 

@@ -89,3 +89,32 @@ def test_other_engines_check_arguments_and_device(q):
     with pytest.raises(q.QpcError) as e:
         q.mlp_ensemble(6, 384)
     assert e.value.code == 8
+
+
+def test_momentum_handles_check_arguments_and_device(q):
+    """PCS projector and t-SURFF accumulator: bad tables are rejected before any device use,
+    and without a GPU the handles report QPC_ERR_NODEVICE (no CPU path)."""
+    torch = pytest.importorskip("torch")
+    lib = q.load()
+    kn = q.linear_knots(32, 6, 0.0, 20.0)
+    h = ctypes.c_void_p()
+    d = q.qpc_dims(32, 6, 4, 1, 0, 2)
+    g = q.qpc_kgrid(6, 3, 2, 0.2, 1.0, 0.0, 3.0, 0.0, 6.0, 0)
+    t = q.pcs_tables(32, 6, 4, kn, 6, 3, 2, 0.2, 1.0, 0.0, 3.0, 0.0, 6.0, 1.0)
+    P = lambda a: a.ctypes.data
+    assert lib.qpc_pcs_create(ctypes.byref(d), ctypes.byref(g), None, P(t["ijl"]), P(t["plm"]), P(t["exm"]), P(t["cps"]), ctypes.byref(h)) == 1
+    ts = q.tsurff_tables(32, 6, 4, kn, 12.0, 0.0, 6, 3, 2, 0.2, 1.0, 0.0, 3.0, 0.0, 6.0)
+    bad = np.full(ts["ib"].size, 40, np.int32)      # spline index outside the grid
+    args = [P(ts[k]) for k in ("kr", "kt", "kp")]
+    assert lib.qpc_tsurff_create(ctypes.byref(d), ctypes.byref(g), *args, bad.size, P(bad), P(ts["b0"]), P(ts["br"]), P(ts["j0"]),
+                                 P(ts["jr"]), P(ts["y0"]), P(ts["e0"]), P(ts["pmat"]), ctypes.byref(h)) == 1
+    assert lib.qpc_pcs_measure(None, 0, None, 0, 1, None) == 1
+    assert lib.qpc_tsurff_accumulate(None, 0, None, 0.05, None, 0) == 1
+    if torch.cuda.is_available():
+        return
+    with pytest.raises(q.QpcError) as e:
+        q.spectrum_c_pcs(6, 3, 2).initialize(32, 6, 4, kn, 0.2, 1.0, 0.0, 3.0, 0.0, 6.0, 1.0, tables=t)
+    assert e.value.code == 8
+    with pytest.raises(q.QpcError) as e:
+        q.spectrum_c_tsf(6, 3, 2).initialize(32, 6, 4, kn, 12.0, 0.0, 0.2, 1.0, 0.0, 3.0, 0.0, 6.0, n_inst=2, tables=ts)
+    assert e.value.code == 8
