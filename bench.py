@@ -32,6 +32,9 @@ oracle port: the reference itself needs x86 and MKL) on all host cores.
 --workload c3arn the same grids with the Arnoldi propagator (one handle and host thread each).
 --workload c3a times the Arnoldi propagator (k_max = 12, dt = 0.1) on --batch wavefunctions
 with their own screened potentials on the N_r = 800, n_l = 41 grid.
+--workload pcs times the PCS momentum distribution (measure_prj) of 256 resident wavefunctions
+(500 |k| x 181 theta, Coulomb waves); --workload tsurff the t-SURFF accumulation after each step
+for the same batch and momenta.
 --workload c1 measures the single large velocity-gauge elliptical instance over a
 window of steps around the pulse peak (a whole 6-cycle pulse at 1800 nm is ~24k steps):
 screened Coulomb V = -(1 + 17 e^{-2r})/r, B-splines order 8 (p = 7), N_r = 2000 on
@@ -504,6 +507,144 @@ def run_c3(args):
     }
 
 
+def _random_states(B, n_l, n_r, seed):
+    """seeded wavefunctions with a decaying radial envelope, S-norm irrelevant to the spectra's cost"""
+    rng = np.random.default_rng(seed)
+    env = np.exp(-np.arange(n_r) / 200.0)
+    return (rng.standard_normal((B, 1, n_l, n_r)) + 1j * rng.standard_normal((B, 1, n_l, n_r))) * env
+
+
+def _pcs_cpu_baseline(tables, states, budget_s):
+    """CPU baseline leg: the oracle's measure_prj, one wavefunction at a time, for about budget_s"""
+    from oracle import momentum_oracle as mo
+    o = {k: tables[k] for k in ("kr", "ijl", "plm", "exm", "cps")}
+    t0 = time.perf_counter()
+    n = 0
+    while time.perf_counter() - t0 < budget_s or n == 0:
+        mo.pcs_measure(o, states[n % len(states)], 0)
+        n += 1
+    return n / (time.perf_counter() - t0), n
+
+
+def _tsurff_cpu_baseline(tables, state, dt, budget_s):
+    """CPU baseline leg: the oracle's accumulate(az0, az1, dt, coef) on one wavefunction for about budget_s"""
+    from oracle import momentum_oracle as mo
+    ors = mo.Tsurff(tables, state.shape[1], state.shape[0], 0)
+    t0 = time.perf_counter()
+    n = 0
+    while time.perf_counter() - t0 < budget_s or n == 0:
+        ors.accumulate(state, dt, (0.01, 0.011))
+        n += 1
+    return n / (time.perf_counter() - t0), n
+
+
+def run_pcs(args):
+    """PCS momentum distribution (spectrum_c_pcs::measure_prj) of a resident batch: 256 wavefunctions of
+    the batched-scan grid (N_r = 800 on [0, 400], p = 6, l < 41), hydrogenic Coulomb waves, |k| in
+    [0.005, 2.5] (500 points), theta_k in [0, pi] (181 points), one phi_k."""
+    import importlib
+    q = importlib.import_module("qpc-tdse-cpc_gb300")
+    B, n_r, p, n_l = args.batch, 800, 6, 41
+    nkr, nkt, nkp = 500, 181, 1
+    t = q.linear_knots(n_r, p, 0.0, 400.0)
+    S, R, _, _, H = q.radial_setup(n_r, p, n_l, t)
+    t0 = time.perf_counter()
+    pcs = q.spectrum_c_pcs(nkr, nkt, nkp).initialize(n_r, p, n_l, t, 0.005, 2.5, 0.0, np.pi, 0.0, 0.0, 1.0)
+    setup_s = time.perf_counter() - t0
+    states = _random_states(B, n_l, n_r, 11)
+    prop = q.propagator_cn_hc_lgwz().initialize(n_r, p, n_l, S, R, H, 0.05, n_inst=B)
+    prop.put(states)
+    K, W = min(args.steps, 10), args.warmup
+    for _ in range(W):
+        pcs.measure_prj(prop)
+    with Clocks() as clk:
+        dev = []
+        for _ in range(K):
+            pcs.measure_prj(prop)
+            dev.append(pcs.last_run_ms())
+        t0 = time.perf_counter()
+        for _ in range(K):
+            out = pcs.measure_prj(states)          # host buffers in and out, copies inside
+        e2e_s = (time.perf_counter() - t0) / K
+    dev_ms = float(np.mean(dev))
+    nch = n_l
+    fl_proj = 4.0 * nkr * B * nch * n_r
+    fl_out = B * nkr * nkt * nkp * (4.0 * nch + 8.0)
+    tfl = (fl_proj + fl_out) / (dev_ms * 1e-3) / 1e12
+    cpu_rate, n_cpu = _pcs_cpu_baseline(pcs.tables, states, min(args.cpu_seconds, 10.0))
+    return {
+        "metric": "wavefunctions/s (PCS momentum distribution measure_prj, 500 x 181 momenta)",
+        "value": B / (dev_ms * 1e-3), "unit": "wavefunctions/s", "n_gpus": 1, "steps": K, "warmup": W,
+        "ms_per_step": dev_ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "c128 (complex FP64)", "data": "synthetic (seeded wavefunctions, numpy default_rng(11))",
+        "config": {"workload": "PCS: %d wavefunctions, N_r=800 on [0,400], p=6, l<41, zc=1, |k| in [0.005,2.5] x 500, "
+                               "theta in [0,pi] x 181, one phi" % B, "inputs": "resident batch (134 MB) > L2"},
+        "e2e": {"value": B / e2e_s, "unit": "wavefunctions/s", "h2d_bytes_per_step": int(states.nbytes),
+                "d2h_bytes_per_step": int(out.nbytes)},
+        "gpu_launches": 2 * K,
+        "roofline": {"bound": "fp64", "kernel": "k_pcs_proj + k_pcs_out (one measurement)", "achieved": tfl,
+                     "peak": FP64_PEAK_TFLOPS, "unit": "TFLOP/s", "frac": tfl / FP64_PEAK_TFLOPS,
+                     "flops_per_launch": fl_proj + fl_out, "flops_projection": fl_proj},
+        "cpu_baseline": {"value": cpu_rate, "unit": "wavefunctions/s", "cores": os.cpu_count(), "kind": "port",
+                         "sample": "%d wavefunctions through the numpy oracle of measure_prj (numpy's BLAS may use every host core)" % n_cpu},
+        "tables_setup_s": setup_s, "clocks": clk.summary(),
+    }
+
+
+def run_tsurff(args):
+    """t-SURFF accumulation after every step (spectrum_c_tsf::accumulate(az0, az1, dt, coef), the
+    driver's call at sphTDSE.cpp:800) for 256 wavefunctions of the batched-scan grid: surface r0 = 200,
+    zc = 0, |k| in [0.005, 2.5] (500 points), theta_k in [0, pi] (181 points), one phi_k."""
+    import importlib
+    q = importlib.import_module("qpc-tdse-cpc_gb300")
+    B, n_r, p, n_l, dt = args.batch, 800, 6, 41, 0.05
+    nkr, nkt, nkp = 500, 181, 1
+    kn = q.linear_knots(n_r, p, 0.0, 400.0)
+    S, R, H, c0 = setup_grid(q, n_r, p, n_l)
+    inten, lam_nm, cep, cyc = c2_workload(B)
+    tabs, nt = field_tables(q, inten, lam_nm, cep, cyc, dt)
+    K, W = min(args.steps, 100), args.warmup
+    ftab = np.stack([tb[:W + K + 1] for tb in tabs])
+    tsf = q.spectrum_c_tsf(nkr, nkt, nkp).initialize(n_r, p, n_l, kn, 200.0, 0.0, 0.005, 2.5, 0.0, np.pi, 0.0, 0.0, n_inst=B)
+    prop = q.propagator_cn_hc_lgwz().initialize(n_r, p, n_l, S, R, H, dt, n_inst=B)
+    prop.put(_random_states(B, n_l, n_r, 12))
+    for i in range(W):
+        prop.propagate(ftab[:, i], ftab[:, i + 1])
+        tsf.accumulate(prop, dt, np.stack([ftab[:, i], ftab[:, i + 1]], 1))
+    with Clocks() as clk:
+        acc_ms = []
+        t0 = time.perf_counter()
+        for i in range(W, W + K):
+            prop.propagate(ftab[:, i], ftab[:, i + 1])
+            tsf.accumulate(prop, dt, np.stack([ftab[:, i], ftab[:, i + 1]], 1))
+            acc_ms.append(tsf.last_run_ms())
+        loop_s = (time.perf_counter() - t0) / K
+    ms = float(np.mean(acc_ms))
+    fl_w = 4.0 * B * nkr * nkt * n_l
+    fl = fl_w + B * nkr * n_l * 30.0 + B * nkr * nkt * nkp * 30.0
+    tfl = fl / (ms * 1e-3) / 1e12
+    w, _ = tsf.get()
+    cpu_rate, n_cpu = _tsurff_cpu_baseline(tsf.tables, _random_states(1, n_l, n_r, 13)[0], dt, min(args.cpu_seconds, 10.0))
+    return {
+        "metric": "wf-steps/s (t-SURFF accumulate, 500 x 181 momenta per wavefunction)",
+        "value": B / (ms * 1e-3), "unit": "wf-steps/s", "n_gpus": 1, "steps": K, "warmup": W,
+        "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "c128 (complex FP64)", "data": "synthetic (seeded wavefunctions and laser parameters)",
+        "config": {"workload": "t-SURFF: %d wavefunctions, N_r=800 on [0,400], p=6, l<41, r0=200, zc=0, |k| in [0.005,2.5] x 500, "
+                               "theta in [0,pi] x 181, one phi, length-gauge propagator step + accumulate per step" % B,
+                   "inputs": "resident batch (134 MB) and spectra (370 MB) > L2"},
+        "with_propagation": {"value": B / loop_s, "unit": "wf-steps/s",
+                             "note": "host loop of propagate(f_i, f_i+1) + accumulate per step, wall clock"},
+        "gpu_launches": 5 * K,
+        "roofline": {"bound": "fp64", "kernel": "k_ts_w (l-sum against Y_lm) + k_ts_u + k_ts_acc", "achieved": tfl,
+                     "peak": FP64_PEAK_TFLOPS, "unit": "TFLOP/s", "frac": tfl / FP64_PEAK_TFLOPS,
+                     "flops_per_launch": fl, "flops_l_sum": fl_w},
+        "cpu_baseline": {"value": cpu_rate, "unit": "wf-steps/s", "cores": os.cpu_count(), "kind": "port",
+                         "sample": "%d accumulates of one wavefunction through the numpy oracle (numpy's BLAS may use every host core)" % n_cpu},
+        "finite": bool(np.isfinite(w).all()), "clocks": clk.summary(),
+    }
+
+
 def cpu_baseline(q, S, R, H, c0, ftab, dt, n_l, budget_s=15.0, threads=None):
     """The CPU oracle (port of the reference's propagator_cn_hc_lgwz), one
     wavefunction per host thread, on a bounded number of steps of the same workload."""
@@ -561,7 +702,7 @@ def main():
     ap.add_argument("--batch", type=int, default=256)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", default="c2", choices=["c2", "c0", "c1", "c3", "c3a", "c3arn"])
+    ap.add_argument("--workload", default="c2", choices=["c2", "c0", "c1", "c3", "c3a", "c3arn", "pcs", "tsurff"])
     args = ap.parse_args()
     if args.workload == "c0":
         print(json.dumps(run_c0(args)))
@@ -577,6 +718,12 @@ def main():
         return
     if args.workload == "c3arn":
         print(json.dumps(run_c3arn(args)))
+        return
+    if args.workload == "pcs":
+        print(json.dumps(run_pcs(args)))
+        return
+    if args.workload == "tsurff":
+        print(json.dumps(run_tsurff(args)))
         return
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))

@@ -420,6 +420,9 @@ int qpc_lgwz_tsurff(qpc_lgwz* prop, qpc_tsurff* h, int32_t mode, const double* a
 int qpc_vgwr_tsurff(qpc_vgwr* prop, qpc_tsurff* h, int32_t mode, const double* a, double dt);
 /* work[inst][kr][kt][kp] complex128 (host); clock[inst][4] = (time, disx, disy, disz) when not NULL */
 int qpc_tsurff_get(qpc_tsurff* h, double* work, double* clock);
+/* device time (CUDA events around the kernels) of the last qpc_pcs_measure / accumulate call */
+int qpc_pcs_last_run(qpc_pcs* h, float* ms);
+int qpc_tsurff_last_run(qpc_tsurff* h, float* ms);
 
 #ifdef __cplusplus
 }

@@ -43,7 +43,7 @@ EXPORTS = (
     "qpc_mask_band", "qpc_lgwz_mask", "qpc_lgwz_dims", "qpc_vgwr_dims", "qpc_coulomb_f", "qpc_coulomb_sigma",
     "qpc_sph_legendre", "qpc_pcs_tables", "qpc_tsurff_tables", "qpc_pcs_create", "qpc_pcs_destroy", "qpc_pcs_measure",
     "qpc_lgwz_pcs", "qpc_tsurff_create", "qpc_tsurff_destroy", "qpc_tsurff_clear", "qpc_tsurff_accumulate",
-    "qpc_lgwz_tsurff", "qpc_vgwr_tsurff", "qpc_tsurff_get",
+    "qpc_lgwz_tsurff", "qpc_vgwr_tsurff", "qpc_tsurff_get", "qpc_pcs_last_run", "qpc_tsurff_last_run",
 )
 SPEC_LMD, SPEC_PMD, SPEC_PAD = 0, 1, 2
 TSURFF_FREE, TSURFF_Z, TSURFF_XY = 0, 1, 2
@@ -171,6 +171,8 @@ def load(path=None):
         "qpc_lgwz_tsurff": (ctypes.c_int, [P, P, i32, P, d]),
         "qpc_vgwr_tsurff": (ctypes.c_int, [P, P, i32, P, d]),
         "qpc_tsurff_get": (ctypes.c_int, [P, P, P]),
+        "qpc_pcs_last_run": (ctypes.c_int, [P, P]),
+        "qpc_tsurff_last_run": (ctypes.c_int, [P, P]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -910,6 +912,12 @@ class spectrum_c_pcs:
         """[inst][kr][kt] (measure_pad, momentum_1e.hpp:358-383)"""
         return self._measure(SPEC_PAD, coef)
 
+    def last_run_ms(self):
+        """device time of the last measurement's kernels"""
+        ms = ctypes.c_float(0)
+        _check(load().qpc_pcs_last_run(self._h, ctypes.byref(ms)))
+        return ms.value
+
 
 class spectrum_c_tsf:
     """t-SURFF momentum spectra on the GPU (spectrum_c_tsf, spherical/spectrum/momentum_1e.hpp:516-1072)
@@ -970,6 +978,12 @@ class spectrum_c_tsf:
         else:
             c = np.ascontiguousarray(coef, dtype=np.complex128).reshape(self.shape)
             _check(lib.qpc_tsurff_accumulate(self._h, mode, _ptr(av), dt, _ptr(c), 0))
+
+    def last_run_ms(self):
+        """device time of the last accumulate's kernels"""
+        ms = ctypes.c_float(0)
+        _check(load().qpc_tsurff_last_run(self._h, ctypes.byref(ms)))
+        return ms.value
 
     def get(self):
         """(work [inst][kr][kt][kp] complex, clock [inst][4] = time, disx, disy, disz)"""

@@ -34,12 +34,12 @@ __device__ __forceinline__ double2 csub(double2 a, double2 b) { return make_doub
 __device__ __forceinline__ double2 cscale(double2 a, double s) { return make_double2(a.x * s, a.y * s); }
 
 // ---------------------------------------------------------------- PCS projector
-// Q[inst][kr][ch] = sum_r ijl[l][r][kr] c[inst][ch][r] for a block of PG instances, one
+// Q[inst][kr][ch] = cps[kr][l] sum_r ijl[l][r][kr] c[inst][ch][r] for a block of PG instances, one
 // channel ch = im n_l + il (l = |m| + il) and 128 consecutive kr; the radial vectors of the
 // block's instances are staged in shared memory chunk by chunk.
 constexpr int PG = 8, PCH = 128;
-__global__ void __launch_bounds__(128) k_pcs_proj(const double* __restrict__ ijlT, const double2* __restrict__ c, double2* __restrict__ Q,
-	int nkr, int n_r, int n_l, int m0, int nch, int n_inst)
+__global__ void __launch_bounds__(128) k_pcs_proj(const double* __restrict__ ijlT, const double2* __restrict__ cps, const double2* __restrict__ c,
+	double2* __restrict__ Q, int nkr, int n_r, int n_l, int m0, int nch, int nl_tot, int n_inst)
 {
 	__shared__ double2 cs[PG][PCH];
 	const int kr = blockIdx.x * 128 + threadIdx.x;
@@ -65,26 +65,27 @@ __global__ void __launch_bounds__(128) k_pcs_proj(const double* __restrict__ ijl
 			}
 		}
 	}
-	if (kr < nkr)
+	if (kr < nkr) {
+		const double2 cp = cps[(size_t)kr * nl_tot + l];
 		for (int g = 0; g < PG; ++g)
-			if (i0 + g < n_inst) Q[((size_t)(i0 + g) * nkr + kr) * nch + ch] = acc[g];
+			if (i0 + g < n_inst) Q[((size_t)(i0 + g) * nkr + kr) * nch + ch] = cmul(cp, acc[g]);
+	}
 }
 
-// LMD[inst][kr][ch] = Q (cps[kr][l] sqrt(2/pi))                      (measure_lmd, 386-403)
-// PMD[inst][kr][kt][kp] = sqrt(2/pi) sum_ch plm exm cps Q             (measure_prj, 337-355)
-// PAD[inst][kr][kt] = 2 sqrt(kr) sum_ch plm cps Q                     (measure_pad, 358-383)
+// With Q = cps <ijl|c> from k_pcs_proj:
+// LMD[inst][kr][ch] = sqrt(2/pi) Q                                   (measure_lmd, 386-403)
+// PMD[inst][kr][kt][kp] = sqrt(2/pi) sum_m exm[kp][m] sum_l plm Q     (measure_prj, 337-355)
+// PAD[inst][kr][kt] = 2 sqrt(kr) sum_m sum_l plm Q                    (measure_pad, 358-383)
+// The l-sums are real x complex; the reference's per-term product plm exm cps <ijl|c> is the same
+// sum regrouped.
 __global__ void k_pcs_out(int kind, const double2* __restrict__ Q, const double* __restrict__ plm, const double2* __restrict__ exm,
-	const double2* __restrict__ cps, const double* __restrict__ kr, double2* __restrict__ out, int nkr, int nkt, int nkp, int n_l, int n_m,
-	int m0, int nl_tot, long total)
+	const double* __restrict__ kr, double2* __restrict__ out, int nkr, int nkt, int nkp, int n_l, int n_m, long total)
 {
 	const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
 	if (idx >= total) return;
 	const int nch = n_m * n_l;
 	if (kind == QPC_SPEC_LMD) {
-		const int ch = (int)(idx % nch);
-		const long ikr = (idx / nch) % nkr;
-		const int l = abs(m0 + ch / n_l) + ch % n_l;
-		out[idx] = cmul(Q[idx], cscale(cps[ikr * nl_tot + l], SQRT_2_OVER_PI));
+		out[idx] = cscale(Q[idx], SQRT_2_OVER_PI);
 		return;
 	}
 	const int per_kr = kind == QPC_SPEC_PMD ? nkt * nkp : nkt;
@@ -92,16 +93,17 @@ __global__ void k_pcs_out(int kind, const double2* __restrict__ Q, const double*
 	const long ikr = (idx / per_kr) % nkr, inst = idx / ((long)per_kr * nkr);
 	const int kt = kind == QPC_SPEC_PMD ? ia / nkp : ia, kp = kind == QPC_SPEC_PMD ? ia % nkp : 0;
 	const double2* q = Q + (inst * nkr + ikr) * nch;
+	const double* pl = plm + (size_t)kt * nch;
 	double2 tmp = make_double2(0.0, 0.0);
 	for (int im = 0; im < n_m; ++im) {
-		const double2 e = exm[(size_t)kp * n_m + im];
+		double2 v = make_double2(0.0, 0.0);
 		for (int il = 0; il < n_l; ++il) {
-			const int ch = im * n_l + il, l = abs(m0 + im) + il;
-			const double p = plm[((size_t)kt * n_m + im) * n_l + il];
-			const double2 cp = cps[ikr * nl_tot + l];
-			double2 t = kind == QPC_SPEC_PMD ? cmul(cmul(cscale(e, p), cp), q[ch]) : cmul(cscale(cp, p), q[ch]);
-			tmp = cadd(tmp, t);
+			const double p = pl[im * n_l + il];
+			const double2 x = q[im * n_l + il];
+			v.x += p * x.x;
+			v.y += p * x.y;
 		}
+		tmp = kind == QPC_SPEC_PMD ? cadd(tmp, cmul(exm[(size_t)kp * n_m + im], v)) : cadd(tmp, v);
 	}
 	out[idx] = kind == QPC_SPEC_PMD ? cscale(tmp, SQRT_2_OVER_PI) : cscale(tmp, sqrt(kr[ikr]) * 2.0);
 }
@@ -239,6 +241,8 @@ struct qpc_pcs {
 	qpc_dims d{};
 	int nkr = 0, nkt = 0, nkp = 0, nl = 0;
 	cudaStream_t st = nullptr;
+	cudaEvent_t ev0 = nullptr, ev1 = nullptr;	// bracket the kernels of the last measurement
+	float last_ms = 0.f;
 	double *ijlT = nullptr, *plm = nullptr, *kr = nullptr;
 	double2 *exm = nullptr, *cps = nullptr;
 	double2 *cbuf = nullptr, *Q = nullptr, *out = nullptr;
@@ -250,6 +254,8 @@ struct qpc_tsurff {
 	qpc_dims d{};
 	int nkr = 0, nkt = 0, nkp = 0, nl = 0, nb = 0, B = 0;
 	cudaStream_t st = nullptr;
+	cudaEvent_t ev0 = nullptr, ev1 = nullptr;	// bracket the kernels of the last accumulate
+	float last_ms = 0.f;
 	int* ib = nullptr;
 	double *b0 = nullptr, *br = nullptr, *j0 = nullptr, *jr = nullptr, *y0T = nullptr, *pm = nullptr;
 	double *kr = nullptr, *coskt = nullptr, *sinkt = nullptr, *coskp = nullptr, *sinkp = nullptr;
@@ -267,6 +273,8 @@ void pcs_free(qpc_pcs* h)
 	cudaSetDevice(h->dev);
 	void* ps[] = {h->ijlT, h->plm, h->kr, h->exm, h->cps, h->cbuf, h->Q, h->out};
 	for (void* p : ps) if (p) cudaFree(p);
+	if (h->ev0) cudaEventDestroy(h->ev0);
+	if (h->ev1) cudaEventDestroy(h->ev1);
 	if (h->st) cudaStreamDestroy(h->st);
 	delete h;
 }
@@ -278,6 +286,8 @@ void ts_free(qpc_tsurff* h)
 	void* ps[] = {h->ib, h->b0, h->br, h->j0, h->jr, h->y0T, h->pm, h->kr, h->coskt, h->sinkt, h->coskp, h->sinkp, h->e0, h->temp, h->temq,
 		h->U, h->W, h->work, h->cbuf, h->dclock, h->da1};
 	for (void* p : ps) if (p) cudaFree(p);
+	if (h->ev0) cudaEventDestroy(h->ev0);
+	if (h->ev1) cudaEventDestroy(h->ev1);
 	if (h->st) cudaStreamDestroy(h->st);
 	delete h;
 }
@@ -302,13 +312,17 @@ int pcs_run(qpc_pcs* h, int kind, const double2* c, int n_inst, double* out)
 		: kind == QPC_SPEC_PMD ? (long)n_inst * h->nkr * h->nkt * h->nkp : (long)n_inst * h->nkr * h->nkt;
 	if (int rc = grow(&h->out, &h->cap_o, total)) return rc;
 	dim3 g1((h->nkr + 127) / 128, nch, (n_inst + PG - 1) / PG);
-	k_pcs_proj<<<g1, 128, 0, h->st>>>(h->ijlT, c, h->Q, h->nkr, d.n_r, d.n_l, d.m0, nch, n_inst);
+	QPC_CUDA(cudaEventRecord(h->ev0, h->st));
+	k_pcs_proj<<<g1, 128, 0, h->st>>>(h->ijlT, h->cps, c, h->Q, h->nkr, d.n_r, d.n_l, d.m0, nch, h->nl, n_inst);
 	QPC_CUDA(cudaGetLastError());
-	k_pcs_out<<<(unsigned)((total + 255) / 256), 256, 0, h->st>>>(kind, h->Q, h->plm, h->exm, h->cps, h->kr, h->out, h->nkr, h->nkt, h->nkp,
-		d.n_l, d.n_m, d.m0, h->nl, total);
+	k_pcs_out<<<(unsigned)((total + 255) / 256), 256, 0, h->st>>>(kind, h->Q, h->plm, h->exm, h->kr, h->out, h->nkr, h->nkt, h->nkp,
+		d.n_l, d.n_m, total);
 	QPC_CUDA(cudaGetLastError());
+	QPC_CUDA(cudaEventRecord(h->ev1, h->st));
 	QPC_CUDA(cudaMemcpyAsync(out, h->out, sizeof(double2) * total, cudaMemcpyDeviceToHost, h->st));
-	return wait_on(h->st);
+	if (int rc = wait_on(h->st)) return rc;
+	QPC_CUDA(cudaEventElapsedTime(&h->last_ms, h->ev0, h->ev1));
+	return QPC_OK;
 }
 
 // one accumulate on device wavefunctions c (host layout)
@@ -331,6 +345,7 @@ int ts_run(qpc_tsurff* h, int mode, const double* a, double dt, const double2* c
 	QPC_CUDA(cudaMemcpyAsync(h->dclock, h->clock.data(), sizeof(double) * 4 * B, cudaMemcpyHostToDevice, h->st));
 	QPC_CUDA(cudaMemcpyAsync(h->da1, a1.data(), sizeof(double) * 2 * B, cudaMemcpyHostToDevice, h->st));
 	const long nsurf = (long)B * nch;
+	QPC_CUDA(cudaEventRecord(h->ev0, h->st));
 	k_ts_prepare<<<(unsigned)((nsurf + 255) / 256), 256, 0, h->st>>>(c, h->ib, h->b0, h->br, h->nb, d.n_r, nsurf, h->temp, h->temq);
 	const long nu = (long)B * h->nkr * nch;
 	k_ts_u<<<(unsigned)((nu + 255) / 256), 256, 0, h->st>>>(mode, h->temp, h->temq, h->j0, h->jr, h->pm, h->pm + nch, h->pm + 2 * nch, h->da1,
@@ -342,7 +357,10 @@ int ts_run(qpc_tsurff* h, int mode, const double* a, double dt, const double2* c
 	k_ts_acc<<<(unsigned)((na + 255) / 256), 256, 0, h->st>>>(mode, h->W, h->e0, h->kr, h->coskt, h->sinkt, h->coskp, h->sinkp, h->dclock, dt,
 		h->nkr, h->nkt, h->nkp, d.n_m, na, h->work);
 	QPC_CUDA(cudaGetLastError());
-	return wait_on(h->st);
+	QPC_CUDA(cudaEventRecord(h->ev1, h->st));
+	if (int rc = wait_on(h->st)) return rc;
+	QPC_CUDA(cudaEventElapsedTime(&h->last_ms, h->ev0, h->ev1));
+	return QPC_OK;
 }
 
 }  // namespace
@@ -361,7 +379,8 @@ int qpc_pcs_create(const qpc_dims* dims, const qpc_kgrid* g, const double* kr, c
 	qpc_pcs* h = new qpc_pcs;
 	h->dev = dev; h->d = *dims; h->nkr = g->nkr; h->nkt = g->nkt; h->nkp = g->nkp; h->nl = lmax_of(*dims) + 1;
 	auto fail = [&](int r) { pcs_free(h); return r; };
-	if (cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking) != cudaSuccess) { set_error("stream creation failed"); return fail(QPC_ERR_CUDA); }
+	if (cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking) != cudaSuccess || cudaEventCreate(&h->ev0) != cudaSuccess ||
+		cudaEventCreate(&h->ev1) != cudaSuccess) { set_error("stream or event creation failed"); return fail(QPC_ERR_CUDA); }
 	const int n = dims->n_r, nl = h->nl, nk = g->nkr, nch = dims->n_m * dims->n_l;
 	std::vector<double> t((size_t)nl * n * nk);
 	for (int k = 0; k < nk; ++k)
@@ -427,7 +446,8 @@ int qpc_tsurff_create(const qpc_dims* dims, const qpc_kgrid* g, const double* kr
 	qpc_tsurff* h = new qpc_tsurff;
 	h->dev = dev; h->d = *dims; h->B = dims->n_inst; h->nkr = g->nkr; h->nkt = g->nkt; h->nkp = g->nkp; h->nb = nb; h->nl = lmax_of(*dims) + 1;
 	auto fail = [&](int r) { ts_free(h); return r; };
-	if (cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking) != cudaSuccess) { set_error("stream creation failed"); return fail(QPC_ERR_CUDA); }
+	if (cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking) != cudaSuccess || cudaEventCreate(&h->ev0) != cudaSuccess ||
+		cudaEventCreate(&h->ev1) != cudaSuccess) { set_error("stream or event creation failed"); return fail(QPC_ERR_CUDA); }
 	const int nch = dims->n_m * dims->n_l, B = h->B;
 	std::vector<int> ibv(ib, ib + nb);
 	if ((rc = upload(&h->ib, nb ? ibv.data() : nullptr, nb))) return fail(rc);
@@ -510,6 +530,20 @@ int qpc_vgwr_tsurff(qpc_vgwr* prop, qpc_tsurff* h, int32_t mode, const double* a
 	QPC_CUDA(cudaSetDevice(h->dev));
 	if (int rc = qpc_vgwr_get_device(prop, (double*)h->cbuf)) return rc;
 	return qpc_tsurff_accumulate(h, mode, a, dt, (const double*)h->cbuf, 1);
+}
+
+int qpc_pcs_last_run(qpc_pcs* h, float* ms)
+{
+	if (!h || !ms) { set_error("NULL argument"); return QPC_ERR_ARGS; }
+	*ms = h->last_ms;
+	return QPC_OK;
+}
+
+int qpc_tsurff_last_run(qpc_tsurff* h, float* ms)
+{
+	if (!h || !ms) { set_error("NULL argument"); return QPC_ERR_ARGS; }
+	*ms = h->last_ms;
+	return QPC_OK;
 }
 
 int qpc_tsurff_get(qpc_tsurff* h, double* work, double* clock)
