@@ -132,6 +132,14 @@ typedef struct qpc_lgwz qpc_lgwz;
  * Errors: QPC_ERR_ARGS, QPC_ERR_NODEVICE, QPC_ERR_NOMEM, QPC_ERR_SINGULAR. */
 int qpc_lgwz_create(const qpc_dims* dims, double dt, const double* S, const double* R, const double* H, qpc_lgwz** out);
 
+/* The same with one potential per wavefunction when h_per_instance != 0: H is then
+ * [n_inst][lmax+1][n_r][p+1] and each instance gets its own field-free factorisation (the
+ * coupling step depends only on S and R, which the batch shares).  For batches that share a
+ * grid but not a potential, such as the screened-Coulomb atoms of a mixed batch
+ * (spherical/potential.hpp:19-29); the reference builds one propagator per potential. */
+int qpc_lgwz_create_ex(const qpc_dims* dims, double dt, const double* S, const double* R, const double* H, int32_t h_per_instance,
+	qpc_lgwz** out);
+
 /* Frees everything the handle owns.  NULL is accepted. */
 int qpc_lgwz_destroy(qpc_lgwz* h);
 

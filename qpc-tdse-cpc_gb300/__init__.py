@@ -44,6 +44,7 @@ EXPORTS = (
     "qpc_sph_legendre", "qpc_pcs_tables", "qpc_tsurff_tables", "qpc_pcs_create", "qpc_pcs_destroy", "qpc_pcs_measure",
     "qpc_lgwz_pcs", "qpc_tsurff_create", "qpc_tsurff_destroy", "qpc_tsurff_clear", "qpc_tsurff_accumulate",
     "qpc_lgwz_tsurff", "qpc_vgwr_tsurff", "qpc_tsurff_get", "qpc_pcs_last_run", "qpc_tsurff_last_run",
+    "qpc_lgwz_create_ex",
 )
 SPEC_LMD, SPEC_PMD, SPEC_PAD = 0, 1, 2
 TSURFF_FREE, TSURFF_Z, TSURFF_XY = 0, 1, 2
@@ -99,6 +100,7 @@ def load(path=None):
         "qpc_gen_eigen": (ctypes.c_int, [i32, i32, P, P, i32, P, P]),
         "qpc_field_sinen": (ctypes.c_int, [i32, d, d, d, d, d, d, i64, P, P]),
         "qpc_lgwz_create": (ctypes.c_int, [P, d, P, P, P, P]),
+        "qpc_lgwz_create_ex": (ctypes.c_int, [P, d, P, P, P, i32, P]),
         "qpc_lgwz_destroy": (ctypes.c_int, [P]),
         "qpc_lgwz_put": (ctypes.c_int, [P, P]),
         "qpc_lgwz_get": (ctypes.c_int, [P, P]),
@@ -361,15 +363,20 @@ class propagator_cn_hc_lgwz:
         self.dims = None
 
     def initialize(self, n_r, p, n_l, S, R, H, dt, n_m=1, m0=0, n_inst=1):
+        """H: [lmax+1][n_r][p+1] shared by the batch, or [n_inst][lmax+1][n_r][p+1] (own potentials)"""
         lib = load()
         self.close()
         d = qpc_dims(n_r, p, n_l, n_m, m0, n_inst)
         h = ctypes.c_void_p()
         S, R, H = _f64(S), _f64(R), _f64(H)
         lmax = max(abs(m0), abs(m0 + n_m - 1)) + n_l - 1
-        if H.shape[0] < lmax + 1:
+        per_inst = H.ndim == 4      # H[inst][l][r][k]: one potential per wavefunction (qpc_lgwz_create_ex)
+        if per_inst and H.shape[0] != n_inst:
+            raise QpcError(1, "H has %d potentials for %d instances" % (H.shape[0], n_inst))
+        if H.shape[-3] < lmax + 1:
             raise QpcError(1, "H needs lmax+1 = %d blocks" % (lmax + 1))
-        _check(lib.qpc_lgwz_create(ctypes.byref(d), dt, _ptr(S), _ptr(R), _ptr(H[:lmax + 1].copy()), ctypes.byref(h)))
+        Hc = _f64(H[:, :lmax + 1] if per_inst else H[:lmax + 1])
+        _check(lib.qpc_lgwz_create_ex(ctypes.byref(d), dt, _ptr(S), _ptr(R), _ptr(Hc), int(per_inst), ctypes.byref(h)))
         self._h = h
         self.dims = d
         self.shape = (n_inst, n_m, n_l, n_r)

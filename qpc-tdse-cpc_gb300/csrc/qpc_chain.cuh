@@ -54,9 +54,11 @@ struct chain_desc {
 	int a;		// applications this step (0 = inactive)
 };
 
+// ffmap (field-free chains only, optional): the instance whose own field-free factors a chain of
+// instance inst uses, at ffmap[inst] * ffstride; without it every instance shares one set.
 template <bool CPL>
 __device__ __forceinline__ chain_desc describe(long ch, long nchains, const int64_t* __restrict__ nta, long step, int jslot,
-	int B, int M, int m0, int N, int L, int np, int NE)
+	int B, int M, int m0, int N, int L, int np, int NE, const int* __restrict__ ffmap = nullptr, long ffstride = 0)
 {
 	chain_desc d{0, 0, 0};
 	if (ch >= nchains) return d;
@@ -76,7 +78,7 @@ __device__ __forceinline__ chain_desc describe(long ch, long nchains, const int6
 		long inst = im_inst / M;
 		int l = il + (m < 0 ? -m : m);
 		d.xoff = im_inst * (long)N * L + il;
-		d.foff = (long)l * N * NE;
+		d.foff = (long)l * N * NE + (ffmap ? (long)ffmap[inst] * ffstride : 0L);
 		d.a = step < nta[inst] ? 1 : 0;
 	}
 	return d;
@@ -102,7 +104,7 @@ template <int P, int G, bool CPL>
 __global__ void __launch_bounds__(128) k_chain(double2* __restrict__ X, double2* __restrict__ Wk,
 	const double2* __restrict__ fac, const double* __restrict__ S, const int64_t* __restrict__ nta,
 	long step, int jslot, int B, int M, int m0, int N, int L, int np, long chbase, long nchains,
-	const double* __restrict__ Fo = nullptr, double* __restrict__ obs = nullptr)
+	const double* __restrict__ Fo = nullptr, double* __restrict__ obs = nullptr, const int* __restrict__ ffmap = nullptr, long ffstride = 0)
 {
 	// chains [chbase, nchains) of this launch (an instance group); nchains is an end index.
 	// Fo/obs (coupling chains only, optional): obs[chain] = <z|F|z> of the chain's vector at
@@ -123,7 +125,7 @@ __global__ void __launch_bounds__(128) k_chain(double2* __restrict__ X, double2*
 	__shared__ int s_a[4][32];
 	const int wib = threadIdx.x >> 5;
 	if (lane < CPW) {
-		chain_desc d = describe<CPL>(ch0 + lane, nchains, nta, step, jslot, B, M, m0, N, L, np, NE);
+		chain_desc d = describe<CPL>(ch0 + lane, nchains, nta, step, jslot, B, M, m0, N, L, np, NE, ffmap, ffstride);
 		s_x[wib][lane] = d.xoff; s_f[wib][lane] = d.foff; s_a[wib][lane] = d.a;
 	}
 	__syncwarp();

@@ -392,7 +392,11 @@ struct qpc_lgwz {
 	double* R = nullptr;      // [N][P+1]
 	double* Vh = nullptr;     // [M][npair+1][L]
 	double* lamp = nullptr;   // [M][npair]
-	double2* ff = nullptr;    // field-free factors [nlh][N][P+1] (row form + 1/D)
+	double2* ff = nullptr;    // field-free factors [nlh][N][P+1] (row form + 1/D); [B][nlh][N][P+1] with hpi
+	int hpi = 0;              // one Hamiltonian (potential) per instance
+	int* ffmap = nullptr;     // device [B]: the instance whose factors a (sorted) instance uses, during a run
+	int* ffmap_id = nullptr;  // device [B]: identity
+	const int* ffmap_cur = nullptr;	// ffmap during a run, ffmap_id otherwise (NULL without hpi)
 	double2* st = nullptr;    // state, engine layout [B][M][N][L]
 	double2* eo = nullptr;    // eigen-basis state [B][M][N][L]
 	double2* wk = nullptr;    // per-chain work vector [B][M][N][L]
@@ -558,7 +562,8 @@ void launch_chain_g(qpc_lgwz* h, cudaStream_t st, int b0, double2* X, const doub
 	unsigned grid = (unsigned)((nwarps + 3) / 4);
 	bool ob = CPL && h->observing;
 	k_chain<P, G, CPL><<<grid, 128, h->chain_smem, st>>>(X, h->wk, fac, h->S, nta, step, jslot, h->B, h->M, h->d.m0,
-		h->N, h->L, h->npair, chbase, chbase + nch, ob ? h->obsF : nullptr, ob ? h->obs : nullptr);
+		h->N, h->L, h->npair, chbase, chbase + nch, ob ? h->obsF : nullptr, ob ? h->obs : nullptr,
+		CPL ? nullptr : h->ffmap_cur, (long)h->nlh * h->N * (h->P + 1));
 	LAUNCH(h);
 }
 
@@ -766,7 +771,7 @@ extern "C" {
 const char* qpc_last_error(void) { return g_err; }
 const char* qpc_version(void) { return "qpc-gb300 engine 1 (sm_103a, complex FP64)"; }
 
-int qpc_lgwz_create(const qpc_dims* dims, double dt, const double* S, const double* R, const double* H, qpc_lgwz** out)
+static int create_impl(const qpc_dims* dims, double dt, const double* S, const double* R, const double* H, int hpi, qpc_lgwz** out)
 {
 	if (!out) { set_error("out is NULL"); return QPC_ERR_ARGS; }
 	*out = nullptr;
@@ -780,7 +785,7 @@ int qpc_lgwz_create(const qpc_dims* dims, double dt, const double* S, const doub
 	if (int rc = check_device(&dev)) return rc;
 	auto* h = new (std::nothrow) qpc_lgwz();
 	if (!h) { set_error("host allocation"); return QPC_ERR_NOMEM; }
-	h->dev = dev; h->d = d; h->N = d.n_r; h->P = d.p; h->L = d.n_l; h->M = d.n_m; h->B = d.n_inst; h->dt = dt;
+	h->dev = dev; h->d = d; h->N = d.n_r; h->P = d.p; h->L = d.n_l; h->M = d.n_m; h->B = d.n_inst; h->dt = dt; h->hpi = hpi ? 1 : 0;
 	long mabs = std::max(std::labs((long)d.m0), std::labs((long)d.m0 + d.n_m - 1));
 	h->lmax = (int)(mabs + d.n_l - 1);
 	h->nlh = h->lmax + 1;
@@ -796,20 +801,23 @@ int qpc_lgwz_create(const qpc_dims* dims, double dt, const double* S, const doub
 		if (cudaStreamCreateWithFlags(&h->gs[g], cudaStreamNonBlocking) != cudaSuccess) { set_error("stream create"); return fail(QPC_ERR_CUDA); }
 		cudaEventCreateWithFlags(&h->gev[g], cudaEventDisableTiming);
 	}
-	// host setup: field-free LDL^T per l, Y10 eigensystems
-	std::vector<double2> ffh((size_t)N * NE * h->nlh);
+	// host setup: field-free LDL^T per l (per instance and l with hpi), Y10 eigensystems
+	const int nff = h->hpi ? h->B : 1;
+	std::vector<double2> ffh((size_t)N * NE * h->nlh * nff);
 	std::vector<double> Lrow((size_t)N * P * 2), Dinv((size_t)N * 2);
-	for (int l = 0; l < h->nlh; ++l) {
-		int bad = qpc_ldlt_csym(N, P, S, H + (size_t)l * N * NE, dt * 0.5, Lrow.data(), Dinv.data());
-		if (bad < 0) { set_error("ldlt arguments"); return fail(QPC_ERR_ARGS); }
-		if (bad > 0) { set_error("zero pivot factorising S + i dt/2 H_%d", l); return fail(QPC_ERR_SINGULAR); }
-		// row form per l: ff[l][r][c] = L(r, r-1-c), ff[l][r][P] = 1/D(r)
-		for (int r = 0; r < N; ++r) {
-			for (int c = 0; c < P; ++c)
-				ffh[((size_t)l * N + r) * NE + c] = make_double2(Lrow[2 * ((size_t)r * P + c)], Lrow[2 * ((size_t)r * P + c) + 1]);
-			ffh[((size_t)l * N + r) * NE + P] = make_double2(Dinv[2 * (size_t)r], Dinv[2 * (size_t)r + 1]);
+	for (int fi = 0; fi < nff; ++fi)
+		for (int l = 0; l < h->nlh; ++l) {
+			const size_t bl = (size_t)fi * h->nlh + l;
+			int bad = qpc_ldlt_csym(N, P, S, H + bl * N * NE, dt * 0.5, Lrow.data(), Dinv.data());
+			if (bad < 0) { set_error("ldlt arguments"); return fail(QPC_ERR_ARGS); }
+			if (bad > 0) { set_error("zero pivot factorising S + i dt/2 H_%d (instance %d)", l, fi); return fail(QPC_ERR_SINGULAR); }
+			// row form per l: ff[l][r][c] = L(r, r-1-c), ff[l][r][P] = 1/D(r)
+			for (int r = 0; r < N; ++r) {
+				for (int c = 0; c < P; ++c)
+					ffh[(bl * N + r) * NE + c] = make_double2(Lrow[2 * ((size_t)r * P + c)], Lrow[2 * ((size_t)r * P + c) + 1]);
+				ffh[(bl * N + r) * NE + P] = make_double2(Dinv[2 * (size_t)r], Dinv[2 * (size_t)r + 1]);
+			}
 		}
-	}
 	h->h_lam.assign((size_t)M * L, 0.0);
 	h->h_P.assign((size_t)M * L * L, 0.0);
 	std::vector<double> Vh((size_t)M * (np + 1) * L, 0.0), lamp((size_t)M * std::max(np, 1), 0.0);
@@ -851,6 +859,16 @@ int qpc_lgwz_create(const qpc_dims* dims, double dt, const double* S, const doub
 		set_error("initial device copies failed");
 		return fail(QPC_ERR_CUDA);
 	}
+	if (h->hpi) {
+		std::vector<int> id(h->B);
+		for (int k = 0; k < h->B; ++k) id[k] = k;
+		if ((rc = dalloc(&h->ffmap, h->B)) || (rc = dalloc(&h->ffmap_id, h->B))) return fail(rc);
+		if (cudaMemcpy(h->ffmap_id, id.data(), sizeof(int) * h->B, cudaMemcpyHostToDevice) != cudaSuccess) {
+			set_error("initial device copies failed");
+			return fail(QPC_ERR_CUDA);
+		}
+		h->ffmap_cur = h->ffmap_id;
+	}
 	size_t smem = sizeof(double2) * 2 * TR * (L | 1);
 	h->chain_smem = sizeof(double) * (size_t)N * NE;
 	if (h->chain_smem > 200 * 1024) { set_error("n_r=%d too large for the shared-memory S band", N); return fail(QPC_ERR_ARGS); }
@@ -861,11 +879,23 @@ int qpc_lgwz_create(const qpc_dims* dims, double dt, const double* S, const doub
 	return QPC_OK;
 }
 
+int qpc_lgwz_create(const qpc_dims* dims, double dt, const double* S, const double* R, const double* H, qpc_lgwz** out)
+{
+	return create_impl(dims, dt, S, R, H, 0, out);
+}
+
+int qpc_lgwz_create_ex(const qpc_dims* dims, double dt, const double* S, const double* R, const double* H, int32_t h_per_instance,
+	qpc_lgwz** out)
+{
+	return create_impl(dims, dt, S, R, H, h_per_instance, out);
+}
+
 int qpc_lgwz_destroy(qpc_lgwz* h)
 {
 	if (!h) return QPC_OK;
 	if (h->stream) cudaStreamSynchronize(h->stream);
 	cudaFree(h->S); cudaFree(h->R); cudaFree(h->Vh); cudaFree(h->lamp); cudaFree(h->ff);
+	cudaFree(h->ffmap); cudaFree(h->ffmap_id);
 	cudaFree(h->st); cudaFree(h->eo); cudaFree(h->wk); cudaFree(h->hostlay); cudaFree(h->fac);
 	cudaFree(h->status); cudaFree(h->red); cudaFree(h->ntf); cudaFree(h->ntt); cudaFree(h->ftab);
 	cudaFree(h->obsF); cudaFree(h->obs); cudaFree(h->dl); cudaFree(h->y10d); cudaFree(h->zdev);
@@ -979,6 +1009,12 @@ static int run_impl(qpc_lgwz* h, const double* ftab, int64_t ld, const int64_t* 
 	}
 	QPC_CUDA(cudaMemcpyAsync(h->ntf, pf.data(), sizeof(int64_t) * B, cudaMemcpyHostToDevice, h->stream));
 	QPC_CUDA(cudaMemcpyAsync(h->ntt, pt.data(), sizeof(int64_t) * B, cudaMemcpyHostToDevice, h->stream));
+	// own potentials: the sorted instance k uses the field-free factors of instance perm[k]
+	struct map_restore { qpc_lgwz* h; ~map_restore() { if (h->hpi) h->ffmap_cur = h->ffmap_id; } } mr{h};
+	if (h->hpi) {
+		QPC_CUDA(cudaMemcpyAsync(h->ffmap, perm.data(), sizeof(int) * B, cudaMemcpyHostToDevice, h->stream));
+		h->ffmap_cur = h->ffmap;
+	}
 	QPC_CUDA(cudaMemsetAsync(h->status, 0, sizeof(int), h->stream));
 	if (!ident) if (int rc = permute_instances(h, perm, false)) return rc;
 	h->ld = anyfield ? (long)ld : 0;

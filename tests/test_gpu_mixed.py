@@ -70,3 +70,40 @@ def test_run_many_reports_the_failing_handle(q):
     f_bad[0, 3] = np.nan
     with pytest.raises(q.QpcError, match="handle 1"):
         q.run_many(props, [f, f_bad], [10, 10])
+
+
+def test_own_potentials_in_one_handle(q, oracle):
+    """five wavefunctions on one grid, each with its own screened potential and pulse (uneven step
+    counts), in one handle (qpc_lgwz_create_ex): each against the oracle with its own Hamiltonian;
+    the single-step path (propagate) against a run of the same steps"""
+    rng = np.random.default_rng(77)
+    n_r, n_l, B = 400, 21, 5
+    insts = [instance(q, rng, n_r, n_l) for _ in range(B)]
+    S, R = insts[0][0], insts[0][1]
+    H = np.stack([x[2] for x in insts])
+    c0 = np.stack([x[3] for x in insts])
+    tabs, nts = [], []
+    for k in range(B):
+        f = pulse(q, rng, nc=2, lam=400.0 + 40.0 * k)
+        tabs.append(f)
+        nts.append(min(f.size - 1, 300 + 37 * k))
+    ld = max(t.size for t in tabs)
+    ftab = np.zeros((B, ld))
+    for k, t in enumerate(tabs):
+        ftab[k, :t.size] = t
+    pr = q.propagator_cn_hc_lgwz().initialize(n_r, 6, n_l, S, R, H, DT, n_inst=B)
+    pr.put(c0)
+    pr.run(ftab, nts, [n + 20 for n in nts])
+    out = pr.get()
+    for k in range(B):
+        g = oracle.grid(S, R, H[k], DT, n_l)
+        ref = oracle.run(g, c0[k].reshape(1, -1), ftab[k:k + 1], [nts[k]], [nts[k] + 20], threads=4)
+        assert rel_l2(out[k].reshape(-1), ref[0]) < 1e-10, k
+    # one step through propagate() uses each instance's own factors too
+    pr.put(c0)
+    pr.propagate(ftab[:, 0], ftab[:, 1])
+    one = pr.get()
+    for k in range(B):
+        g = oracle.grid(S, R, H[k], DT, n_l)
+        ref = oracle.step(g, c0[k].reshape(1, -1), ftab[k, 0], ftab[k, 1])
+        assert rel_l2(one[k].reshape(-1), ref[0]) < 1e-12, k
