@@ -382,6 +382,15 @@ int qpc_sph_legendre(int32_t lmax, double x, double* out);
 int qpc_pcs_tables(const qpc_dims* dims, const double* knots, const qpc_kgrid* grid, double zc, double rb,
 	double* kr, double* kt, double* kp, double* ijl, double* plm, double* exm, double* cps);
 
+/* spectrum_c_pcs::initialize with numerical partial waves (momentum_1e.hpp:487-512, initialize_kr
+ * 150-188), the projection the reference's driver uses for screened potentials: for
+ * V = -(zc + zs e^{-sigma r})/r (pot; QPC_POTENTIAL_HYDROGENIC gives zs = 0) and mass 1, the regular
+ * solution u_l(kr) of the radial equation, normalised to cos(delta) F_l + sin(delta) G_l with the
+ * Coulomb functions of charge zc, replaces F_l in ijl, and cps[kr][l] = e^{i (Delta_l - l pi/2)} with
+ * Delta_l = delta_l + sigma_l.  Same layouts as qpc_pcs_tables. */
+int qpc_pcs_tables_numeric(const qpc_dims* dims, const double* knots, const qpc_kgrid* grid, const qpc_potential* pot,
+	double* kr, double* kt, double* kp, double* ijl, double* plm, double* exm, double* cps);
+
 /* spectrum_c_tsf::initialize (momentum_1e.hpp:778-866) at the surface r0 with Coulomb
  * correction zc: axes as above; the nb <= p+1 splines non-zero at r0 (ib active index,
  * b0 value, br derivative); j0[kr][l] = F_l(-zc/k, k r0)/k, jr[kr][l] = F'_l(-zc/k, k r0);

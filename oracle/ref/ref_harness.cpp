@@ -44,7 +44,8 @@
 //       (eigenstate_sph::initialize + projection, population_1e.hpp:29-118).
 //   pcs    OUT RMAX DT ZC ZS SG COEF KRMIN KRMAX THMIN THMAX PHMIN PHMAX PZC RB FLAG
 //   tsurff OUT RMAX DT ZC ZS SG INIT FIELD NT NFREE MODE R0 TZC KRMIN KRMAX THMIN THMAX PHMIN PHMAX FLAG
-//       momentum spectra (spectrum/momentum_1e.hpp); see cmd_pcs and cmd_tsurff.
+//   pcsnum OUT RMAX DT ZC ZS SG COEF KRMIN KRMAX THMIN THMAX PHMIN PHMAX FLAG
+//       momentum spectra (spectrum/momentum_1e.hpp); see cmd_pcs, cmd_tsurff and cmd_pcsnum.
 #include <spherical/inventory.h>
 #include <omp.h>
 #include <string>
@@ -438,6 +439,46 @@ static int cmd_pcs(int argc, char** argv)
 	return 0;
 }
 
+//   pcsnum OUT RMAX DT ZC ZS SG COEF KRMIN KRMAX THMIN THMAX PHMIN PHMAX FLAG
+//       spectrum_c_pcs::initialize with the numerical partial waves of V = -(ZC + ZS e^{-SG r})/r
+//       (generate_odefun_from_potential, the driver's choice for screened potentials,
+//       binsrc/sphTDSE.cpp:313-316, 340-342), then the three measurements of COEF.
+static int cmd_pcsnum(int argc, char** argv)
+{
+	if (argc < 16) return 1;
+	std::string out = argv[2];
+	double rmax = atof(argv[3]);
+	double zc = atof(argv[5]), zs = atof(argv[6]), sg = atof(argv[7]);
+	const char* cf = argv[8];
+	double krmin = atof(argv[9]), krmax = atof(argv[10]), thmin = atof(argv[11]), thmax = atof(argv[12]);
+	double phmin = atof(argv[13]), phmax = atof(argv[14]);
+	int flag = atoi(argv[15]);
+	omp_set_num_threads(1);
+	auto radi = integrator_radi<dims_t>();
+	radi.initialize(0.0, rmax);
+	auto coef = coefficient<dims_t>();
+	auto v = slurp(cf, 2 * dims_t::n_leng);
+	std::memcpy((double*)coef.data, v.data(), sizeof(double) * v.size());
+	coefficient_view<dims_t> view{coef.data};
+	auto* pcs = new spectrum_c_pcs<dims_t, HNKR, HNKT, HNKP>();
+	if (zs != 0.0) {
+		auto odef = generate_odefun_from_potential(hydrogenic_yukawa{zc, zs, sg}, 1.0);
+		pcs->initialize(radi, krmin, krmax, thmin, thmax, phmin, phmax, odef, flag);
+	} else {
+		auto odef = generate_odefun_from_potential(hydrogenic{zc}, 1.0);
+		pcs->initialize(radi, krmin, krmax, thmin, thmax, phmin, phmax, odef, flag);
+	}
+	dump(out, "kr", pcs->kr, HNKR);
+	dump(out, "ijl", pcs->ijl.data, pcs->ijl.dim.n_leng);
+	dump(out, "cps", pcs->cps.data, 2 * pcs->cps.dim.n_leng);
+	pcs->measure_lmd(view, 1);
+	dump(out, "lmd", pcs->dptr(), 2 * pcs->size());
+	pcs->measure_prj(view, 1);
+	dump(out, "pmd", pcs->dptr(), 2 * pcs->size());
+	delete pcs;
+	return 0;
+}
+
 //   tsurff OUT RMAX DT ZC ZS SG INIT FIELD NT NFREE MODE R0 TZC KRMIN KRMAX THMIN THMAX PHMIN PHMAX FLAG
 //       spectrum_c_tsf::initialize at R0 with Coulomb correction TZC (momentum_1e.hpp:778-866), then the
 //       driver loop with t-SURFF (binsrc/sphTDSE.cpp:786-831, 936-945): MODE "z" propagates with
@@ -525,6 +566,7 @@ int main(int argc, char** argv)
 		else if (c == "mask") rc = cmd_mask(argc, argv);
 		else if (c == "pcs") rc = cmd_pcs(argc, argv);
 		else if (c == "tsurff") rc = cmd_tsurff(argc, argv);
+		else if (c == "pcsnum") rc = cmd_pcsnum(argc, argv);
 		if (rc) std::fprintf(stderr, "bad arguments for %s\n", argv[1]);
 		return rc;
 	} catch (std::exception& e) {

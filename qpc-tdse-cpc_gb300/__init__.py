@@ -44,7 +44,7 @@ EXPORTS = (
     "qpc_sph_legendre", "qpc_pcs_tables", "qpc_tsurff_tables", "qpc_pcs_create", "qpc_pcs_destroy", "qpc_pcs_measure",
     "qpc_lgwz_pcs", "qpc_tsurff_create", "qpc_tsurff_destroy", "qpc_tsurff_clear", "qpc_tsurff_accumulate",
     "qpc_lgwz_tsurff", "qpc_vgwr_tsurff", "qpc_tsurff_get", "qpc_pcs_last_run", "qpc_tsurff_last_run",
-    "qpc_lgwz_create_ex",
+    "qpc_lgwz_create_ex", "qpc_pcs_tables_numeric",
 )
 SPEC_LMD, SPEC_PMD, SPEC_PAD = 0, 1, 2
 TSURFF_FREE, TSURFF_Z, TSURFF_XY = 0, 1, 2
@@ -161,6 +161,7 @@ def load(path=None):
         "qpc_coulomb_sigma": (ctypes.c_int, [d, i32, P]),
         "qpc_sph_legendre": (ctypes.c_int, [i32, d, P]),
         "qpc_pcs_tables": (ctypes.c_int, [P, P, P, d, d, P, P, P, P, P, P, P]),
+        "qpc_pcs_tables_numeric": (ctypes.c_int, [P, P, P, P, P, P, P, P, P, P, P]),
         "qpc_tsurff_tables": (ctypes.c_int, [P, P, P, d, d, P, P, P, P, P, P, P, P, P, P, P, P]),
         "qpc_pcs_create": (ctypes.c_int, [P, P, P, P, P, P, P, P]),
         "qpc_pcs_destroy": (ctypes.c_int, [P]),
@@ -837,6 +838,20 @@ def pcs_tables(n_r, p, n_l, knots, nkr, nkt, nkp, krmin, krmax, ktmin, ktmax, kp
     return t
 
 
+def pcs_tables_numeric(n_r, p, n_l, knots, nkr, nkt, nkp, krmin, krmax, ktmin, ktmax, kpmin, kpmax, potential, flag=0, n_m=1, m0=0):
+    """spectrum_c_pcs::initialize with numerical partial waves of V = -(zc + zs e^{-sigma r})/r
+    (potential = (kind, zc, zs, sigma) as radial_setup takes it); same dict as pcs_tables."""
+    d = qpc_dims(n_r, p, n_l, n_m, m0, 1)
+    g = _kgrid(nkr, nkt, nkp, krmin, krmax, ktmin, ktmax, kpmin, kpmax, flag)
+    pot = qpc_potential(*potential)
+    nl = _lmax(n_l, n_m, m0) + 1
+    t = {"kr": np.zeros(nkr), "kt": np.zeros(nkt), "kp": np.zeros(nkp), "ijl": np.zeros((nkr, nl, n_r)),
+         "plm": np.zeros((nkt, n_m, n_l)), "exm": np.zeros((nkp, n_m), complex), "cps": np.zeros((nkr, nl), complex)}
+    _check(load().qpc_pcs_tables_numeric(ctypes.byref(d), _ptr(_f64(knots)), ctypes.byref(g), ctypes.byref(pot),
+                                         *[_ptr(t[k]) for k in ("kr", "kt", "kp", "ijl", "plm", "exm", "cps")]))
+    return t
+
+
 def tsurff_tables(n_r, p, n_l, knots, r0, zc, nkr, nkt, nkp, krmin, krmax, ktmin, ktmax, kpmin, kpmax, flag=0, n_m=1, m0=0):
     """spectrum_c_tsf::initialize (spherical/spectrum/momentum_1e.hpp:778-866): dict of kr, kt, kp,
     ib, b0, br (splines non-zero at r0), j0, jr [nkr][lmax+1], y0 [nkt][n_m][n_l], e0 [nkp][n_m],
@@ -869,11 +884,20 @@ class spectrum_c_pcs:
         self.nkr, self.nkt, self.nkp = nkr, nkt, nkp
         self._h = None
 
-    def initialize(self, n_r, p, n_l, knots, krmin, krmax, thmin, thmax, phmin, phmax, zc, rb=0.0, flag=0, n_m=1, m0=0, tables=None):
+    def initialize(self, n_r, p, n_l, knots, krmin, krmax, thmin, thmax, phmin, phmax, zc, rb=0.0, flag=0, n_m=1, m0=0, tables=None,
+                   potential=None):
+        """potential = (kind, zc, zs, sigma) selects the numerical partial waves of that potential
+        (pcs_tables_numeric, the reference's numerical PCS); otherwise analytic Coulomb waves of charge
+        zc with the cut-off rb (pcs_tables)."""
         lib = load()
         self.close()
-        t = tables or pcs_tables(n_r, p, n_l, knots, self.nkr, self.nkt, self.nkp, krmin, krmax, thmin, thmax, phmin, phmax, zc, rb,
-                                 flag, n_m, m0)
+        if tables is not None:
+            t = tables
+        elif potential is not None:
+            t = pcs_tables_numeric(n_r, p, n_l, knots, self.nkr, self.nkt, self.nkp, krmin, krmax, thmin, thmax, phmin, phmax, potential,
+                                   flag, n_m, m0)
+        else:
+            t = pcs_tables(n_r, p, n_l, knots, self.nkr, self.nkt, self.nkp, krmin, krmax, thmin, thmax, phmin, phmax, zc, rb, flag, n_m, m0)
         d = qpc_dims(n_r, p, n_l, n_m, m0, 1)
         g = _kgrid(self.nkr, self.nkt, self.nkp, krmin, krmax, thmin, thmax, phmin, phmax, flag)
         h = ctypes.c_void_p()

@@ -12,7 +12,9 @@
 //   * Coulomb phase sigma_l = arg Gamma(l + 1 + i eta): Stirling's series for
 //     ln Gamma (A&S 6.1.41) after shifting the argument, then A&S 14.5.6;
 //   * normalised associated Legendre functions with the Condon-Shortley phase
-//     (Y_lm(theta, 0)) by the standard three-term recurrence in l.
+//     (Y_lm(theta, 0)) by the standard three-term recurrence in l;
+//   * partial waves of screened potentials: the radial equation integrated by the
+//     Dormand-Prince 5(4) pair and matched to F_l, G_l at the asymptotic radius.
 #include "qpc_internal.h"
 #include <algorithm>
 #include <atomic>
@@ -189,6 +191,140 @@ void sph_legendre(int lmax, double x, double* out)
 	}
 }
 
+// F, F', G, G' for l = 0..lmax at rho where Steed's CF2 applies (rho >= 1, outside a repulsive
+// turning point): F as coulomb_f, G_0 = (F_0' - p F_0)/q, G_0' = p G_0 - q F_0 from p + iq = H+'/H+,
+// then G upward (A&S 14.2.1-2), the stable direction for the irregular solution.
+int coulomb_fg(double eta, double rho, int lmax, double* F, double* Fp, double* G, double* Gp)
+{
+	if (!(rho >= 1.0) || (eta > 0.0 && rho < 1.8 * eta)) return 1;
+	int bad = coulomb_f(eta, rho, lmax, F, Fp);
+	double p, q;
+	if (coulomb_cf2(eta, rho, p, q) < 0) ++bad;
+	G[0] = (Fp[0] - p * F[0]) / q;
+	Gp[0] = p * G[0] - q * F[0];
+	for (int l = 0; l < lmax; ++l) {
+		const double L = l + 1, S = L / rho + eta / L, R = std::sqrt(1.0 + (eta / L) * (eta / L));
+		G[l + 1] = (S * G[l] - Gp[l]) / R;
+		Gp[l + 1] = R * G[l] - S * G[l + 1];
+	}
+	return bad;
+}
+
+namespace {
+
+// u'' = -(1 - 2 e0/x - l(l+1)/x^2 - 2 e1 e^{d1 x}/x) u in x = k r for V = -(Z + a e^{-s r})/r and mass m:
+// e0 = -m Z/k, e1 = -m a/k, d1 = -s/k (the scaled radial equation of equation_hydrogenic_yukawa,
+// spherical/spectrum/equation.hpp:66-123).
+struct radial_ode {
+	double e0, e1, d1, ll;
+	void operator()(double x, const double* y, double* dy) const
+	{
+		const double g = 1.0 - 2.0 * e0 / x - ll / (x * x) - (e1 != 0.0 ? 2.0 * e1 * std::exp(d1 * x) / x : 0.0);
+		dy[0] = y[1];
+		dy[1] = -g * y[0];
+	}
+};
+
+// Dormand-Prince 5(4) (J. R. Dormand, P. J. Prince, J. Comput. Appl. Math. 6 (1980) 19) from x0 to x1 with
+// step control on the relative error max|err| / (rtol max|y|); h carries the step size between calls.
+// Returns 0, or 1 if the step count ran out.
+int dopri(const radial_ode& f, double* y, double x0, double x1, double& h, double rtol)
+{
+	static const double c2 = 1.0 / 5, c3 = 3.0 / 10, c4 = 4.0 / 5, c5 = 8.0 / 9;
+	static const double a21 = 1.0 / 5, a31 = 3.0 / 40, a32 = 9.0 / 40, a41 = 44.0 / 45, a42 = -56.0 / 15, a43 = 32.0 / 9;
+	static const double a51 = 19372.0 / 6561, a52 = -25360.0 / 2187, a53 = 64448.0 / 6561, a54 = -212.0 / 729;
+	static const double a61 = 9017.0 / 3168, a62 = -355.0 / 33, a63 = 46732.0 / 5247, a64 = 49.0 / 176, a65 = -5103.0 / 18656;
+	static const double b1 = 35.0 / 384, b3 = 500.0 / 1113, b4 = 125.0 / 192, b5 = -2187.0 / 6784, b6 = 11.0 / 84;
+	static const double e1 = 71.0 / 57600, e3 = -71.0 / 16695, e4 = 71.0 / 1920, e5 = -17253.0 / 339200, e6 = 22.0 / 525, e7 = -1.0 / 40;
+	double x = x0;
+	if (x1 <= x0) return 0;
+	if (!(h > 0.0)) h = std::min(x1 - x0, 1e-3 * std::max(1.0, x0));
+	double k1[2], k2[2], k3[2], k4[2], k5[2], k6[2], k7[2], t[2], yn[2];
+	f(x, y, k1);
+	for (long it = 0; it < 10000000; ++it) {
+		if (x >= x1) return 0;
+		const bool last = x + h >= x1;
+		const double hh = last ? x1 - x : h;
+		for (int i = 0; i < 2; ++i) t[i] = y[i] + hh * a21 * k1[i];
+		f(x + c2 * hh, t, k2);
+		for (int i = 0; i < 2; ++i) t[i] = y[i] + hh * (a31 * k1[i] + a32 * k2[i]);
+		f(x + c3 * hh, t, k3);
+		for (int i = 0; i < 2; ++i) t[i] = y[i] + hh * (a41 * k1[i] + a42 * k2[i] + a43 * k3[i]);
+		f(x + c4 * hh, t, k4);
+		for (int i = 0; i < 2; ++i) t[i] = y[i] + hh * (a51 * k1[i] + a52 * k2[i] + a53 * k3[i] + a54 * k4[i]);
+		f(x + c5 * hh, t, k5);
+		for (int i = 0; i < 2; ++i) t[i] = y[i] + hh * (a61 * k1[i] + a62 * k2[i] + a63 * k3[i] + a64 * k4[i] + a65 * k5[i]);
+		f(x + hh, t, k6);
+		for (int i = 0; i < 2; ++i) yn[i] = y[i] + hh * (b1 * k1[i] + b3 * k3[i] + b4 * k4[i] + b5 * k5[i] + b6 * k6[i]);
+		f(x + hh, yn, k7);
+		double err = 0.0;
+		const double sc = rtol * std::max(std::max(std::fabs(y[0]), std::fabs(y[1])), std::max(std::fabs(yn[0]), std::fabs(yn[1]))) + 1e-300;
+		for (int i = 0; i < 2; ++i)
+			err = std::max(err, std::fabs(hh * (e1 * k1[i] + e3 * k3[i] + e4 * k4[i] + e5 * k5[i] + e6 * k6[i] + e7 * k7[i])) / sc);
+		if (err <= 1.0) {
+			x = last ? x1 : x + hh;
+			y[0] = yn[0]; y[1] = yn[1];
+			k1[0] = k7[0]; k1[1] = k7[1];
+			if (!last) h = hh * std::min(5.0, 0.9 * std::pow(std::max(err, 1e-10), -0.2));
+		} else {
+			h = hh * std::max(0.2, 0.9 * std::pow(err, -0.2));
+		}
+	}
+	return 1;
+}
+
+}  // namespace
+
+// The regular partial wave of V = -(Z + a e^{-s r})/r at x_i = k r_i (ascending), normalised so that
+// asymptotically u = cos(delta) F_l(eta) + sin(delta) G_l(eta), eta = -m Z/k (the solution::initialize
+// of spherical/spectrum/equation.hpp:367-421): started from F_l(-m (Z + a)/k, x) near the origin,
+// integrated through the points to the asymptotic radius max(eta^2 + l, 100, 32 k/s), and matched there
+// to F, G.  *Delta = delta + sigma_l reduced into (-pi/2, pi/2] with the sign carried by u, as the
+// reference's arctangent leaves it.  Returns 0 or a positive error count.
+int coulomb_partial_wave(double Z, double a, double s, double mass, double k, int l, const double* x, int n, double* u, double* Delta)
+{
+	radial_ode f{-mass * Z / k, -mass * a / k, -s / k, (double)l * (l + 1)};
+	const double rtol = 5e-11;
+	int bad = 0;
+	std::vector<double> F(l + 1), Fp(l + 1), G(l + 1), Gp(l + 1);
+	double y[2];
+	const double xin = l == 0 ? 1e-7 : 5e-7 * (l + 1) * l;
+	double x0 = x[0] < xin ? x[0] : xin;
+	if (coulomb_f(f.e0 + f.e1, x0, l, F.data(), Fp.data())) ++bad;
+	y[0] = F[l]; y[1] = Fp[l];
+	double h = 0.0;	// u and y share one scale, lowered together when the solution grows
+	for (int i = 0; i < n; ++i) {
+		if (dopri(f, y, x0, x[i], h, rtol)) ++bad;
+		x0 = x[i];
+		if (std::fabs(y[0]) > 1e150 || std::fabs(y[1]) > 1e150) {
+			for (int j = 0; j < i; ++j) u[j] *= 1e-290;
+			y[0] *= 1e-290; y[1] *= 1e-290;
+		}
+		u[i] = y[0];
+	}
+	const double large = std::max(std::max(f.e0 * f.e0 + l, 100.0), s != 0.0 ? 32.0 * k / s : 0.0);
+	const double eta = s != 0.0 ? f.e0 : f.e0 + f.e1;
+	if (x0 < large) {
+		if (dopri(f, y, x0, large, h, rtol)) ++bad;
+		x0 = large;
+	}
+	if (coulomb_fg(eta, x0, l, F.data(), Fp.data(), G.data(), Gp.data())) ++bad;
+	// y = A (c F + s G): u F' - u' F = A s, u' G - u G' = A c  (Wronskian F'G - FG' = 1)
+	const double As = y[0] * Fp[l] - y[1] * F[l], Ac = y[1] * G[l] - y[0] * Gp[l];
+	const double delta = std::atan2(As, Ac);
+	std::vector<double> sig(l + 1);
+	coulomb_sigma(eta, l, sig.data());
+	double D = delta + sig[l];
+	D = std::remainder(D, PI);	// into [-pi/2, pi/2]
+	if (D <= -0.5 * PI) D += PI;
+	// normalisation with the reduced phase: nm y = cos(D - sigma) F + sin(D - sigma) G at x0
+	const double c = std::cos(D - sig[l]), sn = std::sin(D - sig[l]);
+	const double nm = std::fabs(y[0]) >= std::fabs(y[1]) ? (c * F[l] + sn * G[l]) / y[0] : (c * Fp[l] + sn * Gp[l]) / y[1];
+	for (int i = 0; i < n; ++i) u[i] *= nm;
+	*Delta = D;
+	return bad;
+}
+
 }  // namespace qpc
 
 using namespace qpc;
@@ -346,6 +482,64 @@ int qpc_pcs_tables(const qpc_dims* d, const double* knots, const qpc_kgrid* g, d
 	work();
 	for (auto& t : th) t.join();
 	if (bad.load()) { set_error("Coulomb continued fraction did not converge at %d points", bad.load()); return QPC_ERR_NUMERIC; }
+	return QPC_OK;
+}
+
+// spectrum_c_pcs::initialize with numerical partial waves (momentum_1e.hpp:487-512, initialize_kr 150-188,
+// the "numerical PCS" the driver picks for screened potentials, binsrc/sphTDSE.cpp:313-316, 340-342):
+// for V = -(zc + zs e^{-sigma r})/r and mass 1, u_l(k r) from coulomb_partial_wave on the quadrature
+// points, ijl[kr][l][r] = int B_r u_l dr / k, cps[kr][l] = e^{i (Delta_l - l pi/2)}; the other tables as
+// qpc_pcs_tables.
+int qpc_pcs_tables_numeric(const qpc_dims* d, const double* knots, const qpc_kgrid* g, const qpc_potential* pot, double* kr,
+	double* kt, double* kp, double* ijl, double* plm, double* exm, double* cps)
+{
+	if (!dims_ok(d) || !knots || !pot || !kr || !kt || !kp || !ijl || !plm || !exm || !cps) return QPC_ERR_ARGS;
+	const double Z = pot->zc, A = pot->kind == QPC_POTENTIAL_YUKAWA ? pot->zs : 0.0, sg = pot->kind == QPC_POTENTIAL_YUKAWA ? pot->sigma : 0.0;
+	if (!std::isfinite(Z) || !std::isfinite(A) || !(sg >= 0.0) || (A != 0.0 && !(sg > 0.0))) return QPC_ERR_ARGS;
+	int rc = axes(g, kr, kt, kp);
+	if (rc) return rc;
+	radial_basis B;
+	if ((rc = basis_from(d, knots, B))) return rc;
+	angular(d, g->nkt, kt, g->nkp, kp, plm, exm);
+	const int lmax = lmax_of(d), nl = lmax + 1, n = d->n_r, p = d->p, nq = B.nq, ni = B.nint();
+	// the quadrature points with weight, ascending
+	std::vector<int> pidx;
+	for (int s = p; s < ni - p; ++s)
+		for (int q = 0; q < nq; ++q)
+			if (B.wq[(size_t)s * nq + q] != 0.0 && B.xq[(size_t)s * nq + q] > 0.0) pidx.push_back(s * nq + q);
+	const int np = (int)pidx.size();
+	std::atomic<int> next(0), bad(0);
+	auto work = [&]() {
+		std::vector<double> x(np), u(np), F((size_t)ni * nq, 0.0);
+		for (int job; (job = next.fetch_add(1)) < g->nkr * nl;) {
+			const int ik = job / nl, l = job % nl;
+			const double k = kr[ik];
+			for (int i = 0; i < np; ++i) x[i] = k * B.xq[pidx[i]];
+			double D = 0.0;
+			if (coulomb_partial_wave(Z, A, sg, 1.0, k, l, x.data(), np, u.data(), &D)) bad.fetch_add(1);
+			for (int i = 0; i < np; ++i) F[pidx[i]] = u[i];
+			for (int j = 0; j < n; ++j) {
+				const int a = j + 1;
+				double acc = 0.0;
+				for (int s = a; s <= a + p; ++s) {
+					if (s < p || s >= ni - p) continue;
+					const int jj = a - (s - p);
+					for (int q = 0; q < nq; ++q)
+						acc += B.wq[(size_t)s * nq + q] * F[(size_t)s * nq + q] * B.b0[((size_t)s * (p + 1) + jj) * nq + q];
+				}
+				ijl[((size_t)ik * nl + l) * n + j] = acc / k;
+			}
+			const double ph = D - l * PI / 2.0;
+			cps[2 * ((size_t)ik * nl + l)] = std::cos(ph);
+			cps[2 * ((size_t)ik * nl + l) + 1] = std::sin(ph);
+		}
+	};
+	unsigned nt = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+	std::vector<std::thread> th;
+	for (unsigned i = 1; i < nt; ++i) th.emplace_back(work);
+	work();
+	for (auto& t : th) t.join();
+	if (bad.load()) { set_error("partial-wave integration failed for %d (k, l)", bad.load()); return QPC_ERR_NUMERIC; }
 	return QPC_OK;
 }
 

@@ -48,6 +48,9 @@ Cases (hydrogen unless stated; r in [0, rmax], uniform knots, m = 0):
                     "coul": Coulomb waves zc = 1, |k| uniform in [0.1, 2]; "plane": plane waves
                     with the cut-off at rb = 10, k^2/2 uniform for |k| in [0.2, 1.5]; the tables
                     (kr, kt, kp, ijl, plm, exm, cps) and measure_lmd / measure_prj / measure_pad
+  pcsnum_small.npz  spectrum_c_pcs with numerical partial waves of V = -(1 + 17 e^{-2r})/r (the
+                    driver's choice for screened potentials) on the small grid, "coul" axes:
+                    ijl, cps, measure_lmd and measure_prj of a seeded random state
   tsurff_small.npz  spectrum_c_tsf (momentum_1e.hpp:516-1072) in the driver loop of the
                     length-gauge propagator on the small grid: a seeded random state, 60 steps
                     with f_i = 0.3 sin(0.4 t_i) sin^2(pi t_i / t_60) passed to accumulate(f_i,
@@ -206,6 +209,17 @@ def momentum(d):
                         case + "_lmd": load(d, "lmd", (nk[0], NM, NL), True), case + "_pmd": load(d, "pmd", nk, True),
                         case + "_pad": load(d, "pad", None, True)[:nk[0] * nk[1]].reshape(nk[0], nk[1])})
         np.savez(os.path.join(HERE, tag + ".npz"), **out)
+    # ---- numerical partial waves of a screened potential (the driver's PCS for hydrogenic_yukawa)
+    NR, P, NL, RMAX = 64, 6, 6, 30.0
+    rng = np.random.default_rng(23)
+    c = (rng.standard_normal(NR * NL) + 1j * rng.standard_normal(NR * NL)) * np.exp(-np.tile(np.arange(NR), NL) / 12.0)
+    c.tofile(os.path.join(d, "pcoef.bin"))
+    ZC, ZS, SG = 1.0, 17.0, 2.0
+    run("ref_small", "pcsnum", d, RMAX, 0.05, ZC, ZS, SG, os.path.join(d, "pcoef.bin"), 0.1, 2.0, 0.0, 3.0, 0.0, 6.0, 0)
+    np.savez(os.path.join(HERE, "pcsnum_small.npz"), n_r=NR, p=P, n_l=NL, rmax=RMAX, zc=ZC, zs=ZS, sigma=SG, nkr=nk[0], nkt=nk[1],
+             nkp=nk[2], grid=np.array([0.1, 2.0, 0.0, 3.0, 0.0, 6.0, 0]), coef=c.reshape(1, NL, NR),
+             kr=load(d, "kr"), ijl=load(d, "ijl", (nk[0], NL, NR)), cps=load(d, "cps", (nk[0], NL), True),
+             lmd=load(d, "lmd", (nk[0], 1, NL), True), pmd=load(d, "pmd", nk, True))
     # ---- t-SURFF in the driver loops
     for binary, tag, NR, P, NL, NM, M0, RMAX, mode, r0, tzc in (("ref_small", "tsurff_small", 64, 6, 6, 1, 0, 30.0, "z", 20.0, 0.0),
                                                                  ("ref_ep", "tsurff_ep", 40, 5, 4, 5, -2, 20.0, "xy", 12.0, 1.0)):

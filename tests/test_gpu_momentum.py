@@ -129,3 +129,16 @@ def test_tsurff_batch_against_oracle(q, mode):
     ts.clearwork()
     work, clock = ts.get()
     assert not work.any() and not clock.any()
+
+
+def test_pcs_numeric_partial_waves_match_reference(q):
+    """the numerical PCS for a screened potential (ODE-tolerance-limited agreement, ~1e-9)"""
+    g = golden("pcsnum_small")
+    kmin, kmax, t0, t1, p0, p1, flag = g["grid"]
+    kn = q.linear_knots(int(g["n_r"]), int(g["p"]), 0.0, float(g["rmax"]))
+    pcs = q.spectrum_c_pcs(int(g["nkr"]), int(g["nkt"]), int(g["nkp"])).initialize(
+        int(g["n_r"]), int(g["p"]), int(g["n_l"]), kn, kmin, kmax, t0, t1, p0, p1, 1.0, flag=int(flag),
+        potential=(q.POTENTIAL_YUKAWA, float(g["zc"]), float(g["zs"]), float(g["sigma"])))
+    c = g["coef"][None]
+    assert rel_l2(pcs.measure_lmd(c)[0], g["lmd"]) < 1e-8
+    assert rel_l2(pcs.measure_prj(c)[0], g["pmd"]) < 1e-8

@@ -134,3 +134,28 @@ def test_table_arguments_are_checked(q):
         q.tsurff_tables(64, 6, 6, kn, 31.0, 0.0, 4, 2, 2, 0.1, 1.0, 0, 3, 0, 6)  # surface outside the box
     with pytest.raises(q.QpcError):
         q.coulomb_f(-1.0, 0.0, 3)
+
+
+def test_pcs_numeric_tables_match_reference(q):
+    """numerical partial waves of V = -(1 + 17 e^{-2r})/r: both sides integrate the radial equation
+    to a relative tolerance of 5e-11 (different Runge-Kutta pairs), so they agree to ~1e-9"""
+    g = golden("pcsnum_small")
+    kmin, kmax, t0, t1, p0, p1, flag = g["grid"]
+    kn = q.linear_knots(int(g["n_r"]), int(g["p"]), 0.0, float(g["rmax"]))
+    t = q.pcs_tables_numeric(int(g["n_r"]), int(g["p"]), int(g["n_l"]), kn, int(g["nkr"]), int(g["nkt"]), int(g["nkp"]),
+                             kmin, kmax, t0, t1, p0, p1, (q.POTENTIAL_YUKAWA, float(g["zc"]), float(g["zs"]), float(g["sigma"])), int(flag))
+    assert np.abs(t["cps"] - g["cps"]).max() < 1e-9
+    prod, ref = t["ijl"] * t["cps"][:, :, None], g["ijl"] * g["cps"][:, :, None]
+    assert np.abs(prod - ref).max() < 1e-8 * np.abs(ref).max()
+
+
+def test_pcs_numeric_oracle_matches_reference(q):
+    g = golden("pcsnum_small")
+    kn = q.linear_knots(int(g["n_r"]), int(g["p"]), 0.0, float(g["rmax"]))
+    kmin, kmax, t0, t1, p0, p1, flag = g["grid"]
+    ang = q.pcs_tables(int(g["n_r"]), int(g["p"]), int(g["n_l"]), kn, int(g["nkr"]), int(g["nkt"]), int(g["nkp"]), kmin, kmax,
+                       t0, t1, p0, p1, 1.0)
+    t = {"kr": g["kr"], "ijl": g["ijl"], "cps": g["cps"], "plm": ang["plm"], "exm": ang["exm"]}
+    lmd, pmd, _ = mo.pcs_measure(t, g["coef"], 0)
+    assert rel_l2(lmd, g["lmd"]) < 1e-13
+    assert rel_l2(pmd, g["pmd"]) < 1e-13
