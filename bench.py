@@ -159,7 +159,26 @@ def path_flops(n_r, p, n_l, power=2):
 TRAFFIC_PER_CHAIN_ROW = 84.0
 
 
-def run_engine(args):
+def aggregate_over_ranks(line, batch, device=None):
+    """Replicas only: every rank advances its own batch of `batch` wavefunctions.  The whole job's
+    value is all ranks' wavefunction-steps over the slowest rank's time (MAX over ranks of the
+    per-step time); e2e likewise from the slowest rank.  Needs an initialised process group."""
+    import torch
+    import torch.distributed as dist
+    world = dist.get_world_size()
+    t = torch.tensor([line["ms_per_step"], -(line.get("e2e") or {}).get("value", 0.0)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    out = dict(line)
+    out["n_gpus"] = world
+    out["ms_per_step"] = float(t[0].item())
+    out["value"] = world * batch * 1e3 / out["ms_per_step"]
+    if line.get("e2e"):
+        out["e2e"] = dict(line["e2e"], value=world * float(-t[1].item()))
+    return out
+
+
+def run_engine(args, sync=None):
+    """sync (optional): called right before and right after the timed steps (a barrier across ranks)"""
     import importlib
     q = importlib.import_module("qpc-tdse-cpc_gb300")
     B, n_r, p, n_l, dt = args.batch, 800, 6, 41, 0.05
@@ -181,7 +200,11 @@ def run_engine(args):
     with Clocks() as clk:
         launches1 = prop.launch_count()
         prop.enable_profiling(True)
+        if sync:
+            sync()
         prop.run(ftab[:, W:W + K + 1], np.full(B, K))
+        if sync:
+            sync()
         dev_ms = prop.last_run_ms()
         ktimes = prop.kernel_times()
         prop.enable_profiling(False)
@@ -756,13 +779,13 @@ def main():
         dist.init_process_group("nccl")
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
         dist.barrier()
-        line = run_engine(args)
-        t = torch.tensor([line["ms_per_step"]], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+
+        def sync():
+            torch.cuda.synchronize()
+            dist.barrier()
+            torch.cuda.synchronize()
+        line = aggregate_over_ranks(run_engine(args, sync), args.batch, device="cuda")
         if rank == 0:
-            line["n_gpus"] = world
-            line["ms_per_step"] = float(t.item())
-            line["value"] = world * args.batch * 1e3 / line["ms_per_step"]
             print(json.dumps(line))
         dist.destroy_process_group()
         return
