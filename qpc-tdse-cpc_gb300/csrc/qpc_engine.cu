@@ -601,6 +601,11 @@ int autotune_one(qpc_lgwz* h, int cpl, long step, int jslot, int Bl)
 {
 	int bk = live_bucket(Bl);
 	if (Bl <= 0 || h->gsel[cpl][bk]) return QPC_OK;
+	// QPC_CHAIN_G fixes the lanes per part instead (a candidate that divides P)
+	if (const char* e = getenv("QPC_CHAIN_G")) {
+		const int G = atoi(e);
+		if (std::find(h->gcand.begin(), h->gcand.end(), G) != h->gcand.end()) { h->gsel[cpl][bk] = G; return QPC_OK; }
+	}
 	float best = 1e30f;
 	int bestg = 1;
 	const bool obs_saved = h->observing;
