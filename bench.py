@@ -88,7 +88,8 @@ class Clocks:
 
     def __init__(self):
         self.p = None
-        self.path = os.path.join(ROOT, "gpurun_out", "clocks_bench.csv") if os.path.isdir(os.path.join(ROOT, "gpurun_out")) else "/tmp/clocks_bench.csv"
+        import tempfile
+        self.path = os.environ.get("QPC_CLOCKS_CSV") or os.path.join(tempfile.gettempdir(), "qpc_clocks_%d.csv" % os.getpid())
 
     def __enter__(self):
         try:
@@ -237,7 +238,7 @@ def run_engine(args, sync=None):
     # complex per row) read twice per application, each chain's eigen-basis vector
     # read and written once per application, its work vector through the five passes
     sweep_bytes = live_pairs * n_r * 2 * ((p + 1) * 16 * 2 + 2 * 16 * 2 + 2 * 16 * 5) / launches_per_step
-    # the whole step: every kernel's FP64 flops per wavefunction-step
+    # the whole step: every kernel's FP64 flops per wavefunction-step (path_flops)
     step_flops = path_flops(n_r, p, n_l) * B
     path_tflops = step_flops / (dev_ms / K * 1e-3) / 1e12
     roof = {"bound": "fp64", "kernel": "k_chain<6,G,coupling> (coupling CN chains)", "achieved": achieved,
@@ -289,7 +290,8 @@ def run_engine(args, sync=None):
 
 
 def c1_knots(n_r, p, rmax, frac=0.1):
-    """Quadratic-then-linear knots (no reference generator): the first `frac` of the
+    """Quadratic-then-linear knots (the reference has no such knot generator, functions/basis_bsplines.h:450-526
+    offers linear, sine^2, piecewise and exponential ones): the first `frac` of the
     n_r + 2 - p intervals grow quadratically, the rest are uniform with the matching slope."""
     M = n_r + 2 - p
     Mq = max(1, int(round(frac * M)))
