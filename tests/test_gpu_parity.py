@@ -318,3 +318,30 @@ def test_golden_multi_m(q):
     prop.run(g["f"][None, :], [nt], [nt + nf])
     assert rel_l2(prop.get()[0], g["coef"]) < 1e-12
     assert abs(prop.norm()[0] - g["norm"][0]) < 1e-12 * g["norm"][0]
+
+
+def test_full_size_batched_scan_window(q, oracle):
+    """The 256-wavefunction scan at its full size (N_r = 800 on [0, 400], p = 6, l < 41, fields drawn as
+    the benchmark draws them): 200 steps of the whole batch, three instances against the oracle, and
+    the S-norm of every instance conserved (the Crank-Nicolson step is S-unitary)."""
+    n_r, p, n_l, dt, B, K = 800, 6, 41, 0.05, 256, 200
+    S, R, H = grid(q, n_r, p, n_l, 400.0)
+    c0, _ = q.ground_state(S, H, n_l)
+    rng = np.random.default_rng(2025)
+    inten = 10 ** rng.uniform(np.log10(5e13), np.log10(5e14), B)
+    lam = rng.uniform(400.0, 2000.0, B)
+    cep = rng.uniform(0.0, 2 * np.pi, B)
+    cyc = rng.integers(2, 11, B)
+    ftab = np.stack([q.field_sinen(q.intensity_to_e0(I), q.wavelength_to_w0(l), float(c), 0.0, float(ph / np.pi), dt)[:K + 1]
+                     for I, l, ph, c in zip(inten, lam, cep, cyc)])
+    prop = q.propagator_cn_hc_lgwz().initialize(n_r, p, n_l, S, R, H, dt, n_inst=B)
+    state = np.repeat(c0[None], B, 0)
+    prop.put(state)
+    n0 = prop.norm()
+    prop.run(ftab, np.full(B, K))
+    out = prop.get()
+    assert np.abs(prop.norm() - n0).max() < 1e-11 * n0.max()
+    g = oracle.grid(S, R, H, dt, n_l)
+    for k in (0, 97, 255):
+        ref = oracle.run(g, c0.reshape(1, -1), ftab[k:k + 1], [K], [K], threads=4)
+        assert rel_l2(out[k].reshape(-1), ref[0]) < TOL_SHORT, k
