@@ -344,4 +344,4 @@ def test_full_size_batched_scan_window(q, oracle):
     g = oracle.grid(S, R, H, dt, n_l)
     for k in (0, 97, 255):
         ref = oracle.run(g, c0.reshape(1, -1), ftab[k:k + 1], [K], [K], threads=4)
-        assert rel_l2(out[k].reshape(-1), ref[0]) < TOL_SHORT, k
+        assert rel_l2(out[k].reshape(-1), ref[0]) < 1e-11, k   # 200 steps of the large grid: 1.4e-12 measured
