@@ -494,6 +494,11 @@ def run_c0(args):
         "e2e": {"value": nt / e2e_s, "unit": "wf-steps/s", "h2d_bytes_per_step": (c0.nbytes + f.nbytes) / nt,
                 "d2h_bytes_per_step": out.nbytes / nt},
         "gpu_launches": int(launches), "final_norm": float(norm),
+        "roofline": {"bound": "fp64 (latency: one wavefunction's recurrences are sequential in r)",
+                     "kernel": "whole step", "achieved": path_flops(n_r, p, n_l) * nt / (dev_ms * 1e-3) / 1e12,
+                     "peak": FP64_PEAK_TFLOPS, "unit": "TFLOP/s",
+                     "frac": path_flops(n_r, p, n_l) * nt / (dev_ms * 1e-3) / 1e12 / FP64_PEAK_TFLOPS,
+                     "flops_per_step": path_flops(n_r, p, n_l)},
         "cpu_baseline": cpu, "clocks": clk.summary(),
     }
 
