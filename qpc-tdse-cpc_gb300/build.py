@@ -60,7 +60,7 @@ def build_engine(force=False, verbose=False):
     o_vg = os.path.join(OBJDIR, "qpc_vgwr.o")
     o_mo = os.path.join(OBJDIR, "qpc_momentum_cu.o")
     o_mt = os.path.join(OBJDIR, "qpc_momentum.o")
-    nv = [_nvcc()] + NVCC_ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC"]
+    nv = [_nvcc()] + NVCC_ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC"] + os.environ.get("QPC_NVCC_EXTRA", "").split()
     jobs = [
         nv + ["-c", os.path.join(CSRC, "qpc_engine.cu"), "-o", o_cu],
         nv + ["-c", os.path.join(CSRC, "qpc_noalloc.cu"), "-o", o_na],

@@ -25,6 +25,14 @@
 // latency-bound), G = 1 the fewest idle lanes (many chains).
 #pragma once
 
+// prefetch distances for 1 and 2 partial sums per lane (compile-time tuning)
+#ifndef QPC_CHAIN_PD1
+#define QPC_CHAIN_PD1 16
+#endif
+#ifndef QPC_CHAIN_PD2
+#define QPC_CHAIN_PD2 3
+#endif
+
 namespace qpc {
 
 // Coupling chains come in pairs (+s, -s) that share one factorisation; the
@@ -37,7 +45,7 @@ struct chain_cfg {
 	static constexpr int TPL = P / G;	// partial sums per lane
 	// prefetch distance (columns) of the recurrences: a row costs 2*TPL FP64
 	// instructions (~128*TPL cycles); memory latency is ~600-800 cycles
-	static constexpr int PD = TPL >= 6 ? 1 : (TPL >= 3 ? 2 : (TPL == 2 ? 3 : 4));
+	static constexpr int PD = TPL >= 6 ? 1 : (TPL >= 3 ? 2 : (TPL == 2 ? QPC_CHAIN_PD2 : QPC_CHAIN_PD1));
 	static_assert(P % G == 0, "G must divide P");
 	static_assert(CPW >= 1, "too many lanes per chain");
 };
