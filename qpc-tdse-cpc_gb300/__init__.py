@@ -459,7 +459,8 @@ class propagator_cn_hc_lgwz:
         _check(load().qpc_lgwz_set_profiling(self._h, int(bool(on))))
 
     def tuning(self):
-        """{"lookahead": K, "coupling": {bucket: G}, "fieldfree": {bucket: G}} (G = lanes per part)."""
+        """{"lookahead": K, "coupling": {bucket: G}, "fieldfree": {bucket: G}} (G = lanes per part, -1 = the
+        segmented solver)."""
         out = np.zeros(65, np.int32)
         _check(load().qpc_lgwz_get_tuning(self._h, _ptr(out)))
         return {"lookahead": int(out[0]),

@@ -360,4 +360,308 @@ __global__ void __launch_bounds__(128) k_chain(double2* __restrict__ X, double2*
 	}
 }
 
+// ---------------------------------------------------------------- segmented (latency) variant
+// For few chains the recurrences P2/P4 are the critical path: one row costs ~650 cycles of dependent
+// FP64 work with the GPU otherwise idle.  k_chain_seg cuts each chain into Q segments of Ls rows
+// (Ls >= P, last segment >= P rows) and solves them at once (one lane pair per segment), then joins
+// them: with y0 the solution of a segment whose history is zero and Phi_j the homogeneous solution
+// with a unit value entering from row a - j (forward; b - 1 + j backward), the true values are
+// y = y0 + sum_j Phi_j x_j, where x are the last P values of the previous segment -- a chain of Q
+// small P x P steps.  The Phi depend only on the factors, so they are computed with them (k_spikes
+// for the coupling factors, on the host for the field-free ones).  The two recurrences then take
+// ~Ls + Q row times instead of N; every other pass is row-parallel over the block.
+
+// Phi_j (forward, L y = 0 with y_{a-j} = 1 entering) or Psi_j (backward, L^T x = 0 with
+// x_{b-1+j} = 1 entering) on rows [a, b) of one factor block (rows [N][P+1], L(r, r-k) at
+// [r][k-1]); out[r*P + j - 1].  The same code runs on the host and the device.
+template <int P>
+__host__ __device__ inline void seg_spike(const double2* fs, int N, int a, int b, int j, bool fwd, double2* out)
+{
+	constexpr int NE = P + 1;
+	if (fwd) {
+		for (int r = a; r < b; ++r) {
+			double re = 0.0, im = 0.0;
+			for (int k = 1; k <= P; ++k) {
+				const int src = r - k;
+				double2 y;
+				if (src >= a) y = out[src * P + j - 1];
+				else if (src == a - j && src >= 0) y = make_double2(1.0, 0.0);
+				else continue;
+				const double2 l = fs[r * NE + k - 1];
+				re -= l.x * y.x - l.y * y.y;
+				im -= l.x * y.y + l.y * y.x;
+			}
+			out[r * P + j - 1] = make_double2(re, im);
+		}
+	} else {
+		for (int r = b - 1; r >= a; --r) {
+			double re = 0.0, im = 0.0;
+			for (int k = 1; k <= P; ++k) {
+				const int dst = r + k;
+				if (dst >= N) continue;
+				double2 x;
+				if (dst < b) x = out[dst * P + j - 1];
+				else if (dst == b - 1 + j) x = make_double2(1.0, 0.0);
+				else continue;
+				const double2 l = fs[dst * NE + k - 1];	// L(r+k, r)
+				re -= l.x * x.x - l.y * x.y;
+				im -= l.x * x.y + l.y * x.x;
+			}
+			out[r * P + j - 1] = make_double2(re, im);
+		}
+	}
+}
+
+// spikes of the coupling factor blocks [slot < kf][inst b0 .. b0+Bc)[m][pair]: one thread per
+// (block, segment, j, direction)
+template <int P>
+__global__ void k_spikes(const double2* __restrict__ fac, double2* __restrict__ spf, double2* __restrict__ spb, int B, int b0, int Bc,
+	int M, int np, int N, int Q, int Ls, long total)
+{
+	const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+	if (t >= total) return;
+	const int dir = (int)(t & 1);
+	long u = t >> 1;
+	const int j = (int)(u % P); u /= P;
+	const int seg = (int)(u % Q); u /= Q;
+	const int k = (int)(u % np); u /= np;
+	const int m = (int)(u % M); u /= M;
+	const int i = (int)(u % Bc);
+	const long slot = u / Bc;
+	const long blk = ((slot * B + b0 + i) * M + m) * np + k;
+	const int a = seg * Ls, b = min(N, a + Ls);
+	seg_spike<P>(fac + blk * (long)N * (P + 1), N, a, b, j + 1, dir == 0, (dir == 0 ? spf : spb) + blk * (long)N * P);
+}
+
+// One block per chain (field-free) or per (+s, -s) pair (coupling); the same passes as k_chain, with
+// the recurrences segmented.  spf/spb: the spikes of every factor block, [block][N][P], block =
+// foff / (N (P+1)).  128 threads; segment lanes: warp c handles chain c, lane = 2 segment + part.
+template <int P, bool CPL>
+__global__ void __launch_bounds__(128) k_chain_seg(double2* __restrict__ X, double2* __restrict__ Wk, const double2* __restrict__ fac,
+	const double2* __restrict__ spf, const double2* __restrict__ spb, const double* __restrict__ S, const int64_t* __restrict__ nta,
+	long step, int jslot, int B, int M, int m0, int N, int L, int np, long chbase, long nchains, int Q, int Ls,
+	const int* __restrict__ ffmap, long ffstride)
+{
+	constexpr int NE = P + 1, NC = CPL ? 2 : 1;
+	const unsigned FULL = 0xffffffffu;
+	__shared__ double2 xc[NC][16][P];
+	__shared__ long s_x[NC], s_f[NC];
+	__shared__ int s_a[NC];
+	const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+	const long ch0 = chbase + (long)blockIdx.x * NC;
+	if (tid < NC) {
+		chain_desc d = describe<CPL>(ch0 + tid, nchains, nta, step, jslot, B, M, m0, N, L, np, NE, ffmap, ffstride);
+		s_x[tid] = d.xoff; s_f[tid] = d.foff; s_a[tid] = d.a;
+	}
+	__syncthreads();
+	int amax = 0;
+#pragma unroll
+	for (int c = 0; c < NC; ++c) amax = max(amax, s_a[c]);
+	if (amax == 0) return;	// uniform over the block
+	double* Xd = reinterpret_cast<double*>(X);
+	double* Wd = reinterpret_cast<double*>(Wk);
+	const long rs = 2L * L;
+	for (int app = 0; app < amax; ++app) {
+		// ---- P1: w = S z
+		for (int it = tid; it < NC * N; it += blockDim.x) {
+			const int c = it / N, r = it % N;
+			if (app < s_a[c]) {
+				const double* z = Xd + 2 * s_x[c];
+				double wr = 0.0, wi = 0.0;
+#pragma unroll
+				for (int k = P; k >= 1; --k)
+					if (r - k >= 0) { const double sv = S[(r - k) * NE + k]; wr = fma(sv, z[(long)(r - k) * rs], wr); wi = fma(sv, z[(long)(r - k) * rs + 1], wi); }
+#pragma unroll
+				for (int k = 0; k <= P; ++k)
+					if (r + k < N) { const double sv = S[r * NE + k]; wr = fma(sv, z[(long)(r + k) * rs], wr); wi = fma(sv, z[(long)(r + k) * rs + 1], wi); }
+				Wd[2 * s_x[c] + (long)r * rs] = wr;
+				Wd[2 * s_x[c] + (long)r * rs + 1] = wi;
+			}
+		}
+		__syncthreads();
+		// ---- P2a: y0 = L^-1 w per segment (zero history), lane = 2 segment + part
+		if (warp < NC) {
+			const int c = warp, seg = lane >> 1, part = lane & 1;
+			const bool on = app < s_a[c] && seg < Q;
+			const int a = seg * Ls, b = min(N, a + Ls);
+			const double2* fs = fac + s_f[c];
+			double* wv = Wd + 2 * s_x[c] + part;
+			double hr[P], hi[P];
+			double2 l[P], ln[P];
+#pragma unroll
+			for (int k = 0; k < P; ++k) { hr[k] = 0.0; hi[k] = 0.0; l[k] = make_double2(0.0, 0.0); }	// row a: no history
+			double wcur = (on && a < b) ? wv[(long)a * rs] : 0.0;
+			for (int t = 0; t < Ls; ++t) {
+				const int r = a + t;
+				const bool live = on && r < b;
+				// the next row's factor entries and value, one row ahead
+				const bool nlive = on && r + 1 < b;
+#pragma unroll
+				for (int k = 1; k <= P; ++k) ln[k - 1] = (nlive && t + 1 - k >= 0) ? fs[(long)(r + 1) * NE + k - 1] : make_double2(0.0, 0.0);
+				const double wnext = nlive ? wv[(long)(r + 1) * rs] : 0.0;
+				double acc = live ? wcur : 0.0;
+#pragma unroll
+				for (int k = 0; k < P; ++k)
+					acc = part ? fma(-l[k].x, hi[k], fma(-l[k].y, hr[k], acc)) : fma(-l[k].x, hr[k], fma(l[k].y, hi[k], acc));
+				const double other = __shfl_xor_sync(FULL, acc, 1);
+#pragma unroll
+				for (int k = P - 1; k >= 1; --k) { hr[k] = hr[k - 1]; hi[k] = hi[k - 1]; }
+				hr[0] = part ? other : acc;
+				hi[0] = part ? acc : other;
+				if (live) wv[(long)r * rs] = acc;
+#pragma unroll
+				for (int k = 0; k < P; ++k) l[k] = ln[k];
+				wcur = wnext;
+			}
+		}
+		__syncthreads();
+		// ---- P2b: forward carries x(s)_i = y(a_s - 1 - i), s = 1..Q-1, lane = 2 i + part
+		if (warp < NC) {
+			const int c = warp, i = lane >> 1, part = lane & 1;
+			const bool on = app < s_a[c] && i < P;
+			const double2* sp = spf + (s_f[c] / ((long)N * NE)) * (long)N * P;
+			const double* wv = Wd + 2 * s_x[c] + part;
+			for (int sg = 1; sg < Q; ++sg) {
+				double v = 0.0;
+				if (on) {
+					const int r = sg * Ls - 1 - i;
+					v = wv[(long)r * rs];
+					if (sg >= 2) {
+#pragma unroll
+						for (int jj = 0; jj < P; ++jj) {
+							const double2 ph = sp[(long)r * P + jj], xv = xc[c][sg - 1][jj];
+							v += part ? ph.x * xv.y + ph.y * xv.x : ph.x * xv.x - ph.y * xv.y;
+						}
+					}
+				}
+				__syncwarp();
+				if (on) reinterpret_cast<double*>(&xc[c][sg][i])[part] = v;
+				__syncwarp();
+			}
+		}
+		__syncthreads();
+		// ---- P2c + P3: y = y0 + sum_j Phi_j x(s)_j, then y <- D^-1 y
+		for (int it = tid; it < NC * N; it += blockDim.x) {
+			const int c = it / N, r = it % N;
+			if (app < s_a[c]) {
+				const int sg = r / Ls;
+				const long o = 2 * s_x[c] + (long)r * rs;
+				double yr = Wd[o], yi = Wd[o + 1];
+				if (sg >= 1) {
+					const double2* sp = spf + (s_f[c] / ((long)N * NE)) * (long)N * P + (long)r * P;
+#pragma unroll
+					for (int jj = 0; jj < P; ++jj) {
+						const double2 ph = sp[jj], xv = xc[c][sg][jj];
+						yr += ph.x * xv.x - ph.y * xv.y;
+						yi += ph.x * xv.y + ph.y * xv.x;
+					}
+				}
+				const double2 dv = fac[s_f[c] + (long)r * NE + P];
+				Wd[o] = dv.x * yr - dv.y * yi;
+				Wd[o + 1] = dv.x * yi + dv.y * yr;
+			}
+		}
+		__syncthreads();
+		// ---- P4a: x0 = L^-T y per segment (zero history above), descending
+		if (warp < NC) {
+			const int c = warp, seg = lane >> 1, part = lane & 1;
+			const bool on = app < s_a[c] && seg < Q;
+			const int a = seg * Ls, b = min(N, a + Ls);
+			const double2* fs = fac + s_f[c];
+			double* wv = Wd + 2 * s_x[c] + part;
+			double hr[P], hi[P];
+			double2 l[P], ln[P];
+#pragma unroll
+			for (int k = 0; k < P; ++k) { hr[k] = 0.0; hi[k] = 0.0; l[k] = make_double2(0.0, 0.0); }	// row b-1: no history
+			double wcur = (on && b - 1 >= a) ? wv[(long)(b - 1) * rs] : 0.0;
+			for (int t = 0; t < Ls; ++t) {
+				const int r = b - 1 - t;
+				const bool live = on && r >= a;
+				const bool nlive = on && r - 1 >= a;
+#pragma unroll
+				for (int k = 1; k <= P; ++k) ln[k - 1] = (nlive && t + 1 - k >= 0) ? fs[(long)(r - 1 + k) * NE + k - 1] : make_double2(0.0, 0.0);
+				const double wnext = nlive ? wv[(long)(r - 1) * rs] : 0.0;
+				double acc = live ? wcur : 0.0;
+#pragma unroll
+				for (int k = 0; k < P; ++k)
+					acc = part ? fma(-l[k].x, hi[k], fma(-l[k].y, hr[k], acc)) : fma(-l[k].x, hr[k], fma(l[k].y, hi[k], acc));
+				const double other = __shfl_xor_sync(FULL, acc, 1);
+#pragma unroll
+				for (int k = P - 1; k >= 1; --k) { hr[k] = hr[k - 1]; hi[k] = hi[k - 1]; }
+				hr[0] = part ? other : acc;
+				hi[0] = part ? acc : other;
+				if (live) wv[(long)r * rs] = acc;
+#pragma unroll
+				for (int k = 0; k < P; ++k) l[k] = ln[k];
+				wcur = wnext;
+			}
+		}
+		__syncthreads();
+		// ---- P4b: backward carries x(s)_i = x(b_s + i), s = Q-2 .. 0
+		if (warp < NC) {
+			const int c = warp, i = lane >> 1, part = lane & 1;
+			const bool on = app < s_a[c] && i < P;
+			const double2* sp = spb + (s_f[c] / ((long)N * NE)) * (long)N * P;
+			const double* wv = Wd + 2 * s_x[c] + part;
+			for (int sg = Q - 2; sg >= 0; --sg) {
+				double v = 0.0;
+				if (on) {
+					const int r = (sg + 1) * Ls + i;
+					v = wv[(long)r * rs];
+					if (sg + 1 <= Q - 2) {
+#pragma unroll
+						for (int jj = 0; jj < P; ++jj) {
+							const double2 ph = sp[(long)r * P + jj], xv = xc[c][sg + 1][jj];
+							v += part ? ph.x * xv.y + ph.y * xv.x : ph.x * xv.x - ph.y * xv.y;
+						}
+					}
+				}
+				__syncwarp();
+				if (on) reinterpret_cast<double*>(&xc[c][sg][i])[part] = v;
+				__syncwarp();
+			}
+		}
+		__syncthreads();
+		// ---- P4c + P5: x = x0 + sum_j Psi_j x(s)_j, then z <- 2x - z (pairs: s/d emission after the last application)
+		for (int r = tid; r < N; r += blockDim.x) {
+			const int sg = r / Ls;
+			double xr[NC], xi[NC];
+#pragma unroll
+			for (int c = 0; c < NC; ++c) {
+				xr[c] = 0.0; xi[c] = 0.0;
+				if (app < s_a[c]) {
+					const long o = 2 * s_x[c] + (long)r * rs;
+					xr[c] = Wd[o]; xi[c] = Wd[o + 1];
+					if (sg <= Q - 2) {
+						const double2* sp = spb + (s_f[c] / ((long)N * NE)) * (long)N * P + (long)r * P;
+#pragma unroll
+						for (int jj = 0; jj < P; ++jj) {
+							const double2 ph = sp[jj], xv = xc[c][sg][jj];
+							xr[c] += ph.x * xv.x - ph.y * xv.y;
+							xi[c] += ph.x * xv.y + ph.y * xv.x;
+						}
+					}
+				}
+			}
+			if (CPL) {
+				if (app < s_a[0]) {
+					const long op = 2 * s_x[0] + (long)r * rs, om = 2 * s_x[NC - 1] + (long)r * rs;
+					const double zpr = fma(2.0, xr[0], -Xd[op]), zpi = fma(2.0, xi[0], -Xd[op + 1]);
+					const double zmr = fma(2.0, xr[NC - 1], -Xd[om]), zmi = fma(2.0, xi[NC - 1], -Xd[om + 1]);
+					if (app + 1 < s_a[0]) { Xd[op] = zpr; Xd[op + 1] = zpi; Xd[om] = zmr; Xd[om + 1] = zmi; }
+					else {	// conj(z-bar) = (zmr, -zmi)
+						Xd[op] = zpr + zmr; Xd[op + 1] = zpi - zmi;
+						Xd[om] = zpr - zmr; Xd[om + 1] = zpi + zmi;
+					}
+				}
+			} else if (app < s_a[0]) {
+				const long o = 2 * s_x[0] + (long)r * rs;
+				Xd[o] = fma(2.0, xr[0], -Xd[o]);
+				Xd[o + 1] = fma(2.0, xi[0], -Xd[o + 1]);
+			}
+		}
+		__syncthreads();
+	}
+}
+
 } // namespace qpc

@@ -374,6 +374,9 @@ using namespace qpc;
 
 // ============================================================================ handle
 
+// chain-kernel choice meaning "the segmented solver" (k_chain_seg); 0 in gsel means "not tuned yet"
+constexpr int QPC_SEG = -1;
+
 struct qpc_lgwz {
 	int dev = 0;
 	qpc_dims d{};
@@ -394,6 +397,11 @@ struct qpc_lgwz {
 	double* lamp = nullptr;   // [M][npair]
 	double2* ff = nullptr;    // field-free factors [nlh][N][P+1] (row form + 1/D); [B][nlh][N][P+1] with hpi
 	int hpi = 0;              // one Hamiltonian (potential) per instance
+	// segmented chain solver (k_chain_seg) for handles with few wavefunctions: Q segments of Ls rows and
+	// the spikes [block][N][P] of the coupling factors (per look-ahead slot) and of the field-free ones
+	bool seg_ok = false;
+	int Q = 1, Ls = 0;
+	double2 *spf_c = nullptr, *spb_c = nullptr, *spf_ff = nullptr, *spb_ff = nullptr;
 	int* ffmap = nullptr;     // device [B]: the instance whose factors a (sorted) instance uses, during a run
 	int* ffmap_id = nullptr;  // device [B]: identity
 	const int* ffmap_cur = nullptr;	// ffmap during a run, ffmap_id otherwise (NULL without hpi)
@@ -568,9 +576,26 @@ void launch_chain_g(qpc_lgwz* h, cudaStream_t st, int b0, double2* X, const doub
 }
 
 template <int P, bool CPL>
+void launch_chain_seg(qpc_lgwz* h, cudaStream_t st, int b0, double2* X, const double2* fac, const int64_t* nta, long step, int jslot, int cnt)
+{
+	long per = CPL ? (long)h->M * h->npair * 2 : (long)h->M * h->L;
+	long nch = (long)cnt * per;
+	if (nch <= 0) return;
+	long chbase = (long)b0 * per;
+	unsigned grid = (unsigned)(nch / (CPL ? 2 : 1));
+	k_chain_seg<P, CPL><<<grid, 128, 0, st>>>(X, h->wk, fac, CPL ? h->spf_c : h->spf_ff, CPL ? h->spb_c : h->spb_ff, h->S, nta, step, jslot,
+		h->B, h->M, h->d.m0, h->N, h->L, h->npair, chbase, chbase + nch, h->Q, h->Ls, CPL ? nullptr : h->ffmap_cur,
+		(long)h->nlh * h->N * (h->P + 1));
+	LAUNCH(h);
+}
+
+template <int P, bool CPL>
 void launch_chain(qpc_lgwz* h, cudaStream_t st, int b0, int G, double2* X, const double2* fac, const int64_t* nta, long step, int jslot, int cnt)
 {
+	// G = QPC_SEG (-1): the segmented solver; it has no observation pass, so an observed coupling step uses G = P
+	if (G == QPC_SEG && (!h->seg_ok || (CPL && h->observing))) G = P;
 	switch (G) {
+	case QPC_SEG: launch_chain_seg<P, CPL>(h, st, b0, X, fac, nta, step, jslot, cnt); break;
 	case 1: launch_chain_g<P, 1, CPL>(h, st, b0, X, fac, nta, step, jslot, cnt); break;
 	case 2: if constexpr (P % 2 == 0) launch_chain_g<P, 2, CPL>(h, st, b0, X, fac, nta, step, jslot, cnt); break;
 	case 3: if constexpr (P % 3 == 0) launch_chain_g<P, 3, CPL>(h, st, b0, X, fac, nta, step, jslot, cnt); break;
@@ -601,7 +626,7 @@ int autotune_one(qpc_lgwz* h, int cpl, long step, int jslot, int Bl)
 {
 	int bk = live_bucket(Bl);
 	if (Bl <= 0 || h->gsel[cpl][bk]) return QPC_OK;
-	// QPC_CHAIN_G fixes the lanes per part instead (a candidate that divides P)
+	// QPC_CHAIN_G fixes the lanes per part instead (a candidate that divides P, or -1 for the segmented solver)
 	if (const char* e = getenv("QPC_CHAIN_G")) {
 		const int G = atoi(e);
 		if (std::find(h->gcand.begin(), h->gcand.end(), G) != h->gcand.end()) { h->gsel[cpl][bk] = G; return QPC_OK; }
@@ -667,6 +692,11 @@ void launch_group_step(qpc_lgwz* h, cudaStream_t st, int b0, long step, long ste
 		k_factor<P><<<(unsigned)((nsys + 63) / 64), 64, 0, st>>>(h->fac, h->S, h->R, h->lamp, h->ftab, h->ld,
 			h->ntf, step0, kfac, B, b0, Bfac, M, N, np, h->dt, h->status);
 		LAUNCH(h);
+		if (h->seg_ok) {
+			const long total = (long)kfac * Bfac * M * np * h->Q * P * 2;
+			k_spikes<P><<<(unsigned)((total + 127) / 128), 128, 0, st>>>(h->fac, h->spf_c, h->spb_c, B, b0, Bfac, M, np, N, h->Q, h->Ls, total);
+			LAUNCH(h);
+		}
 	}
 	if (Bc > 0 && (np > 0 || (L & 1))) {
 		int tiles = (N + TR - 1) / TR;
@@ -771,6 +801,20 @@ int permute_instances(qpc_lgwz* h, const std::vector<int>& perm, bool inverse)
 
 } // namespace
 
+// spikes of nblk field-free factor blocks (row form [blk][N][P+1]) for the segmented solver
+template <int P>
+static void host_spikes(const double2* fac, size_t nblk, int N, int Q, int Ls, double2* sf, double2* sb)
+{
+	for (size_t bl = 0; bl < nblk; ++bl)
+		for (int sg = 0; sg < Q; ++sg) {
+			const int a = sg * Ls, b = std::min(N, a + Ls);
+			for (int j = 1; j <= P; ++j) {
+				seg_spike<P>(fac + bl * N * (P + 1), N, a, b, j, true, sf + bl * N * P);
+				seg_spike<P>(fac + bl * N * (P + 1), N, a, b, j, false, sb + bl * N * P);
+			}
+		}
+}
+
 extern "C" {
 
 const char* qpc_last_error(void) { return g_err; }
@@ -864,6 +908,38 @@ static int create_impl(const qpc_dims* dims, double dt, const double* S, const d
 		set_error("initial device copies failed");
 		return fail(QPC_ERR_CUDA);
 	}
+	// segmented chain solver for few wavefunctions: Q <= 16 segments of Ls >= P rows, the last one >= P rows
+	h->seg_ok = h->B <= 8 && np > 0;
+	if (h->seg_ok) {
+		auto fits = [&](int q) { const int ls = (N + q - 1) / q; return ls >= P && N - (q - 1) * ls >= P; };
+		int q = 16;
+		while (q > 1 && !fits(q)) --q;
+		h->seg_ok = q >= 2;
+		h->Q = q;
+		h->Ls = (N + q - 1) / q;
+	}
+	if (h->seg_ok) {
+		const size_t nblk_ff = (size_t)nff * h->nlh, nblk_c = (size_t)h->K * h->B * M * np;
+		std::vector<double2> sf(nblk_ff * N * P), sb(nblk_ff * N * P);
+		switch (P) {
+		case 3: host_spikes<3>(ffh.data(), nblk_ff, N, h->Q, h->Ls, sf.data(), sb.data()); break;
+		case 4: host_spikes<4>(ffh.data(), nblk_ff, N, h->Q, h->Ls, sf.data(), sb.data()); break;
+		case 5: host_spikes<5>(ffh.data(), nblk_ff, N, h->Q, h->Ls, sf.data(), sb.data()); break;
+		case 6: host_spikes<6>(ffh.data(), nblk_ff, N, h->Q, h->Ls, sf.data(), sb.data()); break;
+		case 7: host_spikes<7>(ffh.data(), nblk_ff, N, h->Q, h->Ls, sf.data(), sb.data()); break;
+		case 8: host_spikes<8>(ffh.data(), nblk_ff, N, h->Q, h->Ls, sf.data(), sb.data()); break;
+		}
+		if ((rc = dalloc(&h->spf_ff, sf.size())) || (rc = dalloc(&h->spb_ff, sb.size())) ||
+			(rc = dalloc(&h->spf_c, nblk_c * N * P)) || (rc = dalloc(&h->spb_c, nblk_c * N * P)))
+			return fail(rc);
+		if (cudaMemcpy(h->spf_ff, sf.data(), sizeof(double2) * sf.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
+			cudaMemcpy(h->spb_ff, sb.data(), sizeof(double2) * sb.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
+			cudaMemset(h->spf_c, 0, sizeof(double2) * nblk_c * N * P) != cudaSuccess ||
+			cudaMemset(h->spb_c, 0, sizeof(double2) * nblk_c * N * P) != cudaSuccess) {
+			set_error("initial device copies failed");
+			return fail(QPC_ERR_CUDA);
+		}
+	}
 	if (h->hpi) {
 		std::vector<int> id(h->B);
 		for (int k = 0; k < h->B; ++k) id[k] = k;
@@ -880,6 +956,7 @@ static int create_impl(const qpc_dims* dims, double dt, const double* S, const d
 	set_smem_attrs(h, smem);
 	std::memset(h->gsel, 0, sizeof(h->gsel));
 	for (int g = 1; g <= P; ++g) if (P % g == 0 && (g <= 4 || g == P)) h->gcand.push_back(g);
+	if (h->seg_ok) h->gcand.push_back(QPC_SEG);	// the segmented solver
 	*out = h;
 	return QPC_OK;
 }
@@ -901,6 +978,7 @@ int qpc_lgwz_destroy(qpc_lgwz* h)
 	if (h->stream) cudaStreamSynchronize(h->stream);
 	cudaFree(h->S); cudaFree(h->R); cudaFree(h->Vh); cudaFree(h->lamp); cudaFree(h->ff);
 	cudaFree(h->ffmap); cudaFree(h->ffmap_id);
+	cudaFree(h->spf_c); cudaFree(h->spb_c); cudaFree(h->spf_ff); cudaFree(h->spb_ff);
 	cudaFree(h->st); cudaFree(h->eo); cudaFree(h->wk); cudaFree(h->hostlay); cudaFree(h->fac);
 	cudaFree(h->status); cudaFree(h->red); cudaFree(h->ntf); cudaFree(h->ntt); cudaFree(h->ftab);
 	cudaFree(h->obsF); cudaFree(h->obs); cudaFree(h->dl); cudaFree(h->y10d); cudaFree(h->zdev);
