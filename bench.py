@@ -484,6 +484,16 @@ def run_c0(args):
         dev_ms = prop.last_run_ms()
         launches = prop.launch_count() - l0
     norm = prop.norm()[0]
+    ktimes = None
+    if args.kernel_times:
+        # per-kernel device time (CUDA events around every launch) over 1000 steps of the same pulse
+        prop.put(c0[None])
+        prop.enable_profiling(True)
+        prop.run(f[None, :1001], [1000])
+        ktimes = {k: {"us_per_step": 1e3 * ms / 1000, "launches": n} for k, (ms, n) in prop.kernel_times().items()}
+        ktimes["_step_us_with_events"] = 1e3 * prop.last_run_ms() / 1000
+        prop.enable_profiling(False)
+    tuning = prop.tuning()
     cpu = cpu_baseline(q, S, R, H, c0, f[None, :], dt, n_l, budget_s=args.cpu_seconds) if not args.no_cpu else None
     return {
         "metric": "wavefunction-steps/s (one hydrogen atom, whole 4-cycle pulse)",
@@ -493,7 +503,7 @@ def run_c0(args):
         "config": {"workload": "C0: H atom, N_r=400 on [0,200], p=6, l_max=20, 800 nm, 1e14 W/cm^2, 4 cycles, dt=0.05"},
         "e2e": {"value": nt / e2e_s, "unit": "wf-steps/s", "h2d_bytes_per_step": (c0.nbytes + f.nbytes) / nt,
                 "d2h_bytes_per_step": out.nbytes / nt},
-        "gpu_launches": int(launches), "final_norm": float(norm),
+        "gpu_launches": int(launches), "final_norm": float(norm), "tuning": tuning, "kernel_times": ktimes,
         "roofline": {"bound": "fp64 (latency: one wavefunction's recurrences are sequential in r)",
                      "kernel": "whole step", "achieved": path_flops(n_r, p, n_l) * nt / (dev_ms * 1e-3) / 1e12,
                      "peak": FP64_PEAK_TFLOPS, "unit": "TFLOP/s",
@@ -749,6 +759,7 @@ def main():
     ap.add_argument("--batch", type=int, default=256)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--kernel-times", action="store_true", help="c0: per-kernel device times over 1000 steps")
     ap.add_argument("--workload", default="c2", choices=["c2", "c0", "c1", "c3", "c3a", "c3arn", "pcs", "tsurff"])
     args = ap.parse_args()
     if args.workload == "c0":
