@@ -64,6 +64,23 @@ const char* qpc_last_error(void);
 /* Engine version string; also reports the SM arch the library was built for. */
 const char* qpc_version(void);
 
+/* Bound, in seconds, of every wait of this library's host code for the GPU (process-wide;
+ * default 600 s, or the value of the environment variable QPC_WAIT_LIMIT_S when it is set
+ * before the first wait).  A wait that runs out returns QPC_ERR_TIMEOUT; the work it waited
+ * for stays queued on the handle's stream and the next call on the handle waits for it
+ * again.  Results reach host memory only after a wait has succeeded, so a call that times
+ * out leaves no copy pending into the caller's buffers.  The reference's calls have no such
+ * channel: they run on the calling host thread (its propagate is noexcept, cn_1e.hpp:595).
+ * Errors: QPC_ERR_ARGS for a value that is not positive and finite. */
+int qpc_set_wait_limit(double seconds);
+double qpc_get_wait_limit(void);
+
+/* FP64 FMA throughput of the current device in TFLOP/s (FMA = 2 flops), measured by a probe
+ * kernel of independent DFMA chains timed with CUDA events (best of 5 launches of ~20 ms):
+ * the denominator of the FP64 roofline fractions this engine reports.  No counterpart in the
+ * reference. */
+int qpc_fp64_peak(double* tflops);
+
 /* ---------------------------------------------------------------- setup (host)
  * One-time matrix construction, done on the host as in the reference. */
 
@@ -152,6 +169,10 @@ int qpc_lgwz_put_device(qpc_lgwz* h, const double* dev_coef);
 int qpc_lgwz_get_device(qpc_lgwz* h, double* dev_coef);
 /* The grid and batch size the handle was created with. */
 int qpc_lgwz_dims(qpc_lgwz* h, qpc_dims* dims);
+/* The handle's CUDA stream (a cudaStream_t): every call on the handle is ordered on it,
+ * so a caller can order its own device work (events, copies into put_device buffers)
+ * before or after the engine's.  No counterpart in the reference (it has no device code). */
+int qpc_lgwz_stream(qpc_lgwz* h, void** stream);
 
 /* One call of propagate(coef, ez_ti, ez_tf) (cn_1e.hpp:595-613) for every
  * instance: f_ti[inst], f_tf[inst] are the field at t_i and t_{i+1}. */
@@ -243,7 +264,8 @@ int qpc_lgwz_kernel_times(qpc_lgwz* h, double* ms, int64_t* launches);
  * [lmax+1][n_r][p+1]; propagate(coef, ax_ti, ax_tf, ay_ti, ay_tf) and propagate(coef)
  * (cn_1e.hpp:903-950) per instance; run() the driver loop (sphTDSE.cpp:930-950 for the
  * elliptical pulse) with atab[inst][s][2] = (A_x, A_y)(t_s), s = 0..nt_field[inst].
- * The four coupling transforms are dense n_m n_l x n_m n_l matrices (cuBLAS GEMMs). */
+ * The coupling transforms are dense n_m n_l x n_m n_l matrices, block-diagonal in l-parity,
+ * applied by this library's own FP64 GEMM kernels. */
 typedef struct qpc_vgwr qpc_vgwr;
 int qpc_vgwr_create(const qpc_dims* dims, double dt, const double* S, const double* Rinv, const double* D, const double* H,
 	qpc_vgwr** out);
@@ -258,6 +280,12 @@ int qpc_vgwr_propagate_free(qpc_vgwr* h);
 int qpc_vgwr_run(qpc_vgwr* h, const double* atab, int64_t ld, const int64_t* nt_field, const int64_t* nt_total);
 int qpc_vgwr_norm(qpc_vgwr* h, double* norm);
 int qpc_vgwr_last_run(qpc_vgwr* h, float* ms, int64_t* launches);
+/* Per-kernel timing of qpc_vgwr_run: when on, each launch group is bracketed by CUDA events on
+ * the handle's stream and run() accumulates the times per kind (setting it clears the totals):
+ * ms[3], launches[3] for 0 = the (m,l) transforms (one entry per transform, both parity
+ * blocks), 1 = the coupling Crank-Nicolson solves, 2 = the field-free step. */
+int qpc_vgwr_set_profiling(qpc_vgwr* h, int on);
+int qpc_vgwr_kernel_times(qpc_vgwr* h, double* ms, int64_t* launches);
 
 /* ---------------------------------------------------------------- Arnoldi propagator
  * Replaces propagator_hc_lgwz (spherical/propagator/la_1e.hpp:390-444) with
@@ -329,20 +357,24 @@ int qpc_mlp_predict(qpc_mlp* h, const float* X, int32_t n, float* out);
  * cannot call cudaMalloc -- a framework that owns every device allocation
  * through its own pool, code running while a stream is being captured, or an
  * embedding with a fixed device-memory budget -- this entry point performs the
- * field-free Crank-Nicolson step propagate(coef) of cn_1e.hpp:615-618 on
- * buffers the caller owns, and allocates nothing: its scratch is a fixed array
+ * field-free Crank-Nicolson step of qpc_lgwz_propagate_free on buffers the
+ * caller owns, and allocates nothing: its scratch is a fixed array
  * of 2 * QPC_NOALLOC_MAX_ELEMS complex128 values (32 MiB) compiled into the
  * library, which every GPU that loads the library holds until the process exits.
  *   coef  device, [n_inst][n_m][n_l][n_r] complex128, in/out
  *   S     device, [n_r][p+1] overlap band
- *   ffac  device, [lmax+1][n_r][p+1] complex128: the LDL^T factors of S + i dt/2 H_l,
+ *   ffac  device, [lmax+1][n_r][p+1] complex128 with lmax = n_l - 1 + max(|m0|, |m0+n_m-1|)
+ *         (channel (m, il) uses row l = il + |m|): the LDL^T factors of S + i dt/2 H_l,
  *         entries 0..p-1 of row r = L(r, r-1-c) and entry p = 1/D(r)
  *         (what qpc_ldlt_csym returns, packed per l)
  *   stream  a cudaStream_t (NULL = legacy default stream); the call only enqueues work
  * Limit: n_inst*n_m*n_l*n_r + ceil(n_inst/2) <= QPC_NOALLOC_MAX_ELEMS, otherwise
  * QPC_ERR_ARGS with a message.  The first call on a device looks up the
  * scratch's device address (cudaGetSymbolAddress) with that device current;
- * make that first call before any stream capture.  All calls on a device share
+ * make that first call before any stream capture.  The address is kept per
+ * device for the CUDA runtime's primary context of that device (the context
+ * cudaSetDevice makes current); a caller that makes its own driver-API context
+ * current must not use this entry point.  All calls on a device share
  * the one scratch array and it keeps the previous call's contents, so calls
  * that overlap on the GPU (different streams or host threads) race: serialise
  * them.  Nothing in the scratch needs to start at zero: every call writes what

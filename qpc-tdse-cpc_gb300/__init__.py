@@ -27,7 +27,8 @@ POTENTIAL_YUKAWA = 1
 
 # every symbol include/qpc_gb300.h declares
 EXPORTS = (
-    "qpc_last_error", "qpc_version", "qpc_linear_knots", "qpc_radial_setup", "qpc_y10_coupling",
+    "qpc_last_error", "qpc_version", "qpc_set_wait_limit", "qpc_get_wait_limit", "qpc_fp64_peak",
+    "qpc_lgwz_stream", "qpc_vgwr_set_profiling", "qpc_vgwr_kernel_times", "qpc_linear_knots", "qpc_radial_setup", "qpc_y10_coupling",
     "qpc_y10_eigen", "qpc_ldlt_csym", "qpc_gen_eigen", "qpc_field_sinen", "qpc_lgwz_create",
     "qpc_lgwz_destroy", "qpc_lgwz_put", "qpc_lgwz_get", "qpc_lgwz_put_device", "qpc_lgwz_get_device",
     "qpc_lgwz_propagate", "qpc_lgwz_propagate_free", "qpc_lgwz_run", "qpc_lgwz_norm", "qpc_lgwz_dipole",
@@ -138,6 +139,8 @@ def load(path=None):
         "qpc_vgwr_run": (ctypes.c_int, [P, P, i64, P, P]),
         "qpc_vgwr_norm": (ctypes.c_int, [P, P]),
         "qpc_vgwr_last_run": (ctypes.c_int, [P, P, P]),
+        "qpc_vgwr_set_profiling": (ctypes.c_int, [P, ctypes.c_int]),
+        "qpc_vgwr_kernel_times": (ctypes.c_int, [P, P, P]),
         "qpc_mlp_destroy": (ctypes.c_int, [P]),
         "qpc_mlp_param_count": (ctypes.c_int, [P, P]),
         "qpc_mlp_get_params": (ctypes.c_int, [P, i32, P]),
@@ -156,6 +159,10 @@ def load(path=None):
         "qpc_arnoldi_norm": (ctypes.c_int, [P, P]),
         "qpc_arnoldi_last_run": (ctypes.c_int, [P, P, P]),
         "qpc_lgwz_dims": (ctypes.c_int, [P, P]),
+        "qpc_lgwz_stream": (ctypes.c_int, [P, P]),
+        "qpc_set_wait_limit": (ctypes.c_int, [d]),
+        "qpc_fp64_peak": (ctypes.c_int, [P]),
+        "qpc_get_wait_limit": (d, []),
         "qpc_vgwr_dims": (ctypes.c_int, [P, P]),
         "qpc_coulomb_f": (ctypes.c_int, [d, d, i32, P, P]),
         "qpc_coulomb_sigma": (ctypes.c_int, [d, i32, P]),
@@ -192,6 +199,22 @@ def _ptr(a):
 def _check(rc):
     if rc != QPC_OK:
         raise QpcError(rc, load().qpc_last_error().decode())
+
+
+def set_wait_limit(seconds):
+    """Bound of every host wait of the engine for the GPU (qpc_set_wait_limit)."""
+    _check(load().qpc_set_wait_limit(float(seconds)))
+
+
+def get_wait_limit():
+    return float(load().qpc_get_wait_limit())
+
+
+def fp64_peak():
+    """FP64 FMA throughput of the current device in TFLOP/s (qpc_fp64_peak)."""
+    v = ctypes.c_double(0)
+    _check(load().qpc_fp64_peak(ctypes.byref(v)))
+    return v.value
 
 
 def _f64(a):
@@ -402,6 +425,12 @@ class propagator_cn_hc_lgwz:
         c = np.zeros(self.shape, np.complex128)
         _check(load().qpc_lgwz_get(self._h, _ptr(c)))
         return c
+
+    def stream(self):
+        """The handle's cudaStream_t as an integer (qpc_lgwz_stream)."""
+        v = ctypes.c_void_p()
+        _check(load().qpc_lgwz_stream(self._h, ctypes.byref(v)))
+        return int(v.value or 0)
 
     def put_device(self, dev_ptr):
         _check(load().qpc_lgwz_put_device(self._h, ctypes.c_void_p(dev_ptr)))
@@ -792,6 +821,16 @@ class propagator_cn_hc_vgwr:
         n = ctypes.c_int64(0)
         _check(load().qpc_vgwr_last_run(self._h, ctypes.byref(ms), ctypes.byref(n)))
         return ms.value, n.value
+
+    def enable_profiling(self, on=True):
+        _check(load().qpc_vgwr_set_profiling(self._h, int(bool(on))))
+
+    def kernel_times(self):
+        """{"transform" | "coupling" | "fieldfree": (total ms, launch groups)} of run() while profiling is on."""
+        ms = np.zeros(3)
+        n = np.zeros(3, np.int64)
+        _check(load().qpc_vgwr_kernel_times(self._h, _ptr(ms), _ptr(n)))
+        return {k: (float(ms[i]), int(n[i])) for i, k in enumerate(("transform", "coupling", "fieldfree"))}
 
 
 

@@ -46,7 +46,8 @@ def _run(cmd):
 def build_engine(force=False, verbose=False):
     srcs = [os.path.join(CSRC, f) for f in ("qpc_engine.cu", "qpc_setup.cpp", "qpc_internal.h", "qpc_chain.cuh",
                                              "qpc_noalloc.cu", "qpc_spectra.cpp", "qpc_arnoldi.cu", "qpc_cuda_util.cuh",
-                                             "qpc_mlp.cu", "qpc_vgwr.cu", "qpc_momentum.cu", "qpc_momentum.cpp")]
+                                             "qpc_mlp.cu", "qpc_vgwr.cu", "qpc_momentum.cu", "qpc_momentum.cpp",
+                                             "qpc_gemm.cuh")]
     srcs.append(os.path.join(ROOT, "include", "qpc_gb300.h"))
     if not force and not _stale(LIB, srcs):
         return LIB
@@ -74,7 +75,7 @@ def build_engine(force=False, verbose=False):
     ]
     with cf.ThreadPoolExecutor(len(jobs)) as ex:
         outs = list(ex.map(_run, jobs))
-    _run([_nvcc()] + NVCC_ARCH + ["-shared", o_cu, o_na, o_ar, o_ml, o_vg, o_mo, o_mt, o_cc, o_sp, "-o", LIB + ".tmp", "-lcudart", "-lcublas", "-lcusolver", "-lpthread"])
+    _run([_nvcc()] + NVCC_ARCH + ["-shared", o_cu, o_na, o_ar, o_ml, o_vg, o_mo, o_mt, o_cc, o_sp, "-o", LIB + ".tmp", "-lcudart", "-lcusolver", "-lpthread"])
     os.replace(LIB + ".tmp", LIB)
     if verbose:
         print("".join(outs))
@@ -94,15 +95,18 @@ def build_oracle(force=False):
     return ORACLE_LIB
 
 
-def build_reference_oracle():
-    """Build the reference's own propagator into oracle/_ref/ when the reference
-    checkout is present (only on the development machine; never at run time on
-    a GPU machine)."""
-    ref = "/root/reference/include"
-    if not os.path.isdir(ref):
-        return None
-    _run(["make", "-C", os.path.join(ROOT, "oracle", "ref"), "-j4", "REF_INCLUDE=" + ref])
-    return os.path.join(ROOT, "oracle", "_ref")
+def build_reference_oracle(ref_dir=None):
+    """Build the reference's own propagator into oracle/_ref/ from the reference
+    checkout (test infrastructure: the golden fixtures are made with it).  The
+    checkout is ref_dir, else the environment variable QPC_REFERENCE_DIR, else the
+    development machine's checkout location; nothing is built when none exists (a
+    GPU machine has none)."""
+    cands = [ref_dir, os.environ.get("QPC_REFERENCE_DIR"), "/root/reference"]
+    for c in cands:
+        if c and os.path.isdir(os.path.join(c, "include")):
+            _run(["make", "-C", os.path.join(ROOT, "oracle", "ref"), "-j4", "REF_INCLUDE=" + os.path.join(c, "include")])
+            return os.path.join(ROOT, "oracle", "_ref")
+    return None
 
 
 if __name__ == "__main__":

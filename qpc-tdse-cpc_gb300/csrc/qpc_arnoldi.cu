@@ -728,7 +728,7 @@ long launch_step(qpc_arnoldi* h, const ar_args& g, int Bg, cudaStream_t st, long
 int read_status(qpc_arnoldi* h)
 {
 	int st = 0;
-	QPC_CUDA(cudaMemcpyAsync(&st, h->status, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+	if (int rc = copy_to_host(&st, h->status, sizeof(int), h->stream)) return rc;
 	QPC_CUDA(cudaMemsetAsync(h->status, 0, sizeof(int), h->stream));
 	if (int rc = wait_on(h->stream)) return rc;
 	if (st & ARS_ZERO) { set_error("a wavefunction has zero or non-finite S-norm"); return QPC_ERR_NUMERIC; }
@@ -842,11 +842,16 @@ static int ar_transfer(qpc_arnoldi* h, const double* src, double* dst, bool put,
 	const long nst = (long)h->d.n_inst * h->n;
 	const int tb = 256;
 	const unsigned nb = (unsigned)((nst + tb - 1) / tb);
+	// host buffers are copied with the stream idle (bounded wait first): such a copy then
+	// never waits for queued work, and a wait that runs out leaves no copy pending
 	if (put) {
+		if (kind == cudaMemcpyHostToDevice) if (int rc = wait_on(h->stream)) return rc;
 		QPC_CUDA(cudaMemcpyAsync(h->tmp, src, sizeof(double2) * nst, kind, h->stream));
 		k_ar_to_rmajor<<<nb, tb, 0, h->stream>>>(h->tmp, h->X, h->d.n_r, h->nch, nst);
 	} else {
 		k_ar_to_lmajor<<<nb, tb, 0, h->stream>>>(h->X, h->tmp, h->d.n_r, h->nch, nst);
+		QPC_CUDA(cudaGetLastError());
+		if (kind == cudaMemcpyDeviceToHost) return copy_to_host(dst, h->tmp, sizeof(double2) * nst, h->stream);
 		QPC_CUDA(cudaMemcpyAsync(dst, h->tmp, sizeof(double2) * nst, kind, h->stream));
 	}
 	QPC_CUDA(cudaGetLastError());
@@ -907,6 +912,7 @@ int qpc_arnoldi_run(qpc_arnoldi* h, const double* ez, int64_t ld, const int64_t*
 		h->crit_cap = cap;
 	}
 	std::vector<long long> ntl(nt, nt + B);
+	if (int rc = wait_on(h->stream)) return rc;
 	QPC_CUDA(cudaMemcpyAsync(h->ez, ez, sizeof(double) * cap, cudaMemcpyHostToDevice, h->stream));
 	QPC_CUDA(cudaMemcpyAsync(h->nt, ntl.data(), sizeof(long long) * B, cudaMemcpyHostToDevice, h->stream));
 	ar_args g = make_args(h);
@@ -938,8 +944,8 @@ int qpc_arnoldi_run(qpc_arnoldi* h, const double* ez, int64_t ld, const int64_t*
 	if (int rc = wait_on(h->stream)) return rc;
 	cudaEventElapsedTime(&h->last_ms, h->ev0, h->ev1);
 	h->launches = nl;
-	if (crit) QPC_CUDA(cudaMemcpy(crit, h->crit, cap, cudaMemcpyDeviceToHost));
-	if (msub) QPC_CUDA(cudaMemcpy(msub, h->msub_out, cap, cudaMemcpyDeviceToHost));
+	if (crit) if (int rc = copy_to_host(crit, h->crit, cap, h->stream)) return rc;
+	if (msub) if (int rc = copy_to_host(msub, h->msub_out, cap, h->stream)) return rc;
 	return read_status(h);
 }
 
@@ -957,12 +963,13 @@ int qpc_arnoldi_norm(qpc_arnoldi* h, double* norm)
 	const int B = h->d.n_inst;
 	// one S-norm pass with every instance live at "step 0" of a one-step table
 	std::vector<long long> one(B, 1);
+	if (int rc = wait_on(h->stream)) return rc;
 	QPC_CUDA(cudaMemcpyAsync(h->nt, one.data(), sizeof(long long) * B, cudaMemcpyHostToDevice, h->stream));
 	ar_args g = make_args(h);
 	k_ar_snorm<<<dim3(h->nbe, B), AR_THREADS, 0, h->stream>>>(g, h->X, -1, 0);
 	QPC_CUDA(cudaGetLastError());
 	std::vector<double> nu(B);
-	QPC_CUDA(cudaMemcpyAsync(nu.data(), h->nu0, sizeof(double) * B, cudaMemcpyDeviceToHost, h->stream));
+	if (int rc = copy_to_host(nu.data(), h->nu0, sizeof(double) * B, h->stream)) return rc;
 	QPC_CUDA(cudaMemsetAsync(h->status, 0, sizeof(int), h->stream));
 	if (int rc = wait_on(h->stream)) return rc;
 	for (int k = 0; k < B; ++k) norm[k] = nu[k];

@@ -31,17 +31,37 @@ template <class T> inline int dalloc(T** p, size_t n)
 	return QPC_OK;
 }
 
-// bounded wait: poll the stream, give up after ~600 s of wall time
+// bounded wait: poll the stream until its work is done, give up after
+// wait_limit_s() seconds of wall time with QPC_ERR_TIMEOUT (the work stays
+// queued; a later call on the same stream waits for it again)
 inline int wait_on(cudaStream_t st)
 {
+	struct timespec t0, now;
+	clock_gettime(CLOCK_MONOTONIC, &t0);
+	const double limit = wait_limit_s();
 	for (long it = 0;; ++it) {
 		cudaError_t e = cudaStreamQuery(st);
 		if (e == cudaSuccess) return QPC_OK;
 		if (e != cudaErrorNotReady) { set_error("stream error: %s", cudaGetErrorString(e)); return QPC_ERR_CUDA; }
-		if (it > 6000000) { set_error("timed out waiting for the device"); return QPC_ERR_TIMEOUT; }
-		struct timespec ts = {0, 100000};
+		clock_gettime(CLOCK_MONOTONIC, &now);
+		if ((double)(now.tv_sec - t0.tv_sec) + 1e-9 * (double)(now.tv_nsec - t0.tv_nsec) > limit) {
+			set_error("timed out after %.3g s waiting for the device", limit);
+			return QPC_ERR_TIMEOUT;
+		}
+		struct timespec ts = {0, it < 100 ? 2000L : 100000L};
 		nanosleep(&ts, nullptr);
 	}
+}
+
+// device -> host copy of a result: wait (bounded) for the work queued before it, then
+// copy.  Waiting first means the copy never blocks on queued work (a copy into pageable
+// memory may block inside the driver until the stream reaches it, without a bound), and a
+// wait that runs out leaves no copy pending into a host buffer the caller may free.
+inline int copy_to_host(void* dst, const void* src, size_t bytes, cudaStream_t st)
+{
+	if (int rc = wait_on(st)) return rc;
+	QPC_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, st));
+	return wait_on(st);
 }
 
 } // namespace qpc

@@ -40,6 +40,7 @@
 #include <time.h>
 #include <thread>
 #include <mutex>
+#include <atomic>
 #include <map>
 #include <cstdlib>
 #include "qpc_chain.cuh"
@@ -52,6 +53,21 @@ void set_error(const char* fmt, ...)
 	va_list ap; va_start(ap, fmt);
 	vsnprintf(g_err, sizeof(g_err), fmt, ap);
 	va_end(ap);
+}
+
+// the bound of every host wait; 0 = not set yet (then the environment or the default)
+static std::atomic<double> g_wait_limit{0.0};
+double wait_limit_s()
+{
+	double v = g_wait_limit.load(std::memory_order_relaxed);
+	if (v > 0) return v;
+	const char* e = std::getenv("QPC_WAIT_LIMIT_S");
+	char* end = nullptr;
+	double x = e ? std::strtod(e, &end) : 0.0;
+	v = (e && end != e && x > 0 && std::isfinite(x)) ? x : 600.0;
+	double zero = 0.0;
+	g_wait_limit.compare_exchange_strong(zero, v);
+	return g_wait_limit.load(std::memory_order_relaxed);
 }
 
 
@@ -518,9 +534,7 @@ int wait_stream(qpc_lgwz* h) { return wait_on(h->stream); }
 int read_status(qpc_lgwz* h)
 {
 	int st = 0;
-	QPC_CUDA(cudaMemcpyAsync(&st, h->status, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
-	int rc = wait_stream(h);
-	if (rc) return rc;
+	if (int rc = copy_to_host(&st, h->status, sizeof(int), h->stream)) return rc;
 	if (st & ST_PIVOT) { set_error("zero pivot in a Crank-Nicolson factorisation"); return QPC_ERR_SINGULAR; }
 	if (st & ST_NONFINITE) { set_error("non-finite value in the state"); return QPC_ERR_NUMERIC; }
 	return QPC_OK;
@@ -818,6 +832,67 @@ static void host_spikes(const double2* fac, size_t nblk, int N, int Q, int Ls, d
 extern "C" {
 
 const char* qpc_last_error(void) { return g_err; }
+
+// FP64 FMA throughput probe: every thread advances 8 independent chains of dependent DFMAs
+// (x <- a x + b with the fixed point 1, so values stay normal); one output per thread
+__global__ void __launch_bounds__(256) k_dfma_probe(double* __restrict__ out, int iters, double a, double b)
+{
+	double x[8];
+#pragma unroll
+	for (int i = 0; i < 8; ++i) x[i] = 1.0 + 1e-3 * (threadIdx.x + 37 * i);
+	for (int it = 0; it < iters; ++it) {
+#pragma unroll
+		for (int i = 0; i < 8; ++i) x[i] = fma(x[i], a, b);
+	}
+	double s = 0.0;
+#pragma unroll
+	for (int i = 0; i < 8; ++i) s += x[i];
+	out[(long)blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
+int qpc_fp64_peak(double* tflops)
+{
+	if (!tflops) { set_error("NULL argument"); return QPC_ERR_ARGS; }
+	*tflops = 0.0;
+	int dev = 0;
+	if (int rc = check_device(&dev)) return rc;
+	int nsm = 0;
+	QPC_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+	const int threads = 256, blocks = 4 * nsm, iters = 8192;
+	double* out = nullptr;
+	if (int rc = dalloc(&out, (size_t)blocks * threads)) return rc;	// one value per launched thread
+	cudaStream_t st = nullptr;
+	cudaEvent_t e0 = nullptr, e1 = nullptr;
+	int rc = QPC_OK;
+	if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess || cudaEventCreate(&e0) != cudaSuccess ||
+		cudaEventCreate(&e1) != cudaSuccess) { set_error("stream or event creation failed"); rc = QPC_ERR_CUDA; }
+	float best = 0.f;
+	for (int rep = 0; rep < 6 && !rc; ++rep) {	// the first launch warms up
+		cudaEventRecord(e0, st);
+		k_dfma_probe<<<blocks, threads, 0, st>>>(out, iters, 0.9999999, 1e-7);
+		cudaEventRecord(e1, st);
+		if (cudaGetLastError() != cudaSuccess) { set_error("probe launch failed"); rc = QPC_ERR_CUDA; break; }
+		if ((rc = wait_on(st))) break;
+		float ms = 0.f;
+		cudaEventElapsedTime(&ms, e0, e1);
+		if (rep > 0 && (best == 0.f || ms < best)) best = ms;
+	}
+	if (!rc && best > 0.f) *tflops = 2.0 * 8.0 * iters * (double)blocks * threads / (best * 1e-3) / 1e12;
+	if (!rc) { cudaFree(out); out = nullptr; }	// after a timeout the probe may still be running: keep its buffer
+	if (e0) cudaEventDestroy(e0);
+	if (e1) cudaEventDestroy(e1);
+	if (st) cudaStreamDestroy(st);
+	return rc;
+}
+
+int qpc_set_wait_limit(double seconds)
+{
+	if (!(seconds > 0) || !std::isfinite(seconds)) { set_error("wait limit %g s: must be positive and finite", seconds); return QPC_ERR_ARGS; }
+	g_wait_limit.store(seconds, std::memory_order_relaxed);
+	return QPC_OK;
+}
+
+double qpc_get_wait_limit(void) { return wait_limit_s(); }
 const char* qpc_version(void) { return "qpc-gb300 engine 1 (sm_103a, complex FP64)"; }
 
 static int create_impl(const qpc_dims* dims, double dt, const double* S, const double* R, const double* H, int hpi, qpc_lgwz** out)
@@ -1000,6 +1075,8 @@ int qpc_lgwz_destroy(qpc_lgwz* h)
 static int put_common(qpc_lgwz* h, const double* src, cudaMemcpyKind kind)
 {
 	long sl = state_len(h);
+	// the stream idle first: a copy from pageable memory then never waits for queued work
+	if (kind == cudaMemcpyHostToDevice) if (int rc = wait_stream(h)) return rc;
 	QPC_CUDA(cudaMemcpyAsync(h->hostlay, src, sizeof(double2) * sl, kind, h->stream));
 	long nblk = (long)h->B * h->M;
 	k_to_rmajor<<<(unsigned)((sl + 255) / 256), 256, 0, h->stream>>>(h->hostlay, h->st, h->N, h->L, nblk);
@@ -1014,6 +1091,7 @@ static int get_common(qpc_lgwz* h, double* dst, cudaMemcpyKind kind)
 	k_to_lmajor<<<(unsigned)((sl + 255) / 256), 256, 0, h->stream>>>(h->st, h->hostlay, h->N, h->L, nblk);
 	LAUNCH(h);
 	QPC_CUDA(cudaGetLastError());
+	if (kind == cudaMemcpyDeviceToHost) return copy_to_host(dst, h->hostlay, sizeof(double2) * sl, h->stream);
 	QPC_CUDA(cudaMemcpyAsync(dst, h->hostlay, sizeof(double2) * sl, kind, h->stream));
 	return wait_stream(h);
 }
@@ -1044,12 +1122,21 @@ int qpc_lgwz_dims(qpc_lgwz* h, qpc_dims* dims)
 	*dims = h->d;
 	return QPC_OK;
 }
+int qpc_lgwz_stream(qpc_lgwz* h, void** stream)
+{
+	if (!h || !stream) { set_error("NULL argument"); return QPC_ERR_ARGS; }
+	*stream = (void*)h->stream;
+	return QPC_OK;
+}
 
 static int run_impl(qpc_lgwz* h, const double* ftab, int64_t ld, const int64_t* nt_field, const int64_t* nt_total,
 	const double* F, double* zlist, int64_t ldz)
 {
 	if (!h || !nt_field || !nt_total) { set_error("NULL argument"); return QPC_ERR_ARGS; }
 	QPC_CUDA(cudaSetDevice(h->dev));
+	// the stream idle first (bounded): the copies from host memory below then never wait
+	// for queued work (after a call that timed out, the work it left is waited for here)
+	if (int rc = wait_stream(h)) return rc;
 	h->observing = false;
 	const int B = h->B;
 	long smax = 0;
@@ -1182,8 +1269,7 @@ static int run_impl(qpc_lgwz* h, const double* ftab, int64_t ld, const int64_t* 
 	collect_profile(h);
 	if (F && rc == QPC_OK) {
 		std::vector<double> zh((size_t)B * ldz);
-		QPC_CUDA(cudaMemcpyAsync(zh.data(), h->zdev, sizeof(double) * zh.size(), cudaMemcpyDeviceToHost, h->stream));
-		if (int rc2 = wait_stream(h)) return rc2;
+		if (int rc2 = copy_to_host(zh.data(), h->zdev, sizeof(double) * zh.size(), h->stream)) return rc2;
 		for (int k = 0; k < B; ++k) std::memcpy(zlist + (size_t)perm[k] * ldz, zh.data() + (size_t)k * ldz, sizeof(double) * ldz);
 	}
 	return rc;
@@ -1254,8 +1340,7 @@ int qpc_lgwz_norm(qpc_lgwz* h, double* norm)
 	LAUNCH(h);
 	QPC_CUDA(cudaGetLastError());
 	std::vector<double2> part(nch);
-	QPC_CUDA(cudaMemcpyAsync(part.data(), h->red, sizeof(double2) * nch, cudaMemcpyDeviceToHost, h->stream));
-	if (int rc = wait_stream(h)) return rc;
+	if (int rc = copy_to_host(part.data(), h->red, sizeof(double2) * nch, h->stream)) return rc;
 	long per = (long)h->M * h->L;
 	for (int k = 0; k < h->B; ++k) {
 		double s = 0.0;
@@ -1269,6 +1354,7 @@ int qpc_lgwz_mask(qpc_lgwz* h, const double* M)
 {
 	if (!h || !M) { set_error("NULL argument"); return QPC_ERR_ARGS; }
 	const int N = h->N, P = h->P, NE = P + 1;
+	if (int rc = wait_stream(h)) return rc;
 	if (!h->mLrow) {
 		std::vector<double> S((size_t)N * NE), Lc((size_t)N * NE);
 		QPC_CUDA(cudaMemcpy(S.data(), h->S, sizeof(double) * S.size(), cudaMemcpyDeviceToHost));
@@ -1315,8 +1401,10 @@ int qpc_lgwz_dipole(qpc_lgwz* h, const double* F, double* out)
 {
 	if (!h || !F || !out) { set_error("NULL argument"); return QPC_ERR_ARGS; }
 	const int N = h->N, NE = h->P + 1, L = h->L, M = h->M;
+	if (int rc = wait_stream(h)) return rc;
+	// stream-ordered scratch: freed in stream order, so no later wait can block on it
 	double* dF = nullptr;
-	if (int rc = dalloc(&dF, (size_t)N * NE)) return rc;
+	if (cudaMallocAsync((void**)&dF, sizeof(double) * N * NE, h->stream) != cudaSuccess) { set_error("cudaMallocAsync failed"); return QPC_ERR_NOMEM; }
 	long nch = (long)h->B * M * L;
 	double2* red2 = h->red + nch;
 	int rc = QPC_OK;
@@ -1327,12 +1415,11 @@ int qpc_lgwz_dipole(qpc_lgwz* h, const double* F, double* out)
 		h->launches += 2;
 		if (cudaGetLastError() != cudaSuccess) rc = QPC_ERR_CUDA;
 	}
+	cudaFreeAsync(dF, h->stream);
+	if (rc) { set_error("dipole device step failed"); return rc; }
 	std::vector<double2> lo(nch), hi(nch);
-	if (!rc && (cudaMemcpyAsync(lo.data(), h->red, sizeof(double2) * nch, cudaMemcpyDeviceToHost, h->stream) != cudaSuccess ||
-		cudaMemcpyAsync(hi.data(), red2, sizeof(double2) * nch, cudaMemcpyDeviceToHost, h->stream) != cudaSuccess)) rc = QPC_ERR_CUDA;
-	if (!rc) rc = wait_stream(h);
-	cudaFree(dF);
-	if (rc) { if (rc == QPC_ERR_CUDA) set_error("dipole device step failed"); return rc; }
+	if ((rc = copy_to_host(lo.data(), h->red, sizeof(double2) * nch, h->stream)) ||
+		(rc = copy_to_host(hi.data(), red2, sizeof(double2) * nch, h->stream))) return rc;
 	std::vector<double> y(L);
 	for (int k = 0; k < h->B; ++k) {
 		double re = 0.0, im = 0.0;
@@ -1368,14 +1455,15 @@ int qpc_lgwz_projection(qpc_lgwz* h, const int32_t* n_state, const double* basis
 		poff[c + 1] = poff[c] + n_state[l];
 	}
 	if (nmax == 0) return QPC_OK;
-	double *db = nullptr; long *dbo = nullptr, *dpo = nullptr; int* dn = nullptr; double2* dp = nullptr;
-	int rc = QPC_OK;
-	if ((rc = dalloc(&db, (size_t)boff[nl])) || (rc = dalloc(&dbo, (size_t)nl + 1)) || (rc = dalloc(&dpo, (size_t)nch + 1)) ||
-		(rc = dalloc(&dn, (size_t)nl)) || (rc = dalloc(&dp, (size_t)poff[nch]))) {
-		cudaFree(db); cudaFree(dbo); cudaFree(dpo); cudaFree(dn); cudaFree(dp);
-		return rc;
-	}
-	bool ok = cudaMemcpyAsync(db, basis, sizeof(double) * boff[nl], cudaMemcpyHostToDevice, h->stream) == cudaSuccess &&
+	if (int rc = wait_stream(h)) return rc;
+	// stream-ordered scratch: freed in stream order, so no later wait can block on it
+	void* buf[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+	const size_t bytes[5] = {sizeof(double) * (size_t)std::max<long>(boff[nl], 1), sizeof(long) * (nl + 1), sizeof(long) * (nch + 1),
+		sizeof(int) * (size_t)nl, sizeof(double2) * (size_t)std::max<long>(poff[nch], 1)};
+	bool ok = true;
+	for (int i = 0; i < 5 && ok; ++i) ok = cudaMallocAsync(&buf[i], bytes[i], h->stream) == cudaSuccess;
+	double* db = (double*)buf[0]; long* dbo = (long*)buf[1]; long* dpo = (long*)buf[2]; int* dn = (int*)buf[3]; double2* dp = (double2*)buf[4];
+	ok = ok && cudaMemcpyAsync(db, basis, sizeof(double) * boff[nl], cudaMemcpyHostToDevice, h->stream) == cudaSuccess &&
 		cudaMemcpyAsync(dbo, boff.data(), sizeof(long) * (nl + 1), cudaMemcpyHostToDevice, h->stream) == cudaSuccess &&
 		cudaMemcpyAsync(dpo, poff.data(), sizeof(long) * (nch + 1), cudaMemcpyHostToDevice, h->stream) == cudaSuccess &&
 		cudaMemcpyAsync(dn, n_state, sizeof(int) * nl, cudaMemcpyHostToDevice, h->stream) == cudaSuccess;
@@ -1383,12 +1471,11 @@ int qpc_lgwz_projection(qpc_lgwz* h, const int32_t* n_state, const double* basis
 		long tot = nch * nmax;
 		k_projection<<<(unsigned)((tot + 127) / 128), 128, 0, h->stream>>>(h->st, db, dbo, dn, dpo, N, L, M, h->d.m0, nch, nmax, dp);
 		LAUNCH(h);
-		ok = cudaGetLastError() == cudaSuccess &&
-			cudaMemcpyAsync(proj, dp, sizeof(double2) * poff[nch], cudaMemcpyDeviceToHost, h->stream) == cudaSuccess;
+		ok = cudaGetLastError() == cudaSuccess;
 	}
-	rc = ok ? wait_stream(h) : QPC_ERR_CUDA;
+	int rc = ok ? copy_to_host(proj, dp, sizeof(double2) * poff[nch], h->stream) : QPC_ERR_CUDA;
 	if (!ok) set_error("projection device step failed");
-	cudaFree(db); cudaFree(dbo); cudaFree(dpo); cudaFree(dn); cudaFree(dp);
+	for (int i = 0; i < 5; ++i) if (buf[i]) cudaFreeAsync(buf[i], h->stream);
 	return rc;
 }
 

@@ -21,6 +21,9 @@ void build_basis(radial_basis& B);
 void bspline_eval(const std::vector<double>& t, int s, int p, double x, double* out0, double* out1);
 
 void set_error(const char* fmt, ...);
+// bound of every host wait for the device, in seconds (qpc_set_wait_limit; the
+// environment variable QPC_WAIT_LIMIT_S read at first use; default 600 s)
+double wait_limit_s();
 // real symmetric form D^H Z_c D of a propagator_cn_hc_vgwr coupling (qpc_setup.cpp)
 void vgwr_real_coupling(int n_l, int n_m, int m0, int comp, double* Zr);
 }

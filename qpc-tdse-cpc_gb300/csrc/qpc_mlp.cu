@@ -354,10 +354,14 @@ int backward(qpc_mlp* h, int Mvalid, back_bufs& bb)
 	const int E = h->E, J = h->J, M = h->Mcap;
 	const int maxN = *std::max_element(h->Ns.begin(), h->Ns.end());
 	if (!bb.G2) {
-		int rc;
-		if ((rc = dalloc(&bb.G2, (size_t)E * h->Mcap * maxN)) || (rc = dalloc(&bb.G2b, (size_t)E * h->Mcap * maxN)) ||
-			(rc = dalloc(&bb.G2t, (size_t)E * h->Mcap * maxN)))
-			return rc;
+		// stream-ordered: freed in stream order by free_back, which never blocks
+		const size_t n = (size_t)E * h->Mcap * maxN;
+		if (cudaMallocAsync((void**)&bb.G2, sizeof(float) * n, h->st) != cudaSuccess ||
+			cudaMallocAsync((void**)&bb.G2b, sizeof(__nv_bfloat16) * n, h->st) != cudaSuccess ||
+			cudaMallocAsync((void**)&bb.G2t, sizeof(__nv_bfloat16) * n, h->st) != cudaSuccess) {
+			set_error("cudaMallocAsync of the gradient scratch failed");
+			return QPC_ERR_NOMEM;
+		}
 	}
 	const float scale = 1.0f / ((float)Mvalid * (float)h->n_out);
 	const long sg = (long)h->Mcap * maxN;
@@ -430,11 +434,11 @@ int upload_data(qpc_mlp* h, const float* X, const float* Y, long n)
 	return QPC_OK;
 }
 
-void free_back(back_bufs& bb)
+void free_back(back_bufs& bb, cudaStream_t st)
 {
-	if (bb.G2) cudaFree(bb.G2);
-	if (bb.G2b) cudaFree(bb.G2b);
-	if (bb.G2t) cudaFree(bb.G2t);
+	if (bb.G2) cudaFreeAsync(bb.G2, st);
+	if (bb.G2b) cudaFreeAsync(bb.G2b, st);
+	if (bb.G2t) cudaFreeAsync(bb.G2t, st);
 	bb = back_bufs{};
 }
 
@@ -567,15 +571,15 @@ int qpc_mlp_loss_grad(qpc_mlp* h, const float* X, const float* Y, int32_t n, flo
 	back_bufs bb;
 	int rc = backward(h, n, bb);
 	if (!rc && cudaGetLastError() != cudaSuccess) { set_error("kernel launch failed"); rc = QPC_ERR_CUDA; }
-	if (!rc && cudaStreamSynchronize(h->st) != cudaSuccess) { set_error("device error"); rc = QPC_ERR_CUDA; }
-	free_back(bb);
-	if (rc) return rc;
-	QPC_CUDA(cudaMemcpy(loss, h->loss, sizeof(float) * h->E, cudaMemcpyDeviceToHost));
+	if (!rc) rc = wait_on(h->st);
+	if (rc) { free_back(bb, h->st); return rc; }
+	free_back(bb, h->st);
+	if (int rc2 = copy_to_host(loss, h->loss, sizeof(float) * h->E, h->st)) return rc2;
 	if (grad) {
 		const long np = h->nW + h->nb;
 		std::vector<float> gw((size_t)h->E * h->nW), gbv((size_t)h->E * h->nb);
-		QPC_CUDA(cudaMemcpy(gw.data(), h->gW, sizeof(float) * gw.size(), cudaMemcpyDeviceToHost));
-		QPC_CUDA(cudaMemcpy(gbv.data(), h->gb, sizeof(float) * gbv.size(), cudaMemcpyDeviceToHost));
+		if (int rc2 = copy_to_host(gw.data(), h->gW, sizeof(float) * gw.size(), h->st)) return rc2;
+		if (int rc2 = copy_to_host(gbv.data(), h->gb, sizeof(float) * gbv.size(), h->st)) return rc2;
 		for (int e = 0; e < h->E; ++e) {
 			long o = 0;
 			for (int j = 0; j < h->J; ++j) {
@@ -622,17 +626,15 @@ int qpc_mlp_train(qpc_mlp* h, const float* X, const float* Y, int32_t n, int32_t
 			if ((rc = backward(h, mv, bb))) break;
 			adam(h, lr);
 			if (loss_hist) {
-				if (cudaMemcpyAsync(lb.data(), h->loss, sizeof(float) * h->E, cudaMemcpyDeviceToHost, h->st) != cudaSuccess ||
-					cudaStreamSynchronize(h->st) != cudaSuccess) { rc = QPC_ERR_CUDA; break; }
+				if ((rc = copy_to_host(lb.data(), h->loss, sizeof(float) * h->E, h->st))) break;
 				for (int e = 0; e < h->E; ++e) lsum[e] += lb[e] / nbat;
 			}
 		}
 		if (loss_hist) for (int e = 0; e < h->E; ++e) loss_hist[(size_t)ep * h->E + e] = lsum[e];
 	}
-	if (!rc && cudaGetLastError() != cudaSuccess) rc = QPC_ERR_CUDA;
-	if (!rc && wait_on(h->st)) rc = QPC_ERR_CUDA;
-	free_back(bb);
-	if (rc == QPC_ERR_CUDA) set_error("training step failed on the device");
+	if (!rc && cudaGetLastError() != cudaSuccess) { rc = QPC_ERR_CUDA; set_error("training step failed on the device"); }
+	if (!rc) rc = wait_on(h->st);
+	free_back(bb, h->st);
 	return rc;
 }
 
@@ -655,8 +657,7 @@ int qpc_mlp_predict(qpc_mlp* h, const float* X, int32_t n, float* out)
 		k_mlp_gather<<<dim3(M, h->E), 64, 0, h->st>>>(h->dX, nullptr, h->idx, h->n_in, h->K0, h->n_out, M, h->Act[0], h->ActT[0], nullptr);
 		forward(h);
 		QPC_CUDA(cudaGetLastError());
-		QPC_CUDA(cudaMemcpyAsync(yh.data(), h->Yh, sizeof(float) * yh.size(), cudaMemcpyDeviceToHost, h->st));
-		if (int rc = wait_on(h->st)) return rc;
+		if (int rc = copy_to_host(yh.data(), h->Yh, sizeof(float) * yh.size(), h->st)) return rc;
 		for (int e = 0; e < h->E; ++e)
 			for (int m = 0; m < mv; ++m)
 				std::copy(yh.begin() + ((size_t)e * h->Mcap + m) * h->n_out, yh.begin() + ((size_t)e * h->Mcap + m + 1) * h->n_out,

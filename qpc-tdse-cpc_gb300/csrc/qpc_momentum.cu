@@ -319,8 +319,7 @@ int pcs_run(qpc_pcs* h, int kind, const double2* c, int n_inst, double* out)
 		d.n_l, d.n_m, total);
 	QPC_CUDA(cudaGetLastError());
 	QPC_CUDA(cudaEventRecord(h->ev1, h->st));
-	QPC_CUDA(cudaMemcpyAsync(out, h->out, sizeof(double2) * total, cudaMemcpyDeviceToHost, h->st));
-	if (int rc = wait_on(h->st)) return rc;
+	if (int rc = copy_to_host(out, h->out, sizeof(double2) * total, h->st)) return rc;
 	QPC_CUDA(cudaEventElapsedTime(&h->last_ms, h->ev0, h->ev1));
 	return QPC_OK;
 }
@@ -330,6 +329,8 @@ int ts_run(qpc_tsurff* h, int mode, const double* a, double dt, const double2* c
 {
 	const qpc_dims& d = h->d;
 	const int B = h->B, nch = d.n_m * d.n_l;
+	// the stream idle first (bounded): the copies from host memory below never wait for queued work
+	if (int rc = wait_on(h->st)) return rc;
 	// the clock, as prepare(ax, ay, az, dt) advances it (momentum_1e.hpp:620-626)
 	std::vector<double> a1((size_t)B * 2, 0.0);
 	for (int i = 0; i < B; ++i) {
@@ -410,6 +411,7 @@ int qpc_pcs_measure(qpc_pcs* h, int32_t kind, const double* coef, int32_t on_dev
 	if (!on_device) {
 		const long n = (long)n_inst * h->d.n_m * h->d.n_l * h->d.n_r;
 		if (int rc = grow(&h->cbuf, &h->cap_c, n)) return rc;
+		if (int rc = wait_on(h->st)) return rc;
 		QPC_CUDA(cudaMemcpyAsync(h->cbuf, coef, sizeof(double2) * n, cudaMemcpyHostToDevice, h->st));
 		c = h->cbuf;
 	}
@@ -500,6 +502,7 @@ int qpc_tsurff_accumulate(qpc_tsurff* h, int32_t mode, const double* a, double d
 	const double2* c = (const double2*)coef;
 	if (!on_device) {
 		const long n = (long)h->B * h->d.n_m * h->d.n_l * h->d.n_r;
+		if (int rc = wait_on(h->st)) return rc;
 		QPC_CUDA(cudaMemcpyAsync(h->cbuf, coef, sizeof(double2) * n, cudaMemcpyHostToDevice, h->st));
 		c = h->cbuf;
 	}
@@ -550,8 +553,7 @@ int qpc_tsurff_get(qpc_tsurff* h, double* work, double* clock)
 {
 	if (!h || !work) { set_error("NULL argument"); return QPC_ERR_ARGS; }
 	QPC_CUDA(cudaSetDevice(h->dev));
-	QPC_CUDA(cudaMemcpyAsync(work, h->work, sizeof(double2) * (size_t)h->B * h->nkr * h->nkt * h->nkp, cudaMemcpyDeviceToHost, h->st));
-	if (int rc = wait_on(h->st)) return rc;
+	if (int rc = copy_to_host(work, h->work, sizeof(double2) * (size_t)h->B * h->nkr * h->nkt * h->nkp, h->st)) return rc;
 	if (clock) std::copy(h->clock.begin(), h->clock.end(), clock);
 	return QPC_OK;
 }

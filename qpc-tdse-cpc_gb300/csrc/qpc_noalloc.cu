@@ -28,6 +28,8 @@ static __device__ __align__(256) double2 g_noalloc_scratch[2 * QPC_NOALLOC_MAX_E
 
 namespace {
 
+// device address of the scratch per device ordinal, looked up in the CUDA runtime's
+// primary context of that device (the context cudaSetDevice makes current)
 constexpr int kMaxDevices = 64;
 double2* g_scratch_ptr[kMaxDevices] = {nullptr};
 std::mutex g_scratch_mu;

@@ -15,10 +15,12 @@
 // GB300 mapping: Z couples (m, l) only to (m +- 1, l +- 1), so it keeps il mod 2 and every
 // transform is block-diagonal once the channels are ordered il-even first (the engine's
 // internal order; put/get convert): two dense GEMMs of n_e and n_o = N_ch/2 rows per
-// transform instead of one of N_ch, half the FP64 work.  They run as cuBLAS DGEMM (real
-// P_x1, P_y2, on the state viewed as 2 N_r reals) and ZGEMM (merged, complex), strided
-// over the live wavefunctions.  The angular eigensystems come from cuSOLVER syevd, block by
-// block, on the real symmetric form of each coupling.  The banded CN of each eigen-channel runs one chain per thread: the LU of
+// transform instead of one of N_ch, half the FP64 work.  They run as this library's own
+// FP64 GEMM kernels (qpc_gemm.cuh): real for P_x1, P_y2 and the merged P_y1 P_x2^H, which
+// is real because the two phases cancel (on the state viewed as 2 N_r reals), complex for
+// the merged P_x2 P_x1^H and P_y2 P_y1^H, over the live wavefunctions.  The angular
+// eigensystems come from cuSOLVER syevd (set-up only), block by block, on the real
+// symmetric form of each coupling.  The banded CN of each eigen-channel runs one chain per thread: the LU of
 // S + ifet O is formed row by row with the previous p rows of U in registers, the forward
 // substitution fused, U rows kept in a scratch buffer for the backward substitution.
 // The field-free step uses the LDL^T factors of S + i dt/2 H_l (qpc_ldlt_csym) as
@@ -27,9 +29,10 @@
 #include "qpc_internal.h"
 #include "qpc_cuda_util.cuh"
 #include <cuda_runtime.h>
-#include <cublas_v2.h>
 #include <cusolverDn.h>
+#include "qpc_gemm.cuh"
 #include <cstdlib>
+#include <cstring>
 #include <cmath>
 #include <vector>
 #include <algorithm>
@@ -260,6 +263,26 @@ __global__ void k_vg_real_part(const double2* __restrict__ P, long n, double* __
 	if (t < n) out[t] = P[t].x;
 }
 
+// largest |imaginary part| of a complex block (to confirm a merged transform is real)
+__global__ void k_vg_max_imag(const double2* __restrict__ P, long n, unsigned long long* __restrict__ out)
+{
+	const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+	if (t < n) {
+		const double v = fabs(P[t].y);
+		atomicMax(out, __double_as_longlong(v));	// non-negative doubles order as their bit patterns
+	}
+}
+
+// T[j][k] = conj(R[k][j]) of one n x n block
+__global__ void k_vg_conj_transpose(const double2* __restrict__ R, int n, double2* __restrict__ T)
+{
+	const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+	if (t >= (long)n * n) return;
+	const int j = (int)(t / n), k = (int)(t - (long)j * n);
+	const double2 v = R[(long)k * n + j];
+	T[t] = make_double2(v.x, -v.y);
+}
+
 __global__ void k_vg_snorm(const double2* __restrict__ state, const double* __restrict__ S, int N, int P, int nch, double* out)
 {
 	// one block per instance, fixed-order reduction
@@ -295,7 +318,6 @@ struct qpc_vgwr {
 	double dt = 0;
 	cudaStream_t st = nullptr;
 	cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-	cublasHandle_t cb = nullptr;
 	double *S = nullptr, *Ri = nullptr, *D = nullptr;
 	double *lam[4] = {nullptr, nullptr, nullptr, nullptr};
 	// transforms, block-diagonal in the engine's channel order (il-even channels first):
@@ -304,8 +326,8 @@ struct qpc_vgwr {
 	int nb[2] = {0, 0}, off[2] = {0, 0};
 	long boff[2] = {0, 0}, bsz = 0;
 	int* chmap = nullptr;                          // engine channel -> reference channel im*n_l+il
-	double *Px1 = nullptr, *Py2 = nullptr;        // real blocks
-	double2 *M12 = nullptr, *M23 = nullptr, *M34 = nullptr;  // complex blocks
+	double *Px1 = nullptr, *Py2 = nullptr, *M23 = nullptr;  // real blocks (M23 = P_y1 P_x2^H is real)
+	double2 *M12 = nullptr, *M34 = nullptr;                 // complex blocks
 	double2 *Lrow = nullptr, *Dinv = nullptr;     // field-free factors
 	double2 *X = nullptr, *W = nullptr, *U = nullptr;
 	double* atab = nullptr;
@@ -315,6 +337,15 @@ struct qpc_vgwr {
 	double* nrm = nullptr;
 	float last_ms = 0.f;
 	long launches = 0;
+	// per-kernel timing (qpc_vgwr_set_profiling): events around each launch group,
+	// summed per kind (0 transforms, 1 coupling CN, 2 field-free CN) after the run
+	bool profiling = false;
+	std::vector<cudaEvent_t> evpool;
+	size_t evused = 0;
+	struct mark { int kind; cudaEvent_t a, b; };
+	std::vector<mark> marks;
+	double kms[3] = {0, 0, 0};
+	long kcnt[3] = {0, 0, 0};
 };
 
 namespace {
@@ -326,40 +357,75 @@ void vg_free(qpc_vgwr* h)
 	void* ps[] = {h->S, h->Ri, h->D, h->lam[0], h->lam[1], h->lam[2], h->lam[3], h->Px1, h->Py2, h->M12, h->M23, h->M34, h->Lrow,
 		h->Dinv, h->X, h->W, h->U, h->atab, h->ntt, h->perm, h->nrm, h->chmap};
 	for (void* p : ps) if (p) cudaFree(p);
-	if (h->cb) cublasDestroy(h->cb);
 	if (h->ev0) cudaEventDestroy(h->ev0);
 	if (h->ev1) cudaEventDestroy(h->ev1);
+	for (auto e : h->evpool) cudaEventDestroy(e);
 	if (h->st) cudaStreamDestroy(h->st);
 	delete h;
 }
 
-#define QPC_CUBLAS(call) do { cublasStatus_t s_ = (call); if (s_ != CUBLAS_STATUS_SUCCESS) { \
-	set_error("%s failed: cublas status %d (%s:%d)", #call, (int)s_, __FILE__, __LINE__); return QPC_ERR_CUDA; } } while (0)
+// profiling marks: an event recorded before a launch group (begin) and after it (end)
+cudaEvent_t pool_event(qpc_vgwr* h)
+{
+	if (h->evused == h->evpool.size()) {
+		cudaEvent_t e = nullptr;
+		if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
+		h->evpool.push_back(e);
+	}
+	return h->evpool[h->evused++];
+}
+cudaEvent_t prof_begin(qpc_vgwr* h)
+{
+	if (!h->profiling) return nullptr;
+	cudaEvent_t a = pool_event(h);
+	if (a) cudaEventRecord(a, h->st);
+	return a;
+}
+void prof_end(qpc_vgwr* h, int kind, cudaEvent_t a)
+{
+	if (!a) return;
+	cudaEvent_t b = pool_event(h);
+	if (!b) return;
+	cudaEventRecord(b, h->st);
+	h->marks.push_back({kind, a, b});
+}
+void prof_collect(qpc_vgwr* h)
+{
+	for (auto& m : h->marks) {
+		float ms = 0.f;
+		if (cudaEventElapsedTime(&ms, m.a, m.b) == cudaSuccess) { h->kms[m.kind] += ms; ++h->kcnt[m.kind]; }
+	}
+	h->marks.clear();
+	h->evused = 0;
+}
 
-// out[b] = op(Pm) in[b] for b < nb, state blocks [nch][N] complex.  real: Pm real [nch][nch] on the
-// state viewed as [nch][2N] reals; herm: apply Pm^T (real) or Pm^H (complex).
+// out[b] = op(Pm) in[b] for b < nb, state blocks [nch][N] complex, one GEMM launch per parity
+// block.  real: Pm real [n][n] per block on the state viewed as [n][2N] reals; herm: apply
+// Pm^T (real) or Pm^H (complex).
 int transform(qpc_vgwr* h, const void* Pm, bool real, bool herm, const double2* in, double2* out, int nb)
 {
 	const int nch = h->nch, N = h->N;
 	const long sstate = (long)nch * N;
+	cudaEvent_t pa = prof_begin(h);
 	for (int bl = 0; bl < 2; ++bl) {
 		const int n = h->nb[bl];
 		if (!n) continue;
 		const long o = (long)h->off[bl] * N;
 		if (real) {
-			const double one = 1.0, zero = 0.0;
-			// column-major: out^T (2N x n) = in^T (2N x n) * op(P^T); the row-major block buffer is P^T
-			QPC_CUBLAS(cublasDgemmStridedBatched(h->cb, CUBLAS_OP_N, herm ? CUBLAS_OP_T : CUBLAS_OP_N, 2 * N, n, n, &one,
-				(const double*)(in + o), 2 * N, 2 * sstate, (const double*)Pm + h->boff[bl], n, 0, &zero, (double*)(out + o), 2 * N,
-				2 * sstate, nb));
+			const dim3 g = gemm::grid_for(2 * N, n, nb);
+			const double* A = (const double*)Pm + h->boff[bl];
+			if (herm) gemm::k_dgemm<true><<<g, gemm::THREADS, 0, h->st>>>(A, n, (const double*)(in + o), (double*)(out + o), 2L * N, 2 * sstate, 2 * N);
+			else gemm::k_dgemm<false><<<g, gemm::THREADS, 0, h->st>>>(A, n, (const double*)(in + o), (double*)(out + o), 2L * N, 2 * sstate, 2 * N);
 		} else {
-			const cuDoubleComplex one = make_cuDoubleComplex(1.0, 0.0), zero = make_cuDoubleComplex(0.0, 0.0);
-			QPC_CUBLAS(cublasZgemmStridedBatched(h->cb, CUBLAS_OP_N, herm ? CUBLAS_OP_C : CUBLAS_OP_N, N, n, n, &one,
-				(const cuDoubleComplex*)(in + o), N, sstate, (const cuDoubleComplex*)Pm + h->boff[bl], n, 0, &zero,
-				(cuDoubleComplex*)(out + o), N, sstate, nb));
+			const dim3 g = gemm::grid_for(N, n, nb);
+			const double2* A = (const double2*)Pm + h->boff[bl];
+			if (herm) gemm::k_zgemm<true><<<g, gemm::THREADS, gemm::ZGEMM_SMEM, h->st>>>(A, n, in + o, out + o, (long)N, sstate, N);
+			else gemm::k_zgemm<false><<<g, gemm::THREADS, gemm::ZGEMM_SMEM, h->st>>>(A, n, in + o, out + o, (long)N, sstate, N);
 		}
 		++h->launches;
 	}
+	prof_end(h, 0, pa);
+	QPC_CUDA(cudaGetLastError());
 	return QPC_OK;
 }
 
@@ -375,8 +441,10 @@ int step_t(qpc_vgwr* h, long s, long ld, int nlive, int nff)
 		const int axis = comp < 2 ? 0 : 1;
 		const double sgn = comp == 1 ? 1.0 : -1.0;
 		const long nth = (long)nb * h->nch;
+		cudaEvent_t pa = prof_begin(h);
 		k_vg_cn<P><<<(unsigned)((nth + VG_THREADS - 1) / VG_THREADS), VG_THREADS, 0, h->st>>>(z, h->U, h->S, anti ? h->D : h->Ri, anti,
 			h->lam[comp], coef, h->atab, ld, s, tofs, axis, sgn, h->perm, h->N, h->nch, nb);
+		prof_end(h, 1, pa);
 		++h->launches;
 	};
 	if (nb > 0) {
@@ -384,7 +452,7 @@ int step_t(qpc_vgwr* h, long s, long ld, int nlive, int nff)
 		cn(h->W, 0, 0);
 		if (int rc = transform(h, h->M12, false, false, h->W, h->X, nb)) return rc;
 		cn(h->X, 1, 0);
-		if (int rc = transform(h, h->M23, false, false, h->X, h->W, nb)) return rc;
+		if (int rc = transform(h, h->M23, true, false, h->X, h->W, nb)) return rc;
 		cn(h->W, 2, 0);
 		if (int rc = transform(h, h->M34, false, false, h->W, h->X, nb)) return rc;
 		cn(h->X, 3, 0);
@@ -394,8 +462,10 @@ int step_t(qpc_vgwr* h, long s, long ld, int nlive, int nff)
 	}
 	if (nff > 0) {
 		const long nth = (long)nff * h->nch;
+		cudaEvent_t pa = prof_begin(h);
 		k_vg_ff<P><<<(unsigned)((nth + VG_THREADS - 1) / VG_THREADS), VG_THREADS, 0, h->st>>>(h->X, h->U, h->S, h->Lrow, h->Dinv, h->ntt,
 			h->perm, h->chmap, s, h->N, h->d.n_l, h->d.n_m, h->d.m0, h->nlh, nff);
+		prof_end(h, 2, pa);
 		++h->launches;
 	}
 	if (nb > 0) {
@@ -403,7 +473,7 @@ int step_t(qpc_vgwr* h, long s, long ld, int nlive, int nff)
 		cn(h->W, 3, 1);
 		if (int rc = transform(h, h->M34, false, true, h->W, h->X, nb)) return rc;
 		cn(h->X, 2, 1);
-		if (int rc = transform(h, h->M23, false, true, h->X, h->W, nb)) return rc;
+		if (int rc = transform(h, h->M23, true, true, h->X, h->W, nb)) return rc;
 		cn(h->W, 1, 1);
 		if (int rc = transform(h, h->M12, false, true, h->W, h->X, nb)) return rc;
 		cn(h->X, 0, 1);
@@ -545,8 +615,10 @@ int qpc_vgwr_create(const qpc_dims* dims, double dt, const double* S, const doub
 	if ((cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking)) != cudaSuccess) { set_error("cudaStreamCreateWithFlags failed"); return fail(QPC_ERR_CUDA); }
 	if ((cudaEventCreate(&h->ev0)) != cudaSuccess) { set_error("cudaEventCreate failed"); return fail(QPC_ERR_CUDA); }
 	if ((cudaEventCreate(&h->ev1)) != cudaSuccess) { set_error("cudaEventCreate failed"); return fail(QPC_ERR_CUDA); }
-	if (cublasCreate(&h->cb) != CUBLAS_STATUS_SUCCESS) { set_error("cublasCreate failed"); return fail(QPC_ERR_CUDA); }
-	if (cublasSetStream(h->cb, h->st) != CUBLAS_STATUS_SUCCESS) { set_error("cublasSetStream failed"); return fail(QPC_ERR_CUDA); }
+	for (auto f : {(const void*)gemm::k_zgemm<true>, (const void*)gemm::k_zgemm<false>})
+		if (cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, gemm::ZGEMM_SMEM) != cudaSuccess) {
+			set_error("cudaFuncSetAttribute(ZGEMM shared memory) failed"); return fail(QPC_ERR_CUDA);
+		}
 	const size_t nst = (size_t)h->B * nch * N;
 	// engine channel order: il-even channels first, then il-odd
 	std::vector<int> chmap;
@@ -575,24 +647,43 @@ int qpc_vgwr_create(const qpc_dims* dims, double dt, const double* S, const doub
 	for (int c = 0; c < 4; ++c)
 		if ((rc = dalloc(&dP[c], (size_t)h->bsz))) return fail(rc);
 	if ((rc = device_angular(h, lam, dP))) return fail(rc);
-	// merged transforms P_b P_a^H per block: row-major C = L R^H; column-major C^T = conj(R) L^T
-	// with A_cm = R^T (buffer R, op C) and B_cm = L^T (buffer L)
+	// merged transforms P_b P_a^H per block, C = L R^H: T = R^H materialised, then C = L T
+	// with the library's complex GEMM (set-up only)
+	double2* T = nullptr;
+	double2* C23 = nullptr;
+	unsigned long long* dmax = nullptr;
+	struct tguard { double2** t; double2** c; unsigned long long** m; ~tguard() { if (*t) cudaFree(*t); if (*c) cudaFree(*c); if (*m) cudaFree(*m); } } TG{&T, &C23, &dmax};
+	const int nbmax = std::max(h->nb[0], h->nb[1]);
+	if ((rc = dalloc(&T, (size_t)nbmax * nbmax)) || (rc = dalloc(&C23, (size_t)h->bsz)) || (rc = dalloc(&dmax, 1))) return fail(rc);
 	auto merge = [&](const double2* Ld, const double2* Rd, double2* out) -> int {
-		const cuDoubleComplex one = make_cuDoubleComplex(1.0, 0.0), zero = make_cuDoubleComplex(0.0, 0.0);
 		for (int bl = 0; bl < 2; ++bl) {
 			const int n = h->nb[bl];
 			if (!n) continue;
-			QPC_CUBLAS(cublasZgemm(h->cb, CUBLAS_OP_C, CUBLAS_OP_N, n, n, n, &one, (const cuDoubleComplex*)(Rd + h->boff[bl]), n,
-				(const cuDoubleComplex*)(Ld + h->boff[bl]), n, &zero, (cuDoubleComplex*)(out + h->boff[bl]), n));
+			k_vg_conj_transpose<<<(unsigned)(((long)n * n + 255) / 256), 256, 0, h->st>>>(Rd + h->boff[bl], n, T);
+			gemm::k_zgemm<false><<<gemm::grid_for(n, n, 1), gemm::THREADS, gemm::ZGEMM_SMEM, h->st>>>(Ld + h->boff[bl], n, T,
+				out + h->boff[bl], (long)n, 0L, n);
+			QPC_CUDA(cudaGetLastError());
 		}
 		return QPC_OK;
 	};
-	if ((rc = merge(dP[1], dP[0], h->M12)) || (rc = merge(dP[2], dP[1], h->M23)) || (rc = merge(dP[3], dP[2], h->M34))) return fail(rc);
+	if ((rc = merge(dP[1], dP[0], h->M12)) || (rc = merge(dP[2], dP[1], C23)) || (rc = merge(dP[3], dP[2], h->M34))) return fail(rc);
 	{
 		const long nn = h->bsz;
-		k_vg_real_part<<<(unsigned)((nn + 255) / 256), 256, 0, h->st>>>(dP[0], nn, h->Px1);
-		k_vg_real_part<<<(unsigned)((nn + 255) / 256), 256, 0, h->st>>>(dP[3], nn, h->Py2);
+		const unsigned g = (unsigned)((nn + 255) / 256);
+		k_vg_real_part<<<g, 256, 0, h->st>>>(dP[0], nn, h->Px1);
+		k_vg_real_part<<<g, 256, 0, h->st>>>(dP[3], nn, h->Py2);
+		// P_y1 P_x2^H = Q1^T diag(phi) diag(phi)^H Q2 = Q1^T Q2: the phases cancel exactly
+		// (each term is a product of two purely real or two purely imaginary entries), so it
+		// is applied as a real transform
+		QPC_CUDA(cudaMemsetAsync(dmax, 0, sizeof(unsigned long long), h->st));
+		k_vg_max_imag<<<g, 256, 0, h->st>>>(C23, nn, dmax);
+		k_vg_real_part<<<g, 256, 0, h->st>>>(C23, nn, h->M23);
 		if (cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(h->st) != cudaSuccess) { set_error("transform setup failed"); return fail(QPC_ERR_CUDA); }
+		unsigned long long bits = 0;
+		QPC_CUDA(cudaMemcpy(&bits, dmax, sizeof(bits), cudaMemcpyDeviceToHost));
+		double mi;
+		std::memcpy(&mi, &bits, sizeof(mi));
+		if (!(mi <= 1e-13)) { set_error("merged transform P_y1 P_x2^H is not real (|imag| %g)", mi); return fail(QPC_ERR_NUMERIC); }
 	}
 	if (cudaMemcpy(h->S, S, sizeof(double) * N * NE, cudaMemcpyHostToDevice) != cudaSuccess ||
 		cudaMemcpy(h->Ri, Rinv, sizeof(double) * N * NE, cudaMemcpyHostToDevice) != cudaSuccess ||
@@ -622,11 +713,16 @@ static int vg_copy(qpc_vgwr* h, const double* src, double* dst, cudaMemcpyKind k
 	const long total = (long)h->B * h->nch * h->N;
 	const size_t bytes = sizeof(double2) * (size_t)total;
 	const unsigned nb = (unsigned)((total + 255) / 256);
+	// host buffers are copied with the stream idle (bounded wait first): such a copy then
+	// never waits for queued work, and a wait that runs out leaves no copy pending
 	if (src) {
+		if (kind == cudaMemcpyHostToDevice) if (int rc = wait_on(h->st)) return rc;
 		QPC_CUDA(cudaMemcpyAsync(h->W, src, bytes, kind, h->st));
 		k_vg_permute<<<nb, 256, 0, h->st>>>(h->W, h->X, h->chmap, h->N, h->nch, total, true);
 	} else {
 		k_vg_permute<<<nb, 256, 0, h->st>>>(h->X, h->W, h->chmap, h->N, h->nch, total, false);
+		QPC_CUDA(cudaGetLastError());
+		if (kind == cudaMemcpyDeviceToHost) return copy_to_host(dst, h->W, bytes, h->st);
 		QPC_CUDA(cudaMemcpyAsync(dst, h->W, bytes, kind, h->st));
 	}
 	QPC_CUDA(cudaGetLastError());
@@ -648,6 +744,7 @@ int qpc_vgwr_run(qpc_vgwr* h, const double* atab, int64_t ld, const int64_t* nt_
 {
 	if (!h || !nt_field || !nt_total) { set_error("NULL argument"); return QPC_ERR_ARGS; }
 	cudaSetDevice(h->dev);
+	if (int rc = wait_on(h->st)) return rc;
 	const int B = h->B;
 	long smax = 0;
 	bool anyfield = false;
@@ -701,6 +798,7 @@ int qpc_vgwr_run(qpc_vgwr* h, const double* atab, int64_t ld, const int64_t* nt_
 	if (!ident) if (int rc = permute(h, perm, true)) return rc;
 	if (int rc = wait_on(h->st)) return rc;
 	cudaEventElapsedTime(&h->last_ms, h->ev0, h->ev1);
+	prof_collect(h);
 	return QPC_OK;
 }
 
@@ -729,8 +827,22 @@ int qpc_vgwr_norm(qpc_vgwr* h, double* norm)
 	cudaSetDevice(h->dev);
 	k_vg_snorm<<<h->B, 256, 0, h->st>>>(h->X, h->S, h->N, h->P, h->nch, h->nrm);
 	QPC_CUDA(cudaGetLastError());
-	QPC_CUDA(cudaMemcpyAsync(norm, h->nrm, sizeof(double) * h->B, cudaMemcpyDeviceToHost, h->st));
-	return wait_on(h->st);
+	return copy_to_host(norm, h->nrm, sizeof(double) * h->B, h->st);
+}
+
+int qpc_vgwr_set_profiling(qpc_vgwr* h, int on)
+{
+	if (!h) { set_error("NULL argument"); return QPC_ERR_ARGS; }
+	h->profiling = on != 0;
+	for (int k = 0; k < 3; ++k) { h->kms[k] = 0.0; h->kcnt[k] = 0; }
+	return QPC_OK;
+}
+
+int qpc_vgwr_kernel_times(qpc_vgwr* h, double* ms, int64_t* launches)
+{
+	if (!h || !ms || !launches) { set_error("NULL argument"); return QPC_ERR_ARGS; }
+	for (int k = 0; k < 3; ++k) { ms[k] = h->kms[k]; launches[k] = h->kcnt[k]; }
+	return QPC_OK;
 }
 
 int qpc_vgwr_last_run(qpc_vgwr* h, float* ms, int64_t* launches)

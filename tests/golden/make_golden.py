@@ -2,7 +2,8 @@
 propagator (QPC-TDSE headers compiled by oracle/ref/Makefile into oracle/_ref/).
 
 Run on the development machine, where the reference checkout exists:
-    python tests/golden/make_golden.py [/path/to/reference/include] [--arnoldi] [--vgwr] [--mask] [--multim] [--momentum]
+    python tests/golden/make_golden.py <reference checkout>/include [--arnoldi] [--vgwr] [--mask] [--multim] [--momentum]
+(or with the environment variable QPC_REFERENCE_DIR naming the checkout instead of the argument)
 (those flags regenerate only the named fixtures.)
 The fixtures are committed; the tests only read them.
 
@@ -254,7 +255,12 @@ def momentum(d):
 
 
 def main():
-    ref_include = sys.argv[1] if len(sys.argv) > 1 and not sys.argv[1].startswith("--") else "/root/reference/include"
+    if len(sys.argv) > 1 and not sys.argv[1].startswith("--"):
+        ref_include = sys.argv[1]
+    elif os.environ.get("QPC_REFERENCE_DIR"):
+        ref_include = os.path.join(os.environ["QPC_REFERENCE_DIR"], "include")
+    else:
+        sys.exit("usage: make_golden.py <reference checkout>/include [--flags] (or set QPC_REFERENCE_DIR)")
     build(ref_include)
     if any(a in sys.argv for a in ("--arnoldi", "--vgwr", "--mask", "--multim", "--momentum")):
         with tempfile.TemporaryDirectory() as d:
@@ -331,8 +337,8 @@ def main():
         mask(d)
         multi_m(d)
         momentum(d)
-    with open(os.path.join(HERE, "make_golden.log.json"), "w") as fh:
-        json.dump(meta, fh, indent=1)
+    # what was run, on stdout (kept out of the fixtures directory)
+    print(json.dumps(meta, indent=1))
 
 
 if __name__ == "__main__":

@@ -7,8 +7,9 @@ spacing 0.5 a.u. the reference's own map is not: a 1e-15 change of its input mov
 its result by up to percent over a pulse (Krylov vectors formed by cancellation
 when <v|S|v> is small, and components outside the Krylov space multiplied by the
 interpolating polynomial).  There the GPU is held per step to the oracle applied
-to the GPU's own input (1e-11), and over a run to the oracle's own spread under a
-1e-15 perturbation of the input."""
+to the GPU's own input (1e-11).  Run-level checks take well-conditioned cases and
+allow 100 x the oracle's own spread under a 1e-15 perturbation of the input only
+while that spread is itself tiny (the bound fails the test otherwise)."""
 import numpy as np
 import pytest
 
@@ -41,6 +42,9 @@ def oracle_with_spread(aoracle, g, c0, ez, nt=None):
         ref2, crit2, ms2 = aoracle.run(g, c0 * noise, ez, nt)
         tol = np.maximum(tol, [100 * rel_l2(ref2[k], ref[k]) for k in range(ref.shape[0])])
         stable &= (crit == crit2) & (ms == ms2)
+    # a spread this large means the reference's map is ill-conditioned on this case and the
+    # bound would accept a wrong answer: such a case cannot be checked at run level
+    assert tol.max() <= 1e-10, "oracle spread too large for a run-level check: %s" % tol
     return ref, crit, ms, tol, stable
 
 
@@ -103,7 +107,8 @@ def test_golden_mid_steps(q, tag):
 
 
 def test_uneven_batch_matches_oracle(q, aoracle):
-    """Four instances, own field tables and step counts (one takes no step)."""
+    """Four instances, own field tables and step counts (one takes no step); dt = 0.01, where
+    the reference's map is well conditioned on this grid."""
     s = golden("small_setup")
     a = golden("arnoldi_small")
     rng = np.random.default_rng(7)
@@ -111,10 +116,10 @@ def test_uneven_batch_matches_oracle(q, aoracle):
     c0 = np.stack([a["conv_coef"] * np.exp(1j * k) for k in range(B)])
     ez = 0.06 * rng.standard_normal((B, 6))
     nt = np.array([6, 0, 3, 5])
-    prop = small_prop(q, n_inst=B)
+    prop = small_prop(q, n_inst=B, dt=0.01)
     prop.put(c0[:, None])
     crit, ms = prop.run(ez, nt, want_msub=True)
-    g = aoracle.grid(s["S"], s["R"], s["H"], s["y10"], 0.1, n_l, n_inst=B)
+    g = aoracle.grid(s["S"], s["R"], s["H"], s["y10"], 0.01, n_l, n_inst=B)
     ref, rcrit, rms, tol, stable = oracle_with_spread(aoracle, g, c0.reshape(B, -1), ez, nt)
     c = prop.get().reshape(B, -1)
     for k in range(B):
@@ -135,11 +140,11 @@ def test_several_m_matches_oracle(q, aoracle):
     for im in range(n_m):
         c0[im, 0] = q.ground_state(S, H, n_l, n_m, im, 0, 0, m0)[0][im, 0]
     c0[:, 1] += 0.1 * (rng.standard_normal((n_m, n_r)) * np.exp(-np.arange(n_r) / 8.0))
-    prop = q.propagator_hc_lgwz(12, 1e-14, 1e-8).initialize(n_r, p, n_l, S, R, H, y10, 0.05, n_m=n_m, m0=m0)
+    prop = q.propagator_hc_lgwz(12, 1e-14, 1e-8).initialize(n_r, p, n_l, S, R, H, y10, 0.01, n_m=n_m, m0=m0)
     prop.put(c0[None])
     ez = 0.04 * np.sin(0.3 * np.arange(8))
     crit = prop.run(ez[None, :])
-    g = aoracle.grid(S, R, H, y10, 0.05, n_l, n_m=n_m, m0=m0)
+    g = aoracle.grid(S, R, H, y10, 0.01, n_l, n_m=n_m, m0=m0)
     ref, rcrit, _, tol, stable = oracle_with_spread(aoracle, g, c0.reshape(1, -1), ez)
     assert rel_l2(prop.get().reshape(-1), ref[0]) < tol[0]
     assert np.array_equal(crit[stable], rcrit[stable])
@@ -161,7 +166,7 @@ def _mixed_instance(q, rng, n_r, n_l):
     return S, R, H, c0, e0
 
 
-@pytest.mark.parametrize("n_r,n_l", [(400, 21), (800, 41)])
+@pytest.mark.parametrize("n_r,n_l", [(400, 21), (800, 41), (1600, 61), (2000, 81)])
 def test_mixed_grid_shadowing(q, aoracle, n_r, n_l):
     """kmax = 12, dt = 0.1: every GPU step equals the oracle's step of the GPU's own
     input to 1e-11, along a trajectory through a field ramp."""
@@ -184,26 +189,40 @@ def test_mixed_grid_shadowing(q, aoracle, n_r, n_l):
 
 
 def test_mixed_grid_run_within_reference_spread(q, aoracle):
-    """A 400-step run at kmax = 12, dt = 0.1 on a mixed-grid instance.  The GPU result
-    differs from the oracle's by no more than 100 times the oracle's own change under a
-    1e-15 relative perturbation of the input (floor 1e-10), and conserves the S-norm."""
+    """A 2000-step run at kmax = 12 on a screened-potential instance where the reference's map
+    is well conditioned (64 splines on [0, 30], l < 6, dt = 0.01: criterion 2 throughout).  The
+    GPU result differs from the oracle's by at most max(1e-10, 100 x the oracle's own change
+    under a 1e-15 relative perturbation of the input), the spread itself must stay below
+    1e-8 so that the bound cannot pass a wrong answer, and the S-norm is conserved.
+
+    On the mixed-grid batch's grids (spacing 0.5 a.u., l_max >= 20, dt = 0.1) the reference's
+    map is not continuous at that level: a 1e-15 perturbation moves its 400-step result by
+    1e-3 to 1 (the early steps stop at the absolute 1e-13 breakdown threshold or not, and
+    Gram-Schmidt on nearly cancelled vectors amplifies rounding).  There the GPU is held per
+    step (test_mixed_grid_shadowing) instead."""
     rng = np.random.default_rng(3)
-    n_r, n_l = 400, 21
-    S, R, H, c0, _ = _mixed_instance(q, rng, n_r, n_l)
+    n_r, n_l, dt = 64, 6, 0.01
+    a, b = rng.uniform(0, 17), rng.uniform(1, 3)
+    S, R, _, _, H = q.radial_setup(n_r, 6, n_l, q.linear_knots(n_r, 6, 0.0, 30.0), (q.POTENTIAL_YUKAWA, 1.0, a, b))
+    c0, _ = q.ground_state(S, H, n_l)
     y10 = q.y10_coupling(n_l)
-    nt = 400
-    t = 0.1 * np.arange(nt)
-    ez = 0.053 * np.sin(np.pi * t / (t[-1] + 0.1)) ** 2 * np.sin(0.0759 * t)
-    g = aoracle.grid(S, R, H, y10, 0.1, n_l)
+    nt = 2000
+    t = dt * np.arange(nt)
+    ez = 0.053 * np.sin(np.pi * t / (t[-1] + dt)) ** 2 * np.sin(0.0759 * t)
+    g = aoracle.grid(S, R, H, y10, dt, n_l)
     ref, rcrit, _ = aoracle.run(g, c0.reshape(1, -1), ez)
-    pert = c0.reshape(1, -1) * (1 + 1e-15 * np.random.default_rng(1).standard_normal(c0.size))
-    ref2, _, _ = aoracle.run(g, pert, ez)
-    spread = rel_l2(ref2[0], ref[0])
-    prop = q.propagator_hc_lgwz(12, 1e-14, 1e-8).initialize(n_r, 6, n_l, S, R, H, y10, 0.1)
+    spread = 0.0
+    for seed in (1, 2):
+        pert = c0.reshape(1, -1) * (1 + 1e-15 * np.random.default_rng(seed).standard_normal(c0.size))
+        ref2, _, _ = aoracle.run(g, pert, ez)
+        spread = max(spread, rel_l2(ref2[0], ref[0]))
+    assert spread < 1e-8, "the reference's map is ill-conditioned here (spread %.1e): no run-level check possible" % spread
+    prop = q.propagator_hc_lgwz(12, 1e-14, 1e-8).initialize(n_r, 6, n_l, S, R, H, y10, dt)
     prop.put(c0[None])
-    prop.run(ez[None, :])
+    crit = prop.run(ez[None, :])
     err = rel_l2(prop.get().reshape(-1), ref[0])
     assert err <= max(TOL_FULL, 100 * spread), (err, spread)
+    assert np.array_equal(crit[0], rcrit[0])
     assert abs(prop.norm()[0] - 1.0) < 1e-10
 
 

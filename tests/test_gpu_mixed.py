@@ -1,7 +1,9 @@
 """Mixed-grid batch: wavefunctions with their own radial grid, l_max and potential
 V = -(1 + a e^{-b r})/r, advanced together -- the Crank-Nicolson propagator on one
 handle per grid through qpc_lgwz_run_many, each instance against the CPU oracle
-of the same propagator (1e-10 relative L2, one instance over its full pulse)."""
+of the same propagator (1e-10 relative L2, one instance over its full pulse, the others
+over 200 steps around their pulse peak, up to the largest grid of the mixed-grid batch:
+N_r = 2000, l_max = 80)."""
 import numpy as np
 import pytest
 
@@ -31,7 +33,7 @@ def instance(q, rng, n_r, n_l, p=6):
 
 def test_mixed_grid_cn_batch(q, oracle):
     rng = np.random.default_rng(2025)
-    grids = [(400, 21), (800, 41), (1200, 21), (400, 61)]
+    grids = [(400, 21), (800, 41), (1200, 21), (400, 61), (1600, 61), (2000, 81)]
     props, tabs, nts, cases = [], [], [], []
     for k, (n_r, n_l) in enumerate(grids):
         S, R, H, c0 = instance(q, rng, n_r, n_l)

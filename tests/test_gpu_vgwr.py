@@ -58,3 +58,28 @@ def test_uneven_batch_matches_oracle(q, voracle):
     out = pr.get().reshape(B, -1)
     for k in range(B):
         assert rel_l2(out[k], ref[k]) < 1e-12, k
+
+
+def test_mid_grid_matches_oracle(q, voracle):
+    """A mid-size grid (n_m = 21, m0 = -10, n_l = 21: 441 channels, parity blocks of 220 and 221;
+    N_r = 200, p = 6): the transforms run as the library's own GEMM kernels on sizes that are no
+    multiple of their tiles, with the device eigensystems at that size, against the oracle's
+    dense transforms, 6 field steps and 2 field-free ones."""
+    n_r, p, n_l, n_m, m0, dt = 200, 6, 21, 21, -10, 0.05
+    nlh = max(abs(m0), abs(m0 + n_m - 1)) + n_l
+    S, _, Ri, D, H = q.radial_setup(n_r, p, nlh, q.linear_knots(n_r, p, 0.0, 100.0))
+    rng = np.random.default_rng(31)
+    r = np.arange(n_r)
+    c0 = (rng.standard_normal((1, n_m, n_l, n_r)) + 1j * rng.standard_normal((1, n_m, n_l, n_r))) * np.exp(-r / 25.0)
+    nt = 6
+    t = dt * np.arange(nt + 1)
+    atab = np.stack([0.4 * np.sin(0.3 * t + 0.2), 0.25 * np.cos(0.3 * t)], 1)[None]
+    pr = q.propagator_cn_hc_vgwr().initialize(n_r, p, n_l, n_m, m0, S, Ri, D, H, dt)
+    pr.put(c0)
+    n0 = pr.norm()[0]
+    pr.run(atab, [nt], [nt + 2])
+    got = pr.get().reshape(-1)
+    og = voracle.grid(S, Ri, D, H, dt, n_l, n_m, m0)
+    ref = voracle.run(og, c0.reshape(1, -1), atab, [nt], [nt + 2])
+    assert rel_l2(got, ref[0]) < 1e-12
+    assert abs(pr.norm()[0] - n0) < 1e-12 * n0
