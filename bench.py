@@ -396,6 +396,9 @@ def run_c1(args):
     import importlib
     q = importlib.import_module("qpc-tdse-cpc_gb300")
     n_r, p, n_l, n_m, m0, rmax, dt = 2000, 7, 61, 121, -60, 1000.0, 0.05
+    if args.c1_nm:	# a reduced channel set (for profiling runs); the default is the full C1 grid
+        n_m, n_l = args.c1_nm, args.c1_nl or n_l
+        m0 = -(n_m // 2)
     lam_nm, inten, eps, ncyc = 1800.0, 8e13, 0.5, 6
     kn = c1_knots(n_r, p, rmax)
     nlh = abs(m0) + n_l
@@ -439,6 +442,7 @@ def run_c1(args):
         "dtype": "c128 (complex FP64)", "data": "synthetic (ground state of the screened potential, analytic pulse)",
         "config": {"workload": "C1: V=-(1+17e^-2r)/r, p=7, N_r=2000 on [0,1000] quadratic-then-linear knots, n_m=121 (m0=-60), "
                                "n_l=61 (7381 channels), 1800 nm, eps=0.5, 8e13 W/cm^2, 6 cycles, velocity gauge, dt=0.05",
+                   "n_m": n_m, "m0": m0, "n_l": n_l, "channels": n_m * n_l,
                    "window_start_step": int(s0 + W), "pulse_steps": int(T / dt), "ground_state_energy": float(e_gs)},
         "gpu_launches": int(launches),
         "roofline": {"bound": "fp64", "kernel": "k_dgemm / k_zgemm (m,l) transforms (CUDA events around each transform)",
@@ -860,6 +864,8 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--kernel-times", action="store_true", help="c0: per-kernel device times over 1000 steps")
+    ap.add_argument("--c1-nm", type=int, default=0, help="c1: number of m channels (default: the full 121)")
+    ap.add_argument("--c1-nl", type=int, default=0, help="c1: number of l channels per m (default: the full 61)")
     ap.add_argument("--workload", default="c2", choices=["c2", "c2scan", "c0", "c1", "c3", "c3a", "c3arn", "pcs", "tsurff"])
     args = ap.parse_args()
     if args.workload == "c2scan":

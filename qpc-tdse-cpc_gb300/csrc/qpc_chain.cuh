@@ -433,17 +433,29 @@ __global__ void k_spikes(const double2* __restrict__ fac, double2* __restrict__ 
 	seg_spike<P>(fac + blk * (long)N * (P + 1), N, a, b, j + 1, dir == 0, (dir == 0 ? spf : spb) + blk * (long)N * P);
 }
 
+// Shared memory of k_chain_seg, in double2 units: the factor block [N][P+1] when SFAC, the work
+// vectors [NC][N], and the spike rows the carry chains read, forward [Q][P][P] and backward [Q][P][P].
+__host__ __device__ inline long seg_smem_elems(int N, int P, int NC, int Q, bool sfac)
+{
+	return (sfac ? (long)N * (P + 1) : 0L) + (long)NC * N + 2L * Q * P * P;
+}
+
 // One block per chain (field-free) or per (+s, -s) pair (coupling); the same passes as k_chain, with
 // the recurrences segmented.  spf/spb: the spikes of every factor block, [block][N][P], block =
 // foff / (N (P+1)).  128 threads; segment lanes: warp c handles chain c, lane = 2 segment + part.
-template <int P, bool CPL>
-__global__ void __launch_bounds__(128) k_chain_seg(double2* __restrict__ X, double2* __restrict__ Wk, const double2* __restrict__ fac,
+// The chain is latency-bound (a few dozen blocks in flight), so everything the sequential parts
+// read sits in shared memory: the work vectors always, the rows of the spikes that the carry
+// chains read (P per segment boundary), and the factor block when it fits (SFAC); the passes
+// over all rows (S z, the fix-ups) read the band and the spikes through L1/L2 in parallel.
+template <int P, bool CPL, bool SFAC>
+__global__ void __launch_bounds__(128) k_chain_seg(double2* __restrict__ X, const double2* __restrict__ fac,
 	const double2* __restrict__ spf, const double2* __restrict__ spb, const double* __restrict__ S, const int64_t* __restrict__ nta,
 	long step, int jslot, int B, int M, int m0, int N, int L, int np, long chbase, long nchains, int Q, int Ls,
 	const int* __restrict__ ffmap, long ffstride)
 {
 	constexpr int NE = P + 1, NC = CPL ? 2 : 1;
 	const unsigned FULL = 0xffffffffu;
+	extern __shared__ double2 seg_sm[];
 	__shared__ double2 xc[NC][16][P];
 	__shared__ long s_x[NC], s_f[NC];
 	__shared__ int s_a[NC];
@@ -458,8 +470,25 @@ __global__ void __launch_bounds__(128) k_chain_seg(double2* __restrict__ X, doub
 #pragma unroll
 	for (int c = 0; c < NC; ++c) amax = max(amax, s_a[c]);
 	if (amax == 0) return;	// uniform over the block
+	// the chains of a block share one factor block (a (+s, -s) pair uses one LDL^T)
+	const double2* fblk = fac + s_f[0];
+	const long sblk = (s_f[0] / ((long)N * NE)) * (long)N * P;
+	const double2* spfb = spf + sblk;
+	const double2* spbb = spb + sblk;
+	double2* fsh = seg_sm;
+	double2* wsh = seg_sm + (SFAC ? (long)N * NE : 0L);
+	double2* cfw = wsh + (long)NC * N;	// [sg][i][jj]: forward spike at row sg Ls - 1 - i, sg = 1 .. Q-1
+	double2* cbw = cfw + Q * P * P;	// [sg][i][jj]: backward spike at row (sg + 1) Ls + i, sg = 0 .. Q-2
+	if (SFAC)
+		for (int t = tid; t < N * NE; t += blockDim.x) fsh[t] = fblk[t];
+	for (int t = tid; t < (Q - 1) * P * P; t += blockDim.x) {
+		const int jj = t % P, i = (t / P) % P, sg = t / (P * P);
+		cfw[((sg + 1) * P + i) * P + jj] = spfb[(long)((sg + 1) * Ls - 1 - i) * P + jj];
+		cbw[(sg * P + i) * P + jj] = spbb[(long)((sg + 1) * Ls + i) * P + jj];
+	}
+	__syncthreads();
+	const double2* fs = SFAC ? fsh : fblk;
 	double* Xd = reinterpret_cast<double*>(X);
-	double* Wd = reinterpret_cast<double*>(Wk);
 	const long rs = 2L * L;
 	for (int app = 0; app < amax; ++app) {
 		// ---- P1: w = S z
@@ -470,12 +499,11 @@ __global__ void __launch_bounds__(128) k_chain_seg(double2* __restrict__ X, doub
 				double wr = 0.0, wi = 0.0;
 #pragma unroll
 				for (int k = P; k >= 1; --k)
-					if (r - k >= 0) { const double sv = S[(r - k) * NE + k]; wr = fma(sv, z[(long)(r - k) * rs], wr); wi = fma(sv, z[(long)(r - k) * rs + 1], wi); }
+					if (r - k >= 0) { const double sv = __ldg(S + (r - k) * NE + k); wr = fma(sv, z[(long)(r - k) * rs], wr); wi = fma(sv, z[(long)(r - k) * rs + 1], wi); }
 #pragma unroll
 				for (int k = 0; k <= P; ++k)
-					if (r + k < N) { const double sv = S[r * NE + k]; wr = fma(sv, z[(long)(r + k) * rs], wr); wi = fma(sv, z[(long)(r + k) * rs + 1], wi); }
-				Wd[2 * s_x[c] + (long)r * rs] = wr;
-				Wd[2 * s_x[c] + (long)r * rs + 1] = wi;
+					if (r + k < N) { const double sv = __ldg(S + r * NE + k); wr = fma(sv, z[(long)(r + k) * rs], wr); wi = fma(sv, z[(long)(r + k) * rs + 1], wi); }
+				wsh[c * N + r] = make_double2(wr, wi);
 			}
 		}
 		__syncthreads();
@@ -484,13 +512,12 @@ __global__ void __launch_bounds__(128) k_chain_seg(double2* __restrict__ X, doub
 			const int c = warp, seg = lane >> 1, part = lane & 1;
 			const bool on = app < s_a[c] && seg < Q;
 			const int a = seg * Ls, b = min(N, a + Ls);
-			const double2* fs = fac + s_f[c];
-			double* wv = Wd + 2 * s_x[c] + part;
+			double* wv = reinterpret_cast<double*>(wsh + c * N) + part;
 			double hr[P], hi[P];
 			double2 l[P], ln[P];
 #pragma unroll
 			for (int k = 0; k < P; ++k) { hr[k] = 0.0; hi[k] = 0.0; l[k] = make_double2(0.0, 0.0); }	// row a: no history
-			double wcur = (on && a < b) ? wv[(long)a * rs] : 0.0;
+			double wcur = (on && a < b) ? wv[2L * a] : 0.0;
 			for (int t = 0; t < Ls; ++t) {
 				const int r = a + t;
 				const bool live = on && r < b;
@@ -498,7 +525,7 @@ __global__ void __launch_bounds__(128) k_chain_seg(double2* __restrict__ X, doub
 				const bool nlive = on && r + 1 < b;
 #pragma unroll
 				for (int k = 1; k <= P; ++k) ln[k - 1] = (nlive && t + 1 - k >= 0) ? fs[(long)(r + 1) * NE + k - 1] : make_double2(0.0, 0.0);
-				const double wnext = nlive ? wv[(long)(r + 1) * rs] : 0.0;
+				const double wnext = nlive ? wv[2L * (r + 1)] : 0.0;
 				double acc = live ? wcur : 0.0;
 #pragma unroll
 				for (int k = 0; k < P; ++k)
@@ -508,7 +535,7 @@ __global__ void __launch_bounds__(128) k_chain_seg(double2* __restrict__ X, doub
 				for (int k = P - 1; k >= 1; --k) { hr[k] = hr[k - 1]; hi[k] = hi[k - 1]; }
 				hr[0] = part ? other : acc;
 				hi[0] = part ? acc : other;
-				if (live) wv[(long)r * rs] = acc;
+				if (live) wv[2L * r] = acc;
 #pragma unroll
 				for (int k = 0; k < P; ++k) l[k] = ln[k];
 				wcur = wnext;
@@ -519,17 +546,16 @@ __global__ void __launch_bounds__(128) k_chain_seg(double2* __restrict__ X, doub
 		if (warp < NC) {
 			const int c = warp, i = lane >> 1, part = lane & 1;
 			const bool on = app < s_a[c] && i < P;
-			const double2* sp = spf + (s_f[c] / ((long)N * NE)) * (long)N * P;
-			const double* wv = Wd + 2 * s_x[c] + part;
+			const double* wv = reinterpret_cast<const double*>(wsh + c * N) + part;
 			for (int sg = 1; sg < Q; ++sg) {
 				double v = 0.0;
 				if (on) {
 					const int r = sg * Ls - 1 - i;
-					v = wv[(long)r * rs];
+					v = wv[2L * r];
 					if (sg >= 2) {
 #pragma unroll
 						for (int jj = 0; jj < P; ++jj) {
-							const double2 ph = sp[(long)r * P + jj], xv = xc[c][sg - 1][jj];
+							const double2 ph = cfw[(sg * P + i) * P + jj], xv = xc[c][sg - 1][jj];
 							v += part ? ph.x * xv.y + ph.y * xv.x : ph.x * xv.x - ph.y * xv.y;
 						}
 					}
@@ -545,20 +571,18 @@ __global__ void __launch_bounds__(128) k_chain_seg(double2* __restrict__ X, doub
 			const int c = it / N, r = it % N;
 			if (app < s_a[c]) {
 				const int sg = r / Ls;
-				const long o = 2 * s_x[c] + (long)r * rs;
-				double yr = Wd[o], yi = Wd[o + 1];
+				double2 y = wsh[c * N + r];
 				if (sg >= 1) {
-					const double2* sp = spf + (s_f[c] / ((long)N * NE)) * (long)N * P + (long)r * P;
+					const double2* sp = spfb + (long)r * P;
 #pragma unroll
 					for (int jj = 0; jj < P; ++jj) {
-						const double2 ph = sp[jj], xv = xc[c][sg][jj];
-						yr += ph.x * xv.x - ph.y * xv.y;
-						yi += ph.x * xv.y + ph.y * xv.x;
+						const double2 ph = __ldg(sp + jj), xv = xc[c][sg][jj];
+						y.x += ph.x * xv.x - ph.y * xv.y;
+						y.y += ph.x * xv.y + ph.y * xv.x;
 					}
 				}
-				const double2 dv = fac[s_f[c] + (long)r * NE + P];
-				Wd[o] = dv.x * yr - dv.y * yi;
-				Wd[o + 1] = dv.x * yi + dv.y * yr;
+				const double2 dv = fs[(long)r * NE + P];
+				wsh[c * N + r] = make_double2(dv.x * y.x - dv.y * y.y, dv.x * y.y + dv.y * y.x);
 			}
 		}
 		__syncthreads();
@@ -567,20 +591,19 @@ __global__ void __launch_bounds__(128) k_chain_seg(double2* __restrict__ X, doub
 			const int c = warp, seg = lane >> 1, part = lane & 1;
 			const bool on = app < s_a[c] && seg < Q;
 			const int a = seg * Ls, b = min(N, a + Ls);
-			const double2* fs = fac + s_f[c];
-			double* wv = Wd + 2 * s_x[c] + part;
+			double* wv = reinterpret_cast<double*>(wsh + c * N) + part;
 			double hr[P], hi[P];
 			double2 l[P], ln[P];
 #pragma unroll
 			for (int k = 0; k < P; ++k) { hr[k] = 0.0; hi[k] = 0.0; l[k] = make_double2(0.0, 0.0); }	// row b-1: no history
-			double wcur = (on && b - 1 >= a) ? wv[(long)(b - 1) * rs] : 0.0;
+			double wcur = (on && b - 1 >= a) ? wv[2L * (b - 1)] : 0.0;
 			for (int t = 0; t < Ls; ++t) {
 				const int r = b - 1 - t;
 				const bool live = on && r >= a;
 				const bool nlive = on && r - 1 >= a;
 #pragma unroll
 				for (int k = 1; k <= P; ++k) ln[k - 1] = (nlive && t + 1 - k >= 0) ? fs[(long)(r - 1 + k) * NE + k - 1] : make_double2(0.0, 0.0);
-				const double wnext = nlive ? wv[(long)(r - 1) * rs] : 0.0;
+				const double wnext = nlive ? wv[2L * (r - 1)] : 0.0;
 				double acc = live ? wcur : 0.0;
 #pragma unroll
 				for (int k = 0; k < P; ++k)
@@ -590,7 +613,7 @@ __global__ void __launch_bounds__(128) k_chain_seg(double2* __restrict__ X, doub
 				for (int k = P - 1; k >= 1; --k) { hr[k] = hr[k - 1]; hi[k] = hi[k - 1]; }
 				hr[0] = part ? other : acc;
 				hi[0] = part ? acc : other;
-				if (live) wv[(long)r * rs] = acc;
+				if (live) wv[2L * r] = acc;
 #pragma unroll
 				for (int k = 0; k < P; ++k) l[k] = ln[k];
 				wcur = wnext;
@@ -601,17 +624,16 @@ __global__ void __launch_bounds__(128) k_chain_seg(double2* __restrict__ X, doub
 		if (warp < NC) {
 			const int c = warp, i = lane >> 1, part = lane & 1;
 			const bool on = app < s_a[c] && i < P;
-			const double2* sp = spb + (s_f[c] / ((long)N * NE)) * (long)N * P;
-			const double* wv = Wd + 2 * s_x[c] + part;
+			const double* wv = reinterpret_cast<const double*>(wsh + c * N) + part;
 			for (int sg = Q - 2; sg >= 0; --sg) {
 				double v = 0.0;
 				if (on) {
 					const int r = (sg + 1) * Ls + i;
-					v = wv[(long)r * rs];
+					v = wv[2L * r];
 					if (sg + 1 <= Q - 2) {
 #pragma unroll
 						for (int jj = 0; jj < P; ++jj) {
-							const double2 ph = sp[(long)r * P + jj], xv = xc[c][sg + 1][jj];
+							const double2 ph = cbw[(sg * P + i) * P + jj], xv = xc[c][sg + 1][jj];
 							v += part ? ph.x * xv.y + ph.y * xv.x : ph.x * xv.x - ph.y * xv.y;
 						}
 					}
@@ -630,13 +652,13 @@ __global__ void __launch_bounds__(128) k_chain_seg(double2* __restrict__ X, doub
 			for (int c = 0; c < NC; ++c) {
 				xr[c] = 0.0; xi[c] = 0.0;
 				if (app < s_a[c]) {
-					const long o = 2 * s_x[c] + (long)r * rs;
-					xr[c] = Wd[o]; xi[c] = Wd[o + 1];
+					const double2 w0 = wsh[c * N + r];
+					xr[c] = w0.x; xi[c] = w0.y;
 					if (sg <= Q - 2) {
-						const double2* sp = spb + (s_f[c] / ((long)N * NE)) * (long)N * P + (long)r * P;
+						const double2* sp = spbb + (long)r * P;
 #pragma unroll
 						for (int jj = 0; jj < P; ++jj) {
-							const double2 ph = sp[jj], xv = xc[c][sg][jj];
+							const double2 ph = __ldg(sp + jj), xv = xc[c][sg][jj];
 							xr[c] += ph.x * xv.x - ph.y * xv.y;
 							xi[c] += ph.x * xv.y + ph.y * xv.x;
 						}

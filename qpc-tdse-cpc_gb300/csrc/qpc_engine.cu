@@ -417,6 +417,8 @@ struct qpc_lgwz {
 	// the spikes [block][N][P] of the coupling factors (per look-ahead slot) and of the field-free ones
 	bool seg_ok = false;
 	int Q = 1, Ls = 0;
+	bool seg_sfac[2] = {false, false};	// [coupling]: the factor block staged in shared memory
+	size_t seg_smem[2] = {0, 0};		// [coupling]: dynamic shared memory of k_chain_seg
 	double2 *spf_c = nullptr, *spb_c = nullptr, *spf_ff = nullptr, *spb_ff = nullptr;
 	int* ffmap = nullptr;     // device [B]: the instance whose factors a (sorted) instance uses, during a run
 	int* ffmap_id = nullptr;  // device [B]: identity
@@ -597,9 +599,15 @@ void launch_chain_seg(qpc_lgwz* h, cudaStream_t st, int b0, double2* X, const do
 	if (nch <= 0) return;
 	long chbase = (long)b0 * per;
 	unsigned grid = (unsigned)(nch / (CPL ? 2 : 1));
-	k_chain_seg<P, CPL><<<grid, 128, 0, st>>>(X, h->wk, fac, CPL ? h->spf_c : h->spf_ff, CPL ? h->spb_c : h->spb_ff, h->S, nta, step, jslot,
-		h->B, h->M, h->d.m0, h->N, h->L, h->npair, chbase, chbase + nch, h->Q, h->Ls, CPL ? nullptr : h->ffmap_cur,
-		(long)h->nlh * h->N * (h->P + 1));
+	const size_t smem = h->seg_smem[CPL];
+	if (h->seg_sfac[CPL])
+		k_chain_seg<P, CPL, true><<<grid, 128, smem, st>>>(X, fac, CPL ? h->spf_c : h->spf_ff, CPL ? h->spb_c : h->spb_ff, h->S, nta, step,
+			jslot, h->B, h->M, h->d.m0, h->N, h->L, h->npair, chbase, chbase + nch, h->Q, h->Ls, CPL ? nullptr : h->ffmap_cur,
+			(long)h->nlh * h->N * (h->P + 1));
+	else
+		k_chain_seg<P, CPL, false><<<grid, 128, smem, st>>>(X, fac, CPL ? h->spf_c : h->spf_ff, CPL ? h->spb_c : h->spb_ff, h->S, nta, step,
+			jslot, h->B, h->M, h->d.m0, h->N, h->L, h->npair, chbase, chbase + nch, h->Q, h->Ls, CPL ? nullptr : h->ffmap_cur,
+			(long)h->nlh * h->N * (h->P + 1));
 	LAUNCH(h);
 }
 
@@ -786,10 +794,33 @@ bool raise_attr(int dev, int family, size_t smem)
 	return true;
 }
 
+template <int P>
+void set_seg_smem_attr(qpc_lgwz* h)
+{
+	for (int cpl = 0; cpl < 2; ++cpl) {
+		const size_t smem = h->seg_smem[cpl];
+		if (smem <= 48 * 1024 || !raise_attr(h->dev, 100 + 4 * P + 2 * cpl + (h->seg_sfac[cpl] ? 1 : 0), smem)) continue;
+		if (cpl && h->seg_sfac[1]) cudaFuncSetAttribute(k_chain_seg<P, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+		if (cpl && !h->seg_sfac[1]) cudaFuncSetAttribute(k_chain_seg<P, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+		if (!cpl && h->seg_sfac[0]) cudaFuncSetAttribute(k_chain_seg<P, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+		if (!cpl && !h->seg_sfac[0]) cudaFuncSetAttribute(k_chain_seg<P, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+	}
+}
+
 void set_smem_attrs(qpc_lgwz* h, size_t tr_smem)
 {
 	if (tr_smem > 48 * 1024 && raise_attr(h->dev, 0, tr_smem))
 		cudaFuncSetAttribute(k_transform, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tr_smem);
+	if (h->seg_ok) {
+		switch (h->P) {
+		case 3: set_seg_smem_attr<3>(h); break;
+		case 4: set_seg_smem_attr<4>(h); break;
+		case 5: set_seg_smem_attr<5>(h); break;
+		case 6: set_seg_smem_attr<6>(h); break;
+		case 7: set_seg_smem_attr<7>(h); break;
+		case 8: set_seg_smem_attr<8>(h); break;
+		}
+	}
 	if (!raise_attr(h->dev, h->P, h->chain_smem)) return;
 	switch (h->P) {
 	case 3: set_chain_smem_attr<3>(h->chain_smem); break;
@@ -992,6 +1023,18 @@ static int create_impl(const qpc_dims* dims, double dt, const double* S, const d
 		h->seg_ok = q >= 2;
 		h->Q = q;
 		h->Ls = (N + q - 1) / q;
+		// stage the factor block in shared memory when it fits beside the kernel's static arrays
+		int optin = 0;
+		cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+		const long budget = (long)optin - 8 * 1024;
+		for (int cpl = 0; cpl < 2; ++cpl) {
+			const int nc = cpl ? 2 : 1;
+			const long with = (long)sizeof(double2) * seg_smem_elems(N, P, nc, q, true);
+			const long without = (long)sizeof(double2) * seg_smem_elems(N, P, nc, q, false);
+			h->seg_sfac[cpl] = with <= budget;
+			h->seg_smem[cpl] = (size_t)(h->seg_sfac[cpl] ? with : without);
+			if (!h->seg_sfac[cpl] && without > budget) h->seg_ok = false;
+		}
 	}
 	if (h->seg_ok) {
 		const size_t nblk_ff = (size_t)nff * h->nlh, nblk_c = (size_t)h->K * h->B * M * np;
