@@ -203,6 +203,21 @@ int qpc_lgwz_run_many(int32_t n, qpc_lgwz* const* hs, const double* const* ftab,
 int qpc_lgwz_run_dipole(qpc_lgwz* h, const double* ftab, int64_t ld, const int64_t* nt_field, const int64_t* nt_total,
 	const double* F, double* zlist, int64_t ldz);
 
+/* What the driver loop does to the state after every propagate besides observing
+ * (binsrc/sphTDSE.cpp:797-810): the t-SURFF accumulate (spec::accumulate with f(t_i), f(t_i+1)
+ * during the pulse, the field-free accumulate after it) and then the absorbing mask
+ * (absorber_mask::operator(), absorber.hpp:51-63).  Either may be NULL. */
+typedef struct qpc_run_opts {
+	const double* mask;             /* absorber band [n_r][p+1] (qpc_mask_band), or NULL */
+	struct qpc_tsurff* tsurff;      /* t-SURFF handle over the same grid and batch (dt = the propagator's), or NULL */
+} qpc_run_opts;
+/* qpc_lgwz_run with the per-step t-SURFF accumulate and mask of opts applied to every
+ * instance after each of its steps, on the device, without a host round trip: each coupling
+ * step is then applied as its closing and opening halves around them.  Not combined with the
+ * in-loop dipole (QPC_ERR_ARGS). */
+int qpc_lgwz_run_ex(qpc_lgwz* h, const double* ftab, int64_t ld, const int64_t* nt_field, const int64_t* nt_total,
+	const qpc_run_opts* opts);
+
 /* S-norm per instance, sum over (m,l) of c^H S c
  * (operator_rsym::observe, spherical/operators/1e.hpp:69-89); norm[n_inst]. */
 int qpc_lgwz_norm(qpc_lgwz* h, double* norm);
@@ -278,6 +293,13 @@ int qpc_vgwr_dims(qpc_vgwr* h, qpc_dims* dims);
 int qpc_vgwr_propagate(qpc_vgwr* h, const double* ax_ti, const double* ax_tf, const double* ay_ti, const double* ay_tf);
 int qpc_vgwr_propagate_free(qpc_vgwr* h);
 int qpc_vgwr_run(qpc_vgwr* h, const double* atab, int64_t ld, const int64_t* nt_field, const int64_t* nt_total);
+/* qpc_vgwr_run that also records, for every instance k and step s < nt_total[k], the dipole
+ * xlist[k*ldz + s] = <x>, ylist[k*ldz + s] = <y> of psi_k(t_s) with f(r) = r: F = <Bi|f|Bj>
+ * ([n_r][p+1]), the observation the elliptical driver makes before each step (observable_r,
+ * spherical/observable/1e.hpp:52-129: x = Re(rm + rp)/2, y = Im(rp - rm)/2; recorded at
+ * binsrc/sphTDSE.cpp:515-527 and 933-934).  ldz >= max nt_total. */
+int qpc_vgwr_run_dipole(qpc_vgwr* h, const double* atab, int64_t ld, const int64_t* nt_field, const int64_t* nt_total,
+	const double* F, double* xlist, double* ylist, int64_t ldz);
 int qpc_vgwr_norm(qpc_vgwr* h, double* norm);
 int qpc_vgwr_last_run(qpc_vgwr* h, float* ms, int64_t* launches);
 /* Per-kernel timing of qpc_vgwr_run: when on, each launch group is bracketed by CUDA events on

@@ -35,7 +35,8 @@
 //       the velocity-gauge elliptical propagator propagator_cn_hc_vgwr
 //       (cn_1e.hpp:812-951): FIELD holds NT+1 rows (A_x, A_y) at t_0..t_NT; runs
 //       propagate(coef, ax_i, ax_i+1, ay_i, ay_i+1) for i < NT, then NFREE field-free
-//       steps; writes coef, the S-norm and the eigenvalues of the four couplings.
+//       steps; writes coef, the S-norm, the eigenvalues of the four couplings and the
+//       dipole <x>, <y> before every step (observable_r, the elliptical driver's record).
 //   mask   OUT RMAX DT ZC ZS SG INIT RMIN RMAXM INDEX
 //       absorber_mask (absorber.hpp:40-63) initialised on [RMIN, RMAXM] with exponent INDEX
 //       and applied once to INIT: writes the mask band and the masked coefficients.
@@ -336,10 +337,21 @@ static int cmd_vgwr(int argc, char** argv)
 	auto v = slurp(init, 2 * dims_t::n_leng);
 	std::memcpy((double*)coef.data, v.data(), sizeof(double) * v.size());
 	std::vector<double> f = nt ? slurp(field, 2 * (nt + 1)) : std::vector<double>{};
+	// the elliptical driver's observation before each step (binsrc/sphTDSE.cpp:515-527, 933):
+	// observable_r with f(r) = r, x = Re(rm + rp)/2, y = Im(rp - rm)/2
+	auto obs = observable_r<dims_t>();
+	obs.initialize(radi, angu);
+	std::vector<double> xs, ys;
 	for (size_t it = 0; it < nt + nfree; ++it) {
+		auto rm = obs.observe_rm(coef.data, coef.data);
+		auto rp = obs.observe_rp(coef.data, coef.data);
+		xs.push_back(real(rm + rp) / 2.0);
+		ys.push_back(imag(rp - rm) / 2.0);
 		if (it < nt) prop.propagate(coef, f[2 * it], f[2 * it + 2], f[2 * it + 1], f[2 * it + 3]);
 		else prop.propagate(coef);
 	}
+	dump(out, "xlist", xs.data(), xs.size());
+	dump(out, "ylist", ys.data(), ys.size());
 	dump(out, "coef", coef.data, 2 * dims_t::n_leng);
 	double norm = 0.0;
 	#pragma omp parallel

@@ -28,7 +28,7 @@ POTENTIAL_YUKAWA = 1
 # every symbol include/qpc_gb300.h declares
 EXPORTS = (
     "qpc_last_error", "qpc_version", "qpc_set_wait_limit", "qpc_get_wait_limit", "qpc_fp64_peak",
-    "qpc_lgwz_stream", "qpc_vgwr_set_profiling", "qpc_vgwr_kernel_times", "qpc_linear_knots", "qpc_radial_setup", "qpc_y10_coupling",
+    "qpc_lgwz_stream", "qpc_vgwr_set_profiling", "qpc_vgwr_kernel_times", "qpc_vgwr_run_dipole", "qpc_lgwz_run_ex", "qpc_linear_knots", "qpc_radial_setup", "qpc_y10_coupling",
     "qpc_y10_eigen", "qpc_ldlt_csym", "qpc_gen_eigen", "qpc_field_sinen", "qpc_lgwz_create",
     "qpc_lgwz_destroy", "qpc_lgwz_put", "qpc_lgwz_get", "qpc_lgwz_put_device", "qpc_lgwz_get_device",
     "qpc_lgwz_propagate", "qpc_lgwz_propagate_free", "qpc_lgwz_run", "qpc_lgwz_norm", "qpc_lgwz_dipole",
@@ -66,6 +66,10 @@ class qpc_potential(ctypes.Structure):
 class qpc_dims(ctypes.Structure):
     _fields_ = [("n_r", ctypes.c_int32), ("p", ctypes.c_int32), ("n_l", ctypes.c_int32),
                 ("n_m", ctypes.c_int32), ("m0", ctypes.c_int32), ("n_inst", ctypes.c_int32)]
+
+
+class qpc_run_opts(ctypes.Structure):
+    _fields_ = [("mask", ctypes.c_void_p), ("tsurff", ctypes.c_void_p)]
 
 
 class qpc_kgrid(ctypes.Structure):
@@ -110,6 +114,7 @@ def load(path=None):
         "qpc_lgwz_propagate": (ctypes.c_int, [P, P, P]),
         "qpc_lgwz_propagate_free": (ctypes.c_int, [P]),
         "qpc_lgwz_run": (ctypes.c_int, [P, P, i64, P, P]),
+        "qpc_lgwz_run_ex": (ctypes.c_int, [P, P, i64, P, P, P]),
         "qpc_lgwz_norm": (ctypes.c_int, [P, P]),
         "qpc_lgwz_dipole": (ctypes.c_int, [P, P, P]),
         "qpc_lgwz_projection": (ctypes.c_int, [P, P, P, P]),
@@ -137,6 +142,7 @@ def load(path=None):
         "qpc_vgwr_propagate": (ctypes.c_int, [P, P, P, P, P]),
         "qpc_vgwr_propagate_free": (ctypes.c_int, [P]),
         "qpc_vgwr_run": (ctypes.c_int, [P, P, i64, P, P]),
+        "qpc_vgwr_run_dipole": (ctypes.c_int, [P, P, i64, P, P, P, P, P, i64]),
         "qpc_vgwr_norm": (ctypes.c_int, [P, P]),
         "qpc_vgwr_last_run": (ctypes.c_int, [P, P, P]),
         "qpc_vgwr_set_profiling": (ctypes.c_int, [P, ctypes.c_int]),
@@ -457,6 +463,25 @@ class propagator_cn_hc_lgwz:
         if ftab.shape[0] != self.shape[0]:
             ftab = _f64(np.broadcast_to(ftab, (self.shape[0], ftab.shape[1])))
         _check(load().qpc_lgwz_run(self._h, _ptr(ftab), ftab.shape[1], _ptr(nt_field), _ptr(nt_total)))
+
+    def run_ex(self, ftab, nt_field, nt_total=None, mask=None, tsurff=None):
+        """run() with, after every step of every instance, the t-SURFF accumulate into `tsurff`
+        (a spectrum_c_tsf over the same grid and batch) and then the absorbing mask `mask`
+        (a band from mask_band), as the reference's driver loop applies them
+        (binsrc/sphTDSE.cpp:797-810), all on the device."""
+        nt_field = np.ascontiguousarray(np.broadcast_to(nt_field, (self.shape[0],)), dtype=np.int64)
+        nt_total = nt_field.copy() if nt_total is None else np.ascontiguousarray(
+            np.broadcast_to(nt_total, (self.shape[0],)), dtype=np.int64)
+        mk = None if mask is None else _f64(mask)
+        opts = qpc_run_opts(None if mk is None else mk.ctypes.data, None if tsurff is None else tsurff._h.value)
+        if ftab is None:
+            tab, ld = None, 1
+        else:
+            tab = _f64(np.atleast_2d(ftab))
+            if tab.shape[0] != self.shape[0]:
+                tab = _f64(np.broadcast_to(tab, (self.shape[0], tab.shape[1])))
+            ld = tab.shape[1]
+        _check(load().qpc_lgwz_run_ex(self._h, _ptr(tab), ld, _ptr(nt_field), _ptr(nt_total), ctypes.byref(opts)))
 
     def run_dipole(self, ftab, nt_field, nt_total, F):
         """run() that also returns zlist[inst, s] = <psi(t_s)| f(r) cos(theta) |psi(t_s)>
@@ -810,6 +835,25 @@ class propagator_cn_hc_vgwr:
         nf = np.ascontiguousarray(np.broadcast_to(nt_field, (B,)), dtype=np.int64)
         ntt = nf.copy() if nt_total is None else np.ascontiguousarray(np.broadcast_to(nt_total, (B,)), dtype=np.int64)
         _check(load().qpc_vgwr_run(self._h, _ptr(tab), tab.shape[1], _ptr(nf), _ptr(ntt)))
+
+    def run_dipole(self, atab, nt_field, nt_total, F):
+        """run() that also returns (x, y)[inst, s] = <psi(t_s)| f(r) sin(theta) (cos, sin)(phi) |psi(t_s)>
+        for s < nt_total[inst] (observable_r; F = <B|f|B>, f(r) = r for the dipole)."""
+        B = self.shape[0]
+        nf = np.ascontiguousarray(np.broadcast_to(nt_field, (B,)), dtype=np.int64)
+        ntt = np.ascontiguousarray(np.broadcast_to(nt_total, (B,)), dtype=np.int64)
+        ldz = int(max(1, ntt.max()))
+        x = np.zeros((B, ldz))
+        y = np.zeros((B, ldz))
+        if atab is None:
+            tab, ld = None, 1
+        else:
+            tab = _f64(np.asarray(atab, np.float64).reshape(-1 if np.ndim(atab) == 3 else 1, np.shape(atab)[-2], 2))
+            if tab.shape[0] != B:
+                tab = _f64(np.broadcast_to(tab, (B,) + tab.shape[1:]))
+            ld = tab.shape[1]
+        _check(load().qpc_vgwr_run_dipole(self._h, _ptr(tab), ld, _ptr(nf), _ptr(ntt), _ptr(_f64(F)), _ptr(x), _ptr(y), ldz))
+        return x, y
 
     def norm(self):
         out = np.zeros(self.shape[0])

@@ -50,9 +50,16 @@ struct chain_cfg {
 	static_assert(CPW >= 1, "too many lanes per chain");
 };
 
-__device__ __forceinline__ int coupling_power(long s, long nt)
+// coupling applications of an instance with nt field steps at loop step s.  cmode 0 (fused): the
+// closing half of step s-1 and the opening half of step s together (M^2 with one factorisation);
+// cmode 1: the closing half only; cmode 2: the opening half only (a run that acts on the state
+// between two steps, e.g. with an absorbing mask, splits every coupling step in two)
+__device__ __forceinline__ int coupling_power(long s, long nt, int cmode = 0)
 {
-	if (nt <= 0 || s > nt) return 0;
+	if (nt <= 0) return 0;
+	if (cmode == 1) return (s >= 1 && s <= nt) ? 1 : 0;
+	if (cmode == 2) return s < nt ? 1 : 0;
+	if (s > nt) return 0;
 	return (s == 0 || s == nt) ? 1 : 2;
 }
 
@@ -66,7 +73,7 @@ struct chain_desc {
 // instance inst uses, at ffmap[inst] * ffstride; without it every instance shares one set.
 template <bool CPL>
 __device__ __forceinline__ chain_desc describe(long ch, long nchains, const int64_t* __restrict__ nta, long step, int jslot,
-	int B, int M, int m0, int N, int L, int np, int NE, const int* __restrict__ ffmap = nullptr, long ffstride = 0)
+	int B, int M, int m0, int N, int L, int np, int NE, const int* __restrict__ ffmap = nullptr, long ffstride = 0, int cmode = 0)
 {
 	chain_desc d{0, 0, 0};
 	if (ch >= nchains) return d;
@@ -78,7 +85,7 @@ __device__ __forceinline__ chain_desc describe(long ch, long nchains, const int6
 		long inst = im_inst / M;
 		d.xoff = im_inst * (long)N * L + 2 * k + sign;
 		d.foff = (((long)jslot * B * M + im_inst) * np + k) * (long)N * NE;
-		d.a = coupling_power(step, nta[inst]);
+		d.a = coupling_power(step, nta[inst], cmode);
 	} else {
 		int il = (int)(ch % L);
 		long im_inst = ch / L;
@@ -112,7 +119,8 @@ template <int P, int G, bool CPL>
 __global__ void __launch_bounds__(128) k_chain(double2* __restrict__ X, double2* __restrict__ Wk,
 	const double2* __restrict__ fac, const double* __restrict__ S, const int64_t* __restrict__ nta,
 	long step, int jslot, int B, int M, int m0, int N, int L, int np, long chbase, long nchains,
-	const double* __restrict__ Fo = nullptr, double* __restrict__ obs = nullptr, const int* __restrict__ ffmap = nullptr, long ffstride = 0)
+	const double* __restrict__ Fo = nullptr, double* __restrict__ obs = nullptr, const int* __restrict__ ffmap = nullptr, long ffstride = 0,
+	int cmode = 0)
 {
 	// chains [chbase, nchains) of this launch (an instance group); nchains is an end index.
 	// Fo/obs (coupling chains only, optional): obs[chain] = <z|F|z> of the chain's vector at
@@ -133,7 +141,7 @@ __global__ void __launch_bounds__(128) k_chain(double2* __restrict__ X, double2*
 	__shared__ int s_a[4][32];
 	const int wib = threadIdx.x >> 5;
 	if (lane < CPW) {
-		chain_desc d = describe<CPL>(ch0 + lane, nchains, nta, step, jslot, B, M, m0, N, L, np, NE, ffmap, ffstride);
+		chain_desc d = describe<CPL>(ch0 + lane, nchains, nta, step, jslot, B, M, m0, N, L, np, NE, ffmap, ffstride, cmode);
 		s_x[wib][lane] = d.xoff; s_f[wib][lane] = d.foff; s_a[wib][lane] = d.a;
 	}
 	__syncwarp();
@@ -451,7 +459,7 @@ template <int P, bool CPL, bool SFAC>
 __global__ void __launch_bounds__(128) k_chain_seg(double2* __restrict__ X, const double2* __restrict__ fac,
 	const double2* __restrict__ spf, const double2* __restrict__ spb, const double* __restrict__ S, const int64_t* __restrict__ nta,
 	long step, int jslot, int B, int M, int m0, int N, int L, int np, long chbase, long nchains, int Q, int Ls,
-	const int* __restrict__ ffmap, long ffstride)
+	const int* __restrict__ ffmap, long ffstride, int cmode)
 {
 	constexpr int NE = P + 1, NC = CPL ? 2 : 1;
 	const unsigned FULL = 0xffffffffu;
@@ -462,7 +470,7 @@ __global__ void __launch_bounds__(128) k_chain_seg(double2* __restrict__ X, cons
 	const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 	const long ch0 = chbase + (long)blockIdx.x * NC;
 	if (tid < NC) {
-		chain_desc d = describe<CPL>(ch0 + tid, nchains, nta, step, jslot, B, M, m0, N, L, np, NE, ffmap, ffstride);
+		chain_desc d = describe<CPL>(ch0 + tid, nchains, nta, step, jslot, B, M, m0, N, L, np, NE, ffmap, ffstride, cmode);
 		s_x[tid] = d.xoff; s_f[tid] = d.foff; s_a[tid] = d.a;
 	}
 	__syncthreads();

@@ -41,6 +41,7 @@
 #include <thread>
 #include <mutex>
 #include <atomic>
+#include <functional>
 #include <map>
 #include <cstdlib>
 #include "qpc_chain.cuh"
@@ -113,9 +114,9 @@ constexpr int TR = 32;
 
 __global__ void __launch_bounds__(256) k_transform(const double2* __restrict__ src, double2* __restrict__ dst,
 	const double* __restrict__ Vh, int N, int L, int M, int npair, int forward,
-	const int64_t* __restrict__ ntf, long step, int b0, int B)
+	const int64_t* __restrict__ ntf, long step, int b0, int B, int cmode)
 {
-	// instances [b0, b0+B) of this launch (an instance group)
+	// instances [b0, b0+B) of this launch (an instance group); cmode as in coupling_power
 	extern __shared__ double2 sm[];
 	const int ldt = L | 1;	// odd stride in 16-byte units
 	double2* tin = sm;
@@ -127,7 +128,7 @@ __global__ void __launch_bounds__(256) k_transform(const double2* __restrict__ s
 	int m = (int)(im_inst % M);
 	long inst = im_inst / M;
 	if (inst >= b0 + B) return;
-	if (coupling_power(step, ntf[inst]) == 0) return;
+	if (coupling_power(step, ntf[inst], cmode) == 0) return;
 	int r0 = tile * TR;
 	int nr = min(TR, N - r0);
 	const double2* s = src + (im_inst * (long)N + r0) * L;
@@ -407,6 +408,8 @@ struct qpc_lgwz {
 	int NS = 1;
 	cudaStream_t gs[MAXNS] = {nullptr, nullptr, nullptr, nullptr};
 	cudaEvent_t gev[MAXNS] = {nullptr, nullptr, nullptr, nullptr};
+	cudaEvent_t xev = nullptr;	// main stream -> instance groups, after the per-step extras of a run
+	int* slotmap = nullptr;		// device [B]: the sorted slot of each instance during a run (t-SURFF)
 	double* S = nullptr;      // [N][P+1]
 	double* R = nullptr;      // [N][P+1]
 	double* Vh = nullptr;     // [M][npair+1][L]
@@ -417,6 +420,7 @@ struct qpc_lgwz {
 	// the spikes [block][N][P] of the coupling factors (per look-ahead slot) and of the field-free ones
 	bool seg_ok = false;
 	int Q = 1, Ls = 0;
+	int cmode = 0;	// coupling mode of the launches being enqueued (coupling_power): 0 fused, 1 closing, 2 opening
 	bool seg_sfac[2] = {false, false};	// [coupling]: the factor block staged in shared memory
 	size_t seg_smem[2] = {0, 0};		// [coupling]: dynamic shared memory of k_chain_seg
 	double2 *spf_c = nullptr, *spb_c = nullptr, *spf_ff = nullptr, *spb_ff = nullptr;
@@ -468,11 +472,19 @@ struct qpc_lgwz {
 // t = M c per channel (all lanes, one element each), then c = (L L^T)^-1 t with one lane per
 // real recurrence (channel, real or imaginary part); Lrow[r][j-1] = L(r, r-j),
 // Lcol[r][k-1] = L(r+k, r), dinv[r] = 1/L(r, r).
+// mask_active: inside a run, the instance (sorted slot) takes the mask after loop step s - 1 when
+// 1 <= s <= nt_total (ntt == NULL: every instance, the stand-alone call)
+__device__ __forceinline__ bool mask_active(const int64_t* __restrict__ ntt, long step, long inst)
+{
+	return !ntt || (step >= 1 && step <= ntt[inst]);
+}
+
 __global__ void k_mask_band(const double2* __restrict__ st, double2* __restrict__ t, const double* __restrict__ Mb, int N, int P, int L,
-	long total)
+	long total, const int64_t* __restrict__ ntt = nullptr, long step = 0, long per_inst = 1)
 {
 	const long e = (long)blockIdx.x * blockDim.x + threadIdx.x;
 	if (e >= total) return;
+	if (!mask_active(ntt, step, e / per_inst)) return;
 	const long row = e / L;
 	const int r = (int)(row % N);
 	double2 acc = make_double2(0.0, 0.0);
@@ -491,11 +503,13 @@ __global__ void k_mask_band(const double2* __restrict__ st, double2* __restrict_
 
 template <int P>
 __global__ void k_mask_solve(double2* __restrict__ st, double2* __restrict__ tb, const double* __restrict__ Lrow,
-	const double* __restrict__ Lcol, const double* __restrict__ dinv, int N, int L, long nchain)
+	const double* __restrict__ Lcol, const double* __restrict__ dinv, int N, int L, long nchain,
+	const int64_t* __restrict__ ntt = nullptr, long step = 0, int M = 1)
 {
 	const long c = (long)blockIdx.x * blockDim.x + threadIdx.x;
 	if (c >= nchain) return;
 	const long bm = c / (2L * L);
+	if (!mask_active(ntt, step, bm / M)) return;
 	const int rest = (int)(c - bm * 2L * L);	// l * 2 + part
 	const long stride = 2L * L;
 	double* t = reinterpret_cast<double*>(tb) + bm * N * stride + rest;
@@ -587,7 +601,7 @@ void launch_chain_g(qpc_lgwz* h, cudaStream_t st, int b0, double2* X, const doub
 	bool ob = CPL && h->observing;
 	k_chain<P, G, CPL><<<grid, 128, h->chain_smem, st>>>(X, h->wk, fac, h->S, nta, step, jslot, h->B, h->M, h->d.m0,
 		h->N, h->L, h->npair, chbase, chbase + nch, ob ? h->obsF : nullptr, ob ? h->obs : nullptr,
-		CPL ? nullptr : h->ffmap_cur, (long)h->nlh * h->N * (h->P + 1));
+		CPL ? nullptr : h->ffmap_cur, (long)h->nlh * h->N * (h->P + 1), h->cmode);
 	LAUNCH(h);
 }
 
@@ -603,11 +617,11 @@ void launch_chain_seg(qpc_lgwz* h, cudaStream_t st, int b0, double2* X, const do
 	if (h->seg_sfac[CPL])
 		k_chain_seg<P, CPL, true><<<grid, 128, smem, st>>>(X, fac, CPL ? h->spf_c : h->spf_ff, CPL ? h->spb_c : h->spb_ff, h->S, nta, step,
 			jslot, h->B, h->M, h->d.m0, h->N, h->L, h->npair, chbase, chbase + nch, h->Q, h->Ls, CPL ? nullptr : h->ffmap_cur,
-			(long)h->nlh * h->N * (h->P + 1));
+			(long)h->nlh * h->N * (h->P + 1), h->cmode);
 	else
 		k_chain_seg<P, CPL, false><<<grid, 128, smem, st>>>(X, fac, CPL ? h->spf_c : h->spf_ff, CPL ? h->spb_c : h->spb_ff, h->S, nta, step,
 			jslot, h->B, h->M, h->d.m0, h->N, h->L, h->npair, chbase, chbase + nch, h->Q, h->Ls, CPL ? nullptr : h->ffmap_cur,
-			(long)h->nlh * h->N * (h->P + 1));
+			(long)h->nlh * h->N * (h->P + 1), h->cmode);
 	LAUNCH(h);
 }
 
@@ -643,6 +657,17 @@ int live_bucket(int n) { int b = 0; while ((1 << b) < n) ++b; return b; }
 // events) on scratch buffers (eo / wk / the factor slot of this step, whose
 // contents are about to be overwritten) and keep the fastest.  Runs before
 // the step's forward transform, once per (kernel, live bucket).
+// Tuning decisions are shared by every handle of the process with the same grid shape, so that
+// two handles that do the same work choose the same kernels and give bit-identical results (the
+// candidates differ in rounding); the first handle to meet a (shape, live bucket) times it.
+std::mutex g_tune_mu;
+std::map<std::vector<long>, int> g_tune;
+
+std::vector<long> tune_key(const qpc_lgwz* h, int cpl, int bk)
+{
+	return {h->dev, h->N, h->P, h->L, h->M, h->npair, h->NS, h->hpi, h->seg_ok ? 1 : 0, cpl, bk};
+}
+
 template <int P>
 int autotune_one(qpc_lgwz* h, int cpl, long step, int jslot, int Bl)
 {
@@ -652,6 +677,11 @@ int autotune_one(qpc_lgwz* h, int cpl, long step, int jslot, int Bl)
 	if (const char* e = getenv("QPC_CHAIN_G")) {
 		const int G = atoi(e);
 		if (std::find(h->gcand.begin(), h->gcand.end(), G) != h->gcand.end()) { h->gsel[cpl][bk] = G; return QPC_OK; }
+	}
+	{
+		std::lock_guard<std::mutex> lk(g_tune_mu);
+		auto it = g_tune.find(tune_key(h, cpl, bk));
+		if (it != g_tune.end()) { h->gsel[cpl][bk] = it->second; return QPC_OK; }
 	}
 	float best = 1e30f;
 	int bestg = 1;
@@ -673,7 +703,9 @@ int autotune_one(qpc_lgwz* h, int cpl, long step, int jslot, int Bl)
 		QPC_CUDA(cudaGetLastError());
 		if (tot < best) { best = tot; bestg = G; }
 	}
-	h->gsel[cpl][bk] = bestg;
+	std::lock_guard<std::mutex> lk(g_tune_mu);
+	auto ins = g_tune.emplace(tune_key(h, cpl, bk), bestg);	// a handle tuning concurrently may have stored first
+	h->gsel[cpl][bk] = ins.first->second;
 	return QPC_OK;
 }
 
@@ -726,7 +758,7 @@ void launch_group_step(qpc_lgwz* h, cudaStream_t st, int b0, long step, long ste
 		unsigned grid = (unsigned)((long)Bc * M * tiles);
 		{
 			prof_scope ps(h, QPC_KERNEL_TRANSFORM_FWD, st);
-			k_transform<<<grid, 256, smem, st>>>(h->st, h->eo, h->Vh, N, L, M, np, 1, h->ntf, step, b0, Bc);
+			k_transform<<<grid, 256, smem, st>>>(h->st, h->eo, h->Vh, N, L, M, np, 1, h->ntf, step, b0, Bc, h->cmode);
 			LAUNCH(h);
 		}
 		if (np > 0) {
@@ -735,7 +767,7 @@ void launch_group_step(qpc_lgwz* h, cudaStream_t st, int b0, long step, long ste
 		}
 		{
 			prof_scope ps(h, QPC_KERNEL_TRANSFORM_BWD, st);
-			k_transform<<<grid, 256, smem, st>>>(h->eo, h->st, h->Vh, N, L, M, np, 0, h->ntf, step, b0, Bc);
+			k_transform<<<grid, 256, smem, st>>>(h->eo, h->st, h->Vh, N, L, M, np, 0, h->ntf, step, b0, Bc, h->cmode);
 			LAUNCH(h);
 		}
 	}
@@ -765,6 +797,55 @@ int launch_step_t(qpc_lgwz* h, long step, long step0, int jslot, bool do_factor,
 	for (int g = 0; g < h->NS; ++g)
 		launch_group_step<P>(h, h->gs[g], gb[g], step, step0, jslot, do_factor, kfac, Bc[g], Bf[g], Bc[g]);
 	return QPC_OK;
+}
+
+// What a run does to the state between two steps (the driver loop's t-SURFF accumulate and
+// absorbing mask after each propagate, binsrc/sphTDSE.cpp:800-810), enqueued on the main stream
+// once the instance groups have finished the closing half: fn(step) for loop step `step`.
+struct between_steps {
+	std::function<int(long)> fn;
+};
+
+// Loop step s of a run with work between steps: every coupling step is split in its closing half
+// (the end of step s - 1) and its opening half (step s), with the extras in between; the factors
+// of f(t_s) serve both halves.
+template <int P>
+int launch_split_t(qpc_lgwz* h, long step, long step0, int jslot, bool do_factor, int kfac, const int* gb, const int* Bc, const int* Bf,
+	const between_steps& x)
+{
+	if (int rc = autotune<P>(h, step, jslot, Bc, Bf)) return rc;
+	bool fac = do_factor;
+	if (step > 0) {
+		h->cmode = 1;
+		for (int g = 0; g < h->NS; ++g) launch_group_step<P>(h, h->gs[g], gb[g], step, step0, jslot, fac, kfac, Bc[g], 0, Bc[g]);
+		h->cmode = 0;
+		fac = false;
+		for (int g = 0; g < h->NS; ++g) {
+			QPC_CUDA(cudaEventRecord(h->gev[g], h->gs[g]));
+			QPC_CUDA(cudaStreamWaitEvent(h->stream, h->gev[g], 0));
+		}
+		if (int rc = x.fn(step)) return rc;
+		QPC_CUDA(cudaEventRecord(h->xev, h->stream));
+		for (int g = 0; g < h->NS; ++g) QPC_CUDA(cudaStreamWaitEvent(h->gs[g], h->xev, 0));
+	}
+	h->cmode = 2;
+	for (int g = 0; g < h->NS; ++g) launch_group_step<P>(h, h->gs[g], gb[g], step, step0, jslot, fac, kfac, Bc[g], Bf[g], Bc[g]);
+	h->cmode = 0;
+	return QPC_OK;
+}
+
+int launch_split(qpc_lgwz* h, long step, long step0, int jslot, bool do_factor, int kfac, const int* gb, const int* Bc, const int* Bf,
+	const between_steps& x)
+{
+	switch (h->P) {
+	case 3: return launch_split_t<3>(h, step, step0, jslot, do_factor, kfac, gb, Bc, Bf, x);
+	case 4: return launch_split_t<4>(h, step, step0, jslot, do_factor, kfac, gb, Bc, Bf, x);
+	case 5: return launch_split_t<5>(h, step, step0, jslot, do_factor, kfac, gb, Bc, Bf, x);
+	case 6: return launch_split_t<6>(h, step, step0, jslot, do_factor, kfac, gb, Bc, Bf, x);
+	case 7: return launch_split_t<7>(h, step, step0, jslot, do_factor, kfac, gb, Bc, Bf, x);
+	case 8: return launch_split_t<8>(h, step, step0, jslot, do_factor, kfac, gb, Bc, Bf, x);
+	default: set_error("unsupported B-spline degree %d", h->P); return QPC_ERR_ARGS;
+	}
 }
 
 int launch_step(qpc_lgwz* h, long step, long step0, int jslot, bool do_factor, int kfac, const int* gb, const int* Bc, const int* Bf)
@@ -956,6 +1037,7 @@ static int create_impl(const qpc_dims* dims, double dt, const double* S, const d
 		if (cudaStreamCreateWithFlags(&h->gs[g], cudaStreamNonBlocking) != cudaSuccess) { set_error("stream create"); return fail(QPC_ERR_CUDA); }
 		cudaEventCreateWithFlags(&h->gev[g], cudaEventDisableTiming);
 	}
+	cudaEventCreateWithFlags(&h->xev, cudaEventDisableTiming);
 	// host setup: field-free LDL^T per l (per instance and l with hpi), Y10 eigensystems
 	const int nff = h->hpi ? h->B : 1;
 	std::vector<double2> ffh((size_t)N * NE * h->nlh * nff);
@@ -1100,11 +1182,12 @@ int qpc_lgwz_destroy(qpc_lgwz* h)
 	cudaFree(h->st); cudaFree(h->eo); cudaFree(h->wk); cudaFree(h->hostlay); cudaFree(h->fac);
 	cudaFree(h->status); cudaFree(h->red); cudaFree(h->ntf); cudaFree(h->ntt); cudaFree(h->ftab);
 	cudaFree(h->obsF); cudaFree(h->obs); cudaFree(h->dl); cudaFree(h->y10d); cudaFree(h->zdev);
-	cudaFree(h->mM); cudaFree(h->mLrow); cudaFree(h->mLcol); cudaFree(h->mdinv);
+	cudaFree(h->mM); cudaFree(h->mLrow); cudaFree(h->mLcol); cudaFree(h->mdinv); cudaFree(h->slotmap);
 	for (auto e : h->evpool) cudaEventDestroy(e);
 	for (int g = 0; g < qpc_lgwz::MAXNS; ++g) {
 		if (h->gs[g]) { cudaStreamSynchronize(h->gs[g]); cudaStreamDestroy(h->gs[g]); }
 		if (h->gev[g]) cudaEventDestroy(h->gev[g]);
+		if (g == 0 && h->xev) cudaEventDestroy(h->xev);
 	}
 	if (h->evt0) cudaEventDestroy(h->evt0);
 	if (h->evt1) cudaEventDestroy(h->evt1);
@@ -1172,8 +1255,11 @@ int qpc_lgwz_stream(qpc_lgwz* h, void** stream)
 	return QPC_OK;
 }
 
+static int mask_prepare(qpc_lgwz* h);
+static void mask_enqueue(qpc_lgwz* h, cudaStream_t st, const int64_t* ntt, long step);
+
 static int run_impl(qpc_lgwz* h, const double* ftab, int64_t ld, const int64_t* nt_field, const int64_t* nt_total,
-	const double* F, double* zlist, int64_t ldz)
+	const double* F, double* zlist, int64_t ldz, const qpc_run_opts* opts = nullptr)
 {
 	if (!h || !nt_field || !nt_total) { set_error("NULL argument"); return QPC_ERR_ARGS; }
 	QPC_CUDA(cudaSetDevice(h->dev));
@@ -1190,6 +1276,13 @@ static int run_impl(qpc_lgwz* h, const double* ftab, int64_t ld, const int64_t* 
 		smax = std::max<long>(smax, std::max<long>(nt_total[k], nt_field[k] + (nt_field[k] > 0 ? 1 : 0)));
 	}
 	if (anyfield && !ftab) { set_error("ftab is NULL"); return QPC_ERR_ARGS; }
+	const double* mband = opts ? opts->mask : nullptr;
+	qpc_tsurff* tsf = opts ? opts->tsurff : nullptr;
+	const bool split = mband || tsf;
+	if (split && F) { set_error("the in-loop dipole and the per-step mask or t-SURFF cannot be combined in one run"); return QPC_ERR_ARGS; }
+	if (tsf) if (int rc = tsurff_check_grid(tsf, h->d)) return rc;
+	long ntt_max = 0;
+	for (int k = 0; k < B; ++k) ntt_max = std::max<long>(ntt_max, nt_total[k]);
 	// field table to the device, padded to B*ld
 	size_t need = anyfield ? (size_t)B * ld : 1;
 	if (h->ftab_cap < need) {
@@ -1285,14 +1378,51 @@ static int run_impl(qpc_lgwz* h, const double* ftab, int64_t ld, const int64_t* 
 			Bc[g] = n; Bf[g] = f;
 		}
 	};
+	// per-step extras: the mask band and the slot map the t-SURFF prepare reads
+	std::vector<double> ta((size_t)2 * B);
+	std::vector<int> tact(B);
+	between_steps extras;
+	if (split) {
+		if (mband) {
+			if (int rc = mask_prepare(h)) return rc;
+			QPC_CUDA(cudaMemcpyAsync(h->mM, mband, sizeof(double) * h->N * (h->P + 1), cudaMemcpyHostToDevice, h->stream));
+		}
+		if (tsf) {
+			if (!h->slotmap) if (int rc = dalloc(&h->slotmap, (size_t)B)) return rc;
+			std::vector<int> slot(B);
+			for (int k = 0; k < B; ++k) slot[perm[k]] = k;
+			QPC_CUDA(cudaMemcpyAsync(h->slotmap, slot.data(), sizeof(int) * B, cudaMemcpyHostToDevice, h->stream));
+		}
+		if (int rc = wait_stream(h)) return rc;
+		// after step s - 1 of instance i (1 <= s <= nt_total[i]): accumulate with (f(t_s-1), f(t_s))
+		// while in the pulse, the field-free accumulate (zero field) after it, then the mask
+		extras.fn = [&](long s) -> int {
+			bool any = false;
+			for (int i = 0; i < B; ++i) {
+				tact[i] = (s >= 1 && s <= nt_total[i]) ? 1 : 0;
+				any |= tact[i] != 0;
+				const bool fld = s - 1 < nt_field[i];
+				ta[2 * (size_t)i] = fld ? ftab[(size_t)i * ld + s - 1] : 0.0;
+				ta[2 * (size_t)i + 1] = fld ? ftab[(size_t)i * ld + s] : 0.0;
+			}
+			if (!any) return QPC_OK;
+			if (tsf) if (int rc = tsurff_enqueue_engine(tsf, h->st, h->slotmap, ta.data(), tact.data(), h->dt, (void*)h->stream)) return rc;
+			if (mband) mask_enqueue(h, h->stream, h->ntt, s);
+			return QPC_OK;
+		};
+	}
+	// with extras every coupling step is split and the loop runs one more step (the extras after the last step)
+	const long send = split ? ntt_max + 1 : smax;
 	QPC_CUDA(cudaEventRecord(h->ev0, h->stream));
 	for (int g = 0; g < NS; ++g) QPC_CUDA(cudaStreamWaitEvent(h->gs[g], h->ev0, 0));
-	for (long s = 0; s < smax; ++s) {
+	for (long s = 0; s < send; ++s) {
 		// factors for steps s .. s+K-1 are computed together, into slots 0..K-1
 		int j = (int)(s % h->K);
-		long kf = std::min<long>(h->K, smax - s);
+		long kf = std::min<long>(h->K, send - s);
 		live_counts(s);
-		if (int rc = launch_step(h, s, s - j, j, j == 0, (int)kf, gb.data(), Bc.data(), Bf.data())) return rc;
+		if (split) {
+			if (int rc = launch_split(h, s, s - j, j, j == 0, (int)kf, gb.data(), Bc.data(), Bf.data(), extras)) return rc;
+		} else if (int rc = launch_step(h, s, s - j, j, j == 0, (int)kf, gb.data(), Bc.data(), Bf.data())) return rc;
 	}
 	for (int g = 0; g < NS; ++g) {
 		QPC_CUDA(cudaEventRecord(h->gev[g], h->gs[g]));
@@ -1321,6 +1451,11 @@ static int run_impl(qpc_lgwz* h, const double* ftab, int64_t ld, const int64_t* 
 int qpc_lgwz_run(qpc_lgwz* h, const double* ftab, int64_t ld, const int64_t* nt_field, const int64_t* nt_total)
 {
 	return run_impl(h, ftab, ld, nt_field, nt_total, nullptr, nullptr, 0);
+}
+
+int qpc_lgwz_run_ex(qpc_lgwz* h, const double* ftab, int64_t ld, const int64_t* nt_field, const int64_t* nt_total, const qpc_run_opts* opts)
+{
+	return run_impl(h, ftab, ld, nt_field, nt_total, nullptr, nullptr, 0, opts);
 }
 
 // Several handles at once: one host thread per handle, each driving its handle's
@@ -1393,49 +1528,65 @@ int qpc_lgwz_norm(qpc_lgwz* h, double* norm)
 	return QPC_OK;
 }
 
-int qpc_lgwz_mask(qpc_lgwz* h, const double* M)
+// the Cholesky factor of S for the mask's S^-1, once per handle (absorber.hpp:51-63)
+static int mask_prepare(qpc_lgwz* h)
 {
-	if (!h || !M) { set_error("NULL argument"); return QPC_ERR_ARGS; }
+	if (h->mLrow) return QPC_OK;
 	const int N = h->N, P = h->P, NE = P + 1;
-	if (int rc = wait_stream(h)) return rc;
-	if (!h->mLrow) {
-		std::vector<double> S((size_t)N * NE), Lc((size_t)N * NE);
-		QPC_CUDA(cudaMemcpy(S.data(), h->S, sizeof(double) * S.size(), cudaMemcpyDeviceToHost));
-		int bad = qpc_cholesky_band(N, P, S.data(), Lc.data());
-		if (bad) { set_error("S is not positive definite (pivot %d)", bad); return QPC_ERR_SINGULAR; }
-		std::vector<double> lrow((size_t)N * P, 0.0), lcol((size_t)N * P, 0.0), di(N);
-		for (int r = 0; r < N; ++r) {
-			di[r] = 1.0 / Lc[(size_t)r * NE];
-			for (int j = 1; j <= P; ++j) {
-				if (r - j >= 0) lrow[(size_t)r * P + j - 1] = Lc[(size_t)(r - j) * NE + j];
-				if (r + j < N) lcol[(size_t)r * P + j - 1] = Lc[(size_t)r * NE + j];
-			}
+	std::vector<double> S((size_t)N * NE), Lc((size_t)N * NE);
+	QPC_CUDA(cudaMemcpy(S.data(), h->S, sizeof(double) * S.size(), cudaMemcpyDeviceToHost));
+	int bad = qpc_cholesky_band(N, P, S.data(), Lc.data());
+	if (bad) { set_error("S is not positive definite (pivot %d)", bad); return QPC_ERR_SINGULAR; }
+	std::vector<double> lrow((size_t)N * P, 0.0), lcol((size_t)N * P, 0.0), di(N);
+	for (int r = 0; r < N; ++r) {
+		di[r] = 1.0 / Lc[(size_t)r * NE];
+		for (int j = 1; j <= P; ++j) {
+			if (r - j >= 0) lrow[(size_t)r * P + j - 1] = Lc[(size_t)(r - j) * NE + j];
+			if (r + j < N) lcol[(size_t)r * P + j - 1] = Lc[(size_t)r * NE + j];
 		}
-		int rc;
-		if ((rc = dalloc(&h->mM, (size_t)N * NE)) || (rc = dalloc(&h->mLrow, (size_t)N * P)) || (rc = dalloc(&h->mLcol, (size_t)N * P)) ||
-			(rc = dalloc(&h->mdinv, (size_t)N)))
-			return rc;
-		QPC_CUDA(cudaMemcpy(h->mLrow, lrow.data(), sizeof(double) * lrow.size(), cudaMemcpyHostToDevice));
-		QPC_CUDA(cudaMemcpy(h->mLcol, lcol.data(), sizeof(double) * lcol.size(), cudaMemcpyHostToDevice));
-		QPC_CUDA(cudaMemcpy(h->mdinv, di.data(), sizeof(double) * N, cudaMemcpyHostToDevice));
 	}
-	QPC_CUDA(cudaMemcpyAsync(h->mM, M, sizeof(double) * N * NE, cudaMemcpyHostToDevice, h->stream));
+	int rc;
+	if ((rc = dalloc(&h->mM, (size_t)N * NE)) || (rc = dalloc(&h->mLrow, (size_t)N * P)) || (rc = dalloc(&h->mLcol, (size_t)N * P)) ||
+		(rc = dalloc(&h->mdinv, (size_t)N)))
+		return rc;
+	QPC_CUDA(cudaMemcpy(h->mLrow, lrow.data(), sizeof(double) * lrow.size(), cudaMemcpyHostToDevice));
+	QPC_CUDA(cudaMemcpy(h->mLcol, lcol.data(), sizeof(double) * lcol.size(), cudaMemcpyHostToDevice));
+	QPC_CUDA(cudaMemcpy(h->mdinv, di.data(), sizeof(double) * N, cudaMemcpyHostToDevice));
+	return QPC_OK;
+}
+
+// c <- S^-1 (M c) on the resident state with the band in h->mM, enqueued on st; inside a run
+// (ntt != NULL) only the instances whose step `step - 1` has just finished
+static void mask_enqueue(qpc_lgwz* h, cudaStream_t st, const int64_t* ntt, long step)
+{
+	const int N = h->N, P = h->P;
 	const long total = state_len(h);
-	k_mask_band<<<(unsigned)((total + 255) / 256), 256, 0, h->stream>>>(h->st, h->wk, h->mM, N, P, h->L, total);
+	const long per = (long)h->M * N * h->L;
+	k_mask_band<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(h->st, h->wk, h->mM, N, P, h->L, total, ntt, step, per);
 	LAUNCH(h);
 	const long nchain = 2L * h->B * h->M * h->L;
 	const unsigned nb = (unsigned)((nchain + 63) / 64);
 	switch (P) {
-	case 1: k_mask_solve<1><<<nb, 64, 0, h->stream>>>(h->st, h->wk, h->mLrow, h->mLcol, h->mdinv, N, h->L, nchain); break;
-	case 2: k_mask_solve<2><<<nb, 64, 0, h->stream>>>(h->st, h->wk, h->mLrow, h->mLcol, h->mdinv, N, h->L, nchain); break;
-	case 3: k_mask_solve<3><<<nb, 64, 0, h->stream>>>(h->st, h->wk, h->mLrow, h->mLcol, h->mdinv, N, h->L, nchain); break;
-	case 4: k_mask_solve<4><<<nb, 64, 0, h->stream>>>(h->st, h->wk, h->mLrow, h->mLcol, h->mdinv, N, h->L, nchain); break;
-	case 5: k_mask_solve<5><<<nb, 64, 0, h->stream>>>(h->st, h->wk, h->mLrow, h->mLcol, h->mdinv, N, h->L, nchain); break;
-	case 6: k_mask_solve<6><<<nb, 64, 0, h->stream>>>(h->st, h->wk, h->mLrow, h->mLcol, h->mdinv, N, h->L, nchain); break;
-	case 7: k_mask_solve<7><<<nb, 64, 0, h->stream>>>(h->st, h->wk, h->mLrow, h->mLcol, h->mdinv, N, h->L, nchain); break;
-	default: k_mask_solve<8><<<nb, 64, 0, h->stream>>>(h->st, h->wk, h->mLrow, h->mLcol, h->mdinv, N, h->L, nchain); break;
+	case 1: k_mask_solve<1><<<nb, 64, 0, st>>>(h->st, h->wk, h->mLrow, h->mLcol, h->mdinv, N, h->L, nchain, ntt, step, h->M); break;
+	case 2: k_mask_solve<2><<<nb, 64, 0, st>>>(h->st, h->wk, h->mLrow, h->mLcol, h->mdinv, N, h->L, nchain, ntt, step, h->M); break;
+	case 3: k_mask_solve<3><<<nb, 64, 0, st>>>(h->st, h->wk, h->mLrow, h->mLcol, h->mdinv, N, h->L, nchain, ntt, step, h->M); break;
+	case 4: k_mask_solve<4><<<nb, 64, 0, st>>>(h->st, h->wk, h->mLrow, h->mLcol, h->mdinv, N, h->L, nchain, ntt, step, h->M); break;
+	case 5: k_mask_solve<5><<<nb, 64, 0, st>>>(h->st, h->wk, h->mLrow, h->mLcol, h->mdinv, N, h->L, nchain, ntt, step, h->M); break;
+	case 6: k_mask_solve<6><<<nb, 64, 0, st>>>(h->st, h->wk, h->mLrow, h->mLcol, h->mdinv, N, h->L, nchain, ntt, step, h->M); break;
+	case 7: k_mask_solve<7><<<nb, 64, 0, st>>>(h->st, h->wk, h->mLrow, h->mLcol, h->mdinv, N, h->L, nchain, ntt, step, h->M); break;
+	default: k_mask_solve<8><<<nb, 64, 0, st>>>(h->st, h->wk, h->mLrow, h->mLcol, h->mdinv, N, h->L, nchain, ntt, step, h->M); break;
 	}
 	LAUNCH(h);
+}
+
+int qpc_lgwz_mask(qpc_lgwz* h, const double* M)
+{
+	if (!h || !M) { set_error("NULL argument"); return QPC_ERR_ARGS; }
+	const int N = h->N, NE = h->P + 1;
+	if (int rc = wait_stream(h)) return rc;
+	if (int rc = mask_prepare(h)) return rc;
+	QPC_CUDA(cudaMemcpyAsync(h->mM, M, sizeof(double) * N * NE, cudaMemcpyHostToDevice, h->stream));
+	mask_enqueue(h, h->stream, nullptr, 0);
 	QPC_CUDA(cudaGetLastError());
 	return wait_stream(h);
 }

@@ -126,6 +126,29 @@ __global__ void k_ts_prepare(const double2* __restrict__ c, const int* __restric
 	temq[idx] = s1;
 }
 
+// the same surface values from the length-gauge engine's resident state: r-major [slot][m][r][l],
+// instance inst at slot[inst]; temp/temq in the handle's order [inst][m][l]
+__global__ void k_ts_prepare_eng(const double2* __restrict__ st, const int* __restrict__ slot, const int* __restrict__ ib,
+	const double* __restrict__ b0, const double* __restrict__ br, int nb, int M, int N, int L, long total, double2* __restrict__ temp,
+	double2* __restrict__ temq)
+{
+	const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
+	if (idx >= total) return;
+	const int l = (int)(idx % L);
+	const long im_inst = idx / L;
+	const int m = (int)(im_inst % M);
+	const long inst = im_inst / M;
+	const double2* v = st + ((long)slot[inst] * M + m) * (long)N * L + l;
+	double2 s0 = make_double2(0.0, 0.0), s1 = make_double2(0.0, 0.0);
+	for (int i = 0; i < nb; ++i) {
+		const double2 x = v[(long)ib[i] * L];
+		s0 = cadd(s0, cscale(x, b0[i]));
+		s1 = cadd(s1, cscale(x, br[i]));
+	}
+	temp[idx] = s0;
+	temq[idx] = s1;
+}
+
 // U[inst][kr][ch] = (-i)^(l+1) times the flux term of one channel (accumulate, 627-777):
 //   jdb = -1/2 (j0 temq - jr temp);  z adds -i A_z(t_i+1) j0 (temp(l-1) <l-1|cos|l> + temp(l+1) <l|cos|l+1>);
 //   xy adds the (m -+ 1, l -+ 1) neighbours with ias = i (A_x - i A_y)/2, iap = i (A_x + i A_y)/2.
@@ -198,12 +221,14 @@ __global__ void k_ts_w(const double2* __restrict__ U, const double* __restrict__
 // mode (0.5 k^2 t plus k.(displacement) over the axes the mode carries); clock[inst] = (t, dx, dy, dz)
 __global__ void k_ts_acc(int mode, const double2* __restrict__ W, const double2* __restrict__ e0, const double* __restrict__ kr,
 	const double* __restrict__ coskt, const double* __restrict__ sinkt, const double* __restrict__ coskp, const double* __restrict__ sinkp,
-	const double* __restrict__ clock, double dt, int nkr, int nkt, int nkp, int n_m, long total, double2* __restrict__ work)
+	const double* __restrict__ clock, double dt, int nkr, int nkt, int nkp, int n_m, long total, double2* __restrict__ work,
+	const int* __restrict__ act = nullptr)
 {
 	const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
 	if (idx >= total) return;
 	const int kp = (int)(idx % nkp), kt = (int)((idx / nkp) % nkt);
 	const long ikr = (idx / ((long)nkp * nkt)) % nkr, inst = idx / ((long)nkp * nkt * nkr);
+	if (act && !act[inst]) return;	// this instance takes no accumulate now
 	const double2* w = W + ((inst * nkr + ikr) * nkt + kt) * n_m;
 	double2 s = make_double2(0.0, 0.0);
 	for (int im = 0; im < n_m; ++im) s = cadd(s, cmul(e0[(size_t)kp * n_m + im], w[im]));
@@ -263,6 +288,7 @@ struct qpc_tsurff {
 	double2 *temp = nullptr, *temq = nullptr, *U = nullptr, *W = nullptr, *work = nullptr, *cbuf = nullptr;
 	double *dclock = nullptr, *da1 = nullptr;
 	std::vector<double> clock;	// [inst][4]: time, disx, disy, disz (host, updated in the reference's order)
+	int* dact = nullptr;		// [inst]: takes the accumulate being enqueued (runs of the length-gauge engine)
 };
 
 namespace {
@@ -284,7 +310,7 @@ void ts_free(qpc_tsurff* h)
 	if (!h) return;
 	cudaSetDevice(h->dev);
 	void* ps[] = {h->ib, h->b0, h->br, h->j0, h->jr, h->y0T, h->pm, h->kr, h->coskt, h->sinkt, h->coskp, h->sinkp, h->e0, h->temp, h->temq,
-		h->U, h->W, h->work, h->cbuf, h->dclock, h->da1};
+		h->U, h->W, h->work, h->cbuf, h->dclock, h->da1, h->dact};
 	for (void* p : ps) if (p) cudaFree(p);
 	if (h->ev0) cudaEventDestroy(h->ev0);
 	if (h->ev1) cudaEventDestroy(h->ev1);
@@ -324,16 +350,19 @@ int pcs_run(qpc_pcs* h, int kind, const double2* c, int n_inst, double* out)
 	return QPC_OK;
 }
 
-// one accumulate on device wavefunctions c (host layout)
-int ts_run(qpc_tsurff* h, int mode, const double* a, double dt, const double2* c)
+// one accumulate, enqueued on st without a wait: the surface values come from c (host layout
+// [inst][m][l][r]) or, when eng != NULL, from the length-gauge engine's resident state (eng = the
+// state, slot = the slot of each instance); act (host, may be NULL = every instance) selects the
+// instances that take it.  The clock advances on the host in the reference's order.
+int ts_enqueue(qpc_tsurff* h, int mode, const double* a, double dt, const double2* c, const double2* eng, const int* slot,
+	const int* act, cudaStream_t st)
 {
 	const qpc_dims& d = h->d;
 	const int B = h->B, nch = d.n_m * d.n_l;
-	// the stream idle first (bounded): the copies from host memory below never wait for queued work
-	if (int rc = wait_on(h->st)) return rc;
 	// the clock, as prepare(ax, ay, az, dt) advances it (momentum_1e.hpp:620-626)
 	std::vector<double> a1((size_t)B * 2, 0.0);
 	for (int i = 0; i < B; ++i) {
+		if (act && !act[i]) continue;
 		double* ck = &h->clock[4 * (size_t)i];
 		double ax = 0.0, ay = 0.0, az = 0.0;
 		if (mode == QPC_TSURFF_Z) { az = 0.5 * (a[2 * i] + a[2 * i + 1]); a1[i] = a[2 * i + 1]; }
@@ -343,21 +372,33 @@ int ts_run(qpc_tsurff* h, int mode, const double* a, double dt, const double2* c
 		}
 		ck[0] += dt; ck[1] += ax * dt; ck[2] += ay * dt; ck[3] += az * dt;
 	}
-	QPC_CUDA(cudaMemcpyAsync(h->dclock, h->clock.data(), sizeof(double) * 4 * B, cudaMemcpyHostToDevice, h->st));
-	QPC_CUDA(cudaMemcpyAsync(h->da1, a1.data(), sizeof(double) * 2 * B, cudaMemcpyHostToDevice, h->st));
+	QPC_CUDA(cudaMemcpyAsync(h->dclock, h->clock.data(), sizeof(double) * 4 * B, cudaMemcpyHostToDevice, st));
+	QPC_CUDA(cudaMemcpyAsync(h->da1, a1.data(), sizeof(double) * 2 * B, cudaMemcpyHostToDevice, st));
+	if (act) QPC_CUDA(cudaMemcpyAsync(h->dact, act, sizeof(int) * B, cudaMemcpyHostToDevice, st));
 	const long nsurf = (long)B * nch;
-	QPC_CUDA(cudaEventRecord(h->ev0, h->st));
-	k_ts_prepare<<<(unsigned)((nsurf + 255) / 256), 256, 0, h->st>>>(c, h->ib, h->b0, h->br, h->nb, d.n_r, nsurf, h->temp, h->temq);
+	if (eng) k_ts_prepare_eng<<<(unsigned)((nsurf + 255) / 256), 256, 0, st>>>(eng, slot, h->ib, h->b0, h->br, h->nb, d.n_m, d.n_r, d.n_l, nsurf,
+		h->temp, h->temq);
+	else k_ts_prepare<<<(unsigned)((nsurf + 255) / 256), 256, 0, st>>>(c, h->ib, h->b0, h->br, h->nb, d.n_r, nsurf, h->temp, h->temq);
 	const long nu = (long)B * h->nkr * nch;
-	k_ts_u<<<(unsigned)((nu + 255) / 256), 256, 0, h->st>>>(mode, h->temp, h->temq, h->j0, h->jr, h->pm, h->pm + nch, h->pm + 2 * nch, h->da1,
+	k_ts_u<<<(unsigned)((nu + 255) / 256), 256, 0, st>>>(mode, h->temp, h->temq, h->j0, h->jr, h->pm, h->pm + nch, h->pm + 2 * nch, h->da1,
 		h->nkr, d.n_l, d.n_m, d.m0, h->nl, nu, h->U);
 	const int tw = h->nkt >= 128 ? 128 : 32 * ((h->nkt + 31) / 32);
 	dim3 gw((h->nkt + tw - 1) / tw, h->nkr, B * d.n_m);
-	k_ts_w<<<gw, tw, sizeof(double2) * d.n_l, h->st>>>(h->U, h->y0T, h->nkr, h->nkt, d.n_l, d.n_m, h->W);
+	k_ts_w<<<gw, tw, sizeof(double2) * d.n_l, st>>>(h->U, h->y0T, h->nkr, h->nkt, d.n_l, d.n_m, h->W);
 	const long na = (long)B * h->nkr * h->nkt * h->nkp;
-	k_ts_acc<<<(unsigned)((na + 255) / 256), 256, 0, h->st>>>(mode, h->W, h->e0, h->kr, h->coskt, h->sinkt, h->coskp, h->sinkp, h->dclock, dt,
-		h->nkr, h->nkt, h->nkp, d.n_m, na, h->work);
+	k_ts_acc<<<(unsigned)((na + 255) / 256), 256, 0, st>>>(mode, h->W, h->e0, h->kr, h->coskt, h->sinkt, h->coskp, h->sinkp, h->dclock, dt,
+		h->nkr, h->nkt, h->nkp, d.n_m, na, h->work, act ? h->dact : nullptr);
 	QPC_CUDA(cudaGetLastError());
+	return QPC_OK;
+}
+
+// one accumulate on device wavefunctions c (host layout), waited for
+int ts_run(qpc_tsurff* h, int mode, const double* a, double dt, const double2* c)
+{
+	// the stream idle first (bounded): the copies from host memory never wait for queued work
+	if (int rc = wait_on(h->st)) return rc;
+	QPC_CUDA(cudaEventRecord(h->ev0, h->st));
+	if (int rc = ts_enqueue(h, mode, a, dt, c, nullptr, nullptr, nullptr, h->st)) return rc;
 	QPC_CUDA(cudaEventRecord(h->ev1, h->st));
 	if (int rc = wait_on(h->st)) return rc;
 	QPC_CUDA(cudaEventElapsedTime(&h->last_ms, h->ev0, h->ev1));
@@ -365,6 +406,20 @@ int ts_run(qpc_tsurff* h, int mode, const double* a, double dt, const double2* c
 }
 
 }  // namespace
+
+namespace qpc {
+int tsurff_check_grid(qpc_tsurff* t, const qpc_dims& d)
+{
+	if (d.n_r != t->d.n_r || d.n_l != t->d.n_l || d.n_m != t->d.n_m || d.m0 != t->d.m0 || d.n_inst != t->B) {
+		set_error("grid or batch of the t-SURFF handle differs from the propagator's"); return QPC_ERR_ARGS;
+	}
+	return QPC_OK;
+}
+int tsurff_enqueue_engine(qpc_tsurff* t, const void* st, const int* slot_dev, const double* a, const int* act, double dt, void* stream)
+{
+	return ts_enqueue(t, QPC_TSURFF_Z, a, dt, nullptr, (const double2*)st, slot_dev, act, (cudaStream_t)stream);
+}
+} // namespace qpc
 
 extern "C" {
 
@@ -470,7 +525,7 @@ int qpc_tsurff_create(const qpc_dims* dims, const qpc_kgrid* g, const double* kr
 	if ((rc = dalloc(&h->temp, (size_t)B * nch)) || (rc = dalloc(&h->temq, (size_t)B * nch)) ||
 		(rc = dalloc(&h->U, (size_t)B * g->nkr * nch)) || (rc = dalloc(&h->W, (size_t)B * g->nkr * g->nkt * dims->n_m)) ||
 		(rc = dalloc(&h->work, (size_t)B * g->nkr * g->nkt * g->nkp)) || (rc = dalloc(&h->cbuf, (size_t)B * nch * dims->n_r)) ||
-		(rc = dalloc(&h->dclock, (size_t)4 * B)) || (rc = dalloc(&h->da1, (size_t)2 * B)))
+		(rc = dalloc(&h->dclock, (size_t)4 * B)) || (rc = dalloc(&h->da1, (size_t)2 * B)) || (rc = dalloc(&h->dact, (size_t)B)))
 		return fail(rc);
 	h->clock.assign((size_t)4 * B, 0.0);
 	if (cudaMemset(h->work, 0, sizeof(double2) * (size_t)B * g->nkr * g->nkt * g->nkp) != cudaSuccess) { set_error("cudaMemset failed"); return fail(QPC_ERR_CUDA); }
@@ -508,6 +563,7 @@ int qpc_tsurff_accumulate(qpc_tsurff* h, int32_t mode, const double* a, double d
 	}
 	return ts_run(h, mode, a, dt, c);
 }
+
 
 int qpc_lgwz_tsurff(qpc_lgwz* prop, qpc_tsurff* h, int32_t mode, const double* a, double dt)
 {

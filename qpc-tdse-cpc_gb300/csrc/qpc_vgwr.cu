@@ -283,6 +283,61 @@ __global__ void k_vg_conj_transpose(const double2* __restrict__ R, int n, double
 	T[t] = make_double2(v.x, -v.y);
 }
 
+// In-loop dipole of the elliptical driver (observable_r, spherical/observable/1e.hpp:52-129, recorded
+// before every step at binsrc/sphTDSE.cpp:515-527): rm = sum over the channel pairs (m, l) -> (m+1, l +- 1)
+// of coef * <c_{m,l}| F |c_{m+1,l+-1}> with F = <B|f(r)|B> (f = r) and the sin(theta) e^{-i phi} elements
+// (integrate_sinexp1/2); x = Re rm, y = -Im rm (rp = conj(rm): the +1 elements are the transposed -1
+// ones).  Partial sums per block over a contiguous range of (pair, row) items of one instance, then a
+// fixed-order sum per instance: deterministic.
+constexpr int DIP_THREADS = 256;
+__global__ void __launch_bounds__(DIP_THREADS) k_vg_dip_part(const double2* __restrict__ state, const double* __restrict__ F,
+	const int2* __restrict__ pairs, const double* __restrict__ pcoef, int npairs, int N, int P, int nch,
+	const long long* __restrict__ ntt, const int* __restrict__ perm, long step, double2* __restrict__ part)
+{
+	const int k = blockIdx.y;	// instance slot (sorted order)
+	const int nblk = gridDim.x;
+	double2 acc = make_double2(0.0, 0.0);
+	if (step < ntt[perm[k]]) {
+		const long items = (long)npairs * N;
+		const long per = (items + nblk - 1) / nblk;
+		const long i0 = (long)blockIdx.x * per, i1 = min(items, i0 + per);
+		const double2* x = state + (long)k * nch * N;
+		for (long it = i0 + threadIdx.x; it < i1; it += DIP_THREADS) {
+			const int pr = (int)(it / N), r = (int)(it - (long)pr * N);
+			const int2 ab = pairs[pr];
+			const double2* ca = x + (long)ab.x * N;
+			const double2* cb = x + (long)ab.y * N;
+			double tr = 0.0, ti = 0.0;	// (F c_b)(r)
+			for (int q = 1; q <= P && q <= r; ++q) { const double f = F[(long)(r - q) * (P + 1) + q]; const double2 v = cb[r - q]; tr = fma(f, v.x, tr); ti = fma(f, v.y, ti); }
+			for (int q = 0; q <= P && r + q < N; ++q) { const double f = F[(long)r * (P + 1) + q]; const double2 v = cb[r + q]; tr = fma(f, v.x, tr); ti = fma(f, v.y, ti); }
+			const double2 a = ca[r];
+			const double c = pcoef[pr];
+			// conj(a) * t * c
+			acc.x = fma(c, fma(a.x, tr, a.y * ti), acc.x);
+			acc.y = fma(c, fma(a.x, ti, -(a.y * tr)), acc.y);
+		}
+	}
+	__shared__ double2 sm[DIP_THREADS];
+	sm[threadIdx.x] = acc;
+	__syncthreads();
+	for (int w = DIP_THREADS / 2; w > 0; w >>= 1) {
+		if ((int)threadIdx.x < w) { sm[threadIdx.x].x += sm[threadIdx.x + w].x; sm[threadIdx.x].y += sm[threadIdx.x + w].y; }
+		__syncthreads();
+	}
+	if (threadIdx.x == 0) part[(long)k * nblk + blockIdx.x] = sm[0];
+}
+
+__global__ void k_vg_dip_final(const double2* __restrict__ part, int nblk, int nlive, const long long* __restrict__ ntt,
+	const int* __restrict__ perm, long step, long ldz, double* __restrict__ xs, double* __restrict__ ys)
+{
+	const int k = blockIdx.x * blockDim.x + threadIdx.x;
+	if (k >= nlive || step >= ntt[perm[k]]) return;
+	double2 rm = make_double2(0.0, 0.0);
+	for (int b = 0; b < nblk; ++b) { rm.x += part[(long)k * nblk + b].x; rm.y += part[(long)k * nblk + b].y; }
+	xs[(long)k * ldz + step] = rm.x;
+	ys[(long)k * ldz + step] = -rm.y;
+}
+
 __global__ void k_vg_snorm(const double2* __restrict__ state, const double* __restrict__ S, int N, int P, int nch, double* out)
 {
 	// one block per instance, fixed-order reduction
@@ -346,6 +401,16 @@ struct qpc_vgwr {
 	std::vector<mark> marks;
 	double kms[3] = {0, 0, 0};
 	long kcnt[3] = {0, 0, 0};
+	// in-loop dipole (qpc_vgwr_run_dipole): channel pairs in engine order, their coefficients,
+	// the f(r) band, per-block partials and the recorded lists [B][ldz] in the sorted order
+	int2* dpairs = nullptr;
+	double* dcoef = nullptr;
+	int ndpairs = 0;
+	double* dF = nullptr;
+	double2* dpart = nullptr;
+	double *dxs = nullptr, *dys = nullptr;
+	size_t dcap = 0;
+	int dnblk = 1;
 };
 
 namespace {
@@ -360,6 +425,8 @@ void vg_free(qpc_vgwr* h)
 	if (h->ev0) cudaEventDestroy(h->ev0);
 	if (h->ev1) cudaEventDestroy(h->ev1);
 	for (auto e : h->evpool) cudaEventDestroy(e);
+	void* dp[] = {h->dpairs, h->dcoef, h->dF, h->dpart, h->dxs, h->dys};
+	for (void* p : dp) if (p) cudaFree(p);
 	if (h->st) cudaStreamDestroy(h->st);
 	delete h;
 }
@@ -740,7 +807,44 @@ int qpc_vgwr_dims(qpc_vgwr* h, qpc_dims* dims)
 	return QPC_OK;
 }
 
-int qpc_vgwr_run(qpc_vgwr* h, const double* atab, int64_t ld, const int64_t* nt_field, const int64_t* nt_total)
+// the channel pairs of the dipole observation in the engine's channel order, once per handle
+static int dipole_setup(qpc_vgwr* h)
+{
+	if (h->dpairs) return QPC_OK;
+	const int nl = h->d.n_l, nm = h->d.n_m, m0 = h->d.m0;
+	std::vector<int> chmap(h->nch), inv(h->nch);
+	QPC_CUDA(cudaMemcpy(chmap.data(), h->chmap, sizeof(int) * h->nch, cudaMemcpyDeviceToHost));
+	for (int t = 0; t < h->nch; ++t) inv[chmap[t]] = t;
+	std::vector<int2> pairs;
+	std::vector<double> coef;
+	for (int im = 0; im + 1 < nm; ++im)
+		for (int il = 0; il < nl; ++il) {
+			const long m = m0 + im, l = il + std::labs(m), m2 = m + 1;
+			for (int sgn = 1; sgn >= -1; sgn -= 2) {
+				const long l2 = l + sgn, il2 = l2 - std::labs(m2);
+				if (l2 < 0 || il2 < 0 || il2 >= nl) continue;
+				// integrate_sinexp1 (l + 1) and integrate_sinexp2 (l - 1), spherical/utilities/basisfunc.hpp:243-259
+				const double c = sgn > 0 ? -std::sqrt(double((l + m + 2) * (l + m + 1)) / double((2 * l + 1) * (2 * l + 3)))
+					: std::sqrt(double((l - m) * (l - m - 1)) / double((2 * l + 1) * (2 * l - 1)));
+				pairs.push_back(make_int2(inv[im * nl + il], inv[(im + 1) * nl + (int)il2]));
+				coef.push_back(c);
+			}
+		}
+	h->ndpairs = (int)pairs.size();
+	if (int rc = dalloc(&h->dpairs, std::max<size_t>(pairs.size(), 1))) return rc;
+	if (int rc = dalloc(&h->dcoef, std::max<size_t>(coef.size(), 1))) return rc;
+	if (int rc = dalloc(&h->dF, (size_t)h->N * (h->P + 1))) return rc;
+	h->dnblk = std::max(1, std::min(64, (304 + h->B - 1) / h->B));
+	if (int rc = dalloc(&h->dpart, (size_t)h->B * h->dnblk)) return rc;
+	if (!pairs.empty()) {
+		QPC_CUDA(cudaMemcpy(h->dpairs, pairs.data(), sizeof(int2) * pairs.size(), cudaMemcpyHostToDevice));
+		QPC_CUDA(cudaMemcpy(h->dcoef, coef.data(), sizeof(double) * coef.size(), cudaMemcpyHostToDevice));
+	}
+	return QPC_OK;
+}
+
+static int run_impl(qpc_vgwr* h, const double* atab, int64_t ld, const int64_t* nt_field, const int64_t* nt_total,
+	const double* F, double* xlist, double* ylist, int64_t ldz)
 {
 	if (!h || !nt_field || !nt_total) { set_error("NULL argument"); return QPC_ERR_ARGS; }
 	cudaSetDevice(h->dev);
@@ -754,7 +858,22 @@ int qpc_vgwr_run(qpc_vgwr* h, const double* atab, int64_t ld, const int64_t* nt_
 		smax = std::max<long>(smax, nt_total[k]);
 	}
 	if (anyfield && !atab) { set_error("atab is NULL"); return QPC_ERR_ARGS; }
+	if (F && (!xlist || !ylist || ldz < smax)) { set_error("xlist/ylist NULL or ldz=%lld < max nt_total=%ld", (long long)ldz, smax); return QPC_ERR_ARGS; }
 	if (smax == 0) return QPC_OK;
+	if (F) {
+		if (int rc = dipole_setup(h)) return rc;
+		if ((size_t)B * ldz > h->dcap) {
+			if (h->dxs) cudaFree(h->dxs);
+			if (h->dys) cudaFree(h->dys);
+			h->dxs = h->dys = nullptr; h->dcap = 0;
+			if (int rc = dalloc(&h->dxs, (size_t)B * ldz)) return rc;
+			if (int rc = dalloc(&h->dys, (size_t)B * ldz)) return rc;
+			h->dcap = (size_t)B * ldz;
+		}
+		QPC_CUDA(cudaMemcpyAsync(h->dF, F, sizeof(double) * h->N * (h->P + 1), cudaMemcpyHostToDevice, h->st));
+		QPC_CUDA(cudaMemsetAsync(h->dxs, 0, sizeof(double) * B * ldz, h->st));
+		QPC_CUDA(cudaMemsetAsync(h->dys, 0, sizeof(double) * B * ldz, h->st));
+	}
 	const long cap = anyfield ? (long)B * ld * 2 : 2;
 	if (cap > h->atab_cap) {
 		if (h->atab) cudaFree(h->atab);
@@ -791,6 +910,13 @@ int qpc_vgwr_run(qpc_vgwr* h, const double* atab, int64_t ld, const int64_t* nt_
 			if (s < nt_field[perm[k]]) nlive = k + 1;
 			if (s < nt_total[perm[k]]) nff = k + 1;
 		}
+		if (F && nff > 0 && h->ndpairs > 0) {
+			// the observation before step s (binsrc/sphTDSE.cpp:933-934)
+			k_vg_dip_part<<<dim3((unsigned)h->dnblk, (unsigned)nff), DIP_THREADS, 0, h->st>>>(h->X, h->dF, h->dpairs, h->dcoef,
+				h->ndpairs, h->N, h->P, h->nch, h->ntt, h->perm, s, h->dpart);
+			k_vg_dip_final<<<(unsigned)((nff + 127) / 128), 128, 0, h->st>>>(h->dpart, h->dnblk, nff, h->ntt, h->perm, s, ldz, h->dxs, h->dys);
+			h->launches += 2;
+		}
 		if (int rc = step_dispatch(h, s, anyfield ? ld : 0, nlive, nff)) return rc;
 	}
 	QPC_CUDA(cudaGetLastError());
@@ -799,7 +925,28 @@ int qpc_vgwr_run(qpc_vgwr* h, const double* atab, int64_t ld, const int64_t* nt_
 	if (int rc = wait_on(h->st)) return rc;
 	cudaEventElapsedTime(&h->last_ms, h->ev0, h->ev1);
 	prof_collect(h);
+	if (F) {
+		std::vector<double> xh((size_t)B * ldz), yh((size_t)B * ldz);
+		if (int rc = copy_to_host(xh.data(), h->dxs, sizeof(double) * xh.size(), h->st)) return rc;
+		if (int rc = copy_to_host(yh.data(), h->dys, sizeof(double) * yh.size(), h->st)) return rc;
+		for (int k = 0; k < B; ++k) {
+			std::memcpy(xlist + (size_t)perm[k] * ldz, xh.data() + (size_t)k * ldz, sizeof(double) * ldz);
+			std::memcpy(ylist + (size_t)perm[k] * ldz, yh.data() + (size_t)k * ldz, sizeof(double) * ldz);
+		}
+	}
 	return QPC_OK;
+}
+
+int qpc_vgwr_run(qpc_vgwr* h, const double* atab, int64_t ld, const int64_t* nt_field, const int64_t* nt_total)
+{
+	return run_impl(h, atab, ld, nt_field, nt_total, nullptr, nullptr, nullptr, 0);
+}
+
+int qpc_vgwr_run_dipole(qpc_vgwr* h, const double* atab, int64_t ld, const int64_t* nt_field, const int64_t* nt_total,
+	const double* F, double* xlist, double* ylist, int64_t ldz)
+{
+	if (!F) { set_error("F is NULL"); return QPC_ERR_ARGS; }
+	return run_impl(h, atab, ld, nt_field, nt_total, F, xlist, ylist, ldz);
 }
 
 int qpc_vgwr_propagate(qpc_vgwr* h, const double* ax_ti, const double* ax_tf, const double* ay_ti, const double* ay_tf)

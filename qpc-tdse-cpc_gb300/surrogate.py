@@ -20,12 +20,20 @@ No counterpart in the reference.  Pieces:
                             sin^2 window over the pulse) over w / w0 in [q - 1/2, q + 1/2),
                             log10, floored 8 decades below the maximum (a detector's
                             dynamic range; below it the spectrum is window leakage).
+  * tdse_spectra_elliptical
+                     the fallback for ellipticity != 0 (outside the z-linear training set): the
+                     velocity-gauge elliptical engine (propagator_cn_hc_vgwr) on ELL_GRID from the
+                     ground state, A(t) = A0/sqrt(1 + eps^2) sin^2(pi t/tau) (cos, eps sin)(w t + cep)
+                     with A0 = E0/w; <x>, <y> recorded in the loop (observable_r) and the final state
+                     projected on the field-free eigenstates of every (m, l).  Labels as above, the
+                     harmonic spectrum being S_x + S_y.
   * Surrogate        a 5-member ensemble of 6 -> 4 x 256 GELU -> 384 MLPs trained on the GPU
                      (qpc_mlp: bfloat16 operands, fp32 accumulation, Adam) on standardised
                      targets; query() answers from the ensemble mean when the members agree
                      (mean over outputs of the standard deviation, in standardised units,
-                     below the threshold) and the ellipticity is 0, and runs the TDSE engine
-                     for every other query.
+                     below the threshold) and the ellipticity is 0; every other query is
+                     answered by the TDSE: z-linear queries by the batched length-gauge engine,
+                     elliptical ones always by the velocity-gauge engine.
 """
 import importlib
 import time
@@ -33,6 +41,9 @@ import time
 import numpy as np
 
 C2_GRID = dict(n_r=800, p=6, n_l=41, rmax=400.0, dt=0.05)
+# the elliptical fallback's grid: the scan's radial grid, l <= 20 for |m| <= 20 (the reference's
+# rectangular channel set, 41 x 21 channels)
+ELL_GRID = dict(n_r=800, p=6, l_max=20, rmax=400.0, dt=0.05)
 N_PES, N_HHG = 256, 128
 PES_DECADES, HHG_DECADES = 6.0, 8.0
 
@@ -93,10 +104,14 @@ def _pes_label(proj, energy, u):
     return np.maximum(y, y.max() - PES_DECADES)
 
 
-def _hhg_label(z, dt, w0):
+def _hhg_label(z, dt, w0, z2=None):
+    """harmonic label from the dipole list z (and, for an elliptical pulse, the second component
+    z2: the spectrum is the sum of both components' spectra)"""
     q = _q()
     n = z.size
     om, s = q.hhg_spectrum(z, dt, 0.0, 0.0, dt * (n - 1))
+    if z2 is not None:
+        s = s + q.hhg_spectrum(z2, dt, 0.0, 0.0, dt * (n - 1))[1]
     h = om / w0
     out = np.full(N_HHG, 1e-300)
     for k in range(N_HHG):
@@ -147,6 +162,83 @@ def tdse_spectra(p, grid=C2_GRID, batch=256, setup=None, log=None):
     return pes, hhg, {"wf_steps": wf_steps, "run_s": t_run}
 
 
+def elliptic_vector_potential(intensity, wavelength, cycles, cep, ellipticity, dt):
+    """(nt, A[nt+1][2]): A(t_i) = A0/sqrt(1 + eps^2) sin^2(pi t/tau) (cos, eps sin)(w t + cep) at
+    t_i = i dt, tau = cycles 2 pi / w, A0 = E0 / w, nt = floor(tau / dt)."""
+    q = _q()
+    w0 = q.wavelength_to_w0(wavelength)
+    a0 = q.intensity_to_e0(intensity) / w0
+    tau = cycles * 2 * np.pi / w0
+    nt = int(np.floor(tau / dt + 1e-9))
+    t = dt * np.arange(nt + 1)
+    env = np.sin(np.pi * t / tau) ** 2 / np.sqrt(1.0 + ellipticity ** 2)
+    return nt, np.stack([a0 * env * np.cos(w0 * t + cep), a0 * ellipticity * env * np.sin(w0 * t + cep)], 1)
+
+
+class _EllSetup:
+    """Grid, matrices, ground state (1s in the m = 0, l = 0 channel) and field-free eigenbasis of the
+    elliptical fallback's grid."""
+
+    def __init__(self, grid, emax):
+        q = _q()
+        g = dict(grid)
+        self.g = g
+        L = g["l_max"]
+        self.n_m, self.n_l, self.m0 = 2 * L + 1, L + 1, -L
+        self.lmax = abs(self.m0) + self.n_l - 1
+        kn = q.linear_knots(g["n_r"], g["p"], 0.0, g["rmax"])
+        self.S, self.R, self.Ri, self.D, self.H = q.radial_setup(g["n_r"], g["p"], self.lmax + 1, kn)
+        c, self.e0 = q.ground_state(self.S, self.H, self.n_l, self.n_m, -self.m0, 0, 0, self.m0)
+        self.c0 = c
+        self.n_state, self.basis, self.energies = q.left_eigenbasis(self.S, self.H, self.lmax, emax)
+
+
+def tdse_spectra_elliptical(p, grid=ELL_GRID, batch=16, setup=None, log=None):
+    """PES and HHG labels [n][256], [n][128] for parameter sets p with any ellipticity, from the
+    velocity-gauge elliptical engine in batches of `batch`.  Returns (pes, hhg, info)."""
+    q = _q()
+    n = len(p["intensity"])
+    u = up(p)
+    if setup is None:
+        setup = _EllSetup(grid, emax=max(3.17 * float(u.max()) * 1.5, 1.0))
+    g = setup.g
+    pes = np.zeros((n, N_PES), np.float32)
+    hhg = np.zeros((n, N_HHG), np.float32)
+    wf_steps, t_run = 0, 0.0
+    prop = None
+    for b0 in range(0, n, batch):
+        idx = np.arange(b0, min(n, b0 + batch))
+        B = idx.size
+        tabs = [elliptic_vector_potential(p["intensity"][i], p["wavelength"][i], p["cycles"][i], p["cep"][i], p["ellipticity"][i],
+                                          g["dt"]) for i in idx]
+        nt = np.array([t[0] for t in tabs], np.int64)
+        atab = np.zeros((B, int(nt.max()) + 1, 2))
+        for k, (m, a) in enumerate(tabs):
+            atab[k, :m + 1] = a
+        if prop is None or prop.shape[0] != B:
+            prop = q.propagator_cn_hc_vgwr().initialize(g["n_r"], g["p"], setup.n_l, setup.n_m, setup.m0, setup.S, setup.Ri, setup.D,
+                                                        setup.H, g["dt"], n_inst=B)
+        prop.put(np.broadcast_to(setup.c0, (B,) + setup.c0.shape))
+        t0 = time.time()
+        x, y = prop.run_dipole(atab, nt, nt, setup.R)
+        t_run += time.time() - t0
+        wf_steps += int(nt.sum())
+        c = prop.get()
+        for k, i in enumerate(idx):
+            proj, energy = [], []
+            for im in range(setup.n_m):
+                for il in range(setup.n_l):
+                    l = il + abs(setup.m0 + im)
+                    if setup.n_state[l]:
+                        proj.append(setup.basis[l] @ c[k, im, il])
+                        energy.append(setup.energies[l])
+            pes[i] = _pes_label(np.concatenate(proj), np.concatenate(energy), u[i])
+            hhg[i] = _hhg_label(x[k, :nt[k]], g["dt"], q.wavelength_to_w0(p["wavelength"][i]), y[k, :nt[k]])
+        if log:
+            log("elliptical batch %d-%d: %d wf-steps, %.1f s" % (idx[0], idx[-1], int(nt.sum()), time.time() - t0))
+    return pes, hhg, {"wf_steps": wf_steps, "run_s": t_run}
+
+
 class Surrogate:
     """Ensemble MLP surrogate with TDSE fallback."""
 
@@ -186,17 +278,25 @@ class Surrogate:
         self.threshold = float(np.quantile(dis, quantile))
         return self.threshold
 
-    def query(self, p, threshold=None, setup=None):
+    def query(self, p, threshold=None, setup=None, ell_grid=ELL_GRID, ell_setup=None):
         """Spectra [n][384] for parameter sets p, and the mask of queries the TDSE answered.
-        Out-of-trust queries (disagreement above the threshold, or ellipticity != 0) go to
-        the TDSE engine; a nonzero ellipticity needs an elliptical propagator and raises."""
+        Out-of-trust queries go to the TDSE: those with ellipticity 0 whose disagreement is above
+        the threshold to the batched z-linear engine, and every query with ellipticity != 0 (the
+        network was trained on z-linear pulses only) to the velocity-gauge elliptical engine on
+        ell_grid."""
         thr = self.threshold if threshold is None else threshold
         mean, dis = self.predict(p)
-        fall = (dis > thr) | (p["ellipticity"] != 0)
-        if fall.any():
-            sub = {k: v[fall] for k, v in p.items()}
+        ell = p["ellipticity"] != 0
+        fall = (dis > thr) | ell
+        lin = fall & ~ell
+        if lin.any():
+            sub = {k: v[lin] for k, v in p.items()}
             pes, hhg, _ = tdse_spectra(sub, setup=setup)
-            mean[fall] = np.concatenate([pes, hhg], axis=1)
+            mean[lin] = np.concatenate([pes, hhg], axis=1)
+        if ell.any():
+            sub = {k: v[ell] for k, v in p.items()}
+            pes, hhg, _ = tdse_spectra_elliptical(sub, grid=ell_grid, setup=ell_setup)
+            mean[ell] = np.concatenate([pes, hhg], axis=1)
         return mean, fall
 
 

@@ -183,7 +183,8 @@ def vgwr(d):
         a.tofile(os.path.join(d, "vfield.bin"))
         run(binary, "vgwr", d, RMAX, DT, 1, 0, 0, os.path.join(d, "vinit.bin"), os.path.join(d, "vfield.bin"), nt, nfree)
         out.update(init=c0.reshape(NM, NL, NR), atab=a, coef=load(d, "coef", (NM, NL, NR), True), norm=load(d, "norm"),
-                   zeig=np.stack([load(d, "zeig_" + c) for c in ("x1", "x2", "y1", "y2")]))
+                   zeig=np.stack([load(d, "zeig_" + c) for c in ("x1", "x2", "y1", "y2")]),
+                   xlist=load(d, "xlist"), ylist=load(d, "ylist"))
         np.savez(os.path.join(HERE, tag + ".npz"), **out)
 
 

@@ -1,7 +1,7 @@
 """The spectra surrogate end to end on a small grid: TDSE labels from the batched
 engine, GPU training of the ensemble, and the trust gate that routes queries to the
-TDSE fallback (fallback answers equal the TDSE labels; ellipticity != 0 is refused
-by the z-linear engine)."""
+TDSE fallback (fallback answers equal the TDSE labels); queries with ellipticity != 0
+are always answered by the velocity-gauge elliptical TDSE engine."""
 import importlib
 import time
 
@@ -11,6 +11,7 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 GRID = dict(n_r=200, p=6, n_l=11, rmax=100.0, dt=0.05)
+ELL = dict(n_r=120, p=6, l_max=6, rmax=60.0, dt=0.05)
 
 
 @pytest.fixture(scope="module")
@@ -56,7 +57,30 @@ def test_surrogate_pipeline(sg):
     assert fall.all()
     ref = np.concatenate([pes[:6], hhg[:6]], axis=1)
     assert np.allclose(out, ref, atol=1e-9)
-    # elliptical queries are out of trust and need an elliptical propagator
-    q6["ellipticity"] = np.full(6, 0.5)
-    with pytest.raises(ValueError):
-        s.query(q6, threshold=np.inf, setup=setup)
+    # elliptical queries are out of trust whatever the ensemble says: the velocity-gauge TDSE answers
+    q2 = {k: v[:2].copy() for k, v in p.items()}
+    q2["ellipticity"] = np.array([0.5, -0.3])
+    q2["wavelength"] = np.array([400.0, 450.0])
+    ell_setup = sg._EllSetup(ELL, emax=max(3.17 * float(sg.up(q2).max()) * 1.5, 1.0))
+    out, fall = s.query(q2, threshold=np.inf, setup=setup, ell_grid=ELL, ell_setup=ell_setup)
+    assert fall.all()
+    epes, ehhg, einfo = sg.tdse_spectra_elliptical(q2, grid=ELL, setup=ell_setup)
+    assert einfo["wf_steps"] > 0 and np.all(np.isfinite(epes)) and np.all(np.isfinite(ehhg))
+    assert np.allclose(out, np.concatenate([epes, ehhg], axis=1), atol=1e-9)
+    # an ellipticity-0.5 pulse has a harmonic spectrum unlike the linear one of the same parameters
+    lin = {k: v[:1].copy() for k, v in q2.items()}
+    lin["ellipticity"] = np.zeros(1)
+    lpes, lhhg, _ = sg.tdse_spectra_elliptical(lin, grid=ELL, setup=ell_setup)
+    assert np.linalg.norm(lhhg[0] - ehhg[0]) > 1e-3 * np.linalg.norm(lhhg[0])
+
+
+def test_elliptical_fallback_linear_pulse(sg):
+    """At ellipticity 0 the velocity-gauge fallback sees a pulse along x: finite labels, the
+    dipole response at the driving frequency dominates the harmonic spectrum."""
+    p = {"intensity": np.array([1e14]), "wavelength": np.array([400.0]), "cep": np.array([0.0]),
+         "cycles": np.array([2.0]), "ellipticity": np.zeros(1)}
+    ell_setup = sg._EllSetup(ELL, emax=max(3.17 * float(sg.up(p).max()) * 1.5, 1.0))
+    pes, hhg, info = sg.tdse_spectra_elliptical(p, grid=ELL, setup=ell_setup)
+    assert info["wf_steps"] > 0
+    assert np.all(np.isfinite(pes)) and np.all(np.isfinite(hhg))
+    assert hhg[0, 0] == hhg[0].max()

@@ -83,3 +83,52 @@ def test_mid_grid_matches_oracle(q, voracle):
     ref = voracle.run(og, c0.reshape(1, -1), atab, [nt], [nt + 2])
     assert rel_l2(got, ref[0]) < 1e-12
     assert abs(pr.norm()[0] - n0) < 1e-12 * n0
+
+
+@pytest.mark.parametrize("tag", CASES)
+def test_golden_dipole_list(q, tag):
+    """<x>, <y> before every step (observable_r inside the device loop) against the reference's
+    record of the same run, and the final state unchanged by the observation."""
+    g = golden(tag)
+    n_r, p = int(g["n_r"]), int(g["p"])
+    _, R, _, _, _ = q.radial_setup(n_r, p, 1, q.linear_knots(n_r, p, 0.0, float(g["rmax"])))
+    pr = make(q, g)
+    pr.put(g["init"][None])
+    nt, nf = int(g["nt"]), int(g["nfree"])
+    x, y = pr.run_dipole(g["atab"][None], [nt], [nt + nf], R)
+    scale = np.abs(np.concatenate([g["xlist"], g["ylist"]])).max()
+    assert np.abs(x[0] - g["xlist"]).max() < 1e-12 * scale
+    assert np.abs(y[0] - g["ylist"]).max() < 1e-12 * scale
+    assert rel_l2(pr.get()[0], g["coef"]) < 1e-12
+
+
+def test_dipole_list_uneven_batch(q, voracle):
+    """three instances with their own fields and step counts: each instance's <x>, <y> list against
+    the numpy restatement of observable_r on the oracle's states"""
+    import os
+    import sys
+    from conftest import ROOT
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import observable_oracle as oo
+    g = golden("vgwr_ep6")
+    n_r, p, n_l, n_m, m0 = int(g["n_r"]), int(g["p"]), int(g["n_l"]), int(g["n_m"]), int(g["m0"])
+    _, R, _, _, _ = q.radial_setup(n_r, p, 1, q.linear_knots(n_r, p, 0.0, float(g["rmax"])))
+    B = 3
+    c0 = np.stack([g["init"] * np.exp(0.3j * k) * (1.0 + 0.1 * k) for k in range(B)])
+    nt = 10
+    t = 0.05 * np.arange(nt + 1)
+    atab = np.stack([np.stack([0.2 * (k + 1) * np.sin(0.4 * t + k), 0.1 * np.cos(0.7 * t - k)], 1) for k in range(B)])
+    nf = np.array([10, 4, 0])
+    ntt = np.array([12, 9, 3])
+    pr = make(q, g, B)
+    pr.put(c0)
+    x, y = pr.run_dipole(atab, nf, ntt, R)
+    og = voracle.grid(g["S"], g["RINV"], g["D"], g["H"], float(g["dt"]), n_l, n_m, m0)
+    for k in range(B):
+        c = c0[k].reshape(1, -1)
+        for s in range(ntt[k]):
+            xr, yr = oo.dipole_xy(c[0], R, n_l, n_m, m0)
+            sc = max(abs(xr), abs(yr), 1e-300)
+            assert abs(x[k, s] - xr) < 1e-12 * sc and abs(y[k, s] - yr) < 1e-12 * sc, (k, s)
+            c = voracle.run(og, c, atab[k:k + 1, s:s + 2] if s < nf[k] else atab[k:k + 1, :2], [1 if s < nf[k] else 0], [1])
+        assert np.all(x[k, ntt[k]:] == 0.0)
