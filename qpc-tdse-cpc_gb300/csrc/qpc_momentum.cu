@@ -36,14 +36,16 @@ __device__ __forceinline__ double2 cscale(double2 a, double s) { return make_dou
 // ---------------------------------------------------------------- PCS projector
 // Q[inst][kr][ch] = cps[kr][l] sum_r ijl[l][r][kr] c[inst][ch][r] for a block of PG instances, one
 // channel ch = im n_l + il (l = |m| + il) and 128 consecutive kr; the radial vectors of the
-// block's instances are staged in shared memory chunk by chunk.
+// block's instances are staged in shared memory chunk by chunk.  Grid (instance group, kr tile,
+// channel) with the instance group fastest: the blocks that read one slice of ijl run together,
+// so the slice is read from HBM once and from L2 by the other instance groups.
 constexpr int PG = 8, PCH = 128;
 __global__ void __launch_bounds__(128) k_pcs_proj(const double* __restrict__ ijlT, const double2* __restrict__ cps, const double2* __restrict__ c,
 	double2* __restrict__ Q, int nkr, int n_r, int n_l, int m0, int nch, int nl_tot, int n_inst)
 {
 	__shared__ double2 cs[PG][PCH];
-	const int kr = blockIdx.x * 128 + threadIdx.x;
-	const int ch = blockIdx.y, i0 = blockIdx.z * PG;
+	const int kr = blockIdx.y * 128 + threadIdx.x;
+	const int ch = blockIdx.z, i0 = blockIdx.x * PG;
 	const int im = ch / n_l, il = ch % n_l, l = abs(m0 + im) + il;
 	const double* a = ijlT + (size_t)l * n_r * nkr;
 	double2 acc[PG];
@@ -337,7 +339,7 @@ int pcs_run(qpc_pcs* h, int kind, const double2* c, int n_inst, double* out)
 	long total = kind == QPC_SPEC_LMD ? (long)n_inst * h->nkr * nch
 		: kind == QPC_SPEC_PMD ? (long)n_inst * h->nkr * h->nkt * h->nkp : (long)n_inst * h->nkr * h->nkt;
 	if (int rc = grow(&h->out, &h->cap_o, total)) return rc;
-	dim3 g1((h->nkr + 127) / 128, nch, (n_inst + PG - 1) / PG);
+	dim3 g1((n_inst + PG - 1) / PG, (h->nkr + 127) / 128, nch);
 	QPC_CUDA(cudaEventRecord(h->ev0, h->st));
 	k_pcs_proj<<<g1, 128, 0, h->st>>>(h->ijlT, h->cps, c, h->Q, h->nkr, d.n_r, d.n_l, d.m0, nch, h->nl, n_inst);
 	QPC_CUDA(cudaGetLastError());
@@ -460,7 +462,7 @@ int qpc_pcs_destroy(qpc_pcs* h)
 int qpc_pcs_measure(qpc_pcs* h, int32_t kind, const double* coef, int32_t on_device, int32_t n_inst, double* out)
 {
 	if (!h || !coef || !out || n_inst < 1 || kind < QPC_SPEC_LMD || kind > QPC_SPEC_PAD) { set_error("bad arguments"); return QPC_ERR_ARGS; }
-	if ((n_inst + PG - 1) / PG > 65535) { set_error("n_inst too large"); return QPC_ERR_ARGS; }
+	if ((long)h->d.n_m * h->d.n_l > 65535 || (h->nkr + 127) / 128 > 65535) { set_error("too many channels or momenta for one launch"); return QPC_ERR_ARGS; }
 	QPC_CUDA(cudaSetDevice(h->dev));
 	const double2* c = (const double2*)coef;
 	if (!on_device) {
