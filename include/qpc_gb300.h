@@ -245,6 +245,14 @@ int qpc_lgwz_projection(qpc_lgwz* h, const int32_t* n_state, const double* basis
 int qpc_hhg_spectrum(const double* z, int64_t n, double t0, double dt, double tmin, double tmax, int32_t dipole_type,
 	double* omega, double* spectrum);
 
+/* qpc_hhg_spectrum for n_inst dipole lists at once, on the GPU (the spectrum reduction of a
+ * batched run): list i is z[i*ldz + j], j < n[i], t_j = t0 + j dt, windowed on (tmin[i], tmax[i]);
+ * spectrum[i*kmax + k] = S(w_k) at w_k = 2 pi k / (n[i] dt) for k < kmax (0 for k >= ceil(n[i]/2)).
+ * A direct DFT of the first kmax frequencies (those up to the harmonic orders of interest), not
+ * an FFT of all n/2.  Same arguments and results as qpc_hhg_spectrum to rounding. */
+int qpc_hhg_spectra(int32_t n_inst, const double* z, int64_t ldz, const int64_t* n, double t0, double dt, const double* tmin,
+	const double* tmax, int32_t dipole_type, int64_t kmax, double* spectrum);
+
 /* Photoelectron energy spectrum (|proj|^2 binned over [emin, emax) per unit energy) and
  * ionization yield 1 - sum_{energy < thres} |proj|^2 (ionization_sph::measure_ioyd,
  * spectrum/ionization_1e.hpp:15-51) from n projections (complex) with their energies. */

@@ -28,7 +28,8 @@ POTENTIAL_YUKAWA = 1
 # every symbol include/qpc_gb300.h declares
 EXPORTS = (
     "qpc_last_error", "qpc_version", "qpc_set_wait_limit", "qpc_get_wait_limit", "qpc_fp64_peak",
-    "qpc_lgwz_stream", "qpc_vgwr_set_profiling", "qpc_vgwr_kernel_times", "qpc_vgwr_run_dipole", "qpc_lgwz_run_ex", "qpc_linear_knots", "qpc_radial_setup", "qpc_y10_coupling",
+    "qpc_lgwz_stream", "qpc_vgwr_set_profiling", "qpc_vgwr_kernel_times", "qpc_vgwr_run_dipole", "qpc_lgwz_run_ex",
+    "qpc_hhg_spectra", "qpc_linear_knots", "qpc_radial_setup", "qpc_y10_coupling",
     "qpc_y10_eigen", "qpc_ldlt_csym", "qpc_gen_eigen", "qpc_field_sinen", "qpc_lgwz_create",
     "qpc_lgwz_destroy", "qpc_lgwz_put", "qpc_lgwz_get", "qpc_lgwz_put_device", "qpc_lgwz_get_device",
     "qpc_lgwz_propagate", "qpc_lgwz_propagate_free", "qpc_lgwz_run", "qpc_lgwz_norm", "qpc_lgwz_dipole",
@@ -126,6 +127,7 @@ def load(path=None):
         "qpc_fieldfree_noalloc": (ctypes.c_int, [P, P, P, P, P]),
         "qpc_lgwz_run_dipole": (ctypes.c_int, [P, P, i64, P, P, P, P, i64]),
         "qpc_hhg_spectrum": (ctypes.c_int, [P, i64, d, d, d, d, i32, P, P]),
+        "qpc_hhg_spectra": (ctypes.c_int, [i32, P, i64, P, d, d, P, P, i32, i64, P]),
         "qpc_pes_bin": (ctypes.c_int, [P, P, i64, d, d, i32, d, P, P, P]),
         "qpc_cholesky_band": (ctypes.c_int, [i32, i32, P, P]),
         "qpc_lgwz_run_many": (ctypes.c_int, [i32, P, P, P, P, P, P]),
@@ -341,6 +343,20 @@ def hhg_spectrum(z, dt, t0=0.0, tmin=None, tmax=None, dipole_type=1):
     w, s = np.zeros(nh), np.zeros(nh)
     _check(load().qpc_hhg_spectrum(_ptr(z), n, t0, dt, tmin, tmax, dipole_type, _ptr(w), _ptr(s)))
     return w, s
+
+
+def hhg_spectra(z, n, dt, kmax, t0=0.0, tmin=None, tmax=None, dipole_type=1):
+    """hhg_spectrum of several dipole lists at once on the GPU (qpc_hhg_spectra): z [B][ld], n[B]
+    samples each; returns S [B][kmax] at w_k = 2 pi k / (n[i] dt) (0 past ceil(n[i]/2)).  The window
+    defaults to (t0, t0 + dt (n - 1)) per list."""
+    z = _f64(np.atleast_2d(z))
+    B = z.shape[0]
+    n = np.ascontiguousarray(np.broadcast_to(n, (B,)), dtype=np.int64)
+    tmin = _f64(np.broadcast_to(t0 if tmin is None else tmin, (B,)))
+    tmax = _f64(t0 + dt * (n - 1.0) if tmax is None else np.broadcast_to(tmax, (B,)))
+    out = np.zeros((B, int(kmax)))
+    _check(load().qpc_hhg_spectra(B, _ptr(z), z.shape[1], _ptr(n), t0, dt, _ptr(tmin), _ptr(tmax), dipole_type, int(kmax), _ptr(out)))
+    return out
 
 
 def pes_bin(proj, energy, emin, emax, nbins, thres=0.0):

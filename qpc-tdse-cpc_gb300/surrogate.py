@@ -17,7 +17,8 @@ No counterpart in the reference.  Pieces:
                             discrete continuum broadened beyond its level spacing), times
                             U_p, log10, floored 6 decades below the spectrum's maximum;
                        HHG  harmonic orders 1..128: mean of S(w) (plot_hhs.m restated,
-                            sin^2 window over the pulse) over w / w0 in [q - 1/2, q + 1/2),
+                            sin^2 window over the pulse, evaluated on the GPU by qpc_hhg_spectra)
+                            over w / w0 in [q - 1/2, q + 1/2),
                             log10, floored 8 decades below the maximum (a detector's
                             dynamic range; below it the spectrum is window leakage).
   * tdse_spectra_elliptical
@@ -63,9 +64,30 @@ def draw_params(n, seed):
     }
 
 
-def features(p):
-    return np.stack([np.log10(p["intensity"] / 1e14), (p["wavelength"] - 1200.0) / 800.0, np.sin(p["cep"]), np.cos(p["cep"]),
-                     (p["cycles"] - 6.0) / 4.0, p["ellipticity"]], axis=1).astype(np.float32)
+FEATURES = ("base", "sym")
+IP_H = 0.5   # ionization potential of the scan's atom (hydrogen), a.u.
+
+
+def features(p, kind="base"):
+    """network inputs.  base: log10(I / 1e14 W/cm^2), (lambda - 1200)/800, sin CEP, cos CEP,
+    (cycles - 6)/4, ellipticity.  sym: the CEP enters as sin 2 CEP, cos 2 CEP -- the spectra are
+    exactly invariant under CEP -> CEP + pi (the field changes sign; the atom is symmetric under
+    r -> -r, so |<E|psi>|^2 and |FFT <z>|^2 are unchanged) -- and four derived inputs are added:
+    log of the cutoff order (Ip + 3.17 U_p)/w, log(w/U_p), log(Ip/U_p) and the pulse length in
+    wavelength-cycles, each scaled to about [-1, 1]."""
+    x = np.stack([np.log10(p["intensity"] / 1e14), (p["wavelength"] - 1200.0) / 800.0, np.sin(p["cep"]), np.cos(p["cep"]),
+                  (p["cycles"] - 6.0) / 4.0, p["ellipticity"]], axis=1)
+    if kind == "base":
+        return x.astype(np.float32)
+    if kind != "sym":
+        raise ValueError("unknown feature set %r" % (kind,))
+    x[:, 2], x[:, 3] = np.sin(2 * p["cep"]), np.cos(2 * p["cep"])
+    q = _q()
+    u = up(p)
+    w0 = np.array([q.wavelength_to_w0(l) for l in p["wavelength"]])
+    extra = np.stack([(np.log((IP_H + 3.17 * u) / w0) - 4.0) / 2.0, (np.log(w0 / u) + 2.0) / 3.0, np.log(IP_H / u) / 3.0,
+                      (p["cycles"] * p["wavelength"] / 1000.0 - 8.0) / 6.0], axis=1)
+    return np.concatenate([x, extra], axis=1).astype(np.float32)
 
 
 def up(p):
@@ -104,14 +126,8 @@ def _pes_label(proj, energy, u):
     return np.maximum(y, y.max() - PES_DECADES)
 
 
-def _hhg_label(z, dt, w0, z2=None):
-    """harmonic label from the dipole list z (and, for an elliptical pulse, the second component
-    z2: the spectrum is the sum of both components' spectra)"""
-    q = _q()
-    n = z.size
-    om, s = q.hhg_spectrum(z, dt, 0.0, 0.0, dt * (n - 1))
-    if z2 is not None:
-        s = s + q.hhg_spectrum(z2, dt, 0.0, 0.0, dt * (n - 1))[1]
+def _hhg_bin(om, s, w0):
+    """mean spectrum over harmonic orders q in [k + 1/2, k + 3/2), log10, floored"""
     h = om / w0
     out = np.full(N_HHG, 1e-300)
     for k in range(N_HHG):
@@ -120,6 +136,25 @@ def _hhg_label(z, dt, w0, z2=None):
             out[k] = max(float(s[sel].mean()), 1e-300)
     y = np.log10(out)
     return np.maximum(y, y.max() - HHG_DECADES)
+
+
+def _hhg_labels(z, n, dt, w0, z2=None):
+    """harmonic labels of a batch from its dipole lists z [B][ld] (n[i] samples each; for elliptical
+    pulses z2 holds the second component and the spectrum is the sum of both), with the spectra
+    evaluated on the GPU (qpc_hhg_spectra) up to the frequencies the 128 orders need."""
+    q = _q()
+    n = np.asarray(n, np.int64)
+    w0 = np.asarray(w0, float)
+    kneed = np.minimum((n + 1) // 2, np.floor((N_HHG + 0.5) * w0 * n * dt / (2 * np.pi)).astype(np.int64) + 2)
+    kmax = int(max(1, kneed.max()))
+    s = q.hhg_spectra(z, n, dt, kmax)
+    if z2 is not None:
+        s = s + q.hhg_spectra(z2, n, dt, kmax)
+    out = np.zeros((n.size, N_HHG), np.float32)
+    for i in range(n.size):
+        om = 2 * np.pi / (n[i] * dt) * np.arange(kmax)
+        out[i] = _hhg_bin(om, s[i], w0[i])
+    return out
 
 
 def tdse_spectra(p, grid=C2_GRID, batch=256, setup=None, log=None):
@@ -156,7 +191,7 @@ def tdse_spectra(p, grid=C2_GRID, batch=256, setup=None, log=None):
         proj = prop.projection(setup.n_state, setup.basis).reshape(B, -1)
         for k, i in enumerate(idx):
             pes[i] = _pes_label(proj[k], setup.energy, u[i])
-            hhg[i] = _hhg_label(z[k, :nt[k]], g["dt"], q.wavelength_to_w0(p["wavelength"][i]))
+        hhg[idx] = _hhg_labels(z, nt, g["dt"], [q.wavelength_to_w0(p["wavelength"][i]) for i in idx])
         if log:
             log("batch %d-%d: %d wf-steps, %.1f s" % (idx[0], idx[-1], int(nt.sum()), time.time() - t0))
     return pes, hhg, {"wf_steps": wf_steps, "run_s": t_run}
@@ -233,7 +268,7 @@ def tdse_spectra_elliptical(p, grid=ELL_GRID, batch=16, setup=None, log=None):
                         proj.append(setup.basis[l] @ c[k, im, il])
                         energy.append(setup.energies[l])
             pes[i] = _pes_label(np.concatenate(proj), np.concatenate(energy), u[i])
-            hhg[i] = _hhg_label(x[k, :nt[k]], g["dt"], q.wavelength_to_w0(p["wavelength"][i]), y[k, :nt[k]])
+        hhg[idx] = _hhg_labels(x, nt, g["dt"], [q.wavelength_to_w0(p["wavelength"][i]) for i in idx], y)
         if log:
             log("elliptical batch %d-%d: %d wf-steps, %.1f s" % (idx[0], idx[-1], int(nt.sum()), time.time() - t0))
     return pes, hhg, {"wf_steps": wf_steps, "run_s": t_run}
@@ -242,8 +277,9 @@ def tdse_spectra_elliptical(p, grid=ELL_GRID, batch=16, setup=None, log=None):
 class Surrogate:
     """Ensemble MLP surrogate with TDSE fallback."""
 
-    def __init__(self, n_members=5, n_hidden=256, n_layers=4, seed=0):
+    def __init__(self, n_members=5, n_hidden=256, n_layers=4, seed=0, features="base"):
         self.n_members, self.n_hidden, self.n_layers, self.seed = n_members, n_hidden, n_layers, seed
+        self.features = features
         self.net = None
 
     def fit(self, p, pes, hhg, epochs=400, batch=256, lr=1e-3, stages=1):
@@ -251,7 +287,7 @@ class Surrogate:
         learning rate falls by 3x each (the optimiser state carries over).  Returns the loss
         history [epochs][members]."""
         q = _q()
-        X = features(p)
+        X = features(p, self.features)
         Y = np.concatenate([pes, hhg], axis=1).astype(np.float64)
         self.mu = Y.mean(axis=0)
         self.sd = np.maximum(Y.std(axis=0), 1e-3)
@@ -267,7 +303,7 @@ class Surrogate:
     def predict(self, p):
         """(mean [n][384], disagreement [n]) in label units; disagreement is the mean over
         outputs of the members' standard deviation in standardised units."""
-        y = self.net.predict(features(p)).astype(np.float64)
+        y = self.net.predict(features(p, self.features)).astype(np.float64)
         mean = y.mean(axis=0) * self.sd + self.mu
         dis = y.std(axis=0).mean(axis=1)
         return mean, dis

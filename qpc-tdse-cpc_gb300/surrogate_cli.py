@@ -63,10 +63,10 @@ def fit(a):
     if a.curve:
         for frac in (0.25, 0.5):
             m = int(nfit * frac)
-            s = sg.Surrogate(seed=a.seed)
+            s = sg.Surrogate(seed=a.seed, features=a.features)
             s.fit(sub(0, m), pes[:m], hhg[:m], epochs=int(a.epochs / frac), batch=a.batch, lr=a.lr, stages=a.stages)
             curve.append({"n_fit": m, "holdout_rel_l2_mean": float(_errors(sg, s, te, pes[ntr:], hhg[ntr:])[0].mean())})
-    s = sg.Surrogate(seed=a.seed)
+    s = sg.Surrogate(seed=a.seed, features=a.features)
     t0 = time.time()
     hist = s.fit(tr, pes[:nfit], hhg[:nfit], epochs=a.epochs, batch=a.batch, lr=a.lr, stages=a.stages)
     train_s = time.time() - t0
@@ -87,7 +87,7 @@ def fit(a):
     qps = 65536 / (time.time() - t0)
     rep = {
         "files": [os.path.basename(f) for f in files], "n_fit": int(nfit), "n_validation": int(nval), "n_holdout": int(a.holdout),
-        "epochs": a.epochs, "batch": a.batch, "lr": a.lr, "lr_stages": a.stages, "train_s": train_s,
+        "features": a.features, "epochs": a.epochs, "batch": a.batch, "lr": a.lr, "lr_stages": a.stages, "train_s": train_s,
         "final_train_loss": [float(x) for x in hist[-1]],
         "holdout_rel_l2_mean": float(e_all.mean()), "holdout_rel_l2_median": float(np.median(e_all)),
         "holdout_rel_l2_p90": float(np.quantile(e_all, 0.9)),
@@ -127,6 +127,7 @@ def main():
     f.add_argument("--stages", type=int, default=3)
     f.add_argument("--quantile", type=float, default=0.9)
     f.add_argument("--seed", type=int, default=0)
+    f.add_argument("--features", default="base", choices=sg.FEATURES)
     f.add_argument("--out", default=None)
     a = ap.parse_args()
     generate(a) if a.cmd == "generate" else fit(a)
