@@ -427,11 +427,14 @@ def run_c1(args):
     clocks = clk.summary()
     n1 = prop.norm()[0]
     nch = n_l * n_m
-    ne, no = n_m * ((n_l + 1) // 2), n_m * (n_l // 2)   # il-even / il-odd channels: the transforms are block-diagonal
-    blk = ne * ne + no * no
-    # per step: 6 real transforms (P_x1, P_y2 and the real merged P_y1 P_x2^H, each twice) on
-    # 2 N_r reals and 4 complex ones (the merged P_x2 P_x1^H and P_y2 P_y1^H, each twice)
-    gemm_flops = 6 * 2.0 * (2 * n_r) * blk + 4 * 8.0 * n_r * blk
+    # the transforms act per il-parity block and m-parity set (csrc/qpc_vgwr.cu): a transform is one
+    # real GEMM per set, n_set x n_set on 2 N_r reals per channel; 10 transforms per step
+    sq = 0
+    for par in range(2):
+        for mpar in range(2):
+            n_set = sum(1 for im in range(n_m) if im % 2 == mpar) * sum(1 for il in range(n_l) if il % 2 == par)
+            sq += n_set * n_set
+    gemm_flops = 10 * 2.0 * (2 * n_r) * sq
     tr_ms, tr_n = ktimes["transform"]
     tfl = gemm_flops * K / (tr_ms * 1e-3) / 1e12 if tr_n else None
     peak = fp64_peak()
@@ -445,7 +448,7 @@ def run_c1(args):
                    "n_m": n_m, "m0": m0, "n_l": n_l, "channels": n_m * n_l,
                    "window_start_step": int(s0 + W), "pulse_steps": int(T / dt), "ground_state_energy": float(e_gs)},
         "gpu_launches": int(launches),
-        "roofline": {"bound": "fp64", "kernel": "k_dgemm / k_zgemm (m,l) transforms (CUDA events around each transform)",
+        "roofline": {"bound": "fp64", "kernel": "k_dgemm (m,l) transforms with their pairing steps (CUDA events around each transform)",
                      "achieved": tfl, "peak": peak["tflops"], "peak_source": peak["source"],
                      "unit": "TFLOP/s", "frac": tfl / peak["tflops"] if tfl else None, "flops_per_step": gemm_flops,
                      "transform_ms_per_step": tr_ms / K, "share_of_step": tr_ms / dev_ms},

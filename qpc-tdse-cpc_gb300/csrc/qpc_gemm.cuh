@@ -3,10 +3,10 @@
 //
 //   C[b] = op(A) B[b],  b < batch
 //
-// A is one n x n matrix shared by the batch (row-major, leading dimension n), op(A) is A,
-// A^T (real) or A^H (complex).  B[b] and C[b] are K x X row-major with leading dimension ld
-// and batch stride sb: the state block [channel][r] of one wavefunction, K = M = n
-// channels, X = 2 N_r reals (a real transform of a complex state) or N_r complex values.
+// A is one real n x n matrix shared by the batch (row-major, leading dimension n), op(A) is A
+// or A^T.  B[b] and C[b] are K x X row-major with leading dimension ld and batch stride sb: the
+// rows [channel][2 N_r reals] of one m-parity set of one wavefunction's state (a real transform
+// of a complex state), K = M = n channels.
 //
 // GB300 mapping.  FP64 runs at ~1.2 TFLOP/s (one warp-wide DFMA per ~64 cycles per SM
 // sub-partition), HBM at ~6.7 TB/s: a transform with n ~ 3700 does ~n/2 flops per byte it
@@ -16,8 +16,8 @@
 // K advances in slices of 16 staged in shared memory (double-buffered, one barrier per
 // slice), the next slice's global values prefetched into registers while the current one
 // is consumed.  The tensor-core FP64 path (DMMA) shares the FP64 pipe on this part and
-// measured slower than DFMA, so the product is plain DFMA.  Complex products use the
-// 4-multiplication form; the conjugate transpose is folded into the A-tile load.
+// measured slower than DFMA, so the product is plain DFMA; the transpose is folded into the
+// A-tile load.
 #pragma once
 #include <cuda_runtime.h>
 
@@ -100,95 +100,6 @@ __global__ void __launch_bounds__(THREADS, 2) k_dgemm(const double* __restrict__
 #pragma unroll
 		for (int c = 0; c < 4; ++c) {
 			const int gx = x0 + 4 * tx + c;
-			if (gx < X) Cb[(long)gi * ld + gx] = acc[a][c];
-		}
-	}
-}
-
-// complex: C[b][i][x] = sum_j op(A)(i, j) B[b][j][x]; HERM: op(A)(i, j) = conj(A[j][i])
-// (dynamic shared memory: ZGEMM_SMEM bytes, above the 48 KB static limit)
-constexpr int ZGEMM_SMEM = 2 * 2 * BK * BM * (int)sizeof(double2);
-template <bool HERM>
-__global__ void __launch_bounds__(THREADS, 1) k_zgemm(const double2* __restrict__ A, int n, const double2* __restrict__ B,
-	double2* __restrict__ C, long ld, long sb, int X)
-{
-	extern __shared__ __align__(16) double2 zsm[];
-	double2 (*As)[BK][BM] = reinterpret_cast<double2 (*)[BK][BM]>(zsm);
-	double2 (*Bs)[BK][BX] = reinterpret_cast<double2 (*)[BK][BX]>(zsm + 2 * BK * BM);
-	const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
-	const int i0 = blockIdx.y * BM, x0 = blockIdx.x * BX;
-	const double2* Bb = B + (long)blockIdx.z * sb;
-	double2* Cb = C + (long)blockIdx.z * sb;
-	double2 ra[4], rb[4];
-	auto load = [&](int k0) {
-#pragma unroll
-		for (int q = 0; q < 4; ++q) {
-			const int e = tid + q * THREADS;
-			int ii, kk;
-			if (HERM) { kk = e >> 6; ii = e & 63; }
-			else { ii = e >> 4; kk = e & 15; }
-			const int gi = i0 + ii, gk = k0 + kk;
-			double2 v = make_double2(0.0, 0.0);
-			if (gi < n && gk < n) {
-				v = HERM ? A[(long)gk * n + gi] : A[(long)gi * n + gk];
-				if (HERM) v.y = -v.y;
-			}
-			ra[q] = v;
-			const int bk = e >> 6, bx = e & 63;
-			const int gb = k0 + bk, gx = x0 + bx;
-			rb[q] = (gb < n && gx < X) ? Bb[(long)gb * ld + gx] : make_double2(0.0, 0.0);
-		}
-	};
-	auto store = [&](int buf) {
-#pragma unroll
-		for (int q = 0; q < 4; ++q) {
-			const int e = tid + q * THREADS;
-			int ii, kk;
-			if (HERM) { kk = e >> 6; ii = e & 63; }
-			else { ii = e >> 4; kk = e & 15; }
-			As[buf][kk][ii] = ra[q];
-			Bs[buf][e >> 6][e & 63] = rb[q];
-		}
-	};
-	double2 acc[4][4];
-#pragma unroll
-	for (int a = 0; a < 4; ++a)
-#pragma unroll
-		for (int c = 0; c < 4; ++c) acc[a][c] = make_double2(0.0, 0.0);
-	const int nk = (n + BK - 1) / BK;
-	load(0);
-	store(0);
-	__syncthreads();
-	for (int t = 0; t < nk; ++t) {
-		const int buf = t & 1;
-		if (t + 1 < nk) load((t + 1) * BK);
-#pragma unroll
-		for (int k = 0; k < BK; ++k) {
-			double2 av[4], bv[4];
-#pragma unroll
-			for (int a = 0; a < 4; ++a) av[a] = As[buf][k][ty + 16 * a];
-#pragma unroll
-			for (int c = 0; c < 4; ++c) bv[c] = Bs[buf][k][tx + 16 * c];
-#pragma unroll
-			for (int a = 0; a < 4; ++a)
-#pragma unroll
-				for (int c = 0; c < 4; ++c) {
-					acc[a][c].x = fma(av[a].x, bv[c].x, acc[a][c].x);
-					acc[a][c].y = fma(av[a].x, bv[c].y, acc[a][c].y);
-					acc[a][c].x = fma(-av[a].y, bv[c].y, acc[a][c].x);
-					acc[a][c].y = fma(av[a].y, bv[c].x, acc[a][c].y);
-				}
-		}
-		if (t + 1 < nk) store(buf ^ 1);
-		__syncthreads();
-	}
-#pragma unroll
-	for (int a = 0; a < 4; ++a) {
-		const int gi = i0 + ty + 16 * a;
-		if (gi >= n) continue;
-#pragma unroll
-		for (int c = 0; c < 4; ++c) {
-			const int gx = x0 + tx + 16 * c;
 			if (gx < X) Cb[(long)gi * ld + gx] = acc[a][c];
 		}
 	}

@@ -12,15 +12,15 @@
 // transforms are merged, P_x2 P_x1^H etc. (cn_1e.hpp:884-889).  F is the field-free CN of
 // every (m,l) channel.
 //
-// GB300 mapping: Z couples (m, l) only to (m +- 1, l +- 1), so it keeps il mod 2 and every
-// transform is block-diagonal once the channels are ordered il-even first (the engine's
-// internal order; put/get convert): two dense GEMMs of n_e and n_o = N_ch/2 rows per
-// transform instead of one of N_ch, half the FP64 work.  They run as this library's own
-// FP64 GEMM kernels (qpc_gemm.cuh): real for P_x1, P_y2 and the merged P_y1 P_x2^H, which
-// is real because the two phases cancel (on the state viewed as 2 N_r reals), complex for
-// the merged P_x2 P_x1^H and P_y2 P_y1^H, over the live wavefunctions.  The angular
-// eigensystems come from cuSOLVER syevd (set-up only), block by block, on the real
-// symmetric form of each coupling.  The banded CN of each eigen-channel runs one chain per thread: the LU of
+// GB300 mapping: Z couples (m, l) only to (m +- 1, l +- 1), so it keeps il mod 2 (two parity
+// blocks) and, inside a block, pairs the im-even with the im-odd channels only: Z = [[0, C], [C^T, 0]].
+// The SVD of C gives its eigenvectors in pairs (u, +-v)/sqrt 2, so a transform is two real GEMMs of
+// half the size (U on one m-parity set, V on the other) and an elementwise pairing step, and each
+// backward transform merges with the next forward one into one pair of real GEMMs: per step 10
+// transforms of 2 n^2 N flops each (n = block size) instead of the reference's dense complex
+// N_ch x N_ch products.  The GEMMs are this library's own FP64 kernels (qpc_gemm.cuh), over the
+// live wavefunctions; the SVDs come from cuSOLVER gesvd at set-up.  The banded CN of each
+// eigen-channel runs one chain per thread: the LU of
 // S + ifet O is formed row by row with the previous p rows of U in registers, the forward
 // substitution fused, U rows kept in a scratch buffer for the backward substitution.
 // The field-free step uses the LDL^T factors of S + i dt/2 H_l (qpc_ldlt_csym) as
@@ -221,26 +221,65 @@ __global__ void __launch_bounds__(VG_THREADS) k_vg_ff(double2* __restrict__ stat
 	}
 }
 
-// One il-parity block of a transform: P[k][j] = conj(phi(ch_j)) q_k[j] from the block's
-// eigenvectors (column-major, as syevd returns them), ch_j the block's j-th channel;
-// conj(phi_m) = (-i)^(im) when phase is set, else 1.
-__global__ void k_vg_pblock(const double* __restrict__ Q, int nb, const int* __restrict__ chl, int nl, bool phase,
-	double2* __restrict__ P)
+// out[i][k] = in[i + k n]: a column-major n x n matrix (as cuSOLVER returns it) to row-major
+__global__ void k_vg_transpose(const double* __restrict__ in, int n, double* __restrict__ out)
 {
 	const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
-	if (t >= (long)nb * nb) return;
-	const int k = (int)(t / nb), j = (int)(t - (long)k * nb);
-	const double v = Q[(long)k * nb + j];
-	double2 out = make_double2(v, 0.0);
-	if (phase) {
-		switch ((chl[j] / nl) & 3) {
-		case 1: out = make_double2(0.0, -v); break;
-		case 2: out = make_double2(-v, 0.0); break;
-		case 3: out = make_double2(0.0, v); break;
-		default: break;
+	if (t >= (long)n * n) return;
+	const int i = (int)(t / n), k = (int)(t - (long)i * n);
+	out[t] = in[(long)k * n + i];
+}
+
+// out[i][k] = s[i] in[i][k] (row-major n x n)
+__global__ void k_vg_scale_rows(const double* __restrict__ in, const double* __restrict__ sg, int n, double* __restrict__ out)
+{
+	const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+	if (t >= (long)n * n) return;
+	out[t] = sg[t / n] * in[t];
+}
+
+// The parity blocks of a transform in the engine's order: block b spans channels off[b] ..
+// off[b] + na[b] + ns[b]; its larger m-parity set (na[b] channels) comes first, then the smaller
+// one (ns[b]).  Eigen-channel order in a block: k+ (k < ns), the null channels (ns <= k < na),
+// k- (row na + k, k < ns).
+struct vg_blocks {
+	int off[2], na[2], ns[2];
+};
+
+// The pairing step of a transform, in place on the live instances of X: forward
+// w(k+-) = (gA a_k +- gB b_k)/sqrt 2 and w(null k) = gA a_k after the GEMMs a = U^T z_A, b = V^T z_B;
+// inverse a'_k = conj(gA) (w(k+) + w(k-))/sqrt 2, b'_k = conj(gB) (w(k+) - w(k-))/sqrt 2,
+// a'(null k) = conj(gA) w(null k) before the GEMMs z_A = U a', z_B = V b'.  g = the common phase of a
+// set under the component's phase matrix (1, or -i for the im-odd set).
+__global__ void k_vg_butterfly(double2* __restrict__ X, vg_blocks bk, int N, int nch, int nlive, int inv, double2 g0A, double2 g0B,
+	double2 g1A, double2 g1B)
+{
+	const long per = (long)(bk.na[0] + bk.na[1]) * N;
+	const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+	if (t >= (long)nlive * per) return;
+	const long inst = t / per, e = t - inst * per;
+	const int row = (int)(e / N), r = (int)(e - (long)row * N);
+	const int b = row < bk.na[0] ? 0 : 1;
+	const int k = b ? row - bk.na[0] : row;
+	const double2 gA = b ? g1A : g0A, gB = b ? g1B : g0B;
+	double2* base = X + (inst * nch + bk.off[b]) * (long)N + r;
+	double2* pa = base + (long)k * N;
+	const double h = 0.70710678118654752440;
+	if (k < bk.ns[b]) {
+		double2* pb = base + (long)(bk.na[b] + k) * N;
+		const double2 a = *pa, c = *pb;
+		if (!inv) {
+			const double2 x = cmul(gA, a), y = cmul(gB, c);
+			*pa = make_double2((x.x + y.x) * h, (x.y + y.y) * h);
+			*pb = make_double2((x.x - y.x) * h, (x.y - y.y) * h);
+		} else {
+			const double2 sm = make_double2((a.x + c.x) * h, (a.y + c.y) * h), df = make_double2((a.x - c.x) * h, (a.y - c.y) * h);
+			*pa = cmul(make_double2(gA.x, -gA.y), sm);
+			*pb = cmul(make_double2(gB.x, -gB.y), df);
 		}
+	} else {
+		*pa = inv ? cmul(make_double2(gA.x, -gA.y), *pa) : cmul(gA, *pa);
 	}
-	P[t] = out;
 }
 
 // engine channel order (il-even channels first) <-> the reference's [m][l] order
@@ -255,32 +294,6 @@ __global__ void k_vg_permute(const double2* __restrict__ src, double2* __restric
 	const long o = k * per + (long)chmap[t] * N + r;
 	if (to_engine) dst[i] = src[o];
 	else dst[o] = src[i];
-}
-
-__global__ void k_vg_real_part(const double2* __restrict__ P, long n, double* __restrict__ out)
-{
-	const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
-	if (t < n) out[t] = P[t].x;
-}
-
-// largest |imaginary part| of a complex block (to confirm a merged transform is real)
-__global__ void k_vg_max_imag(const double2* __restrict__ P, long n, unsigned long long* __restrict__ out)
-{
-	const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
-	if (t < n) {
-		const double v = fabs(P[t].y);
-		atomicMax(out, __double_as_longlong(v));	// non-negative doubles order as their bit patterns
-	}
-}
-
-// T[j][k] = conj(R[k][j]) of one n x n block
-__global__ void k_vg_conj_transpose(const double2* __restrict__ R, int n, double2* __restrict__ T)
-{
-	const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
-	if (t >= (long)n * n) return;
-	const int j = (int)(t / n), k = (int)(t - (long)j * n);
-	const double2 v = R[(long)k * n + j];
-	T[t] = make_double2(v.x, -v.y);
 }
 
 // In-loop dipole of the elliptical driver (observable_r, spherical/observable/1e.hpp:52-129, recorded
@@ -375,14 +388,18 @@ struct qpc_vgwr {
 	cudaEvent_t ev0 = nullptr, ev1 = nullptr;
 	double *S = nullptr, *Ri = nullptr, *D = nullptr;
 	double *lam[4] = {nullptr, nullptr, nullptr, nullptr};
-	// transforms, block-diagonal in the engine's channel order (il-even channels first):
-	// block b (b = 0 even, 1 odd) has nb[b] rows at channel offset off[b] and is stored at
-	// element offset boff[b]
-	int nb[2] = {0, 0}, off[2] = {0, 0};
-	long boff[2] = {0, 0}, bsz = 0;
+	// transforms, block-diagonal in the engine's channel order: block b (0: il even, 1: il odd)
+	// spans nb[b] channels from off[b]; inside it the larger m-parity set (na[b] channels, im
+	// parity apar[b]) comes first, then the smaller one (nb[b] - na[b])
+	int nb[2] = {0, 0}, off[2] = {0, 0}, na[2] = {0, 0}, apar[2] = {0, 0};
 	int* chmap = nullptr;                          // engine channel -> reference channel im*n_l+il
-	double *Px1 = nullptr, *Py2 = nullptr, *M23 = nullptr;  // real blocks (M23 = P_y1 P_x2^H is real)
-	double2 *M12 = nullptr, *M34 = nullptr;                 // complex blocks
+	// real transform matrices [mat][block][set] (row-major, set 0: na x na, set 1: ns x ns) in
+	// tmbuf: mat 0 = U~_x1 (forward x1 = its transpose, backward = itself), 1 = U~_y2 (the same for
+	// y2), 2 = M12 = U~_x2^T U~_x1, 3 = M23 = U~_y1^T U~_x2, 4 = M34 = U~_y2^T U~_y1 (merged backward
+	// and forward transforms; their transposes run the mirror half)
+	double* tmbuf = nullptr;
+	double* tm[5][2][2] = {};
+	double2 gam[4][2][2] = {};                    // [component][block][set]: the set's common phase
 	double2 *Lrow = nullptr, *Dinv = nullptr;     // field-free factors
 	double2 *X = nullptr, *W = nullptr, *U = nullptr;
 	double* atab = nullptr;
@@ -419,7 +436,7 @@ void vg_free(qpc_vgwr* h)
 {
 	if (!h) return;
 	cudaSetDevice(h->dev);
-	void* ps[] = {h->S, h->Ri, h->D, h->lam[0], h->lam[1], h->lam[2], h->lam[3], h->Px1, h->Py2, h->M12, h->M23, h->M34, h->Lrow,
+	void* ps[] = {h->S, h->Ri, h->D, h->lam[0], h->lam[1], h->lam[2], h->lam[3], h->tmbuf, h->Lrow,
 		h->Dinv, h->X, h->W, h->U, h->atab, h->ntt, h->perm, h->nrm, h->chmap};
 	for (void* p : ps) if (p) cudaFree(p);
 	if (h->ev0) cudaEventDestroy(h->ev0);
@@ -466,34 +483,47 @@ void prof_collect(qpc_vgwr* h)
 	h->evused = 0;
 }
 
-// out[b] = op(Pm) in[b] for b < nb, state blocks [nch][N] complex, one GEMM launch per parity
-// block.  real: Pm real [n][n] per block on the state viewed as [n][2N] reals; herm: apply
-// Pm^T (real) or Pm^H (complex).
-int transform(qpc_vgwr* h, const void* Pm, bool real, bool herm, const double2* in, double2* out, int nb)
+// the GEMM part of a transform: out rows of every set = op(matrix mat of the set) times the in rows
+// of the same set, live instances, on the state viewed as [channel][2 N] reals (the matrices are
+// real); trans: apply the transposes
+void gemm_sets(qpc_vgwr* h, int mat, bool trans, const double2* in, double2* out, int nlive)
 {
-	const int nch = h->nch, N = h->N;
-	const long sstate = (long)nch * N;
-	cudaEvent_t pa = prof_begin(h);
-	for (int bl = 0; bl < 2; ++bl) {
-		const int n = h->nb[bl];
-		if (!n) continue;
-		const long o = (long)h->off[bl] * N;
-		if (real) {
-			const dim3 g = gemm::grid_for(2 * N, n, nb);
-			const double* A = (const double*)Pm + h->boff[bl];
-			if (herm) gemm::k_dgemm<true><<<g, gemm::THREADS, 0, h->st>>>(A, n, (const double*)(in + o), (double*)(out + o), 2L * N, 2 * sstate, 2 * N);
+	const int N = h->N;
+	const long sstate = (long)h->nch * N;
+	for (int b = 0; b < 2; ++b)
+		for (int st = 0; st < 2; ++st) {
+			const int n = st ? h->nb[b] - h->na[b] : h->na[b];
+			if (!n) continue;
+			const long o = (long)(h->off[b] + (st ? h->na[b] : 0)) * N;
+			const dim3 g = gemm::grid_for(2 * N, n, nlive);
+			const double* A = h->tm[mat][b][st];
+			if (trans) gemm::k_dgemm<true><<<g, gemm::THREADS, 0, h->st>>>(A, n, (const double*)(in + o), (double*)(out + o), 2L * N, 2 * sstate, 2 * N);
 			else gemm::k_dgemm<false><<<g, gemm::THREADS, 0, h->st>>>(A, n, (const double*)(in + o), (double*)(out + o), 2L * N, 2 * sstate, 2 * N);
-		} else {
-			const dim3 g = gemm::grid_for(N, n, nb);
-			const double2* A = (const double2*)Pm + h->boff[bl];
-			if (herm) gemm::k_zgemm<true><<<g, gemm::THREADS, gemm::ZGEMM_SMEM, h->st>>>(A, n, in + o, out + o, (long)N, sstate, N);
-			else gemm::k_zgemm<false><<<g, gemm::THREADS, gemm::ZGEMM_SMEM, h->st>>>(A, n, in + o, out + o, (long)N, sstate, N);
+			++h->launches;
 		}
-		++h->launches;
-	}
+}
+
+// the pairing step of component c's transform (forward or inverse) on X
+void butterfly(qpc_vgwr* h, double2* X, int c, bool inv, int nlive)
+{
+	vg_blocks bk;
+	for (int b = 0; b < 2; ++b) { bk.off[b] = h->off[b]; bk.na[b] = h->na[b]; bk.ns[b] = h->nb[b] - h->na[b]; }
+	const long total = (long)nlive * (h->na[0] + h->na[1]) * h->N;
+	if (total <= 0) return;
+	k_vg_butterfly<<<(unsigned)((total + 255) / 256), 256, 0, h->st>>>(X, bk, h->N, h->nch, nlive, inv ? 1 : 0, h->gam[c][0][0],
+		h->gam[c][0][1], h->gam[c][1][0], h->gam[c][1][1]);
+	++h->launches;
+}
+
+// one transform between the l basis and the eigen-channels of components: forward to c1 (c0 < 0),
+// backward from c0 (c1 < 0), or merged backward from c0 and forward to c1 with matrix mat
+void transform(qpc_vgwr* h, int c0, int c1, int mat, bool trans, double2* in, double2* out, int nlive)
+{
+	cudaEvent_t pa = prof_begin(h);
+	if (c0 >= 0) butterfly(h, in, c0, true, nlive);
+	gemm_sets(h, mat, trans, in, out, nlive);
+	if (c1 >= 0) butterfly(h, out, c1, false, nlive);
 	prof_end(h, 0, pa);
-	QPC_CUDA(cudaGetLastError());
-	return QPC_OK;
 }
 
 template <int P>
@@ -514,16 +544,18 @@ int step_t(qpc_vgwr* h, long s, long ld, int nlive, int nff)
 		prof_end(h, 1, pa);
 		++h->launches;
 	};
+	// components x1 (0), x2 (1), y1 (2), y2 (3); each backward transform is merged with the next
+	// forward one (matrices M12, M23, M34, transposed in the mirror half)
 	if (nb > 0) {
-		if (int rc = transform(h, h->Px1, true, false, h->X, h->W, nb)) return rc;
+		transform(h, -1, 0, 0, true, h->X, h->W, nb);
 		cn(h->W, 0, 0);
-		if (int rc = transform(h, h->M12, false, false, h->W, h->X, nb)) return rc;
+		transform(h, 0, 1, 2, false, h->W, h->X, nb);
 		cn(h->X, 1, 0);
-		if (int rc = transform(h, h->M23, true, false, h->X, h->W, nb)) return rc;
+		transform(h, 1, 2, 3, false, h->X, h->W, nb);
 		cn(h->W, 2, 0);
-		if (int rc = transform(h, h->M34, false, false, h->W, h->X, nb)) return rc;
+		transform(h, 2, 3, 4, false, h->W, h->X, nb);
 		cn(h->X, 3, 0);
-		if (int rc = transform(h, h->Py2, true, true, h->X, h->W, nb)) return rc;
+		transform(h, 3, -1, 1, false, h->X, h->W, nb);
 		// W holds the live instances' states; the others are still in X
 		QPC_CUDA(cudaMemcpyAsync(h->X, h->W, sizeof(double2) * (size_t)nb * h->nch * h->N, cudaMemcpyDeviceToDevice, h->st));
 	}
@@ -536,17 +568,18 @@ int step_t(qpc_vgwr* h, long s, long ld, int nlive, int nff)
 		++h->launches;
 	}
 	if (nb > 0) {
-		if (int rc = transform(h, h->Py2, true, false, h->X, h->W, nb)) return rc;
+		transform(h, -1, 3, 1, true, h->X, h->W, nb);
 		cn(h->W, 3, 1);
-		if (int rc = transform(h, h->M34, false, true, h->W, h->X, nb)) return rc;
+		transform(h, 3, 2, 4, true, h->W, h->X, nb);
 		cn(h->X, 2, 1);
-		if (int rc = transform(h, h->M23, true, true, h->X, h->W, nb)) return rc;
+		transform(h, 2, 1, 3, true, h->X, h->W, nb);
 		cn(h->W, 1, 1);
-		if (int rc = transform(h, h->M12, false, true, h->W, h->X, nb)) return rc;
+		transform(h, 1, 0, 2, true, h->W, h->X, nb);
 		cn(h->X, 0, 1);
-		if (int rc = transform(h, h->Px1, true, true, h->X, h->W, nb)) return rc;
+		transform(h, 0, -1, 0, false, h->X, h->W, nb);
 		QPC_CUDA(cudaMemcpyAsync(h->X, h->W, sizeof(double2) * (size_t)nb * h->nch * h->N, cudaMemcpyDeviceToDevice, h->st));
 	}
+	QPC_CUDA(cudaGetLastError());
 	return QPC_OK;
 }
 
@@ -576,74 +609,132 @@ int permute(qpc_vgwr* h, const std::vector<int>& perm, bool inverse)
 	return QPC_OK;
 }
 
-// Angular eigensystems on the device, block by block (cuSOLVER syevd): Z couples (m, l) to
-// (m +- 1, l +- 1) only, so it keeps il mod 2 and every transform is block-diagonal in the
-// engine's channel order.  With D = diag(i^(m - m0)) the -i couplings are real symmetric,
-// Z_R(y1) = -Z_R(x1) and Z_R(y2) = -Z_R(x2): two problems per block give all four couplings
-// (lam_y = -lam_x, same real eigenvectors).  Writes lam[c] in the engine's eigen order (even
-// block's ascending eigenvalues, then the odd block's) and the complex blocks dP[c].
-int device_angular(qpc_vgwr* h, std::vector<double> lam[4], double2* dP[4])
+// Angular eigensystems on the device, block by block.  Z_c couples (m, l) only to (m +- 1, l +- 1):
+// it keeps il mod 2 (the parity blocks) and flips the parity of im, so inside a block it pairs the
+// im-even with the im-odd channels only: Z = [[0, C], [C^T, 0]] with C = Z[A, B] (A the larger
+// m-parity set).  From the SVD C = U Sigma V^T its eigenvectors are (u_k, +-v_k)/sqrt 2 with
+// eigenvalues +-sigma_k, and (u_k, 0) with eigenvalue 0 for the |A| - |B| left singular vectors
+// beyond; so every transform is two real GEMMs of half the size (U on the A rows, V on the B rows)
+// and a pairing step.  With D = diag(i^(m - m0)) the -i couplings are real symmetric,
+// Z_R(y1) = -Z_R(x1) and Z_R(y2) = -Z_R(x2): one SVD per block and coupling type (Y11 for x1/y1,
+// Q11 for x2/y2, cuSOLVER gesvd, set-up only) gives all four couplings (lam_y = -lam_x).  The
+// phase (-i)^im that x2 and y1 carry is (-1)^(im/2) on im-even channels and -i (-1)^((im-1)/2) on
+// im-odd ones: the signs go into the rows of U~ = diag(s) U, the common -i into the pairing step.
+// Writes lam[c] in the engine's eigen order and the matrices tm.
+int device_transforms(qpc_vgwr* h, std::vector<int>& chmap, std::vector<double> lam[4])
 {
 	const int nl = h->d.n_l, nm = h->d.n_m, N = h->nch;
 	cusolverDnHandle_t sol = nullptr;
 	if (cusolverDnCreate(&sol) != CUSOLVER_STATUS_SUCCESS) { set_error("cusolverDnCreate failed"); return QPC_ERR_CUDA; }
 	struct guard { cusolverDnHandle_t s; std::vector<void*> p; ~guard() { for (void* q : p) if (q) cudaFree(q); if (s) cusolverDnDestroy(s); } } G{sol, {}};
 	if (cusolverDnSetStream(sol, h->st) != CUSOLVER_STATUS_SUCCESS) { set_error("cusolverDnSetStream failed"); return QPC_ERR_CUDA; }
-	std::vector<int> chl[2];
-	for (int ch = 0; ch < N; ++ch) chl[(ch % nl) % 2].push_back(ch);
-	int* d_info = nullptr;
+	auto scratch = [&](double** p, size_t n) -> int { int rc = dalloc(p, n); G.p.push_back(*p); return rc; };
 	int rc;
+	int* d_info = nullptr;
 	if ((rc = dalloc(&d_info, 1))) return rc;
 	G.p.push_back(d_info);
 	for (int c = 0; c < 4; ++c) lam[c].assign(N, 0.0);
+	// matrix storage: 5 matrices per block and set
+	size_t tot = 0;
+	for (int b = 0; b < 2; ++b) {
+		const size_t a = (size_t)h->na[b], sn = (size_t)(h->nb[b] - h->na[b]);
+		tot += 5 * (a * a + sn * sn);
+	}
+	if ((rc = dalloc(&h->tmbuf, std::max<size_t>(tot, 1)))) return rc;
+	{
+		size_t o = 0;
+		for (int m = 0; m < 5; ++m)
+			for (int b = 0; b < 2; ++b)
+				for (int st = 0; st < 2; ++st) {
+					const size_t n = st ? (size_t)(h->nb[b] - h->na[b]) : (size_t)h->na[b];
+					h->tm[m][b][st] = h->tmbuf + o;
+					o += n * n;
+				}
+	}
+	// the base singular vectors U (set 0) / V (set 1) of Y11 (base 0) and Q11 (base 1), row-major
+	// [i][k] = k-th singular vector's entry i, in scratch: ub[base][block][set]
+	double* ub[2][2][2] = {};
 	std::vector<double> Zr((size_t)N * N);
-	for (int base = 0; base < 2; ++base) {	// 0: Y11 (x1, y1), 1: Q11 (x2, y2)
+	for (int base = 0; base < 2; ++base) {
 		vgwr_real_coupling(nl, nm, h->d.m0, base, Zr.data());
 		const int cx = base == 0 ? 0 : 1, cy = base == 0 ? 2 : 3;
-		for (int bl = 0; bl < 2; ++bl) {
-			const int nb = (int)chl[bl].size();
-			if (!nb) continue;
-			std::vector<double> blk((size_t)nb * nb);
-			for (int a = 0; a < nb; ++a)
-				for (int b = 0; b < nb; ++b) blk[(size_t)a * nb + b] = Zr[(size_t)chl[bl][a] * N + chl[bl][b]];
-			double *A = nullptr, *W = nullptr, *work = nullptr;
-			int* dch = nullptr;
-			if ((rc = dalloc(&A, (size_t)nb * nb)) || (rc = dalloc(&W, (size_t)nb)) || (rc = dalloc(&dch, (size_t)nb))) {
-				G.p.push_back(A); G.p.push_back(W); G.p.push_back(dch);
+		for (int b = 0; b < 2; ++b) {
+			const int na = h->na[b], ns = h->nb[b] - h->na[b], o = h->off[b];
+			if ((rc = scratch(&ub[base][b][0], (size_t)std::max(na * na, 1))) || (rc = scratch(&ub[base][b][1], (size_t)std::max(ns * ns, 1))))
 				return rc;
+			if (!na) continue;
+			if (!ns) {	// no partner set: Z is zero on the block, the transform is the identity
+				std::vector<double> I((size_t)na * na, 0.0);
+				for (int i = 0; i < na; ++i) I[(size_t)i * na + i] = 1.0;
+				QPC_CUDA(cudaMemcpy(ub[base][b][0], I.data(), sizeof(double) * I.size(), cudaMemcpyHostToDevice));
+				continue;
 			}
-			G.p.push_back(A); G.p.push_back(W); G.p.push_back(dch);
-			QPC_CUDA(cudaMemcpy(A, blk.data(), sizeof(double) * blk.size(), cudaMemcpyHostToDevice));
-			QPC_CUDA(cudaMemcpy(dch, chl[bl].data(), sizeof(int) * nb, cudaMemcpyHostToDevice));
+			std::vector<double> Ccm((size_t)na * ns);	// column-major na x ns
+			for (int j = 0; j < ns; ++j)
+				for (int i = 0; i < na; ++i) Ccm[(size_t)j * na + i] = Zr[(size_t)chmap[o + i] * N + chmap[o + na + j]];
+			double *A = nullptr, *Sg = nullptr, *Ucm = nullptr, *work = nullptr, *rwork = nullptr;
+			if ((rc = scratch(&A, Ccm.size())) || (rc = scratch(&Sg, (size_t)ns)) || (rc = scratch(&Ucm, (size_t)na * na)) ||
+				(rc = scratch(&rwork, (size_t)ns)))
+				return rc;
+			QPC_CUDA(cudaMemcpy(A, Ccm.data(), sizeof(double) * Ccm.size(), cudaMemcpyHostToDevice));
 			int lwork = 0;
-			if (cusolverDnDsyevd_bufferSize(sol, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, nb, A, nb, W, &lwork) != CUSOLVER_STATUS_SUCCESS) {
-				set_error("syevd buffer size failed"); return QPC_ERR_CUDA;
+			if (cusolverDnDgesvd_bufferSize(sol, na, ns, &lwork) != CUSOLVER_STATUS_SUCCESS) { set_error("gesvd buffer size failed"); return QPC_ERR_CUDA; }
+			if ((rc = scratch(&work, (size_t)std::max(lwork, 1)))) return rc;
+			// VT (ns x ns, column-major) is V row-major: VT[k + j ns] = v_k[j] = V_rm[j][k]
+			if (cusolverDnDgesvd(sol, 'A', 'A', na, ns, A, na, Sg, Ucm, na, ub[base][b][1], ns, work, lwork, rwork, d_info) != CUSOLVER_STATUS_SUCCESS) {
+				set_error("gesvd failed"); return QPC_ERR_CUDA;
 			}
-			if ((rc = dalloc(&work, (size_t)std::max(lwork, 1)))) return rc;
-			G.p.push_back(work);
-			if (cusolverDnDsyevd(sol, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, nb, A, nb, W, work, lwork, d_info) != CUSOLVER_STATUS_SUCCESS) {
-				set_error("syevd failed"); return QPC_ERR_CUDA;
-			}
-			// syevd runs on the handle's stream, which does not synchronise with the legacy
-			// stream the copies below use
+			k_vg_transpose<<<(unsigned)(((long)na * na + 255) / 256), 256, 0, h->st>>>(Ucm, na, ub[base][b][0]);
+			QPC_CUDA(cudaGetLastError());
 			QPC_CUDA(cudaStreamSynchronize(h->st));
 			int info = 0;
 			QPC_CUDA(cudaMemcpy(&info, d_info, sizeof(int), cudaMemcpyDeviceToHost));
-			if (info) { set_error("syevd info %d", info); return QPC_ERR_NUMERIC; }
-			std::vector<double> w(nb);
-			QPC_CUDA(cudaMemcpy(w.data(), W, sizeof(double) * nb, cudaMemcpyDeviceToHost));
-			for (int k = 0; k < nb; ++k) {
-				lam[cx][h->off[bl] + k] = w[k];
-				lam[cy][h->off[bl] + k] = -w[k];
+			if (info) { set_error("gesvd info %d", info); return QPC_ERR_NUMERIC; }
+			std::vector<double> sg(ns);
+			QPC_CUDA(cudaMemcpy(sg.data(), Sg, sizeof(double) * ns, cudaMemcpyDeviceToHost));
+			for (int k = 0; k < ns; ++k) {
+				lam[cx][o + k] = sg[k];
+				lam[cx][o + na + k] = -sg[k];
+				lam[cy][o + k] = -sg[k];
+				lam[cy][o + na + k] = sg[k];
 			}
-			// phases: x1 none, y1 (-i)^im; x2 (-i)^im, y2 none
-			const unsigned nbk = (unsigned)(((long)nb * nb + 255) / 256);
-			k_vg_pblock<<<nbk, 256, 0, h->st>>>(A, nb, dch, nl, base == 1, dP[cx] + h->boff[bl]);
-			k_vg_pblock<<<nbk, 256, 0, h->st>>>(A, nb, dch, nl, base == 0, dP[cy] + h->boff[bl]);
+		}
+	}
+	// U~_c = diag(s) U for the components with the phase (x2, y1), U itself for x1, y2; merged
+	// M12 = U~_x2^T U~_x1, M23 = U~_y1^T U~_x2, M34 = U~_y2^T U~_y1 per block and set
+	for (int b = 0; b < 2; ++b)
+		for (int st = 0; st < 2; ++st) {
+			const int n = st ? h->nb[b] - h->na[b] : h->na[b];
+			if (!n) continue;
+			const int o = h->off[b] + (st ? h->na[b] : 0);
+			std::vector<double> sgn(n);
+			for (int i = 0; i < n; ++i) {
+				const int im = chmap[o + i] / nl;
+				sgn[i] = ((im & 1) ? ((im - 1) / 2) & 1 : (im / 2) & 1) ? -1.0 : 1.0;
+			}
+			double *ds = nullptr, *ux2 = nullptr, *uy1 = nullptr;
+			if ((rc = scratch(&ds, (size_t)n)) || (rc = scratch(&ux2, (size_t)n * n)) || (rc = scratch(&uy1, (size_t)n * n))) return rc;
+			QPC_CUDA(cudaMemcpy(ds, sgn.data(), sizeof(double) * n, cudaMemcpyHostToDevice));
+			const unsigned g = (unsigned)(((long)n * n + 255) / 256);
+			QPC_CUDA(cudaMemcpyAsync(h->tm[0][b][st], ub[0][b][st], sizeof(double) * n * n, cudaMemcpyDeviceToDevice, h->st));
+			QPC_CUDA(cudaMemcpyAsync(h->tm[1][b][st], ub[1][b][st], sizeof(double) * n * n, cudaMemcpyDeviceToDevice, h->st));
+			k_vg_scale_rows<<<g, 256, 0, h->st>>>(ub[1][b][st], ds, n, ux2);
+			k_vg_scale_rows<<<g, 256, 0, h->st>>>(ub[0][b][st], ds, n, uy1);
+			const dim3 gg = gemm::grid_for(n, n, 1);
+			gemm::k_dgemm<true><<<gg, gemm::THREADS, 0, h->st>>>(ux2, n, h->tm[0][b][st], h->tm[2][b][st], (long)n, 0L, n);
+			gemm::k_dgemm<true><<<gg, gemm::THREADS, 0, h->st>>>(uy1, n, ux2, h->tm[3][b][st], (long)n, 0L, n);
+			gemm::k_dgemm<true><<<gg, gemm::THREADS, 0, h->st>>>(h->tm[1][b][st], n, uy1, h->tm[4][b][st], (long)n, 0L, n);
 			QPC_CUDA(cudaGetLastError());
 			QPC_CUDA(cudaStreamSynchronize(h->st));
 		}
-	}
+	// the common phase of each set under each component: -i for an im-odd set of x2 and y1, else 1
+	for (int c = 0; c < 4; ++c)
+		for (int b = 0; b < 2; ++b)
+			for (int st = 0; st < 2; ++st) {
+				const int par = st ? 1 - h->apar[b] : h->apar[b];
+				const bool phase = c == 1 || c == 2;
+				h->gam[c][b][st] = (phase && par == 1) ? make_double2(0.0, -1.0) : make_double2(1.0, 0.0);
+			}
 	return QPC_OK;
 }
 
@@ -682,76 +773,35 @@ int qpc_vgwr_create(const qpc_dims* dims, double dt, const double* S, const doub
 	if ((cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking)) != cudaSuccess) { set_error("cudaStreamCreateWithFlags failed"); return fail(QPC_ERR_CUDA); }
 	if ((cudaEventCreate(&h->ev0)) != cudaSuccess) { set_error("cudaEventCreate failed"); return fail(QPC_ERR_CUDA); }
 	if ((cudaEventCreate(&h->ev1)) != cudaSuccess) { set_error("cudaEventCreate failed"); return fail(QPC_ERR_CUDA); }
-	for (auto f : {(const void*)gemm::k_zgemm<true>, (const void*)gemm::k_zgemm<false>})
-		if (cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, gemm::ZGEMM_SMEM) != cudaSuccess) {
-			set_error("cudaFuncSetAttribute(ZGEMM shared memory) failed"); return fail(QPC_ERR_CUDA);
-		}
 	const size_t nst = (size_t)h->B * nch * N;
-	// engine channel order: il-even channels first, then il-odd
+	// engine channel order: the il-even block, then the il-odd one; inside a block the larger
+	// im-parity set first (the im-even one on a tie)
 	std::vector<int> chmap;
 	for (int par = 0; par < 2; ++par) {
 		h->off[par] = (int)chmap.size();
-		for (int ch = 0; ch < nch; ++ch) if ((ch % d.n_l) % 2 == par) chmap.push_back(ch);
+		int cnt[2] = {0, 0};
+		for (int ch = 0; ch < nch; ++ch) if ((ch % d.n_l) % 2 == par) ++cnt[(ch / d.n_l) & 1];
+		h->apar[par] = cnt[1] > cnt[0] ? 1 : 0;
+		for (int set = 0; set < 2; ++set) {
+			const int ip = set ? 1 - h->apar[par] : h->apar[par];
+			for (int ch = 0; ch < nch; ++ch)
+				if ((ch % d.n_l) % 2 == par && ((ch / d.n_l) & 1) == ip) chmap.push_back(ch);
+		}
 		h->nb[par] = (int)chmap.size() - h->off[par];
+		h->na[par] = cnt[h->apar[par]];
 	}
-	h->boff[0] = 0;
-	h->boff[1] = (long)h->nb[0] * h->nb[0];
-	h->bsz = h->boff[1] + (long)h->nb[1] * h->nb[1];
 	int rc;
 	if ((rc = dalloc(&h->S, (size_t)N * NE)) || (rc = dalloc(&h->Ri, (size_t)N * NE)) || (rc = dalloc(&h->D, (size_t)N * NE)) ||
 		(rc = dalloc(&h->lam[0], nch)) || (rc = dalloc(&h->lam[1], nch)) || (rc = dalloc(&h->lam[2], nch)) || (rc = dalloc(&h->lam[3], nch)) ||
-		(rc = dalloc(&h->Px1, (size_t)h->bsz)) || (rc = dalloc(&h->Py2, (size_t)h->bsz)) || (rc = dalloc(&h->M12, (size_t)h->bsz)) ||
-		(rc = dalloc(&h->M23, (size_t)h->bsz)) || (rc = dalloc(&h->M34, (size_t)h->bsz)) || (rc = dalloc(&h->chmap, (size_t)nch)) ||
+		(rc = dalloc(&h->chmap, (size_t)nch)) ||
 		(rc = dalloc(&h->Lrow, (size_t)h->nlh * N * P)) || (rc = dalloc(&h->Dinv, (size_t)h->nlh * N)) ||
 		(rc = dalloc(&h->X, nst)) || (rc = dalloc(&h->W, nst)) || (rc = dalloc(&h->U, nst * NE)) || (rc = dalloc(&h->ntt, (size_t)h->B)) ||
 		(rc = dalloc(&h->perm, (size_t)h->B)) || (rc = dalloc(&h->nrm, (size_t)h->B)))
 		return fail(rc);
 	if (cudaMemcpy(h->chmap, chmap.data(), sizeof(int) * nch, cudaMemcpyHostToDevice) != cudaSuccess) { set_error("upload"); return fail(QPC_ERR_CUDA); }
-	// angular eigensystems, block by block on the device; complex blocks P_c
+	// angular eigensystems and the transform matrices, block by block on the device
 	std::vector<double> lam[4];
-	double2* dP[4] = {nullptr, nullptr, nullptr, nullptr};
-	struct pguard { double2** p; ~pguard() { for (int c = 0; c < 4; ++c) if (p[c]) cudaFree(p[c]); } } PG{dP};
-	for (int c = 0; c < 4; ++c)
-		if ((rc = dalloc(&dP[c], (size_t)h->bsz))) return fail(rc);
-	if ((rc = device_angular(h, lam, dP))) return fail(rc);
-	// merged transforms P_b P_a^H per block, C = L R^H: T = R^H materialised, then C = L T
-	// with the library's complex GEMM (set-up only)
-	double2* T = nullptr;
-	double2* C23 = nullptr;
-	unsigned long long* dmax = nullptr;
-	struct tguard { double2** t; double2** c; unsigned long long** m; ~tguard() { if (*t) cudaFree(*t); if (*c) cudaFree(*c); if (*m) cudaFree(*m); } } TG{&T, &C23, &dmax};
-	const int nbmax = std::max(h->nb[0], h->nb[1]);
-	if ((rc = dalloc(&T, (size_t)nbmax * nbmax)) || (rc = dalloc(&C23, (size_t)h->bsz)) || (rc = dalloc(&dmax, 1))) return fail(rc);
-	auto merge = [&](const double2* Ld, const double2* Rd, double2* out) -> int {
-		for (int bl = 0; bl < 2; ++bl) {
-			const int n = h->nb[bl];
-			if (!n) continue;
-			k_vg_conj_transpose<<<(unsigned)(((long)n * n + 255) / 256), 256, 0, h->st>>>(Rd + h->boff[bl], n, T);
-			gemm::k_zgemm<false><<<gemm::grid_for(n, n, 1), gemm::THREADS, gemm::ZGEMM_SMEM, h->st>>>(Ld + h->boff[bl], n, T,
-				out + h->boff[bl], (long)n, 0L, n);
-			QPC_CUDA(cudaGetLastError());
-		}
-		return QPC_OK;
-	};
-	if ((rc = merge(dP[1], dP[0], h->M12)) || (rc = merge(dP[2], dP[1], C23)) || (rc = merge(dP[3], dP[2], h->M34))) return fail(rc);
-	{
-		const long nn = h->bsz;
-		const unsigned g = (unsigned)((nn + 255) / 256);
-		k_vg_real_part<<<g, 256, 0, h->st>>>(dP[0], nn, h->Px1);
-		k_vg_real_part<<<g, 256, 0, h->st>>>(dP[3], nn, h->Py2);
-		// P_y1 P_x2^H = Q1^T diag(phi) diag(phi)^H Q2 = Q1^T Q2: the phases cancel exactly
-		// (each term is a product of two purely real or two purely imaginary entries), so it
-		// is applied as a real transform
-		QPC_CUDA(cudaMemsetAsync(dmax, 0, sizeof(unsigned long long), h->st));
-		k_vg_max_imag<<<g, 256, 0, h->st>>>(C23, nn, dmax);
-		k_vg_real_part<<<g, 256, 0, h->st>>>(C23, nn, h->M23);
-		if (cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(h->st) != cudaSuccess) { set_error("transform setup failed"); return fail(QPC_ERR_CUDA); }
-		unsigned long long bits = 0;
-		QPC_CUDA(cudaMemcpy(&bits, dmax, sizeof(bits), cudaMemcpyDeviceToHost));
-		double mi;
-		std::memcpy(&mi, &bits, sizeof(mi));
-		if (!(mi <= 1e-13)) { set_error("merged transform P_y1 P_x2^H is not real (|imag| %g)", mi); return fail(QPC_ERR_NUMERIC); }
-	}
+	if ((rc = device_transforms(h, chmap, lam))) return fail(rc);
 	if (cudaMemcpy(h->S, S, sizeof(double) * N * NE, cudaMemcpyHostToDevice) != cudaSuccess ||
 		cudaMemcpy(h->Ri, Rinv, sizeof(double) * N * NE, cudaMemcpyHostToDevice) != cudaSuccess ||
 		cudaMemcpy(h->D, D, sizeof(double) * N * NE, cudaMemcpyHostToDevice) != cudaSuccess ||
