@@ -240,9 +240,9 @@ def run_engine(args, sync=None):
     # the drop-in adapter's per-step path (propagate(coef, f_ti, f_tf) of the C++ binding): the
     # whole batch state copied to the device and back around every single step, as a caller
     # that keeps the reference's host-side driver loop sees it
-    Kp = min(K, 5)
+    Kpp = min(K, 5)
     t0 = time.perf_counter()
-    for i in range(Kp):
+    for i in range(Kpp):
         prop.put(host_in)
         prop.propagate(ftab[:, W + i], ftab[:, W + i + 1])
         out = prop.get()
@@ -305,7 +305,7 @@ def run_engine(args, sync=None):
         "dtype": "c128 (complex FP64)", "data": "synthetic (seeded laser parameters, numpy default_rng(2025))",
         "config": c2_config(B, n_r, p, n_l, dt),
         "e2e": {"value": e2e, "unit": "wf-steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
-        "e2e_per_step_propagate": {"value": B * Kp / pp_s, "unit": "wf-steps/s", "steps": Kp,
+        "e2e_per_step_propagate": {"value": B * Kpp / pp_s, "unit": "wf-steps/s", "steps": Kpp,
                                    "h2d_bytes_per_step": state_bytes + 2 * B * 8, "d2h_bytes_per_step": state_bytes,
                                    "path": "put + propagate(f_ti, f_tf) + get per step, host buffers (wall clock)"},
         "plain_1wf": {"value": plain, "unit": "wf-steps/s", "ratio_batched_over_plain": value / plain},

@@ -75,12 +75,12 @@ def test_surrogate_pipeline(sg):
 
 
 def test_elliptical_fallback_linear_pulse(sg):
-    """At ellipticity 0 the velocity-gauge fallback sees a pulse along x: finite labels, the
-    dipole response at the driving frequency dominates the harmonic spectrum."""
+    """At ellipticity 0 the velocity-gauge fallback sees a pulse along x: finite labels, the low
+    harmonic orders decades above the high ones (the short pulse has no plateau up there)."""
     p = {"intensity": np.array([1e14]), "wavelength": np.array([400.0]), "cep": np.array([0.0]),
          "cycles": np.array([2.0]), "ellipticity": np.zeros(1)}
     ell_setup = sg._EllSetup(ELL, emax=max(3.17 * float(sg.up(p).max()) * 1.5, 1.0))
     pes, hhg, info = sg.tdse_spectra_elliptical(p, grid=ELL, setup=ell_setup)
     assert info["wf_steps"] > 0
     assert np.all(np.isfinite(pes)) and np.all(np.isfinite(hhg))
-    assert hhg[0, 0] == hhg[0].max()
+    assert hhg[0, :8].max() > hhg[0, -32:].max() + 2.0
