@@ -174,8 +174,9 @@ def path_flops(n_r, p, n_l, power=2):
     return chains_c + chains_f + factor + n_r * (fwd + bwd)
 
 
-# DRAM bytes per chain-row of the coupling chain kernel (both applications), from the
-# ncu capture summarised in profiles/k_chain_c2.md
+# DRAM bytes per chain-row of the coupling chain kernel (both applications): one ncu capture
+# of a coupling-chain launch on this workload, dram__bytes_read.sum + dram__bytes_write.sum
+# divided by the chain-rows the launch processed
 TRAFFIC_PER_CHAIN_ROW = 84.0
 
 
@@ -275,7 +276,7 @@ def run_engine(args, sync=None):
             "peak_source": fp64_peak()["source"],
             "flops_per_launch": fl, "launch_ms": launch_ms, "concurrent_streams": launches_per_step,
             "traffic": (TRAFFIC_PER_CHAIN_ROW * 2 * live_pairs * n_r / launches_per_step) if TRAFFIC_PER_CHAIN_ROW else None,
-            "traffic_source": "ncu dram__bytes_read+write of k_chain coupling launches, profiles/k_chain_c2.md, scaled by chain-rows",
+            "traffic_source": "ncu dram__bytes_read+write of one k_chain coupling launch, scaled by chain-rows",
             "hbm": {"achieved_gbs": sweep_bytes / (launch_ms * 1e-3) / 1e9 if sw_n else None,
                     "peak_gbs": peaks.get("hbm_gbs"), "bytes_per_launch": sweep_bytes},
             "path": {"flops_per_wf_step": path_flops(n_r, p, n_l), "achieved_tflops": path_tflops,

@@ -20,9 +20,10 @@
 // transforms of 2 n^2 N flops each (n = block size) instead of the reference's dense complex
 // N_ch x N_ch products.  The GEMMs are this library's own FP64 kernels (qpc_gemm.cuh), over the
 // live wavefunctions; the SVDs come from cuSOLVER gesvd at set-up.  The banded CN of each
-// eigen-channel runs one chain per thread: the LU of
-// S + ifet O is formed row by row with the previous p rows of U in registers, the forward
-// substitution fused, U rows kept in a scratch buffer for the backward substitution.
+// eigen-channel runs one chain per thread as z := 2 (S + ifet O)^-1 S z - z: a real LU for the
+// d/dr components (ifet real), an LU that uses the symmetry of S + ifet/r for the 1/r components,
+// formed row by row with the previous p rows of U in registers and the forward substitution fused,
+// U rows kept in a scratch buffer for the backward substitution.
 // The field-free step uses the LDL^T factors of S + i dt/2 H_l (qpc_ldlt_csym) as
 // x = 2 (S + i dt/2 H)^-1 S c - c.  State layout [inst][m][l][r] complex128, the
 // reference's own.  All arithmetic is complex FP64.
@@ -54,87 +55,91 @@ __device__ __forceinline__ double2 crcp(double2 y)
 	return make_double2(y.x / d, -y.y / d);
 }
 
-// one coupling component on the live prefix of instances: z := (S + ifet O)^-1 (S - ifet O) z
-// per (instance, eigen-channel), ifet = lam[ch] * coef * f_inst with coef complex
-// (anti = O anti-symmetric with O(r, r+k) = band[r][k] for k > 0).
-// f_inst = sgn * A[(inst*ld + step + tofs)*2 + axis] / 2.
+// One coupling component on the live prefix of instances: z := (S + e O)^-1 (S - e O) z per
+// (instance, eigen-channel), computed as z := 2 (S + e O)^-1 S z - z (S - e O = 2 S - (S + e O)),
+// so the right-hand side is the real band S times z.  e = lam[ch] * coef * f_inst with
+// f_inst = sgn * A[(inst*ld + step + tofs)*2 + axis] / 2.  A channel with e = 0 has M = I and is
+// left as it is.  One chain per thread: the factorisation is formed row by row with the previous
+// P rows of U in registers (diagonal kept as its reciprocal) and the forward substitution fused;
+// the U rows and y go to a scratch array for the backward pass, laid out element-major over the
+// threads ((row * elements + e) * threads + t) so that a warp's stores and loads are contiguous.
+
+// anti-symmetric O (d/dr: O(r, r+c) = band[r][c], O(r+c, r) = -band[r][c], c > 0) with e real
+// (x1, y1): A = S + e O is a real non-symmetric band, factorised by a real LU without pivoting.
+// Scratch per row: U(i, i+1..i+P), 1/U(i, i), Re y, Im y.
 template <int P>
-__global__ void __launch_bounds__(VG_THREADS) k_vg_cn(double2* __restrict__ state, double2* __restrict__ ubuf, const double* __restrict__ S,
-	const double* __restrict__ O, bool anti, const double* __restrict__ lam, double2 coef, const double* __restrict__ atab, long ld,
-	long step, int tofs, int axis, double sgn, const int* __restrict__ perm, int N, int nch, int nlive)
+__global__ void __launch_bounds__(VG_THREADS) k_vg_cn_anti(double2* __restrict__ state, double* __restrict__ scr, const double* __restrict__ S,
+	const double* __restrict__ O, const double* __restrict__ lam, double cre, const double* __restrict__ atab, long ld, long step, int tofs,
+	int axis, double sgn, const int* __restrict__ perm, int N, int nch, int nlive)
 {
+	const long nth = (long)nlive * nch;
 	const long t = (long)blockIdx.x * VG_THREADS + threadIdx.x;
-	if (t >= (long)nlive * nch) return;
+	if (t >= nth) return;
 	const int k = (int)(t / nch), ch = (int)(t - (long)k * nch);
 	const double f = sgn * atab[((long)perm[k] * ld + step + tofs) * 2 + axis] / 2.0;
-	const double lm = lam[ch] * f;
-	const double2 ifet = make_double2(lm * coef.x, lm * coef.y);
+	const double e = lam[ch] * f * cre;
+	if (e == 0.0) return;
+	constexpr int NE = P + 1, NS = P + 3;
 	double2* z = state + t * N;
-	double2* U = ubuf + t * (long)N * (P + 1);
-	constexpr int NE = P + 1;
-	// window: U rows of the previous P rows (row i-1-q at slot q), entries c = 0..P for column row+c
-	double2 Uw[P][NE];
-	double2 yw[P], zw[P];	// y and the input z of the previous P rows (z is overwritten by y)
+	double Uw[P][NE];	// slot q: row i-1-q, [0] = 1/U(row, row), [c] = U(row, row + c)
+	double2 yw[P], zw[P];	// y and z of the previous P rows
 #pragma unroll
 	for (int q = 0; q < P; ++q) {
 		yw[q] = zw[q] = make_double2(0.0, 0.0);
 #pragma unroll
-		for (int c = 0; c < NE; ++c) Uw[q][c] = make_double2(0.0, 0.0);
+		for (int c = 0; c < NE; ++c) Uw[q][c] = 0.0;
 	}
 	for (int i = 0; i < N; ++i) {
-		// row i of A+ and rhs = (A- z)_i; lower entries at columns i-P..i-1 (index q = i-col-1)
-		double2 lo[P], up[NE];
-		double2 rhs = make_double2(0.0, 0.0);
+		// row i of A: lo[q] = A(i, i-1-q), up[c] = A(i, i+c); w = (S z)_i
+		double lo[P], up[NE];
+		double2 w = make_double2(0.0, 0.0);
 #pragma unroll
 		for (int q = 0; q < P; ++q) {
-			int j = q + 1;
-			lo[q] = make_double2(0.0, 0.0);
-			if (i - j >= 0) {
-				double s = S[(long)(i - j) * NE + j], o = O[(long)(i - j) * NE + j];
-				double ol = anti ? -o : o;
-				double2 fo = make_double2(ifet.x * ol, ifet.y * ol);
-				lo[q] = make_double2(s + fo.x, fo.y);
-				double2 am = make_double2(s - fo.x, -fo.y);
-				double2 pr = cmul(am, zw[q]);
-				rhs.x += pr.x; rhs.y += pr.y;
+			lo[q] = 0.0;
+			if (i - 1 - q >= 0) {
+				const double sv = S[(long)(i - 1 - q) * NE + q + 1], ov = O[(long)(i - 1 - q) * NE + q + 1];
+				lo[q] = fma(-e, ov, sv);
+				w.x = fma(sv, zw[q].x, w.x);
+				w.y = fma(sv, zw[q].y, w.y);
 			}
 		}
+		const double2 zi = z[i];
 #pragma unroll
 		for (int c = 0; c < NE; ++c) {
-			up[c] = make_double2(0.0, 0.0);
+			up[c] = 0.0;
 			if (i + c < N) {
-				double s = S[(long)i * NE + c], o = O[(long)i * NE + c];
-				double2 fo = make_double2(ifet.x * o, ifet.y * o);
-				up[c] = make_double2(s + fo.x, fo.y);
-				double2 am = make_double2(s - fo.x, -fo.y);
-				double2 pr = cmul(am, z[i + c]);
-				rhs.x += pr.x; rhs.y += pr.y;
+				const double sv = S[(long)i * NE + c], ov = O[(long)i * NE + c];
+				up[c] = fma(e, ov, sv);
+				const double2 zc = c ? z[i + c] : zi;
+				w.x = fma(sv, zc.x, w.x);
+				w.y = fma(sv, zc.y, w.y);
 			}
 		}
-		// eliminate columns i-P .. i-1 in ascending order (q = P-1 .. 0); multiplier l_q
-		double2 lq[P];
+		// eliminate columns i-P .. i-1 in ascending order; a missing row has a zero window slot
+		double l[P];
 #pragma unroll
 		for (int qq = P - 1; qq >= 0; --qq) {
-			// column col = i-1-qq; its U row sits at window slot qq with U(col, col) = Uw[qq][0]
-			double2 a = lo[qq];
-			lq[qq] = make_double2(0.0, 0.0);
-			if (i - 1 - qq < 0) continue;
-			double2 l = cmul(a, crcp(Uw[qq][0]));
-			lq[qq] = l;
-			// update the remaining entries of row i: columns col+1 .. col+P
+			l[qq] = lo[qq] * Uw[qq][0];
 #pragma unroll
 			for (int c = 1; c < NE; ++c) {
-				int dc = c - 1 - qq;	// column col+c relative to i (negative: lower, >= 0: upper)
-				if (dc < 0) lo[-dc - 1] = csub(lo[-dc - 1], cmul(l, Uw[qq][c]));
-				else if (dc < NE) up[dc] = csub(up[dc], cmul(l, Uw[qq][c]));
+				const int dc = c - 1 - qq;	// column (i-1-qq)+c relative to i
+				if (dc < 0) lo[-dc - 1] = fma(-l[qq], Uw[qq][c], lo[-dc - 1]);
+				else up[dc] = fma(-l[qq], Uw[qq][c], up[dc]);
 			}
 		}
-		// forward substitution y_i = rhs_i - sum_q l_q y_{i-1-q}
-		double2 y = rhs;
+		double2 y = w;
 #pragma unroll
-		for (int q = 0; q < P; ++q) y = csub(y, cmul(lq[q], yw[q]));
-		// shift the windows, store U row i and y_i
-		const double2 zi = z[i];
+		for (int q = 0; q < P; ++q) {
+			y.x = fma(-l[q], yw[q].x, y.x);
+			y.y = fma(-l[q], yw[q].y, y.y);
+		}
+		const double ri = 1.0 / up[0];
+		double* sr = scr + (long)i * NS * nth + t;
+#pragma unroll
+		for (int c = 1; c < NE; ++c) sr[(c - 1) * nth] = up[c];
+		sr[P * nth] = ri;
+		sr[(P + 1) * nth] = y.x;
+		sr[(P + 2) * nth] = y.y;
 #pragma unroll
 		for (int q = P - 1; q > 0; --q) {
 			yw[q] = yw[q - 1];
@@ -144,26 +149,137 @@ __global__ void __launch_bounds__(VG_THREADS) k_vg_cn(double2* __restrict__ stat
 		}
 		yw[0] = y;
 		zw[0] = zi;
+		Uw[0][0] = ri;
 #pragma unroll
-		for (int c = 0; c < NE; ++c) {
-			Uw[0][c] = up[c];
-			U[(long)i * NE + c] = up[c];
-		}
-		z[i] = y;
+		for (int c = 1; c < NE; ++c) Uw[0][c] = up[c];
 	}
-	// backward substitution x_i = (y_i - sum_c U(i, i+c) x_{i+c}) / U(i, i)
+	// backward: x_i = (y_i - sum_c U(i, i+c) x_{i+c}) / U(i, i); z_i := 2 x_i - z_i
 	double2 xw[P];
 #pragma unroll
 	for (int q = 0; q < P; ++q) xw[q] = make_double2(0.0, 0.0);
 	for (int i = N - 1; i >= 0; --i) {
-		double2 v = z[i];
+		const double* sr = scr + (long)i * NS * nth + t;
+		double2 v = make_double2(sr[(P + 1) * nth], sr[(P + 2) * nth]);
 #pragma unroll
-		for (int c = 1; c < NE; ++c) v = csub(v, cmul(U[(long)i * NE + c], xw[c - 1]));
-		double2 x = cmul(v, crcp(U[(long)i * NE]));
+		for (int c = 1; c < NE; ++c) {
+			const double u = sr[(c - 1) * nth];
+			v.x = fma(-u, xw[c - 1].x, v.x);
+			v.y = fma(-u, xw[c - 1].y, v.y);
+		}
+		const double ri = sr[P * nth];
+		const double2 x = make_double2(v.x * ri, v.y * ri);
 #pragma unroll
 		for (int q = P - 1; q > 0; --q) xw[q] = xw[q - 1];
 		xw[0] = x;
-		z[i] = x;
+		const double2 zi = z[i];
+		z[i] = make_double2(fma(2.0, x.x, -zi.x), fma(2.0, x.y, -zi.y));
+	}
+}
+
+// symmetric O (1/r) with e = i b imaginary (x2, y2): A = S + i b O is complex symmetric, so in the
+// row-by-row LU the multipliers of row i are U(col, i) / U(col, col) from the window (no elimination
+// of the lower part) and only the upper part U(i, i..i+P) is formed.  Scratch per row (complex):
+// U(i, i+1..i+P), 1/U(i, i), y.
+template <int P>
+__global__ void __launch_bounds__(VG_THREADS) k_vg_cn_sym(double2* __restrict__ state, double2* __restrict__ scr, const double* __restrict__ S,
+	const double* __restrict__ O, const double* __restrict__ lam, double cim, const double* __restrict__ atab, long ld, long step, int tofs,
+	int axis, double sgn, const int* __restrict__ perm, int N, int nch, int nlive)
+{
+	const long nth = (long)nlive * nch;
+	const long t = (long)blockIdx.x * VG_THREADS + threadIdx.x;
+	if (t >= nth) return;
+	const int k = (int)(t / nch), ch = (int)(t - (long)k * nch);
+	const double f = sgn * atab[((long)perm[k] * ld + step + tofs) * 2 + axis] / 2.0;
+	const double b = lam[ch] * f * cim;
+	if (b == 0.0) return;
+	constexpr int NE = P + 1, NS = P + 2;
+	double2* z = state + t * N;
+	double2 Uw[P][NE];	// slot q: row i-1-q, [0] = 1/U(row, row), [c] = U(row, row + c)
+	double2 yw[P], zw[P];
+#pragma unroll
+	for (int q = 0; q < P; ++q) {
+		yw[q] = zw[q] = make_double2(0.0, 0.0);
+#pragma unroll
+		for (int c = 0; c < NE; ++c) Uw[q][c] = make_double2(0.0, 0.0);
+	}
+	for (int i = 0; i < N; ++i) {
+		double2 w = make_double2(0.0, 0.0);
+#pragma unroll
+		for (int q = 0; q < P; ++q)
+			if (i - 1 - q >= 0) {
+				const double sv = S[(long)(i - 1 - q) * NE + q + 1];
+				w.x = fma(sv, zw[q].x, w.x);
+				w.y = fma(sv, zw[q].y, w.y);
+			}
+		const double2 zi = z[i];
+		double2 up[NE];
+#pragma unroll
+		for (int c = 0; c < NE; ++c) {
+			up[c] = make_double2(0.0, 0.0);
+			if (i + c < N) {
+				const double sv = S[(long)i * NE + c], ov = O[(long)i * NE + c];
+				up[c] = make_double2(sv, b * ov);
+				const double2 zc = c ? z[i + c] : zi;
+				w.x = fma(sv, zc.x, w.x);
+				w.y = fma(sv, zc.y, w.y);
+			}
+		}
+		// multipliers L(i, i-1-q) = U(i-1-q, i) / U(i-1-q, i-1-q); zero for a missing row
+		double2 l[P];
+#pragma unroll
+		for (int q = 0; q < P; ++q) l[q] = cmul(Uw[q][q + 1], Uw[q][0]);
+		// U(i, i+c) = A(i, i+c) - sum_q L(i, i-1-q) U(i-1-q, i+c), over rows with i+c within their band
+#pragma unroll
+		for (int c = 0; c < P; ++c)
+#pragma unroll
+			for (int q = 0; q + c + 1 <= P; ++q) {
+				const double2 u = Uw[q][c + 1 + q];
+				up[c].x = fma(-l[q].x, u.x, fma(l[q].y, u.y, up[c].x));
+				up[c].y = fma(-l[q].x, u.y, fma(-l[q].y, u.x, up[c].y));
+			}
+		double2 y = w;
+#pragma unroll
+		for (int q = 0; q < P; ++q) {
+			y.x = fma(-l[q].x, yw[q].x, fma(l[q].y, yw[q].y, y.x));
+			y.y = fma(-l[q].x, yw[q].y, fma(-l[q].y, yw[q].x, y.y));
+		}
+		const double2 ri = crcp(up[0]);
+		double2* sr = scr + (long)i * NS * nth + t;
+#pragma unroll
+		for (int c = 1; c < NE; ++c) sr[(c - 1) * nth] = up[c];
+		sr[P * nth] = ri;
+		sr[(P + 1) * nth] = y;
+#pragma unroll
+		for (int q = P - 1; q > 0; --q) {
+			yw[q] = yw[q - 1];
+			zw[q] = zw[q - 1];
+#pragma unroll
+			for (int c = 0; c < NE; ++c) Uw[q][c] = Uw[q - 1][c];
+		}
+		yw[0] = y;
+		zw[0] = zi;
+		Uw[0][0] = ri;
+#pragma unroll
+		for (int c = 1; c < NE; ++c) Uw[0][c] = up[c];
+	}
+	double2 xw[P];
+#pragma unroll
+	for (int q = 0; q < P; ++q) xw[q] = make_double2(0.0, 0.0);
+	for (int i = N - 1; i >= 0; --i) {
+		const double2* sr = scr + (long)i * NS * nth + t;
+		double2 v = sr[(P + 1) * nth];
+#pragma unroll
+		for (int c = 1; c < NE; ++c) {
+			const double2 u = sr[(c - 1) * nth];
+			v.x = fma(-u.x, xw[c - 1].x, fma(u.y, xw[c - 1].y, v.x));
+			v.y = fma(-u.x, xw[c - 1].y, fma(-u.y, xw[c - 1].x, v.y));
+		}
+		const double2 x = cmul(v, sr[P * nth]);
+#pragma unroll
+		for (int q = P - 1; q > 0; --q) xw[q] = xw[q - 1];
+		xw[0] = x;
+		const double2 zi = z[i];
+		z[i] = make_double2(fma(2.0, x.x, -zi.x), fma(2.0, x.y, -zi.y));
 	}
 }
 
@@ -401,7 +517,8 @@ struct qpc_vgwr {
 	double* tm[5][2][2] = {};
 	double2 gam[4][2][2] = {};                    // [component][block][set]: the set's common phase
 	double2 *Lrow = nullptr, *Dinv = nullptr;     // field-free factors
-	double2 *X = nullptr, *W = nullptr, *U = nullptr;
+	double2 *X = nullptr, *W = nullptr;
+	double2* U = nullptr;                          // CN scratch: (p + 2) complex per chain-row
 	double* atab = nullptr;
 	long atab_cap = 0;
 	long long* ntt = nullptr;
@@ -533,14 +650,18 @@ int step_t(qpc_vgwr* h, long s, long ld, int nlive, int nff)
 	const int nb = nlive;
 	auto cn = [&](double2* z, int comp, int tofs) {
 		const bool anti = comp == 0 || comp == 2;
-		const double q = h->dt * 0.5 / 2.0;
-		const double2 coef = anti ? make_double2(-q, 0.0) : make_double2(0.0, q);
+		const double q = h->dt * 0.5 / 2.0;	// e = lam f (-q) for d/dr, i lam f q for 1/r
 		const int axis = comp < 2 ? 0 : 1;
 		const double sgn = comp == 1 ? 1.0 : -1.0;
 		const long nth = (long)nb * h->nch;
+		const unsigned grid = (unsigned)((nth + VG_THREADS - 1) / VG_THREADS);
 		cudaEvent_t pa = prof_begin(h);
-		k_vg_cn<P><<<(unsigned)((nth + VG_THREADS - 1) / VG_THREADS), VG_THREADS, 0, h->st>>>(z, h->U, h->S, anti ? h->D : h->Ri, anti,
-			h->lam[comp], coef, h->atab, ld, s, tofs, axis, sgn, h->perm, h->N, h->nch, nb);
+		if (anti)
+			k_vg_cn_anti<P><<<grid, VG_THREADS, 0, h->st>>>(z, (double*)h->U, h->S, h->D, h->lam[comp], -q, h->atab, ld, s, tofs, axis, sgn,
+				h->perm, h->N, h->nch, nb);
+		else
+			k_vg_cn_sym<P><<<grid, VG_THREADS, 0, h->st>>>(z, h->U, h->S, h->Ri, h->lam[comp], q, h->atab, ld, s, tofs, axis, sgn, h->perm,
+				h->N, h->nch, nb);
 		prof_end(h, 1, pa);
 		++h->launches;
 	};
@@ -795,7 +916,7 @@ int qpc_vgwr_create(const qpc_dims* dims, double dt, const double* S, const doub
 		(rc = dalloc(&h->lam[0], nch)) || (rc = dalloc(&h->lam[1], nch)) || (rc = dalloc(&h->lam[2], nch)) || (rc = dalloc(&h->lam[3], nch)) ||
 		(rc = dalloc(&h->chmap, (size_t)nch)) ||
 		(rc = dalloc(&h->Lrow, (size_t)h->nlh * N * P)) || (rc = dalloc(&h->Dinv, (size_t)h->nlh * N)) ||
-		(rc = dalloc(&h->X, nst)) || (rc = dalloc(&h->W, nst)) || (rc = dalloc(&h->U, nst * NE)) || (rc = dalloc(&h->ntt, (size_t)h->B)) ||
+		(rc = dalloc(&h->X, nst)) || (rc = dalloc(&h->W, nst)) || (rc = dalloc(&h->U, nst * (NE + 1))) || (rc = dalloc(&h->ntt, (size_t)h->B)) ||
 		(rc = dalloc(&h->perm, (size_t)h->B)) || (rc = dalloc(&h->nrm, (size_t)h->B)))
 		return fail(rc);
 	if (cudaMemcpy(h->chmap, chmap.data(), sizeof(int) * nch, cudaMemcpyHostToDevice) != cudaSuccess) { set_error("upload"); return fail(QPC_ERR_CUDA); }
