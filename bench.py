@@ -175,9 +175,9 @@ def path_flops(n_r, p, n_l, power=2):
 
 
 # DRAM bytes per chain-row of the coupling chain kernel (both applications): one ncu capture
-# of a coupling-chain launch on this workload, dram__bytes_read.sum + dram__bytes_write.sum
-# divided by the chain-rows the launch processed
-TRAFFIC_PER_CHAIN_ROW = 84.0
+# of a coupling-chain launch at G = 3 (64 instances x 40 chains x 800 rows, two applications),
+# dram__bytes_read.sum + dram__bytes_write.sum divided by the chain-rows the launch processed
+TRAFFIC_PER_CHAIN_ROW = 252.0
 
 
 def aggregate_over_ranks(line, batch, device=None):

@@ -120,7 +120,7 @@ __global__ void __launch_bounds__(128) k_chain(double2* __restrict__ X, double2*
 	const double2* __restrict__ fac, const double* __restrict__ S, const int64_t* __restrict__ nta,
 	long step, int jslot, int B, int M, int m0, int N, int L, int np, long chbase, long nchains,
 	const double* __restrict__ Fo = nullptr, double* __restrict__ obs = nullptr, const int* __restrict__ ffmap = nullptr, long ffstride = 0,
-	int cmode = 0)
+	int cmode = 0, int sstage = 1)
 {
 	// chains [chbase, nchains) of this launch (an instance group); nchains is an end index.
 	// Fo/obs (coupling chains only, optional): obs[chain] = <z|F|z> of the chain's vector at
@@ -128,9 +128,15 @@ __global__ void __launch_bounds__(128) k_chain(double2* __restrict__ X, double2*
 	// application at step 0, after the first of two applications otherwise.
 	using C = chain_cfg<P, G, CPL>;
 	constexpr int NE = C::NE, LPC = C::LPC, CPW = C::CPW, TPL = C::TPL, PD = C::PD;
-	extern __shared__ double sS[];	// S band [N][P+1]
-	for (int t = threadIdx.x; t < N * NE; t += blockDim.x) sS[t] = S[t];
-	__syncthreads();
+	// S band [N][P+1]: staged in shared memory per block (sstage), or read through L1, which
+	// leaves the shared memory to more resident blocks
+	extern __shared__ double sS[];
+	const double* Sb = S;
+	if (sstage) {
+		for (int t = threadIdx.x; t < N * NE; t += blockDim.x) sS[t] = S[t];
+		__syncthreads();
+		Sb = sS;
+	}
 	const unsigned FULL = 0xffffffffu;
 	const int lane = threadIdx.x & 31;
 	const long warp = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -212,10 +218,10 @@ __global__ void __launch_bounds__(128) k_chain(double2* __restrict__ X, double2*
 					double w = 0.0;
 #pragma unroll
 					for (int k = P; k >= 1; --k)
-						if (r - k >= 0) w = fma(sS[(r - k) * NE + k], z[(long)(r - k) * rs], w);
+						if (r - k >= 0) w = fma(Sb[(r - k) * NE + k], z[(long)(r - k) * rs], w);
 #pragma unroll
 					for (int k = 0; k <= P; ++k)
-						if (r + k < N) w = fma(sS[r * NE + k], z[(long)(r + k) * rs], w);
+						if (r + k < N) w = fma(Sb[r * NE + k], z[(long)(r + k) * rs], w);
 					Wd[2 * d.xoff + part + (long)r * rs] = w;
 				}
 			}

@@ -457,6 +457,7 @@ struct qpc_lgwz {
 	int gsel[2][32];
 	std::vector<int> gcand;
 	size_t chain_smem = 0;
+	int chain_sstage = 1;	// k_chain stages the S band in shared memory (QPC_CHAIN_SSTAGE=0: read through L1)
 	// optional per-kernel timing (CUDA events around each launch on the handle's stream)
 	bool profiling = false;
 	std::vector<cudaEvent_t> evpool;
@@ -599,9 +600,9 @@ void launch_chain_g(qpc_lgwz* h, cudaStream_t st, int b0, double2* X, const doub
 	long nwarps = (nch + C::CPW - 1) / C::CPW;
 	unsigned grid = (unsigned)((nwarps + 3) / 4);
 	bool ob = CPL && h->observing;
-	k_chain<P, G, CPL><<<grid, 128, h->chain_smem, st>>>(X, h->wk, fac, h->S, nta, step, jslot, h->B, h->M, h->d.m0,
-		h->N, h->L, h->npair, chbase, chbase + nch, ob ? h->obsF : nullptr, ob ? h->obs : nullptr,
-		CPL ? nullptr : h->ffmap_cur, (long)h->nlh * h->N * (h->P + 1), h->cmode);
+	k_chain<P, G, CPL><<<grid, 128, h->chain_sstage ? h->chain_smem : 0, st>>>(X, h->wk, fac, h->S, nta, step, jslot, h->B, h->M,
+		h->d.m0, h->N, h->L, h->npair, chbase, chbase + nch, ob ? h->obsF : nullptr, ob ? h->obs : nullptr,
+		CPL ? nullptr : h->ffmap_cur, (long)h->nlh * h->N * (h->P + 1), h->cmode, h->chain_sstage);
 	LAUNCH(h);
 }
 
@@ -1152,7 +1153,8 @@ static int create_impl(const qpc_dims* dims, double dt, const double* S, const d
 	}
 	size_t smem = sizeof(double2) * 2 * TR * (L | 1);
 	h->chain_smem = sizeof(double) * (size_t)N * NE;
-	if (h->chain_smem > 200 * 1024) { set_error("n_r=%d too large for the shared-memory S band", N); return fail(QPC_ERR_ARGS); }
+	if (const char* e = getenv("QPC_CHAIN_SSTAGE")) h->chain_sstage = atoi(e) ? 1 : 0;
+	if (h->chain_sstage && h->chain_smem > 200 * 1024) { set_error("n_r=%d too large for the shared-memory S band", N); return fail(QPC_ERR_ARGS); }
 	set_smem_attrs(h, smem);
 	std::memset(h->gsel, 0, sizeof(h->gsel));
 	for (int g = 1; g <= P; ++g) if (P % g == 0 && (g <= 4 || g == P)) h->gcand.push_back(g);
