@@ -253,6 +253,16 @@ int qpc_hhg_spectrum(const double* z, int64_t n, double t0, double dt, double tm
 int qpc_hhg_spectra(int32_t n_inst, const double* z, int64_t ldz, const int64_t* n, double t0, double dt, const double* tmin,
 	const double* tmax, int32_t dipole_type, int64_t kmax, double* spectrum);
 
+/* C = A B in FP64 on the bf16 tensor cores by exact digit slices (the product the velocity-gauge
+ * transforms use): A [n][K] (row stride lda), B [K][M] (ldb), C [n][M] (ldc), host buffers.  Each
+ * row of A and column of B is cut into 9 digits of 7 bits under the power of two of its largest
+ * element; the digit products are summed exactly (fp32 tensor accumulation of integers below 2^24,
+ * int64 across chunks) and rounded to FP64 once.  The error is near K 2^(ea_i + eb_j - 61), with
+ * 2^ea_i and 2^eb_j the row's and column's powers of two: below an FP64 GEMM's own rounding.
+ * ms (optional): device time of splitting B and the product. */
+int qpc_dgemm_slices(int64_t n, int64_t M, int64_t K, const double* A, int64_t lda, const double* B, int64_t ldb, double* C,
+	int64_t ldc, float* ms);
+
 /* Photoelectron energy spectrum (|proj|^2 binned over [emin, emax) per unit energy) and
  * ionization yield 1 - sum_{energy < thres} |proj|^2 (ionization_sph::measure_ioyd,
  * spectrum/ionization_1e.hpp:15-51) from n projections (complex) with their energies. */

@@ -29,7 +29,7 @@ POTENTIAL_YUKAWA = 1
 EXPORTS = (
     "qpc_last_error", "qpc_version", "qpc_set_wait_limit", "qpc_get_wait_limit", "qpc_fp64_peak",
     "qpc_lgwz_stream", "qpc_vgwr_set_profiling", "qpc_vgwr_kernel_times", "qpc_vgwr_run_dipole", "qpc_lgwz_run_ex",
-    "qpc_hhg_spectra", "qpc_linear_knots", "qpc_radial_setup", "qpc_y10_coupling",
+    "qpc_hhg_spectra", "qpc_dgemm_slices", "qpc_linear_knots", "qpc_radial_setup", "qpc_y10_coupling",
     "qpc_y10_eigen", "qpc_ldlt_csym", "qpc_gen_eigen", "qpc_field_sinen", "qpc_lgwz_create",
     "qpc_lgwz_destroy", "qpc_lgwz_put", "qpc_lgwz_get", "qpc_lgwz_put_device", "qpc_lgwz_get_device",
     "qpc_lgwz_propagate", "qpc_lgwz_propagate_free", "qpc_lgwz_run", "qpc_lgwz_norm", "qpc_lgwz_dipole",
@@ -128,6 +128,7 @@ def load(path=None):
         "qpc_lgwz_run_dipole": (ctypes.c_int, [P, P, i64, P, P, P, P, i64]),
         "qpc_hhg_spectrum": (ctypes.c_int, [P, i64, d, d, d, d, i32, P, P]),
         "qpc_hhg_spectra": (ctypes.c_int, [i32, P, i64, P, d, d, P, P, i32, i64, P]),
+        "qpc_dgemm_slices": (ctypes.c_int, [i64, i64, i64, P, i64, P, i64, P, i64, P]),
         "qpc_pes_bin": (ctypes.c_int, [P, P, i64, d, d, i32, d, P, P, P]),
         "qpc_cholesky_band": (ctypes.c_int, [i32, i32, P, P]),
         "qpc_lgwz_run_many": (ctypes.c_int, [i32, P, P, P, P, P, P]),
@@ -357,6 +358,21 @@ def hhg_spectra(z, n, dt, kmax, t0=0.0, tmin=None, tmax=None, dipole_type=1):
     out = np.zeros((B, int(kmax)))
     _check(load().qpc_hhg_spectra(B, _ptr(z), z.shape[1], _ptr(n), t0, dt, _ptr(tmin), _ptr(tmax), dipole_type, int(kmax), _ptr(out)))
     return out
+
+
+def dgemm_slices(A, B, timed=False):
+    """C = A B in FP64 on the tensor cores by exact bf16 digit slices (qpc_dgemm_slices), the
+    product the velocity-gauge transforms use.  With timed=True also returns the device time in ms
+    of splitting B and the product."""
+    A, B = _f64(np.atleast_2d(A)), _f64(np.atleast_2d(B))
+    n, K = A.shape
+    if B.shape[0] != K:
+        raise ValueError("inner dimensions differ: %s %s" % (A.shape, B.shape))
+    M = B.shape[1]
+    C = np.zeros((n, M))
+    ms = np.zeros(1, np.float32)
+    _check(load().qpc_dgemm_slices(n, M, K, _ptr(A), K, _ptr(B), M, _ptr(C), M, _ptr(ms)))
+    return (C, float(ms[0])) if timed else C
 
 
 def pes_bin(proj, energy, emin, emax, nbins, thres=0.0):

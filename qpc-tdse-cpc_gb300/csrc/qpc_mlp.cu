@@ -501,7 +501,8 @@ int qpc_mlp_create(int32_t n_in, int32_t n_hidden, int32_t n_layers, int32_t n_o
 		return fail(QPC_ERR_CUDA);
 	}
 	cast_all(h);
-	if (cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(h->st) != cudaSuccess) { set_error("cast failed"); return fail(QPC_ERR_CUDA); }
+	if (cudaGetLastError() != cudaSuccess) { set_error("cast failed"); return fail(QPC_ERR_CUDA); }
+	if (int rc2 = wait_on(h->st)) return fail(rc2);
 	*out = h;
 	return QPC_OK;
 }
@@ -546,7 +547,7 @@ static int params_io(qpc_mlp* h, int32_t member, float* host, bool get)
 	if (!get) {
 		cast_all(h);
 		QPC_CUDA(cudaGetLastError());
-		QPC_CUDA(cudaStreamSynchronize(h->st));
+		if (int rc = wait_on(h->st)) return rc;
 	}
 	return QPC_OK;
 }

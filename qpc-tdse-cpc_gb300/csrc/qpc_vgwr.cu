@@ -32,6 +32,7 @@
 #include <cuda_runtime.h>
 #include <cusolverDn.h>
 #include "qpc_gemm.cuh"
+#include "qpc_ozaki.cuh"
 #include <cstdlib>
 #include <cstring>
 #include <cmath>
@@ -516,6 +517,13 @@ struct qpc_vgwr {
 	double* tmbuf = nullptr;
 	double* tm[5][2][2] = {};
 	double2 gam[4][2][2] = {};                    // [component][block][set]: the set's common phase
+	// slice-product GEMM (qpc_ozaki.cuh): digit slices and exponent fields of every matrix per
+	// orientation [mat][block][set][trans], and the scratch for the state's slices
+	bool slices = true;
+	__nv_bfloat16* sdA[5][2][2][2] = {};
+	int* seA[5][2][2][2] = {};
+	__nv_bfloat16* sdB = nullptr;
+	int* seB = nullptr;
 	double2 *Lrow = nullptr, *Dinv = nullptr;     // field-free factors
 	double2 *X = nullptr, *W = nullptr;
 	double2* U = nullptr;                          // CN scratch: (p + 2) complex per chain-row
@@ -559,8 +567,15 @@ void vg_free(qpc_vgwr* h)
 	if (h->ev0) cudaEventDestroy(h->ev0);
 	if (h->ev1) cudaEventDestroy(h->ev1);
 	for (auto e : h->evpool) cudaEventDestroy(e);
-	void* dp[] = {h->dpairs, h->dcoef, h->dF, h->dpart, h->dxs, h->dys};
+	void* dp[] = {h->dpairs, h->dcoef, h->dF, h->dpart, h->dxs, h->dys, h->sdB, h->seB};
 	for (void* p : dp) if (p) cudaFree(p);
+	for (int m = 0; m < 5; ++m)
+		for (int b = 0; b < 2; ++b)
+			for (int st = 0; st < 2; ++st)
+				for (int tr = 0; tr < 2; ++tr) {
+					if (h->sdA[m][b][st][tr]) cudaFree(h->sdA[m][b][st][tr]);
+					if (h->seA[m][b][st][tr]) cudaFree(h->seA[m][b][st][tr]);
+				}
 	if (h->st) cudaStreamDestroy(h->st);
 	delete h;
 }
@@ -612,6 +627,16 @@ void gemm_sets(qpc_vgwr* h, int mat, bool trans, const double2* in, double2* out
 			const int n = st ? h->nb[b] - h->na[b] : h->na[b];
 			if (!n) continue;
 			const long o = (long)(h->off[b] + (st ? h->na[b] : 0)) * N;
+			if (h->slices) {
+				// the state's rows of this set as the [n][2 N nlive] right operand: element (k, j) of
+				// instance j / (2 N) at channel k, real j % (2 N); the product written back the same way
+				const long J = 2L * N * nlive;
+				oz_split(oz::operand{(const double*)(in + o), 2L * N, 1, 2 * sstate, 2L * N}, n, J, h->seB, h->sdB, h->st);
+				oz_gemm(h->sdA[mat][b][st][trans ? 1 : 0], h->seA[mat][b][st][trans ? 1 : 0], h->sdB, h->seB, n, J, n, (double*)(out + o),
+					2L * N, 2L * N, 2 * sstate, h->st);
+				h->launches += 3;
+				continue;
+			}
 			const dim3 g = gemm::grid_for(2 * N, n, nlive);
 			const double* A = h->tm[mat][b][st];
 			if (trans) gemm::k_dgemm<true><<<g, gemm::THREADS, 0, h->st>>>(A, n, (const double*)(in + o), (double*)(out + o), 2L * N, 2 * sstate, 2 * N);
@@ -807,7 +832,7 @@ int device_transforms(qpc_vgwr* h, std::vector<int>& chmap, std::vector<double> 
 			}
 			k_vg_transpose<<<(unsigned)(((long)na * na + 255) / 256), 256, 0, h->st>>>(Ucm, na, ub[base][b][0]);
 			QPC_CUDA(cudaGetLastError());
-			QPC_CUDA(cudaStreamSynchronize(h->st));
+			if ((rc = wait_on(h->st))) return rc;
 			int info = 0;
 			QPC_CUDA(cudaMemcpy(&info, d_info, sizeof(int), cudaMemcpyDeviceToHost));
 			if (info) { set_error("gesvd info %d", info); return QPC_ERR_NUMERIC; }
@@ -846,8 +871,23 @@ int device_transforms(qpc_vgwr* h, std::vector<int>& chmap, std::vector<double> 
 			gemm::k_dgemm<true><<<gg, gemm::THREADS, 0, h->st>>>(uy1, n, ux2, h->tm[3][b][st], (long)n, 0L, n);
 			gemm::k_dgemm<true><<<gg, gemm::THREADS, 0, h->st>>>(h->tm[1][b][st], n, uy1, h->tm[4][b][st], (long)n, 0L, n);
 			QPC_CUDA(cudaGetLastError());
-			QPC_CUDA(cudaStreamSynchronize(h->st));
+			if ((rc = wait_on(h->st))) return rc;
 		}
+	// digit slices of every matrix in both orientations for the slice-product GEMM: op(A)(i, k) =
+	// A[i n + k] (trans 0) or A[k n + i] (trans 1), rows of op(A) are the split's columns
+	if (h->slices)
+		for (int m = 0; m < 5; ++m)
+			for (int b = 0; b < 2; ++b)
+				for (int st = 0; st < 2; ++st) {
+					const long n = st ? h->nb[b] - h->na[b] : h->na[b];
+					if (!n) continue;
+					for (int tr = 0; tr < 2; ++tr) {
+						if ((rc = dalloc(&h->sdA[m][b][st][tr], oz_digits_elems(n, n))) || (rc = dalloc(&h->seA[m][b][st][tr], (size_t)n))) return rc;
+						const oz::operand o = tr ? oz::operand{h->tm[m][b][st], n, 1, 0, n} : oz::operand{h->tm[m][b][st], 1, n, 0, n};
+						if ((rc = oz_split(o, n, n, h->seA[m][b][st][tr], h->sdA[m][b][st][tr], h->st))) return rc;
+					}
+				}
+	if ((rc = wait_on(h->st))) return rc;
 	// the common phase of each set under each component: -i for an im-odd set of x2 and y1, else 1
 	for (int c = 0; c < 4; ++c)
 		for (int b = 0; b < 2; ++b)
@@ -920,6 +960,14 @@ int qpc_vgwr_create(const qpc_dims* dims, double dt, const double* S, const doub
 		(rc = dalloc(&h->perm, (size_t)h->B)) || (rc = dalloc(&h->nrm, (size_t)h->B)))
 		return fail(rc);
 	if (cudaMemcpy(h->chmap, chmap.data(), sizeof(int) * nch, cudaMemcpyHostToDevice) != cudaSuccess) { set_error("upload"); return fail(QPC_ERR_CUDA); }
+	// the transforms' GEMMs: exact bf16 digit slices on the tensor cores (default), or the FP64
+	// DFMA kernel (QPC_VG_GEMM=dfma)
+	if (const char* e = std::getenv("QPC_VG_GEMM")) h->slices = std::strcmp(e, "dfma") != 0;
+	if (h->slices) {
+		const long J = 2L * N * h->B;
+		const long nmax = std::max({(long)h->na[0], (long)h->na[1], (long)(h->nb[0] - h->na[0]), (long)(h->nb[1] - h->na[1]), 1L});
+		if ((rc = dalloc(&h->sdB, oz_digits_elems(J, nmax))) || (rc = dalloc(&h->seB, (size_t)J))) return fail(rc);
+	}
 	// angular eigensystems and the transform matrices, block by block on the device
 	std::vector<double> lam[4];
 	if ((rc = device_transforms(h, chmap, lam))) return fail(rc);

@@ -6,8 +6,11 @@ No counterpart in the reference.  Pieces:
                      log-uniform in [5e13, 5e14] W/cm^2, wavelength uniform in
                      [400, 2000] nm, CEP uniform in [0, 2 pi), integer sin^2 cycles 2..10,
                      ellipticity 0 (the length-gauge engine is z-linear).
-  * features         6 network inputs: log10(I / 1e14 W/cm^2), (lambda - 1200)/800,
-                     sin CEP, cos CEP, (cycles - 6)/4, ellipticity.
+  * features         network inputs.  "sym" (default, 10 inputs): log10(I / 1e14 W/cm^2),
+                     (lambda - 1200)/800, sin 2 CEP, cos 2 CEP (the spectra are invariant under
+                     CEP -> CEP + pi), (cycles - 6)/4, ellipticity, and four derived ones (cutoff
+                     order, w/U_p, Ip/U_p, pulse length); "base" (6 inputs): the first six with
+                     sin CEP, cos CEP.
   * tdse_spectra     runs the batched Crank-Nicolson engine (hydrogen, B-splines of
                      degree 6, N_r = 800 on [0, 400], l < 41, dt = 0.05) from the ground
                      state through each pulse, recording <z>(t) in the loop, then projects
@@ -68,7 +71,7 @@ FEATURES = ("base", "sym")
 IP_H = 0.5   # ionization potential of the scan's atom (hydrogen), a.u.
 
 
-def features(p, kind="base"):
+def features(p, kind="sym"):
     """network inputs.  base: log10(I / 1e14 W/cm^2), (lambda - 1200)/800, sin CEP, cos CEP,
     (cycles - 6)/4, ellipticity.  sym: the CEP enters as sin 2 CEP, cos 2 CEP -- the spectra are
     exactly invariant under CEP -> CEP + pi (the field changes sign; the atom is symmetric under
@@ -277,7 +280,7 @@ def tdse_spectra_elliptical(p, grid=ELL_GRID, batch=16, setup=None, log=None):
 class Surrogate:
     """Ensemble MLP surrogate with TDSE fallback."""
 
-    def __init__(self, n_members=5, n_hidden=256, n_layers=4, seed=0, features="base"):
+    def __init__(self, n_members=5, n_hidden=256, n_layers=4, seed=0, features="sym"):
         self.n_members, self.n_hidden, self.n_layers, self.seed = n_members, n_hidden, n_layers, seed
         self.features = features
         self.net = None

@@ -127,7 +127,7 @@ def main():
     f.add_argument("--stages", type=int, default=3)
     f.add_argument("--quantile", type=float, default=0.9)
     f.add_argument("--seed", type=int, default=0)
-    f.add_argument("--features", default="base", choices=sg.FEATURES)
+    f.add_argument("--features", default="sym", choices=sg.FEATURES)
     f.add_argument("--out", default=None)
     a = ap.parse_args()
     generate(a) if a.cmd == "generate" else fit(a)
