@@ -115,8 +115,12 @@ __device__ __forceinline__ void msub_operands(double vr, double vi, int part, do
 	w = part ? __longlong_as_double(__double_as_longlong(vr) ^ (long long)0x8000000000000000ull) : vi;
 }
 
+// warps per block of k_chain: one staged S band serves every warp of a block (the launch chooses
+// 1..CHAIN_MAXW warps; 4 unless the engine is told otherwise)
+constexpr int CHAIN_MAXW = 5;
+
 template <int P, int G, bool CPL>
-__global__ void __launch_bounds__(128) k_chain(double2* __restrict__ X, double2* __restrict__ Wk,
+__global__ void __launch_bounds__(CHAIN_MAXW * 32) k_chain(double2* __restrict__ X, double2* __restrict__ Wk,
 	const double2* __restrict__ fac, const double* __restrict__ S, const int64_t* __restrict__ nta,
 	long step, int jslot, int B, int M, int m0, int N, int L, int np, long chbase, long nchains,
 	const double* __restrict__ Fo = nullptr, double* __restrict__ obs = nullptr, const int* __restrict__ ffmap = nullptr, long ffstride = 0,
@@ -143,8 +147,8 @@ __global__ void __launch_bounds__(128) k_chain(double2* __restrict__ X, double2*
 	const long ch0 = chbase + warp * CPW;
 	if (ch0 >= nchains) return;
 	// chain descriptors of this warp, once, in shared memory
-	__shared__ long s_x[4][32], s_f[4][32];
-	__shared__ int s_a[4][32];
+	__shared__ long s_x[CHAIN_MAXW][32], s_f[CHAIN_MAXW][32];
+	__shared__ int s_a[CHAIN_MAXW][32];
 	const int wib = threadIdx.x >> 5;
 	if (lane < CPW) {
 		chain_desc d = describe<CPL>(ch0 + lane, nchains, nta, step, jslot, B, M, m0, N, L, np, NE, ffmap, ffstride, cmode);
@@ -468,6 +472,7 @@ __global__ void __launch_bounds__(128) k_chain_seg(double2* __restrict__ X, cons
 	const int* __restrict__ ffmap, long ffstride, int cmode)
 {
 	constexpr int NE = P + 1, NC = CPL ? 2 : 1;
+	static_assert(2 * P <= 16, "carry lanes: 16 h + 2 i + part");
 	const unsigned FULL = 0xffffffffu;
 	extern __shared__ double2 seg_sm[];
 	__shared__ double2 xc[NC][16][P];
@@ -556,26 +561,33 @@ __global__ void __launch_bounds__(128) k_chain_seg(double2* __restrict__ X, cons
 			}
 		}
 		__syncthreads();
-		// ---- P2b: forward carries x(s)_i = y(a_s - 1 - i), s = 1..Q-1, lane = 2 i + part
+		// ---- P2b: forward carries x(s)_i = y(a_s - 1 - i), s = 1..Q-1.  lane = 16 h + 2 i + part: the
+		// two halves h of the sum over j run on separate lanes (two FMAs per term) and are joined by
+		// one shuffle, so a carry step costs ceil(P/2) * 2 + 1 FP64 instructions
 		if (warp < NC) {
-			const int c = warp, i = lane >> 1, part = lane & 1;
+			constexpr int HJ = (P + 1) / 2;
+			const int c = warp, h = lane >> 4, i = (lane & 15) >> 1, part = lane & 1;
 			const bool on = app < s_a[c] && i < P;
 			const double* wv = reinterpret_cast<const double*>(wsh + c * N) + part;
 			for (int sg = 1; sg < Q; ++sg) {
 				double v = 0.0;
 				if (on) {
 					const int r = sg * Ls - 1 - i;
-					v = wv[2L * r];
+					if (h == 0) v = wv[2L * r];
 					if (sg >= 2) {
 #pragma unroll
-						for (int jj = 0; jj < P; ++jj) {
-							const double2 ph = cfw[(sg * P + i) * P + jj], xv = xc[c][sg - 1][jj];
-							v += part ? ph.x * xv.y + ph.y * xv.x : ph.x * xv.x - ph.y * xv.y;
+						for (int q = 0; q < HJ; ++q) {
+							const int jj = h * HJ + q;
+							if (jj < P) {
+								const double2 ph = cfw[(sg * P + i) * P + jj], xv = xc[c][sg - 1][jj];
+								v = part ? fma(ph.x, xv.y, fma(ph.y, xv.x, v)) : fma(ph.x, xv.x, fma(-ph.y, xv.y, v));
+							}
 						}
 					}
 				}
+				v += __shfl_xor_sync(FULL, v, 16);
 				__syncwarp();
-				if (on) reinterpret_cast<double*>(&xc[c][sg][i])[part] = v;
+				if (on && h == 0) reinterpret_cast<double*>(&xc[c][sg][i])[part] = v;
 				__syncwarp();
 			}
 		}
@@ -634,26 +646,31 @@ __global__ void __launch_bounds__(128) k_chain_seg(double2* __restrict__ X, cons
 			}
 		}
 		__syncthreads();
-		// ---- P4b: backward carries x(s)_i = x(b_s + i), s = Q-2 .. 0
+		// ---- P4b: backward carries x(s)_i = x(b_s + i), s = Q-2 .. 0, lanes as in P2b
 		if (warp < NC) {
-			const int c = warp, i = lane >> 1, part = lane & 1;
+			constexpr int HJ = (P + 1) / 2;
+			const int c = warp, h = lane >> 4, i = (lane & 15) >> 1, part = lane & 1;
 			const bool on = app < s_a[c] && i < P;
 			const double* wv = reinterpret_cast<const double*>(wsh + c * N) + part;
 			for (int sg = Q - 2; sg >= 0; --sg) {
 				double v = 0.0;
 				if (on) {
 					const int r = (sg + 1) * Ls + i;
-					v = wv[2L * r];
+					if (h == 0) v = wv[2L * r];
 					if (sg + 1 <= Q - 2) {
 #pragma unroll
-						for (int jj = 0; jj < P; ++jj) {
-							const double2 ph = cbw[(sg * P + i) * P + jj], xv = xc[c][sg + 1][jj];
-							v += part ? ph.x * xv.y + ph.y * xv.x : ph.x * xv.x - ph.y * xv.y;
+						for (int q = 0; q < HJ; ++q) {
+							const int jj = h * HJ + q;
+							if (jj < P) {
+								const double2 ph = cbw[(sg * P + i) * P + jj], xv = xc[c][sg + 1][jj];
+								v = part ? fma(ph.x, xv.y, fma(ph.y, xv.x, v)) : fma(ph.x, xv.x, fma(-ph.y, xv.y, v));
+							}
 						}
 					}
 				}
+				v += __shfl_xor_sync(FULL, v, 16);
 				__syncwarp();
-				if (on) reinterpret_cast<double*>(&xc[c][sg][i])[part] = v;
+				if (on && h == 0) reinterpret_cast<double*>(&xc[c][sg][i])[part] = v;
 				__syncwarp();
 			}
 		}

@@ -458,6 +458,7 @@ struct qpc_lgwz {
 	std::vector<int> gcand;
 	size_t chain_smem = 0;
 	int chain_sstage = 1;	// k_chain stages the S band in shared memory (QPC_CHAIN_SSTAGE=0: read through L1)
+	int chain_warps = 4;	// warps per k_chain block, sharing one staged S band (QPC_CHAIN_WARPS)
 	// optional per-kernel timing (CUDA events around each launch on the handle's stream)
 	bool profiling = false;
 	std::vector<cudaEvent_t> evpool;
@@ -598,9 +599,10 @@ void launch_chain_g(qpc_lgwz* h, cudaStream_t st, int b0, double2* X, const doub
 	if (nch <= 0) return;
 	long chbase = (long)b0 * per;
 	long nwarps = (nch + C::CPW - 1) / C::CPW;
-	unsigned grid = (unsigned)((nwarps + 3) / 4);
+	const int wpb = h->chain_warps;
+	unsigned grid = (unsigned)((nwarps + wpb - 1) / wpb);
 	bool ob = CPL && h->observing;
-	k_chain<P, G, CPL><<<grid, 128, h->chain_sstage ? h->chain_smem : 0, st>>>(X, h->wk, fac, h->S, nta, step, jslot, h->B, h->M,
+	k_chain<P, G, CPL><<<grid, 32 * wpb, h->chain_sstage ? h->chain_smem : 0, st>>>(X, h->wk, fac, h->S, nta, step, jslot, h->B, h->M,
 		h->d.m0, h->N, h->L, h->npair, chbase, chbase + nch, ob ? h->obsF : nullptr, ob ? h->obs : nullptr,
 		CPL ? nullptr : h->ffmap_cur, (long)h->nlh * h->N * (h->P + 1), h->cmode, h->chain_sstage);
 	LAUNCH(h);
@@ -1154,6 +1156,7 @@ static int create_impl(const qpc_dims* dims, double dt, const double* S, const d
 	size_t smem = sizeof(double2) * 2 * TR * (L | 1);
 	h->chain_smem = sizeof(double) * (size_t)N * NE;
 	if (const char* e = getenv("QPC_CHAIN_SSTAGE")) h->chain_sstage = atoi(e) ? 1 : 0;
+	if (const char* e = getenv("QPC_CHAIN_WARPS")) h->chain_warps = std::max(1, std::min(CHAIN_MAXW, atoi(e)));
 	if (h->chain_sstage && h->chain_smem > 200 * 1024) { set_error("n_r=%d too large for the shared-memory S band", N); return fail(QPC_ERR_ARGS); }
 	set_smem_attrs(h, smem);
 	std::memset(h->gsel, 0, sizeof(h->gsel));
