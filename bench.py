@@ -449,16 +449,36 @@ def run_c1(args):
                    "n_m": n_m, "m0": m0, "n_l": n_l, "channels": n_m * n_l,
                    "window_start_step": int(s0 + W), "pulse_steps": int(T / dt), "ground_state_energy": float(e_gs)},
         "gpu_launches": int(launches),
-        "roofline": {"bound": "fp64", "kernel": "k_dgemm (m,l) transforms with their pairing steps (CUDA events around each transform)",
-                     "achieved": tfl, "peak": peak["tflops"], "peak_source": peak["source"],
-                     "unit": "TFLOP/s", "frac": tfl / peak["tflops"] if tfl else None, "flops_per_step": gemm_flops,
-                     "transform_ms_per_step": tr_ms / K, "share_of_step": tr_ms / dev_ms},
+        "roofline": c1_roofline(gemm_flops, tr_ms, tr_n, K, dev_ms, peak),
         "kernels": {k: {"ms_total": v[0], "launch_groups": v[1]} for k, v in ktimes.items()},
         "norm_drift_over_window": abs(n1 - n0) / n0,
         "setup_s": setup_s,
         "clocks": clocks,
     }
     return line
+
+
+def c1_roofline(gemm_flops, tr_ms, tr_n, K, dev_ms, peak):
+    """Roofline of the C1 transforms.  With the slice-product GEMM (the default) every FP64 product
+    is 45 bf16 digit-pair products on the tensor cores: the bound is the tensor pipe, achieved =
+    45 x the FP64 flops / transform time against the measured bf16 peak, and the FP64-equivalent
+    rate is reported beside it against the FP64 (DFMA) peak.  With QPC_VG_GEMM=dfma the bound is
+    the FP64 pipe."""
+    tfl = gemm_flops * K / (tr_ms * 1e-3) / 1e12 if tr_n else None
+    common = {"transform_ms_per_step": tr_ms / K, "share_of_step": tr_ms / dev_ms, "fp64_flops_per_step": gemm_flops}
+    if os.environ.get("QPC_VG_GEMM", "slices") == "dfma":
+        return {"bound": "fp64", "kernel": "k_dgemm (m,l) transforms with their pairing steps (CUDA events around each transform)",
+                "achieved": tfl, "peak": peak["tflops"], "peak_source": peak["source"], "unit": "TFLOP/s",
+                "frac": tfl / peak["tflops"] if tfl else None, **common}
+    bf = load_peaks().get("bf16_tflops")
+    ach = 45 * tfl if tfl else None
+    return {"bound": "tensor", "kernel": "k_oz_gemm slice products (9 x 7-bit digits, 45 bf16 pair products per FP64 product) "
+                                         "with splitting and pairing steps (CUDA events around each transform)",
+            "achieved": ach, "peak": bf, "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst, cuBLAS)", "unit": "TFLOP/s",
+            "frac": ach / bf if (ach and bf) else None, "traffic": None,
+            "fp64_equivalent": {"achieved": tfl, "peak": peak["tflops"], "peak_source": peak["source"],
+                                "ratio_to_fp64_peak": tfl / peak["tflops"] if tfl else None},
+            **common}
 
 
 def arnoldi_flops(n_r, p, n_l, kmax):

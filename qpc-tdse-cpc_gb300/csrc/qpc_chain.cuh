@@ -101,12 +101,6 @@ __device__ __forceinline__ chain_desc describe(long ch, long nchains, const int6
 
 __device__ __forceinline__ double part_of(double2 v, int part) { return part ? v.y : v.x; }
 
-// own part of (l * v), complex l and v
-__device__ __forceinline__ double cmul_part(double2 l, double vr, double vi, int part)
-{
-	return part ? fma(l.x, vi, l.y * vr) : fma(l.x, vr, -l.y * vi);
-}
-
 // operands for acc -= part(l * v) as two FMAs, acc = fma(-l.x, u, fma(l.y, w, acc)):
 // real part u = vr, w = vi; imaginary part u = vi, w = -vr (sign flip as an integer op)
 __device__ __forceinline__ void msub_operands(double vr, double vi, int part, double& u, double& w)
@@ -114,6 +108,17 @@ __device__ __forceinline__ void msub_operands(double vr, double vi, int part, do
 	u = part ? vi : vr;
 	w = part ? __longlong_as_double(__double_as_longlong(vr) ^ (long long)0x8000000000000000ull) : vi;
 }
+
+// own part of (l * v), complex l and v, as l.x u - l.y w with the operands of msub_operands: the
+// same two FP64 instructions on both parts (a select between two FP64 expressions would make a
+// warp with both parts issue both)
+__device__ __forceinline__ double cmul_part(double2 l, double vr, double vi, int part)
+{
+	double u, w;
+	msub_operands(vr, vi, part, u, w);
+	return fma(l.x, u, -l.y * w);
+}
+
 
 // warps per block of k_chain: one staged S band serves every warp of a block (the launch chooses
 // 1..CHAIN_MAXW warps; 4 unless the engine is told otherwise)
@@ -546,9 +551,14 @@ __global__ void __launch_bounds__(128) k_chain_seg(double2* __restrict__ X, cons
 				for (int k = 1; k <= P; ++k) ln[k - 1] = (nlive && t + 1 - k >= 0) ? fs[(long)(r + 1) * NE + k - 1] : make_double2(0.0, 0.0);
 				const double wnext = nlive ? wv[2L * (r + 1)] : 0.0;
 				double acc = live ? wcur : 0.0;
+				// own part of acc - l y with the same two FMAs on both parts (operands chosen by
+				// integer selects, so the warp issues no FP64 instruction twice)
 #pragma unroll
-				for (int k = 0; k < P; ++k)
-					acc = part ? fma(-l[k].x, hi[k], fma(-l[k].y, hr[k], acc)) : fma(-l[k].x, hr[k], fma(l[k].y, hi[k], acc));
+				for (int k = 0; k < P; ++k) {
+					double u, w;
+					msub_operands(hr[k], hi[k], part, u, w);
+					acc = fma(-l[k].x, u, fma(l[k].y, w, acc));
+				}
 				const double other = __shfl_xor_sync(FULL, acc, 1);
 #pragma unroll
 				for (int k = P - 1; k >= 1; --k) { hr[k] = hr[k - 1]; hi[k] = hi[k - 1]; }
@@ -580,7 +590,9 @@ __global__ void __launch_bounds__(128) k_chain_seg(double2* __restrict__ X, cons
 							const int jj = h * HJ + q;
 							if (jj < P) {
 								const double2 ph = cfw[(sg * P + i) * P + jj], xv = xc[c][sg - 1][jj];
-								v = part ? fma(ph.x, xv.y, fma(ph.y, xv.x, v)) : fma(ph.x, xv.x, fma(-ph.y, xv.y, v));
+								double u, w;
+								msub_operands(xv.x, xv.y, part, u, w);	// own part of ph xv = ph.x u - ph.y w
+								v = fma(ph.x, u, fma(-ph.y, w, v));
 							}
 						}
 					}
@@ -631,9 +643,14 @@ __global__ void __launch_bounds__(128) k_chain_seg(double2* __restrict__ X, cons
 				for (int k = 1; k <= P; ++k) ln[k - 1] = (nlive && t + 1 - k >= 0) ? fs[(long)(r - 1 + k) * NE + k - 1] : make_double2(0.0, 0.0);
 				const double wnext = nlive ? wv[2L * (r - 1)] : 0.0;
 				double acc = live ? wcur : 0.0;
+				// own part of acc - l y with the same two FMAs on both parts (operands chosen by
+				// integer selects, so the warp issues no FP64 instruction twice)
 #pragma unroll
-				for (int k = 0; k < P; ++k)
-					acc = part ? fma(-l[k].x, hi[k], fma(-l[k].y, hr[k], acc)) : fma(-l[k].x, hr[k], fma(l[k].y, hi[k], acc));
+				for (int k = 0; k < P; ++k) {
+					double u, w;
+					msub_operands(hr[k], hi[k], part, u, w);
+					acc = fma(-l[k].x, u, fma(l[k].y, w, acc));
+				}
 				const double other = __shfl_xor_sync(FULL, acc, 1);
 #pragma unroll
 				for (int k = P - 1; k >= 1; --k) { hr[k] = hr[k - 1]; hi[k] = hi[k - 1]; }
@@ -663,7 +680,9 @@ __global__ void __launch_bounds__(128) k_chain_seg(double2* __restrict__ X, cons
 							const int jj = h * HJ + q;
 							if (jj < P) {
 								const double2 ph = cbw[(sg * P + i) * P + jj], xv = xc[c][sg + 1][jj];
-								v = part ? fma(ph.x, xv.y, fma(ph.y, xv.x, v)) : fma(ph.x, xv.x, fma(-ph.y, xv.y, v));
+								double u, w;
+								msub_operands(xv.x, xv.y, part, u, w);	// own part of ph xv = ph.x u - ph.y w
+								v = fma(ph.x, u, fma(-ph.y, w, v));
 							}
 						}
 					}

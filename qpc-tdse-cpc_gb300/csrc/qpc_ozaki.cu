@@ -71,7 +71,8 @@ __global__ void k_oz_split(operand o, long K, long J, long Kp, const int* __rest
 	}
 }
 
-// digit pairs (s, t) with s + t < NS, in the order the product visits them
+// digit pairs (s, t) with s + t < NS in order of their level d = s + t: the levels 0..3 (the first
+// LOPAIR pairs) and 4..NS-1 are summed by separate launches, each with one int64 accumulator
 struct pair_table {
 	unsigned char s[NS * (NS + 1) / 2], t[NS * (NS + 1) / 2];
 };
@@ -79,11 +80,12 @@ __host__ __device__ constexpr pair_table make_pairs()
 {
 	pair_table p{};
 	int q = 0;
-	for (int s = 0; s < NS; ++s)
-		for (int t = 0; s + t < NS; ++t) { p.s[q] = (unsigned char)s; p.t[q] = (unsigned char)t; ++q; }
+	for (int d = 0; d < NS; ++d)
+		for (int s = 0; s <= d; ++s) { p.s[q] = (unsigned char)s; p.t[q] = (unsigned char)(d - s); ++q; }
 	return p;
 }
 constexpr int NPAIR = NS * (NS + 1) / 2;
+constexpr int LOPAIR = 10;	// pairs of levels 0..3
 __constant__ pair_table c_pairs = make_pairs();
 
 // the product's pipeline: one stage holds a 64 x 64 digit tile of A (rows of the output tile, 64
@@ -127,10 +129,14 @@ __device__ __forceinline__ void advance(cursor& c, long Kp)
 // Db [NS][M][Kp] and the exponent fields ea [n], eb [M]; out(i, j) at
 // out + (j / jdiv) * jouter + i * istride + (j % jdiv).  128 threads, output tile 64 x 64 (warps
 // 2 x 2 of 32 x 32), NSTAGE-deep cp.async pipeline over the (pair, chunk, k) stages.
+// HI = true: the pairs of levels 0..3, their exact sum (units of 2^-35) stored to hsum [n][M];
+// HI = false: the pairs of levels 4..NS-1 (units of 2^-70), combined with hsum into out.
+template <bool HI>
 __global__ void __launch_bounds__(THREADS) k_oz_gemm(const __nv_bfloat16* __restrict__ Da, const int* __restrict__ ea,
-	const __nv_bfloat16* __restrict__ Db, const int* __restrict__ eb, long n, long M, long Kp, double* __restrict__ out, long istride,
-	long jdiv, long jouter)
+	const __nv_bfloat16* __restrict__ Db, const int* __restrict__ eb, long n, long M, long Kp, long long* __restrict__ hsum,
+	double* __restrict__ out, long istride, long jdiv, long jouter)
 {
+	constexpr int P0 = HI ? 0 : LOPAIR, P1 = HI ? LOPAIR : NPAIR;
 	extern __shared__ __align__(128) __nv_bfloat16 sm[];
 	const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 	const int gid = lane >> 2, tig = lane & 3;
@@ -141,7 +147,7 @@ __global__ void __launch_bounds__(THREADS) k_oz_gemm(const __nv_bfloat16* __rest
 
 	// producer: stage of cursor c into slot
 	auto load_stage = [&](const cursor& c, int slot) {
-		if (c.p >= NPAIR) return;
+		if (c.p >= P1) return;
 		const long kc1 = c.kc0 + KC < Kp ? c.kc0 + KC : Kp;
 		const __nv_bfloat16* A = Da + (long)c_pairs.s[c.p] * sa;
 		const __nv_bfloat16* B = Db + (long)c_pairs.t[c.p] * sb;
@@ -159,16 +165,16 @@ __global__ void __launch_bounds__(THREADS) k_oz_gemm(const __nv_bfloat16* __rest
 		}
 	};
 
-	long long hi[2][4][4], lo[2][4][4];
+	long long isum[2][4][4];
 	float acc[2][4][4];
 #pragma unroll
 	for (int i = 0; i < 2; ++i)
 #pragma unroll
 		for (int j = 0; j < 4; ++j)
 #pragma unroll
-			for (int q = 0; q < 4; ++q) { hi[i][j][q] = lo[i][j][q] = 0; acc[i][j][q] = 0.f; }
+			for (int q = 0; q < 4; ++q) { isum[i][j][q] = 0; acc[i][j][q] = 0.f; }
 
-	cursor prod{0, 0, 0}, cons{0, 0, 0};
+	cursor prod{P0, 0, 0}, cons{P0, 0, 0};
 #pragma unroll
 	for (int st = 0; st < NSTAGE - 1; ++st) {
 		load_stage(prod, st);
@@ -176,7 +182,7 @@ __global__ void __launch_bounds__(THREADS) k_oz_gemm(const __nv_bfloat16* __rest
 		advance(prod, Kp);
 	}
 	int slot = 0;
-	while (cons.p < NPAIR) {
+	while (cons.p < P1) {
 		asm volatile("cp.async.wait_group %0;\n" ::"n"(NSTAGE - 2));
 		__syncthreads();
 		// refill the slot consumed in the previous iteration
@@ -222,9 +228,7 @@ __global__ void __launch_bounds__(THREADS) k_oz_gemm(const __nv_bfloat16* __rest
 				for (int j = 0; j < 4; ++j)
 #pragma unroll
 					for (int q = 0; q < 4; ++q) {
-						const long long v = (long long)__float2int_rn(acc[i][j][q]) << sh;
-						if (d <= 3) hi[i][j][q] += v;
-						else lo[i][j][q] += v;
+						isum[i][j][q] += (long long)__float2int_rn(acc[i][j][q]) << sh;
 						acc[i][j][q] = 0.f;
 					}
 		}
@@ -242,12 +246,14 @@ __global__ void __launch_bounds__(THREADS) k_oz_gemm(const __nv_bfloat16* __rest
 				const long row = rowA0 + wm + i * 16 + gid + 8 * (q >> 1);
 				const long col = rowB0 + wn + j * 8 + tig * 2 + (q & 1);
 				if (row >= n || col >= M) continue;
+				if (HI) { hsum[row * M + col] = isum[i][j][q]; continue; }
+				const long long hi = hsum[row * M + col], lo = isum[i][j][q];
 				const int ef_a = ea[row], ef_b = eb[col];
 				const int e = (ef_a ? ef_a - 1022 : -1022) + (ef_b ? ef_b - 1022 : -1022);
 				// the exact total T = hi 2^35 + lo (units of 2^-70) as th 2^30 + tl with both parts
 				// exact in FP64 (|th| < 2^53 for K <= 4096, 0 <= tl < 2^30): one rounding, in the fma
-				const long long th = hi[i][j][q] * 32 + (lo[i][j][q] >> 30);
-				const long long tl = lo[i][j][q] & ((1ll << 30) - 1);
+				const long long th = hi * 32 + (lo >> 30);
+				const long long tl = lo & ((1ll << 30) - 1);
 				const double v = fma((double)th, 0x1p-40, (double)tl * 0x1p-70);
 				const long qq = col / jdiv, rr = col - qq * jdiv;
 				out[qq * jouter + row * istride + rr] = scalbn(v, e);
@@ -283,14 +289,23 @@ int oz_gemm(const __nv_bfloat16* Da, const int* ea, const __nv_bfloat16* Db, con
 	if (gy > 65535 || gx > 2147483647L) { set_error("oz_gemm: too large"); return QPC_ERR_ARGS; }
 	static bool attr = false;	// the opt-in shared-memory size, once per process (all devices alike)
 	if (!attr) {
-		if (cudaFuncSetAttribute(oz::k_oz_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)oz::GEMM_SMEM) != cudaSuccess) {
+		if (cudaFuncSetAttribute(oz::k_oz_gemm<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)oz::GEMM_SMEM) != cudaSuccess ||
+			cudaFuncSetAttribute(oz::k_oz_gemm<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)oz::GEMM_SMEM) != cudaSuccess) {
 			set_error("oz_gemm: shared-memory attribute");
 			return QPC_ERR_CUDA;
 		}
 		attr = true;
 	}
-	oz::k_oz_gemm<<<dim3((unsigned)gx, (unsigned)gy), oz::THREADS, oz::GEMM_SMEM, st>>>(Da, ea, Db, eb, n, M, oz::pad16(K), out, istride,
-		jdiv, jouter);
+	// the exact sums of the digit levels 0..3, from the first launch to the second (stream-ordered)
+	long long* hsum = nullptr;
+	if (cudaMallocAsync((void**)&hsum, sizeof(long long) * (size_t)n * (size_t)M, st) != cudaSuccess) {
+		set_error("oz_gemm: cudaMallocAsync of %ld x %ld level sums", n, M);
+		return QPC_ERR_NOMEM;
+	}
+	const dim3 grid((unsigned)gx, (unsigned)gy);
+	oz::k_oz_gemm<true><<<grid, oz::THREADS, oz::GEMM_SMEM, st>>>(Da, ea, Db, eb, n, M, oz::pad16(K), hsum, out, istride, jdiv, jouter);
+	oz::k_oz_gemm<false><<<grid, oz::THREADS, oz::GEMM_SMEM, st>>>(Da, ea, Db, eb, n, M, oz::pad16(K), hsum, out, istride, jdiv, jouter);
+	cudaFreeAsync(hsum, st);
 	return cudaGetLastError() == cudaSuccess ? QPC_OK : QPC_ERR_CUDA;
 }
 
