@@ -456,6 +456,57 @@ __global__ void k_spikes(const double2* __restrict__ fac, double2* __restrict__ 
 	seg_spike<P>(fac + blk * (long)N * (P + 1), N, a, b, j + 1, dir == 0, (dir == 0 ? spf : spb) + blk * (long)N * P);
 }
 
+// One segment's recurrence with zero history, for the forward (L^-1, rows a .. b-1) or the backward
+// (L^-T, rows b-1 .. a) solve: lane pair (part 0, 1) of a segment, work vector wv (own part, stride
+// 2 doubles), factor rows fs (L(r, r-k) at fs[r (P+1) + k - 1]).  The factor entries and the value
+// of the next row are fetched one row ahead.
+template <int P, bool FWD>
+__device__ __forceinline__ void seg_recurrence(double* wv, const double2* fs, int a, int b, int Ls, bool on, int part)
+{
+	constexpr int NE = P + 1;
+	const unsigned FULL = 0xffffffffu;
+	double hr[P], hi[P];
+	double2 l[P], ln[P];
+#pragma unroll
+	for (int k = 0; k < P; ++k) { hr[k] = 0.0; hi[k] = 0.0; l[k] = make_double2(0.0, 0.0); }
+	const int r0 = FWD ? a : b - 1;
+	double wcur = (on && a < b) ? wv[2L * r0] : 0.0;
+	for (int t = 0; t < Ls; ++t) {
+		const int r = FWD ? a + t : b - 1 - t;
+		const int rn = FWD ? r + 1 : r - 1;
+		const bool live = on && t < b - a;
+		const bool nlive = on && t + 1 < b - a;
+#pragma unroll
+		for (int k = 1; k <= P; ++k) {
+			const long li = FWD ? (long)rn * NE + (k - 1) : (long)(rn + k) * NE + (k - 1);	// L(rn, rn-k) | L(rn+k, rn)
+			ln[k - 1] = (nlive && t + 1 - k >= 0) ? fs[li] : make_double2(0.0, 0.0);
+		}
+		const double wnext = nlive ? wv[2L * rn] : 0.0;
+		double acc = live ? wcur : 0.0;
+		// own part of acc - l y with the same two FMAs on both parts (operands chosen by integer
+		// selects, so the warp issues no FP64 instruction twice)
+#pragma unroll
+		for (int k = 0; k < P; ++k) {
+			double u, w;
+			msub_operands(hr[k], hi[k], part, u, w);
+			acc = fma(-l[k].x, u, fma(l[k].y, w, acc));
+		}
+		const double other = __shfl_xor_sync(FULL, acc, 1);
+#pragma unroll
+		for (int k = P - 1; k >= 1; --k) { hr[k] = hr[k - 1]; hi[k] = hi[k - 1]; }
+		hr[0] = part ? other : acc;
+		hi[0] = part ? acc : other;
+		if (live) wv[2L * r] = acc;
+#pragma unroll
+		for (int k = 0; k < P; ++k) l[k] = ln[k];
+		wcur = wnext;
+	}
+}
+
+// threads of a k_chain_seg block: the sequential parts run on one warp per chain, the passes over
+// all rows on every warp (8 warps: two per SM sub-partition, to hide the latency of their loads)
+constexpr int SEG_THREADS = 256;
+
 // Shared memory of k_chain_seg, in double2 units: the factor block [N][P+1] when SFAC, the work
 // vectors [NC][N], and the spike rows the carry chains read, forward [Q][P][P] and backward [Q][P][P].
 __host__ __device__ inline long seg_smem_elems(int N, int P, int NC, int Q, bool sfac)
@@ -465,13 +516,13 @@ __host__ __device__ inline long seg_smem_elems(int N, int P, int NC, int Q, bool
 
 // One block per chain (field-free) or per (+s, -s) pair (coupling); the same passes as k_chain, with
 // the recurrences segmented.  spf/spb: the spikes of every factor block, [block][N][P], block =
-// foff / (N (P+1)).  128 threads; segment lanes: warp c handles chain c, lane = 2 segment + part.
+// foff / (N (P+1)).  SEG_THREADS threads; segment lanes: warp c handles chain c, lane = 2 segment + part.
 // The chain is latency-bound (a few dozen blocks in flight), so everything the sequential parts
 // read sits in shared memory: the work vectors always, the rows of the spikes that the carry
 // chains read (P per segment boundary), and the factor block when it fits (SFAC); the passes
 // over all rows (S z, the fix-ups) read the band and the spikes through L1/L2 in parallel.
 template <int P, bool CPL, bool SFAC>
-__global__ void __launch_bounds__(128) k_chain_seg(double2* __restrict__ X, const double2* __restrict__ fac,
+__global__ void __launch_bounds__(SEG_THREADS, 1) k_chain_seg(double2* __restrict__ X, const double2* __restrict__ fac,
 	const double2* __restrict__ spf, const double2* __restrict__ spb, const double* __restrict__ S, const int64_t* __restrict__ nta,
 	long step, int jslot, int B, int M, int m0, int N, int L, int np, long chbase, long nchains, int Q, int Ls,
 	const int* __restrict__ ffmap, long ffstride, int cmode)
@@ -503,13 +554,19 @@ __global__ void __launch_bounds__(128) k_chain_seg(double2* __restrict__ X, cons
 	double2* wsh = seg_sm + (SFAC ? (long)N * NE : 0L);
 	double2* cfw = wsh + (long)NC * N;	// [sg][i][jj]: forward spike at row sg Ls - 1 - i, sg = 1 .. Q-1
 	double2* cbw = cfw + Q * P * P;	// [sg][i][jj]: backward spike at row (sg + 1) Ls + i, sg = 0 .. Q-2
-	if (SFAC)
-		for (int t = tid; t < N * NE; t += blockDim.x) fsh[t] = fblk[t];
+	if (SFAC) {
+		// the factor block, 16-byte asynchronous copies (all in flight at once)
+		const uint32_t fbase = (uint32_t)__cvta_generic_to_shared(fsh);
+		for (int t = tid; t < N * NE; t += blockDim.x)
+			asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(fbase + 16u * (uint32_t)t), "l"(fblk + t));
+		asm volatile("cp.async.commit_group;\n" ::);
+	}
 	for (int t = tid; t < (Q - 1) * P * P; t += blockDim.x) {
 		const int jj = t % P, i = (t / P) % P, sg = t / (P * P);
 		cfw[((sg + 1) * P + i) * P + jj] = spfb[(long)((sg + 1) * Ls - 1 - i) * P + jj];
 		cbw[(sg * P + i) * P + jj] = spbb[(long)((sg + 1) * Ls + i) * P + jj];
 	}
+	if (SFAC) asm volatile("cp.async.wait_group 0;\n" ::);
 	__syncthreads();
 	const double2* fs = SFAC ? fsh : fblk;
 	double* Xd = reinterpret_cast<double*>(X);
@@ -534,41 +591,8 @@ __global__ void __launch_bounds__(128) k_chain_seg(double2* __restrict__ X, cons
 		// ---- P2a: y0 = L^-1 w per segment (zero history), lane = 2 segment + part
 		if (warp < NC) {
 			const int c = warp, seg = lane >> 1, part = lane & 1;
-			const bool on = app < s_a[c] && seg < Q;
-			const int a = seg * Ls, b = min(N, a + Ls);
-			double* wv = reinterpret_cast<double*>(wsh + c * N) + part;
-			double hr[P], hi[P];
-			double2 l[P], ln[P];
-#pragma unroll
-			for (int k = 0; k < P; ++k) { hr[k] = 0.0; hi[k] = 0.0; l[k] = make_double2(0.0, 0.0); }	// row a: no history
-			double wcur = (on && a < b) ? wv[2L * a] : 0.0;
-			for (int t = 0; t < Ls; ++t) {
-				const int r = a + t;
-				const bool live = on && r < b;
-				// the next row's factor entries and value, one row ahead
-				const bool nlive = on && r + 1 < b;
-#pragma unroll
-				for (int k = 1; k <= P; ++k) ln[k - 1] = (nlive && t + 1 - k >= 0) ? fs[(long)(r + 1) * NE + k - 1] : make_double2(0.0, 0.0);
-				const double wnext = nlive ? wv[2L * (r + 1)] : 0.0;
-				double acc = live ? wcur : 0.0;
-				// own part of acc - l y with the same two FMAs on both parts (operands chosen by
-				// integer selects, so the warp issues no FP64 instruction twice)
-#pragma unroll
-				for (int k = 0; k < P; ++k) {
-					double u, w;
-					msub_operands(hr[k], hi[k], part, u, w);
-					acc = fma(-l[k].x, u, fma(l[k].y, w, acc));
-				}
-				const double other = __shfl_xor_sync(FULL, acc, 1);
-#pragma unroll
-				for (int k = P - 1; k >= 1; --k) { hr[k] = hr[k - 1]; hi[k] = hi[k - 1]; }
-				hr[0] = part ? other : acc;
-				hi[0] = part ? acc : other;
-				if (live) wv[2L * r] = acc;
-#pragma unroll
-				for (int k = 0; k < P; ++k) l[k] = ln[k];
-				wcur = wnext;
-			}
+			const int a0 = seg * Ls, b0 = min(N, a0 + Ls);
+			seg_recurrence<P, true>(reinterpret_cast<double*>(wsh + c * N) + part, fs, a0, b0, Ls, app < s_a[c] && seg < Q, part);
 		}
 		__syncthreads();
 		// ---- P2b: forward carries x(s)_i = y(a_s - 1 - i), s = 1..Q-1.  lane = 16 h + 2 i + part: the
@@ -627,40 +651,8 @@ __global__ void __launch_bounds__(128) k_chain_seg(double2* __restrict__ X, cons
 		// ---- P4a: x0 = L^-T y per segment (zero history above), descending
 		if (warp < NC) {
 			const int c = warp, seg = lane >> 1, part = lane & 1;
-			const bool on = app < s_a[c] && seg < Q;
-			const int a = seg * Ls, b = min(N, a + Ls);
-			double* wv = reinterpret_cast<double*>(wsh + c * N) + part;
-			double hr[P], hi[P];
-			double2 l[P], ln[P];
-#pragma unroll
-			for (int k = 0; k < P; ++k) { hr[k] = 0.0; hi[k] = 0.0; l[k] = make_double2(0.0, 0.0); }	// row b-1: no history
-			double wcur = (on && b - 1 >= a) ? wv[2L * (b - 1)] : 0.0;
-			for (int t = 0; t < Ls; ++t) {
-				const int r = b - 1 - t;
-				const bool live = on && r >= a;
-				const bool nlive = on && r - 1 >= a;
-#pragma unroll
-				for (int k = 1; k <= P; ++k) ln[k - 1] = (nlive && t + 1 - k >= 0) ? fs[(long)(r - 1 + k) * NE + k - 1] : make_double2(0.0, 0.0);
-				const double wnext = nlive ? wv[2L * (r - 1)] : 0.0;
-				double acc = live ? wcur : 0.0;
-				// own part of acc - l y with the same two FMAs on both parts (operands chosen by
-				// integer selects, so the warp issues no FP64 instruction twice)
-#pragma unroll
-				for (int k = 0; k < P; ++k) {
-					double u, w;
-					msub_operands(hr[k], hi[k], part, u, w);
-					acc = fma(-l[k].x, u, fma(l[k].y, w, acc));
-				}
-				const double other = __shfl_xor_sync(FULL, acc, 1);
-#pragma unroll
-				for (int k = P - 1; k >= 1; --k) { hr[k] = hr[k - 1]; hi[k] = hi[k - 1]; }
-				hr[0] = part ? other : acc;
-				hi[0] = part ? acc : other;
-				if (live) wv[2L * r] = acc;
-#pragma unroll
-				for (int k = 0; k < P; ++k) l[k] = ln[k];
-				wcur = wnext;
-			}
+			const int a0 = seg * Ls, b0 = min(N, a0 + Ls);
+			seg_recurrence<P, false>(reinterpret_cast<double*>(wsh + c * N) + part, fs, a0, b0, Ls, app < s_a[c] && seg < Q, part);
 		}
 		__syncthreads();
 		// ---- P4b: backward carries x(s)_i = x(b_s + i), s = Q-2 .. 0, lanes as in P2b

@@ -618,11 +618,11 @@ void launch_chain_seg(qpc_lgwz* h, cudaStream_t st, int b0, double2* X, const do
 	unsigned grid = (unsigned)(nch / (CPL ? 2 : 1));
 	const size_t smem = h->seg_smem[CPL];
 	if (h->seg_sfac[CPL])
-		k_chain_seg<P, CPL, true><<<grid, 128, smem, st>>>(X, fac, CPL ? h->spf_c : h->spf_ff, CPL ? h->spb_c : h->spb_ff, h->S, nta, step,
+		k_chain_seg<P, CPL, true><<<grid, SEG_THREADS, smem, st>>>(X, fac, CPL ? h->spf_c : h->spf_ff, CPL ? h->spb_c : h->spb_ff, h->S, nta, step,
 			jslot, h->B, h->M, h->d.m0, h->N, h->L, h->npair, chbase, chbase + nch, h->Q, h->Ls, CPL ? nullptr : h->ffmap_cur,
 			(long)h->nlh * h->N * (h->P + 1), h->cmode);
 	else
-		k_chain_seg<P, CPL, false><<<grid, 128, smem, st>>>(X, fac, CPL ? h->spf_c : h->spf_ff, CPL ? h->spb_c : h->spb_ff, h->S, nta, step,
+		k_chain_seg<P, CPL, false><<<grid, SEG_THREADS, smem, st>>>(X, fac, CPL ? h->spf_c : h->spf_ff, CPL ? h->spb_c : h->spb_ff, h->S, nta, step,
 			jslot, h->B, h->M, h->d.m0, h->N, h->L, h->npair, chbase, chbase + nch, h->Q, h->Ls, CPL ? nullptr : h->ffmap_cur,
 			(long)h->nlh * h->N * (h->P + 1), h->cmode);
 	LAUNCH(h);
