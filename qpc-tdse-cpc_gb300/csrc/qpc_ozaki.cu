@@ -5,6 +5,7 @@
 #include "qpc_ozaki.cuh"
 #include <cuda_runtime.h>
 #include <vector>
+#include <cstdlib>
 
 namespace qpc {
 namespace oz {
@@ -260,9 +261,270 @@ __global__ void __launch_bounds__(THREADS) k_oz_gemm(const __nv_bfloat16* __rest
 			}
 }
 
+// ---------------------------------------------------------------- tcgen05 form of the product
+// The same digit-pair products on the 5th-generation tensor cores: one thread issues
+// tcgen05.mma.cta_group::1.kind::f16 (bf16 x bf16 -> fp32, M = 128, N = 64, K = 16) on operand tiles
+// in shared memory (the 128-byte-swizzled K-major layout that cp.async writes: 16-byte chunk c of row r
+// at c ^ (r & 7), 8-row groups 1024 bytes apart); the fp32 accumulator of an output tile lives in 64
+// columns of tensor memory.  Each stage's MMAs are committed to that stage's mbarrier, which frees the
+// stage for the next cp.async refill.  At the end of an exact-sum chunk every thread reads its output
+// row from tensor memory (tcgen05.ld) into its int64 level accumulators, and the next chunk starts the
+// accumulator afresh.  Every mbarrier wait is bounded: a wait that runs out sets *err and the kernel
+// finishes without waiting further (the host reports QPC_ERR_TIMEOUT).
+// tile 128 x 128 (M x N), 8 warps: warps w and w + 4 read the tensor-memory lanes 32 (w % 4) .. + 31,
+// columns 64 (w / 4) .. + 63, so a thread holds 64 outputs of one row; 6 stages of 32 KB, one CTA per SM
+constexpr int TC_M = 128, TC_N = 128, TC_KS = 64, TC_NST = 6, TC_THREADS = 256, TC_COLS_T = 64;
+constexpr uint32_t TC_A_BYTES = TC_M * TC_KS * 2, TC_B_BYTES = TC_N * TC_KS * 2, TC_STAGE_BYTES = TC_A_BYTES + TC_B_BYTES;
+constexpr uint32_t TC_TMEM_COLS = 128;
+constexpr size_t TC_SMEM = (size_t)TC_STAGE_BYTES * TC_NST + 1024 + 8 * TC_NST + 16;
+// instruction descriptor, kind::f16: D fp32 (bits 4-5 = 1), A and B bf16 (bits 7-9, 10-12 = 1), both
+// K-major (bits 15, 16 = 0), N >> 3 at bits 17-22, M >> 4 at bits 24-28
+constexpr uint32_t TC_IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(TC_N >> 3) << 17) | ((uint32_t)(TC_M >> 4) << 24);
+
+// shared-memory matrix descriptor of a 128-byte-swizzled K-major tile at byte address saddr: start
+// address >> 4 (bits 0-13), leading byte offset 16 (encoded 1, unused for this layout), stride byte
+// offset 1024 between 8-row groups (bits 32-45), descriptor version 1 (bits 46-47), swizzle mode
+// 128B (2 at bits 61-63)
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr)
+{
+	return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)1 << 16) | ((uint64_t)(1024 >> 4) << 32) | ((uint64_t)1 << 46) |
+		((uint64_t)2 << 61);
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t a, uint32_t count)
+{
+	asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(a), "r"(count) : "memory");
+}
+
+// bounded wait for the completion of the phase with the given parity
+__device__ __forceinline__ bool mbar_wait(uint32_t a, uint32_t parity)
+{
+	for (long it = 0; it < (1L << 22); ++it) {
+		uint32_t ok;
+		asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n}\n"
+			: "=r"(ok) : "r"(a), "r"(parity) : "memory");
+		if (ok) return true;
+	}
+	return false;
+}
+
+__device__ __forceinline__ void tc_mma(uint32_t tmem, uint64_t adesc, uint64_t bdesc, uint32_t accumulate)
+{
+	asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\ttcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n"
+		::"r"(tmem), "l"(adesc), "l"(bdesc), "r"(TC_IDESC), "r"(accumulate) : "memory");
+}
+
+__device__ __forceinline__ void tc_commit(uint32_t mbar)
+{
+	asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(mbar) : "memory");
+}
+
+// 32 consecutive fp32 columns of this thread's tensor-memory lane
+__device__ __forceinline__ void tc_ld32(uint32_t taddr, uint32_t (&v)[32])
+{
+	asm volatile("tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+		"%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];\n"
+		: "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]), "=r"(v[8]), "=r"(v[9]),
+		  "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]),
+		  "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]), "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]),
+		  "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+		: "r"(taddr));
+	asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+}
+
+template <bool HI>
+__global__ void __launch_bounds__(TC_THREADS, 1) k_oz_gemm_tc(const __nv_bfloat16* __restrict__ Da, const int* __restrict__ ea,
+	const __nv_bfloat16* __restrict__ Db, const int* __restrict__ eb, long n, long M, long Kp, long long* __restrict__ hsum,
+	double* __restrict__ out, long istride, long jdiv, long jouter, int* __restrict__ err)
+{
+	constexpr int P0 = HI ? 0 : LOPAIR, P1 = HI ? LOPAIR : NPAIR;
+	extern __shared__ __align__(1024) unsigned char tsm[];
+	const uint32_t sraw = smem_u32(tsm);
+	const uint32_t sbase = (sraw + 1023u) & ~1023u;	// stages at 1024-byte boundaries (the swizzle's period)
+	const uint32_t bars = sbase + TC_STAGE_BYTES * TC_NST;	// TC_NST mbarriers, then the tensor-memory address
+	const uint32_t tslot = bars + 8 * TC_NST;
+	const int tid = threadIdx.x, warp = tid >> 5;
+	const long rowA0 = (long)blockIdx.y * TC_M, rowB0 = (long)blockIdx.x * TC_N;
+	const long sa = n * Kp, sb = M * Kp;
+
+	if (tid == 0) {
+		for (int q = 0; q < TC_NST; ++q) mbar_init(bars + 8 * q, 1);
+		asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+	}
+	if (warp == 0) {
+		asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(tslot), "r"(TC_TMEM_COLS) : "memory");
+		asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+	}
+	asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+	__syncthreads();
+	asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+	uint32_t tmem;
+	asm volatile("ld.shared.u32 %0, [%1];\n" : "=r"(tmem) : "r"(tslot) : "memory");
+
+	// this thread's copies, fixed for the whole tile: rows r_u = tid / 8 + 32 u of A and of B (u < 4),
+	// 16-byte chunk ch = tid % 8 of each row's 64-wide k window; source offsets without the slice and
+	// the stage's k, destinations within a stage (r_u % 8 is the same for every u)
+	const int ch = tid & 7, r0 = tid >> 3;
+	const uint32_t dofs = (uint32_t)(r0 * 128 + ((ch ^ (r0 & 7)) << 4));
+	// (32-bit: a slice holds fewer than 2^31 digits, checked by the host)
+	constexpr int RSTEP = TC_THREADS / 8, UA = TC_M / RSTEP, UB = TC_N / RSTEP;
+	uint32_t srcA[UA], srcB[UB];
+	unsigned okA = 0, okB = 0;
+#pragma unroll
+	for (int u = 0; u < UA; ++u) {
+		const long row = rowA0 + r0 + RSTEP * u;
+		srcA[u] = (uint32_t)((row < n ? row : 0) * Kp + ch * 8);
+		okA |= (row < n ? 1u : 0u) << u;
+	}
+#pragma unroll
+	for (int u = 0; u < UB; ++u) {
+		const long row = rowB0 + r0 + RSTEP * u;
+		srcB[u] = (uint32_t)((row < M ? row : 0) * Kp + ch * 8);
+		okB |= (row < M ? 1u : 0u) << u;
+	}
+	auto load_stage = [&](const cursor& c, int slot) {
+		if (c.p >= P1) return;
+		const long kc1 = c.kc0 + KC < Kp ? c.kc0 + KC : Kp;
+		const bool kin = c.k0 + ch * 8 < kc1;
+		const __nv_bfloat16* A = Da + (long)c_pairs.s[c.p] * sa + c.k0;
+		const __nv_bfloat16* B = Db + (long)c_pairs.t[c.p] * sb + c.k0;
+		const uint32_t dA = sbase + (uint32_t)slot * TC_STAGE_BYTES + dofs, dB = dA + TC_A_BYTES;
+#pragma unroll
+		for (int u = 0; u < UA; ++u) {
+			const bool v = kin && ((okA >> u) & 1u);
+			cp16(dA + (uint32_t)(u * RSTEP * 128), v ? A + srcA[u] : Da, v);
+		}
+#pragma unroll
+		for (int u = 0; u < UB; ++u) {
+			const bool v = kin && ((okB >> u) & 1u);
+			cp16(dB + (uint32_t)(u * RSTEP * 128), v ? B + srcB[u] : Db, v);
+		}
+	};
+
+	long long isum[TC_COLS_T];
+#pragma unroll
+	for (int j = 0; j < TC_COLS_T; ++j) isum[j] = 0;
+	// stage i is loaded TC_LD stages ahead into the slot of stage i - TC_MD, whose MMAs (committed
+	// TC_MD iterations earlier) must be done: loads TC_LD deep, MMAs TC_MD deep (measured: 1 and
+	// TC_NST - 1 beat 2 and TC_NST - 2, the loads are what the kernel waits for)
+	constexpr int TC_MD = 1, TC_LD = TC_NST - TC_MD;
+	cursor prod{P0, 0, 0}, cons{P0, 0, 0};
+#pragma unroll
+	for (int q = 0; q < TC_LD; ++q) {
+		load_stage(prod, q);
+		asm volatile("cp.async.commit_group;\n" ::);
+		advance(prod, Kp);
+	}
+	uint32_t parity = 0, pending = 0;	// per stage: phase parity to wait for, commit not yet waited for
+	bool fresh = true, ok = true;
+	int slot = 0;
+	const int lq = warp & 3, cbase = (warp >> 2) * TC_COLS_T;	// lane quarter and first column of this warp
+	const uint32_t trow = tmem + ((uint32_t)(lq * 32) << 16) + (uint32_t)cbase;
+	while (cons.p < P1) {
+		asm volatile("cp.async.wait_group %0;\n" ::"n"(TC_LD - 1));
+		asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");	// cp.async data -> the tensor core's view
+		// the block stops together when any thread's wait ran out (no further MMA is issued)
+		if (__syncthreads_or(ok ? 0 : 1)) break;
+		asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+		if (tid == 0) {
+			const uint32_t aS = sbase + (uint32_t)slot * TC_STAGE_BYTES, bS = aS + TC_A_BYTES;
+#pragma unroll
+			for (int kk = 0; kk < TC_KS / 16; ++kk)
+				tc_mma(tmem, sw128_desc(aS + 32u * kk), sw128_desc(bS + 32u * kk), (fresh && kk == 0) ? 0u : 1u);
+			tc_commit(bars + 8 * slot);
+		}
+		pending |= 1u << slot;
+		fresh = false;
+		// refill the slot of stage i - TC_MD (stage i + TC_LD goes there) once its MMAs are done
+		const int prev = (slot + TC_NST - TC_MD) % TC_NST;
+		if (pending & (1u << prev)) {
+			if (ok && !mbar_wait(bars + 8 * prev, (parity >> prev) & 1u)) { ok = false; atomicExch(err, 1); }
+			parity ^= 1u << prev;
+			pending &= ~(1u << prev);
+		}
+		load_stage(prod, prev);
+		asm volatile("cp.async.commit_group;\n" ::);
+		advance(prod, Kp);
+		// end of an exact-sum chunk: the accumulator into the level sums, the next chunk starts afresh
+		const int p = cons.p;
+		advance(cons, Kp);
+		if (cons.p != p || cons.k0 == cons.kc0) {
+			if (ok && !mbar_wait(bars + 8 * slot, (parity >> slot) & 1u)) { ok = false; atomicExch(err, 1); }
+			parity ^= 1u << slot;
+			pending &= ~(1u << slot);
+			asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+			const int d = c_pairs.s[p] + c_pairs.t[p];
+			const int sh = d <= 3 ? BITS * (3 - d) : BITS * (NS - 1 - d);
+#pragma unroll
+			for (int h = 0; h < TC_COLS_T / 32; ++h) {
+				uint32_t v[32];
+				tc_ld32(trow + 32u * h, v);
+#pragma unroll
+				for (int j = 0; j < 32; ++j) isum[32 * h + j] += (long long)__float2int_rn(__uint_as_float(v[j])) << sh;
+			}
+			asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+			fresh = true;
+		}
+		slot = (slot + 1) % TC_NST;
+	}
+	asm volatile("cp.async.wait_group 0;\n" ::);
+	// MMAs still in flight after a wait ran out: wait for their commits (bounded) before the tensor
+	// memory is freed
+	for (int q = 0; q < TC_NST; ++q)
+		if (pending & (1u << q)) mbar_wait(bars + 8 * q, (parity >> q) & 1u);
+	// row i of the tile is tensor-memory lane i: thread (warp, lane) holds output row 32 (warp % 4) + lane,
+	// columns cbase .. cbase + 63
+	const long row = rowA0 + lq * 32 + (tid & 31);
+	if (row < n) {
+		const int ef_a = ea[row];
+#pragma unroll
+		for (int j = 0; j < TC_COLS_T; ++j) {
+			const long col = rowB0 + cbase + j;
+			if (col >= M) continue;
+			if (HI) { hsum[row * M + col] = isum[j]; continue; }
+			const long long hi = hsum[row * M + col], lo = isum[j];
+			const int ef_b = eb[col];
+			const int e = (ef_a ? ef_a - 1022 : -1022) + (ef_b ? ef_b - 1022 : -1022);
+			const long long th = hi * 32 + (lo >> 30);
+			const long long tl = lo & ((1ll << 30) - 1);
+			const double v = fma((double)th, 0x1p-40, (double)tl * 0x1p-70);
+			const long qq = col / jdiv, rr = col - qq * jdiv;
+			out[qq * jouter + row * istride + rr] = scalbn(v, e);
+		}
+	}
+	asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+	__syncthreads();
+	if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(TC_TMEM_COLS) : "memory");
+}
+
 } // namespace oz
 
 size_t oz_digits_elems(long J, long K) { return (size_t)oz::NS * (size_t)J * (size_t)oz::pad16(K); }
+
+// a wait of the tensor-core product that ran out (set by k_oz_gemm_tc, read and cleared by oz_check)
+__device__ int g_oz_err;
+
+// the product on the 5th-generation tensor cores (tcgen05, the default), or with the warp-level
+// mma.sync kernel when QPC_OZ_TC=0 in the environment; both form the same exact sums
+static bool oz_use_tc()
+{
+	const char* e = std::getenv("QPC_OZ_TC");
+	return !(e && std::atoi(e) == 0);
+}
+
+int oz_check(cudaStream_t st)
+{
+	int* ep = nullptr;
+	if (cudaGetSymbolAddress((void**)&ep, g_oz_err) != cudaSuccess) { set_error("oz_check: symbol"); return QPC_ERR_CUDA; }
+	int h = 0;
+	if (int rc = copy_to_host(&h, ep, sizeof(int), st)) return rc;
+	if (h) {
+		cudaMemsetAsync(ep, 0, sizeof(int), st);
+		set_error("tensor-core product: an mbarrier wait ran out");
+		return QPC_ERR_TIMEOUT;
+	}
+	return QPC_OK;
+}
 
 // exponent fields ef[J] and digit slices D[NS][J][pad16(K)] of an operand, enqueued on st
 int oz_split(const oz::operand& o, long K, long J, int* ef, __nv_bfloat16* D, cudaStream_t st)
@@ -301,6 +563,25 @@ int oz_gemm(const __nv_bfloat16* Da, const int* ea, const __nv_bfloat16* Db, con
 	if (cudaMallocAsync((void**)&hsum, sizeof(long long) * (size_t)n * (size_t)M, st) != cudaSuccess) {
 		set_error("oz_gemm: cudaMallocAsync of %ld x %ld level sums", n, M);
 		return QPC_ERR_NOMEM;
+	}
+	if (oz_use_tc() && n * oz::pad16(K) < (1L << 31) && M * oz::pad16(K) < (1L << 31)) {
+		static bool tattr = false;
+		if (!tattr) {
+			if (cudaFuncSetAttribute(oz::k_oz_gemm_tc<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)oz::TC_SMEM) != cudaSuccess ||
+				cudaFuncSetAttribute(oz::k_oz_gemm_tc<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)oz::TC_SMEM) != cudaSuccess) {
+				set_error("oz_gemm: shared-memory attribute (tcgen05)");
+				cudaFreeAsync(hsum, st);
+				return QPC_ERR_CUDA;
+			}
+			tattr = true;
+		}
+		int* ep = nullptr;
+		if (cudaGetSymbolAddress((void**)&ep, g_oz_err) != cudaSuccess) { set_error("oz_gemm: symbol"); cudaFreeAsync(hsum, st); return QPC_ERR_CUDA; }
+		const dim3 tg((unsigned)((M + oz::TC_N - 1) / oz::TC_N), (unsigned)((n + oz::TC_M - 1) / oz::TC_M));
+		oz::k_oz_gemm_tc<true><<<tg, oz::TC_THREADS, oz::TC_SMEM, st>>>(Da, ea, Db, eb, n, M, oz::pad16(K), hsum, out, istride, jdiv, jouter, ep);
+		oz::k_oz_gemm_tc<false><<<tg, oz::TC_THREADS, oz::TC_SMEM, st>>>(Da, ea, Db, eb, n, M, oz::pad16(K), hsum, out, istride, jdiv, jouter, ep);
+		cudaFreeAsync(hsum, st);
+		return cudaGetLastError() == cudaSuccess ? QPC_OK : QPC_ERR_CUDA;
 	}
 	const dim3 grid((unsigned)gx, (unsigned)gy);
 	oz::k_oz_gemm<true><<<grid, oz::THREADS, oz::GEMM_SMEM, st>>>(Da, ea, Db, eb, n, M, oz::pad16(K), hsum, out, istride, jdiv, jouter);
@@ -357,6 +638,7 @@ extern "C" int qpc_dgemm_slices(int64_t n, int64_t M, int64_t K, const double* A
 	if (!rc) rc = oz_gemm(Da, ea, Db, eb, n, M, K, dC, ldc, M, 0, st);
 	if (!rc) cudaEventRecord(e1, st);
 	if (!rc) rc = wait_on(st);
+	if (!rc) rc = oz_check(st);
 	if (!rc && ms) cudaEventElapsedTime(ms, e0, e1);
 	if (!rc) rc = copy_to_host(C, dC, sizeof(double) * (size_t)n * ldc, st);
 	release();

@@ -15,8 +15,9 @@
 // column's power of two) and the pairs left out (s + t >= NS) keep the error near
 // K 2^(ea_i + eb_j - 61), an order of magnitude below the rounding of an FP64 dot product.  The FP64
 // pipe does no work in the inner loops (GB300 issues FP64 at a small fraction of the bf16 tensor
-// rate): splitting uses integer operations on the FP64 bit patterns, and the products run as
-// mma.sync.m16n8k16 bf16 x bf16 -> fp32.
+// rate): splitting uses integer operations on the FP64 bit patterns, and the products run on the
+// tensor cores, as tcgen05.mma with the accumulator in tensor memory (the default) or as the
+// warp-level mma.sync.m16n8k16 bf16 x bf16 -> fp32 (QPC_OZ_TC=0).
 #pragma once
 #include <cuda_runtime.h>
 #include <cuda_bf16.h>
@@ -45,6 +46,8 @@ inline long pad16(long K) { return (K + 15) / 16 * 16; }
 // host wrappers (qpc_ozaki.cu), enqueued on st without a wait
 size_t oz_digits_elems(long J, long K);
 int oz_split(const oz::operand& o, long K, long J, int* ef, __nv_bfloat16* D, cudaStream_t st);
+// QPC_ERR_TIMEOUT (and clears it) when a wait of the tensor-core product ran out since the last check
+int oz_check(cudaStream_t st);
 int oz_gemm(const __nv_bfloat16* Da, const int* ea, const __nv_bfloat16* Db, const int* eb, long n, long M, long K, double* out,
 	long istride, long jdiv, long jouter, cudaStream_t st);
 

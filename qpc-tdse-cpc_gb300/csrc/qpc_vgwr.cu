@@ -1142,6 +1142,7 @@ static int run_impl(qpc_vgwr* h, const double* atab, int64_t ld, const int64_t* 
 	QPC_CUDA(cudaEventRecord(h->ev1, h->st));
 	if (!ident) if (int rc = permute(h, perm, true)) return rc;
 	if (int rc = wait_on(h->st)) return rc;
+	if (h->slices) if (int rc = oz_check(h->st)) return rc;
 	cudaEventElapsedTime(&h->last_ms, h->ev0, h->ev1);
 	prof_collect(h);
 	if (F) {

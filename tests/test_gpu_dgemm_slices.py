@@ -11,6 +11,14 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
+@pytest.fixture(params=["mma.sync", "tcgen05"], autouse=True)
+def product_path(request, monkeypatch):
+    """every case on both tensor-core paths of the product (warp-level mma.sync, and tcgen05 with the
+    accumulator in tensor memory), selected per call by QPC_OZ_TC"""
+    monkeypatch.setenv("QPC_OZ_TC", "1" if request.param == "tcgen05" else "0")
+    return request.param
+
+
 def _check(q, A, B, c=4.0):
     C = q.dgemm_slices(A, B)
     ref = A @ B
@@ -60,6 +68,16 @@ def test_deterministic(q):
     rng = np.random.default_rng(5)
     A, B = rng.standard_normal((50, 700)), rng.standard_normal((700, 60))
     assert np.array_equal(q.dgemm_slices(A, B), q.dgemm_slices(A, B))
+
+
+def test_paths_agree(q, monkeypatch):
+    """both tensor-core paths form the same exact sums: identical results, tiles of either path ragged"""
+    rng = np.random.default_rng(7)
+    A, B = rng.standard_normal((300, 1500)), rng.standard_normal((1500, 170))
+    monkeypatch.setenv("QPC_OZ_TC", "0")
+    C0 = q.dgemm_slices(A, B)
+    monkeypatch.setenv("QPC_OZ_TC", "1")
+    assert np.array_equal(C0, q.dgemm_slices(A, B))
 
 
 def test_bit_exact_against_oracle(q):
