@@ -11,11 +11,13 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-@pytest.fixture(params=["mma.sync", "tcgen05"], autouse=True)
+@pytest.fixture(params=["mma.sync", "tcgen05", "tcgen05+tma", "tcgen05+tma, warp-specialised"], autouse=True)
 def product_path(request, monkeypatch):
-    """every case on both tensor-core paths of the product (warp-level mma.sync, and tcgen05 with the
-    accumulator in tensor memory), selected per call by QPC_OZ_TC"""
-    monkeypatch.setenv("QPC_OZ_TC", "1" if request.param == "tcgen05" else "0")
+    """every case on each tensor-core path of the product (warp-level mma.sync; tcgen05 with the
+    accumulator in tensor memory, operands by cp.async, by TMA from one thread, or by TMA with producer,
+    MMA and epilogue warps), selected per call by QPC_OZ_TC and QPC_OZ_TMA"""
+    monkeypatch.setenv("QPC_OZ_TC", "0" if request.param == "mma.sync" else "1")
+    monkeypatch.setenv("QPC_OZ_TMA", {"tcgen05+tma": "1", "tcgen05+tma, warp-specialised": "2"}.get(request.param, "0"))
     return request.param
 
 
@@ -77,6 +79,11 @@ def test_paths_agree(q, monkeypatch):
     monkeypatch.setenv("QPC_OZ_TC", "0")
     C0 = q.dgemm_slices(A, B)
     monkeypatch.setenv("QPC_OZ_TC", "1")
+    monkeypatch.setenv("QPC_OZ_TMA", "0")
+    assert np.array_equal(C0, q.dgemm_slices(A, B))
+    monkeypatch.setenv("QPC_OZ_TMA", "1")
+    assert np.array_equal(C0, q.dgemm_slices(A, B))
+    monkeypatch.setenv("QPC_OZ_TMA", "2")
     assert np.array_equal(C0, q.dgemm_slices(A, B))
 
 
