@@ -472,7 +472,12 @@ def c1_roofline(gemm_flops, tr_ms, tr_n, K, dev_ms, peak):
                 "frac": tfl / peak["tflops"] if tfl else None, **common}
     bf = load_peaks().get("bf16_tflops")
     ach = 45 * tfl if tfl else None
-    return {"bound": "tensor", "kernel": "k_oz_gemm slice products (9 x 7-bit digits, 45 bf16 pair products per FP64 product) "
+    if os.environ.get("QPC_OZ_TC", "1") == "0":
+        kname = "k_oz_gemm (mma.sync)"
+    else:
+        kname = {"0": "k_oz_gemm_tc (tcgen05, cp.async operands)", "1": "k_oz_gemm_tma (tcgen05, TMA from one thread)"}.get(
+            os.environ.get("QPC_OZ_TMA", "2"), "k_oz_gemm_ws (tcgen05, TMA producer / MMA / epilogue warps)")
+    return {"bound": "tensor", "kernel": kname + ": slice products (9 x 7-bit digits, 45 bf16 pair products per FP64 product) "
                                          "with splitting and pairing steps (CUDA events around each transform)",
             "achieved": ach, "peak": bf, "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst, cuBLAS)", "unit": "TFLOP/s",
             "frac": ach / bf if (ach and bf) else None, "traffic": None,
