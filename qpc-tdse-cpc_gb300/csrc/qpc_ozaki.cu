@@ -653,13 +653,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_oz_gemm_tma(const __grid_cons
 // ---------------------------------------------------------------- warp-specialised tcgen05 + TMA
 // Warps 0-7 read the accumulator at the end of each exact-sum chunk (as k_oz_gemm_tc); warp 8 lane 0
 // issues the TMA loads, warp 9 lane 0 the MMAs.  Their hand-offs are mbarriers: full[s] (TMA bytes
-// landed: MMA may read stage s), empty[s] (the stage's MMAs done: TMA may refill it), tfull (the
-// chunk's MMAs done: the accumulator may be read), tempty (all 256 epilogue threads read it: the next
-// chunk may overwrite it).  The MMA warp never waits for its own MMAs inside a chunk, so the tensor
-// core always has the stages that have arrived queued.  Every wait is bounded; a role whose wait runs
+// landed: MMA may read stage s), empty[s] (the stage's MMAs done: TMA may refill it), and per
+// accumulator (two in tensor memory, used by alternate chunks) tfull (the chunk's MMAs done: the
+// accumulator may be read) and tempty (all 256 epilogue threads read it: it may be overwritten).  The
+// MMA warp never waits for its own MMAs, and while the epilogue reads one accumulator the MMAs of the
+// next chunk fill the other.  Every wait is bounded; a role whose wait runs
 // out sets *err and stops, and the others then run out as well.
 constexpr int WS_EPI = 256, WS_THREADS = WS_EPI + 64;
-constexpr size_t WS_SMEM = (size_t)TC_STAGE_BYTES * TC_NST + 1024 + 16 * TC_NST + 32;
+constexpr size_t WS_SMEM = (size_t)TC_STAGE_BYTES * TC_NST + 1024 + 16 * TC_NST + 48;
 
 template <bool HI>
 __global__ void __launch_bounds__(WS_THREADS, 1) k_oz_gemm_ws(const __grid_constant__ CUtensorMap mapA,
@@ -670,19 +671,21 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_oz_gemm_ws(const __grid_const
 	extern __shared__ __align__(1024) unsigned char tsm[];
 	const uint32_t sraw = smem_u32(tsm);
 	const uint32_t sbase = (sraw + 1023u) & ~1023u;
+	// two accumulators in tensor memory (columns 0-127 and 128-255), used by alternate chunks, each with
+	// its own "full" and "empty" barrier
 	const uint32_t fullb = sbase + TC_STAGE_BYTES * TC_NST, emptyb = fullb + 8 * TC_NST;
-	const uint32_t tfull = emptyb + 8 * TC_NST, tempty = tfull + 8, tslot = tempty + 8;
+	const uint32_t tfull = emptyb + 8 * TC_NST, tempty = tfull + 16, tslot = tempty + 16;
 	const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 	const long rowA0 = (long)blockIdx.y * TC_M, rowB0 = (long)blockIdx.x * TC_N;
 
 	if (tid == 0) {
 		for (int q = 0; q < TC_NST; ++q) { mbar_init(fullb + 8 * q, 1); mbar_init(emptyb + 8 * q, 1); }
-		mbar_init(tfull, 1);
-		mbar_init(tempty, WS_EPI);
+		mbar_init(tfull, 1); mbar_init(tfull + 8, 1);
+		mbar_init(tempty, WS_EPI); mbar_init(tempty + 8, WS_EPI);
 		asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
 	}
 	if (warp == 0) {
-		asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(tslot), "r"(TC_TMEM_COLS) : "memory");
+		asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(tslot), "r"(2 * TC_TMEM_COLS) : "memory");
 		asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
 	}
 	asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
@@ -715,29 +718,31 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_oz_gemm_ws(const __grid_const
 		// ---- MMA issuer
 		if (lane == 0) {
 			cursor c{P0, 0, 0};
-			uint32_t fpar = 0, tpar = 0;
-			bool fresh = true, first_chunk = true;
+			uint32_t fpar = 0, tpar = 0;	// tpar bit b: parity of accumulator b's "empty" barrier
+			bool fresh = true;
+			long chunk = 0;
 			for (long q = 0; c.p < P1; ++q) {
-				const int slot = (int)(q % TC_NST);
-				if (fresh && !first_chunk) {	// the epilogue has read the previous chunk's accumulator
-					if (!mbar_wait(tempty, tpar)) { atomicExch(err, 1); break; }
-					tpar ^= 1u;
+				const int slot = (int)(q % TC_NST), buf = (int)(chunk & 1);
+				if (fresh && chunk >= 2) {	// the epilogue has read this accumulator's previous chunk
+					if (!mbar_wait(tempty + 8 * buf, (tpar >> buf) & 1u)) { atomicExch(err, 1); break; }
+					tpar ^= 1u << buf;
 				}
 				if (!mbar_wait(fullb + 8 * slot, (fpar >> slot) & 1u)) { atomicExch(err, 1); break; }
 				fpar ^= 1u << slot;
 				asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
 				const uint32_t aS = sbase + (uint32_t)slot * TC_STAGE_BYTES, bS = aS + TC_A_BYTES;
+				const uint32_t tacc = tmem + (uint32_t)(buf * TC_TMEM_COLS);
 #pragma unroll
 				for (int kk = 0; kk < TC_KS / 16; ++kk)
-					tc_mma(tmem, sw128_desc(aS + 32u * kk), sw128_desc(bS + 32u * kk), (fresh && kk == 0) ? 0u : 1u);
+					tc_mma(tacc, sw128_desc(aS + 32u * kk), sw128_desc(bS + 32u * kk), (fresh && kk == 0) ? 0u : 1u);
 				tc_commit(emptyb + 8 * slot);
 				fresh = false;
 				const int p = c.p;
 				advance(c, Kp);
 				if (c.p != p || c.k0 == c.kc0) {	// end of an exact-sum chunk
-					tc_commit(tfull);
+					tc_commit(tfull + 8 * buf);
 					fresh = true;
-					first_chunk = false;
+					++chunk;
 				}
 			}
 		}
@@ -749,14 +754,17 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_oz_gemm_ws(const __grid_const
 		const int lq = warp & 3, cbase = (warp >> 2) * TC_COLS_T;
 		const uint32_t trow = tmem + ((uint32_t)(lq * 32) << 16) + (uint32_t)cbase;
 		cursor c{P0, 0, 0};
-		uint32_t tpar = 0;
+		uint32_t tpar = 0;	// bit b: parity of accumulator b's "full" barrier
+		long chunk = 0;
 		bool ok = true;
 		while (c.p < P1) {
 			const int p = c.p;
 			advance(c, Kp);
 			if (!(c.p != p || c.k0 == c.kc0)) continue;
-			if (ok && !mbar_wait(tfull, tpar)) { ok = false; atomicExch(err, 1); }
-			tpar ^= 1u;
+			const int buf = (int)(chunk & 1);
+			++chunk;
+			if (ok && !mbar_wait(tfull + 8 * buf, (tpar >> buf) & 1u)) { ok = false; atomicExch(err, 1); }
+			tpar ^= 1u << buf;
 			if (!ok) break;
 			asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
 			__syncwarp();
@@ -765,12 +773,12 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_oz_gemm_ws(const __grid_const
 #pragma unroll
 			for (int h = 0; h < TC_COLS_T / 32; ++h) {
 				uint32_t v[32];
-				tc_ld32(trow + 32u * h, v);
+				tc_ld32(trow + (uint32_t)(buf * TC_TMEM_COLS) + 32u * h, v);
 #pragma unroll
 				for (int j = 0; j < 32; ++j) isum[32 * h + j] += (long long)__float2int_rn(__uint_as_float(v[j])) << sh;
 			}
 			asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
-			asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(tempty) : "memory");
+			asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(tempty + 8 * buf) : "memory");
 		}
 		const long row = rowA0 + lq * 32 + lane;
 		if (ok && row < n) {
@@ -794,7 +802,7 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_oz_gemm_ws(const __grid_const
 	asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
 	__syncthreads();
 	__syncwarp();
-	if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(TC_TMEM_COLS) : "memory");
+	if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(2 * TC_TMEM_COLS) : "memory");
 }
 
 } // namespace oz
