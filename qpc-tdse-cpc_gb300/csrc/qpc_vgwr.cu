@@ -284,6 +284,141 @@ __global__ void __launch_bounds__(VG_THREADS) k_vg_cn_sym(double2* __restrict__ 
 	}
 }
 
+// k_vg_cn_sym on a lane pair per chain: lane 2t + part holds part (0 real, 1 imaginary) of the
+// chain's complex values and forms only its own part of every product (two FP64 instructions with
+// operands chosen by integer selects, as on one lane), taking the partner's part by a shuffle within
+// the pair.  The window of U rows is kept as own parts.  Scratch (doubles): part of element e of row i
+// of chain t at ((i NS + e) nth + t) 2 + part, NS = P + 2.
+__device__ __forceinline__ double pair_other(double v, unsigned pm) { return __shfl_xor_sync(pm, v, 1); }
+
+// own part of a b from own (ao, bo) and partner (ae, be) parts: real ao bo - ae be, imaginary
+// ae bo + ao be
+__device__ __forceinline__ double own_mul(double ao, double ae, double bo, double be, int part)
+{
+	const double X = part ? ae : ao;
+	const double Y = part ? ao : __longlong_as_double(__double_as_longlong(ae) ^ (long long)0x8000000000000000ull);
+	return fma(X, bo, Y * be);
+}
+// acc - own part of a b
+__device__ __forceinline__ double own_msub(double acc, double ao, double ae, double bo, double be, int part)
+{
+	const double X = part ? ae : ao;
+	const double Y = part ? ao : __longlong_as_double(__double_as_longlong(ae) ^ (long long)0x8000000000000000ull);
+	return fma(-X, bo, fma(-Y, be, acc));
+}
+
+template <int P>
+__global__ void __launch_bounds__(VG_THREADS) k_vg_cn_sym2(double2* __restrict__ state, double* __restrict__ scr, const double* __restrict__ S,
+	const double* __restrict__ O, const double* __restrict__ lam, double cim, const double* __restrict__ atab, long ld, long step, int tofs,
+	int axis, double sgn, const int* __restrict__ perm, int N, int nch, int nlive)
+{
+	const long nth = (long)nlive * nch;
+	const long tt = (long)blockIdx.x * VG_THREADS + threadIdx.x;
+	const long t = tt >> 1;
+	const int part = (int)(tt & 1);
+	const unsigned pm = 3u << (threadIdx.x & 30);	// the lane pair of this chain
+	if (t >= nth) return;	// both lanes of a pair leave together
+	const int k = (int)(t / nch), ch = (int)(t - (long)k * nch);
+	const double f = sgn * atab[((long)perm[k] * ld + step + tofs) * 2 + axis] / 2.0;
+	const double b = lam[ch] * f * cim;
+	if (b == 0.0) return;	// both lanes: the same chain
+	constexpr int NE = P + 1, NS = P + 2;
+	double* z = reinterpret_cast<double*>(state + t * N) + part;	// own part, stride 2
+	double Uw[P][NE];	// own parts: slot q = row i-1-q, [0] = 1/U(row, row), [c] = U(row, row + c)
+	double yw[P], yo[P], zw[P];	// y own / partner parts, z own part of the previous P rows
+#pragma unroll
+	for (int q = 0; q < P; ++q) {
+		yw[q] = yo[q] = zw[q] = 0.0;
+#pragma unroll
+		for (int c = 0; c < NE; ++c) Uw[q][c] = 0.0;
+	}
+	for (int i = 0; i < N; ++i) {
+		double w = 0.0;	// own part of (S z)_i
+#pragma unroll
+		for (int q = 0; q < P; ++q)
+			if (i - 1 - q >= 0) w = fma(S[(long)(i - 1 - q) * NE + q + 1], zw[q], w);
+		const double zi = z[2L * i];
+		double up[NE];	// own parts of A(i, i+c) = S + i b O
+#pragma unroll
+		for (int c = 0; c < NE; ++c) {
+			up[c] = 0.0;
+			if (i + c < N) {
+				const double sv = S[(long)i * NE + c];
+				up[c] = part ? b * O[(long)i * NE + c] : sv;
+				w = fma(sv, c ? z[2L * (i + c)] : zi, w);
+			}
+		}
+		// multipliers L(i, i-1-q) = U(i-1-q, i) / U(i-1-q, i-1-q), both parts
+		double lo[P], le[P];
+#pragma unroll
+		for (int q = 0; q < P; ++q) {
+			const double uo = Uw[q][q + 1], ue = pair_other(uo, pm);
+			const double ro = Uw[q][0], re = pair_other(ro, pm);
+			lo[q] = own_mul(uo, ue, ro, re, part);
+			le[q] = pair_other(lo[q], pm);
+		}
+		// U(i, i+c) = A(i, i+c) - sum_q L(i, i-1-q) U(i-1-q, i+c)
+#pragma unroll
+		for (int c = 0; c < P; ++c)
+#pragma unroll
+			for (int q = 0; q + c + 1 <= P; ++q) {
+				const double uo = Uw[q][c + 1 + q], ue = pair_other(uo, pm);
+				up[c] = own_msub(up[c], lo[q], le[q], uo, ue, part);
+			}
+		double y = w;
+#pragma unroll
+		for (int q = 0; q < P; ++q) y = own_msub(y, lo[q], le[q], yw[q], yo[q], part);
+		// 1 / U(i, i): |U|^2 from both parts, own part of the conjugate over it
+		const double u0e = pair_other(up[0], pm);
+		const double d = fma(up[0], up[0], u0e * u0e);
+		const double rinv = 1.0 / d;
+		const double ri = part ? -up[0] * rinv : up[0] * rinv;
+		double* sr = scr + ((long)i * NS * nth + t) * 2 + part;
+#pragma unroll
+		for (int c = 1; c < NE; ++c) sr[(long)(c - 1) * nth * 2] = up[c];
+		sr[(long)P * nth * 2] = ri;
+		sr[(long)(P + 1) * nth * 2] = y;
+		const double ye = pair_other(y, pm);
+#pragma unroll
+		for (int q = P - 1; q > 0; --q) {
+			yw[q] = yw[q - 1];
+			yo[q] = yo[q - 1];
+			zw[q] = zw[q - 1];
+#pragma unroll
+			for (int c = 0; c < NE; ++c) Uw[q][c] = Uw[q - 1][c];
+		}
+		yw[0] = y;
+		yo[0] = ye;
+		zw[0] = zi;
+		Uw[0][0] = ri;
+#pragma unroll
+		for (int c = 1; c < NE; ++c) Uw[0][c] = up[c];
+	}
+	// backward: x_i = (y_i - sum_c U(i, i+c) x_{i+c}) / U(i, i); z_i := 2 x_i - z_i
+	double xw[P], xe[P];
+#pragma unroll
+	for (int q = 0; q < P; ++q) xw[q] = xe[q] = 0.0;
+	for (int i = N - 1; i >= 0; --i) {
+		const double* sr = scr + ((long)i * NS * nth + t) * 2 + part;
+		double v = sr[(long)(P + 1) * nth * 2];
+#pragma unroll
+		for (int c = 1; c < NE; ++c) {
+			const double uo = sr[(long)(c - 1) * nth * 2], ue = pair_other(uo, pm);
+			v = own_msub(v, uo, ue, xw[c - 1], xe[c - 1], part);
+		}
+		const double ro = sr[(long)P * nth * 2], re = pair_other(ro, pm);
+		const double ve = pair_other(v, pm);
+		const double x = own_mul(v, ve, ro, re, part);
+		const double xo = pair_other(x, pm);
+#pragma unroll
+		for (int q = P - 1; q > 0; --q) { xw[q] = xw[q - 1]; xe[q] = xe[q - 1]; }
+		xw[0] = x;
+		xe[0] = xo;
+		const double zi = z[2L * i];
+		z[2L * i] = fma(2.0, x, -zi);
+	}
+}
+
 // field-free step of every (instance, m, l) channel whose instance is still running:
 // x = 2 (S + i dt/2 H_l)^-1 S c - c with the LDL^T factors Lrow[l][r][k-1] = L(r, r-k),
 // Dinv[l][r] (qpc_ldlt_csym); y kept in the scratch buffer
@@ -685,8 +820,8 @@ int step_t(qpc_vgwr* h, long s, long ld, int nlive, int nff)
 			k_vg_cn_anti<P><<<grid, VG_THREADS, 0, h->st>>>(z, (double*)h->U, h->S, h->D, h->lam[comp], -q, h->atab, ld, s, tofs, axis, sgn,
 				h->perm, h->N, h->nch, nb);
 		else
-			k_vg_cn_sym<P><<<grid, VG_THREADS, 0, h->st>>>(z, h->U, h->S, h->Ri, h->lam[comp], q, h->atab, ld, s, tofs, axis, sgn, h->perm,
-				h->N, h->nch, nb);
+			k_vg_cn_sym2<P><<<(unsigned)((2 * nth + VG_THREADS - 1) / VG_THREADS), VG_THREADS, 0, h->st>>>(z, (double*)h->U, h->S, h->Ri,
+				h->lam[comp], q, h->atab, ld, s, tofs, axis, sgn, h->perm, h->N, h->nch, nb);
 		prof_end(h, 1, pa);
 		++h->launches;
 	};
