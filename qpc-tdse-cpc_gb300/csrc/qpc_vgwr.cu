@@ -179,115 +179,10 @@ __global__ void __launch_bounds__(VG_THREADS) k_vg_cn_anti(double2* __restrict__
 
 // symmetric O (1/r) with e = i b imaginary (x2, y2): A = S + i b O is complex symmetric, so in the
 // row-by-row LU the multipliers of row i are U(col, i) / U(col, col) from the window (no elimination
-// of the lower part) and only the upper part U(i, i..i+P) is formed.  Scratch per row (complex):
-// U(i, i+1..i+P), 1/U(i, i), y.
-template <int P>
-__global__ void __launch_bounds__(VG_THREADS) k_vg_cn_sym(double2* __restrict__ state, double2* __restrict__ scr, const double* __restrict__ S,
-	const double* __restrict__ O, const double* __restrict__ lam, double cim, const double* __restrict__ atab, long ld, long step, int tofs,
-	int axis, double sgn, const int* __restrict__ perm, int N, int nch, int nlive)
-{
-	const long nth = (long)nlive * nch;
-	const long t = (long)blockIdx.x * VG_THREADS + threadIdx.x;
-	if (t >= nth) return;
-	const int k = (int)(t / nch), ch = (int)(t - (long)k * nch);
-	const double f = sgn * atab[((long)perm[k] * ld + step + tofs) * 2 + axis] / 2.0;
-	const double b = lam[ch] * f * cim;
-	if (b == 0.0) return;
-	constexpr int NE = P + 1, NS = P + 2;
-	double2* z = state + t * N;
-	double2 Uw[P][NE];	// slot q: row i-1-q, [0] = 1/U(row, row), [c] = U(row, row + c)
-	double2 yw[P], zw[P];
-#pragma unroll
-	for (int q = 0; q < P; ++q) {
-		yw[q] = zw[q] = make_double2(0.0, 0.0);
-#pragma unroll
-		for (int c = 0; c < NE; ++c) Uw[q][c] = make_double2(0.0, 0.0);
-	}
-	for (int i = 0; i < N; ++i) {
-		double2 w = make_double2(0.0, 0.0);
-#pragma unroll
-		for (int q = 0; q < P; ++q)
-			if (i - 1 - q >= 0) {
-				const double sv = S[(long)(i - 1 - q) * NE + q + 1];
-				w.x = fma(sv, zw[q].x, w.x);
-				w.y = fma(sv, zw[q].y, w.y);
-			}
-		const double2 zi = z[i];
-		double2 up[NE];
-#pragma unroll
-		for (int c = 0; c < NE; ++c) {
-			up[c] = make_double2(0.0, 0.0);
-			if (i + c < N) {
-				const double sv = S[(long)i * NE + c], ov = O[(long)i * NE + c];
-				up[c] = make_double2(sv, b * ov);
-				const double2 zc = c ? z[i + c] : zi;
-				w.x = fma(sv, zc.x, w.x);
-				w.y = fma(sv, zc.y, w.y);
-			}
-		}
-		// multipliers L(i, i-1-q) = U(i-1-q, i) / U(i-1-q, i-1-q); zero for a missing row
-		double2 l[P];
-#pragma unroll
-		for (int q = 0; q < P; ++q) l[q] = cmul(Uw[q][q + 1], Uw[q][0]);
-		// U(i, i+c) = A(i, i+c) - sum_q L(i, i-1-q) U(i-1-q, i+c), over rows with i+c within their band
-#pragma unroll
-		for (int c = 0; c < P; ++c)
-#pragma unroll
-			for (int q = 0; q + c + 1 <= P; ++q) {
-				const double2 u = Uw[q][c + 1 + q];
-				up[c].x = fma(-l[q].x, u.x, fma(l[q].y, u.y, up[c].x));
-				up[c].y = fma(-l[q].x, u.y, fma(-l[q].y, u.x, up[c].y));
-			}
-		double2 y = w;
-#pragma unroll
-		for (int q = 0; q < P; ++q) {
-			y.x = fma(-l[q].x, yw[q].x, fma(l[q].y, yw[q].y, y.x));
-			y.y = fma(-l[q].x, yw[q].y, fma(-l[q].y, yw[q].x, y.y));
-		}
-		const double2 ri = crcp(up[0]);
-		double2* sr = scr + (long)i * NS * nth + t;
-#pragma unroll
-		for (int c = 1; c < NE; ++c) sr[(c - 1) * nth] = up[c];
-		sr[P * nth] = ri;
-		sr[(P + 1) * nth] = y;
-#pragma unroll
-		for (int q = P - 1; q > 0; --q) {
-			yw[q] = yw[q - 1];
-			zw[q] = zw[q - 1];
-#pragma unroll
-			for (int c = 0; c < NE; ++c) Uw[q][c] = Uw[q - 1][c];
-		}
-		yw[0] = y;
-		zw[0] = zi;
-		Uw[0][0] = ri;
-#pragma unroll
-		for (int c = 1; c < NE; ++c) Uw[0][c] = up[c];
-	}
-	double2 xw[P];
-#pragma unroll
-	for (int q = 0; q < P; ++q) xw[q] = make_double2(0.0, 0.0);
-	for (int i = N - 1; i >= 0; --i) {
-		const double2* sr = scr + (long)i * NS * nth + t;
-		double2 v = sr[(P + 1) * nth];
-#pragma unroll
-		for (int c = 1; c < NE; ++c) {
-			const double2 u = sr[(c - 1) * nth];
-			v.x = fma(-u.x, xw[c - 1].x, fma(u.y, xw[c - 1].y, v.x));
-			v.y = fma(-u.x, xw[c - 1].y, fma(-u.y, xw[c - 1].x, v.y));
-		}
-		const double2 x = cmul(v, sr[P * nth]);
-#pragma unroll
-		for (int q = P - 1; q > 0; --q) xw[q] = xw[q - 1];
-		xw[0] = x;
-		const double2 zi = z[i];
-		z[i] = make_double2(fma(2.0, x.x, -zi.x), fma(2.0, x.y, -zi.y));
-	}
-}
-
-// k_vg_cn_sym on a lane pair per chain: lane 2t + part holds part (0 real, 1 imaginary) of the
-// chain's complex values and forms only its own part of every product (two FP64 instructions with
-// operands chosen by integer selects, as on one lane), taking the partner's part by a shuffle within
-// the pair.  The window of U rows is kept as own parts.  Scratch (doubles): part of element e of row i
+// of the lower part) and only the upper part U(i, i..i+P) is formed.  Each chain runs on a lane pair:
+// lane 2t + part holds part (0 real, 1 imaginary) of the chain's complex values and forms only its own
+// part of every product (two FP64 instructions with operands chosen by integer selects), taking the
+// partner's part by a shuffle within the pair.  The window of U rows is kept as own parts.  Scratch (doubles): part of element e of row i
 // of chain t at ((i NS + e) nth + t) 2 + part, NS = P + 2.
 __device__ __forceinline__ double pair_other(double v, unsigned pm) { return __shfl_xor_sync(pm, v, 1); }
 
