@@ -66,81 +66,78 @@ __device__ __forceinline__ double2 crcp(double2 y)
 // threads ((row * elements + e) * threads + t) so that a warp's stores and loads are contiguous.
 
 // anti-symmetric O (d/dr: O(r, r+c) = band[r][c], O(r+c, r) = -band[r][c], c > 0) with e real
-// (x1, y1): A = S + e O is a real non-symmetric band, factorised by a real LU without pivoting.
-// Scratch per row: U(i, i+1..i+P), 1/U(i, i), Re y, Im y.
+// (x1, y1): A = S + e O is a real non-symmetric band, factorised by a real LU without pivoting.  Each
+// chain runs on a lane pair: the factor is real, so the real (part 0) and imaginary (part 1) parts of
+// the solve are independent; both lanes form the same LU and each solves its own part.  Scratch (doubles) per row: U(i, i+1..i+P), 1/U(i, i) (written by part 0), y real, y imaginary,
+// element e of row i of chain t at (i NSA + e) nth + t, NSA = P + 3.
 template <int P>
-__global__ void __launch_bounds__(VG_THREADS) k_vg_cn_anti(double2* __restrict__ state, double* __restrict__ scr, const double* __restrict__ S,
+__global__ void __launch_bounds__(VG_THREADS) k_vg_cn_anti2(double2* __restrict__ state, double* __restrict__ scr, const double* __restrict__ S,
 	const double* __restrict__ O, const double* __restrict__ lam, double cre, const double* __restrict__ atab, long ld, long step, int tofs,
 	int axis, double sgn, const int* __restrict__ perm, int N, int nch, int nlive)
 {
 	const long nth = (long)nlive * nch;
-	const long t = (long)blockIdx.x * VG_THREADS + threadIdx.x;
+	const long tt = (long)blockIdx.x * VG_THREADS + threadIdx.x;
+	const long t = tt >> 1;
+	const int part = (int)(tt & 1);
 	if (t >= nth) return;
 	const int k = (int)(t / nch), ch = (int)(t - (long)k * nch);
 	const double f = sgn * atab[((long)perm[k] * ld + step + tofs) * 2 + axis] / 2.0;
 	const double e = lam[ch] * f * cre;
 	if (e == 0.0) return;
 	constexpr int NE = P + 1, NS = P + 3;
-	double2* z = state + t * N;
+	double* z = reinterpret_cast<double*>(state + t * N) + part;	// own part, stride 2
 	double Uw[P][NE];	// slot q: row i-1-q, [0] = 1/U(row, row), [c] = U(row, row + c)
-	double2 yw[P], zw[P];	// y and z of the previous P rows
+	double yw[P], zw[P];	// own parts of y and z of the previous P rows
 #pragma unroll
 	for (int q = 0; q < P; ++q) {
-		yw[q] = zw[q] = make_double2(0.0, 0.0);
+		yw[q] = zw[q] = 0.0;
 #pragma unroll
 		for (int c = 0; c < NE; ++c) Uw[q][c] = 0.0;
 	}
 	for (int i = 0; i < N; ++i) {
-		// row i of A: lo[q] = A(i, i-1-q), up[c] = A(i, i+c); w = (S z)_i
 		double lo[P], up[NE];
-		double2 w = make_double2(0.0, 0.0);
+		double w = 0.0;
 #pragma unroll
 		for (int q = 0; q < P; ++q) {
 			lo[q] = 0.0;
 			if (i - 1 - q >= 0) {
 				const double sv = S[(long)(i - 1 - q) * NE + q + 1], ov = O[(long)(i - 1 - q) * NE + q + 1];
 				lo[q] = fma(-e, ov, sv);
-				w.x = fma(sv, zw[q].x, w.x);
-				w.y = fma(sv, zw[q].y, w.y);
+				w = fma(sv, zw[q], w);
 			}
 		}
-		const double2 zi = z[i];
+		const double zi = z[2L * i];
 #pragma unroll
 		for (int c = 0; c < NE; ++c) {
 			up[c] = 0.0;
 			if (i + c < N) {
 				const double sv = S[(long)i * NE + c], ov = O[(long)i * NE + c];
 				up[c] = fma(e, ov, sv);
-				const double2 zc = c ? z[i + c] : zi;
-				w.x = fma(sv, zc.x, w.x);
-				w.y = fma(sv, zc.y, w.y);
+				w = fma(sv, c ? z[2L * (i + c)] : zi, w);
 			}
 		}
-		// eliminate columns i-P .. i-1 in ascending order; a missing row has a zero window slot
 		double l[P];
 #pragma unroll
 		for (int qq = P - 1; qq >= 0; --qq) {
 			l[qq] = lo[qq] * Uw[qq][0];
 #pragma unroll
 			for (int c = 1; c < NE; ++c) {
-				const int dc = c - 1 - qq;	// column (i-1-qq)+c relative to i
+				const int dc = c - 1 - qq;
 				if (dc < 0) lo[-dc - 1] = fma(-l[qq], Uw[qq][c], lo[-dc - 1]);
 				else up[dc] = fma(-l[qq], Uw[qq][c], up[dc]);
 			}
 		}
-		double2 y = w;
+		double y = w;
 #pragma unroll
-		for (int q = 0; q < P; ++q) {
-			y.x = fma(-l[q], yw[q].x, y.x);
-			y.y = fma(-l[q], yw[q].y, y.y);
-		}
+		for (int q = 0; q < P; ++q) y = fma(-l[q], yw[q], y);
 		const double ri = 1.0 / up[0];
 		double* sr = scr + (long)i * NS * nth + t;
+		if (part == 0) {
 #pragma unroll
-		for (int c = 1; c < NE; ++c) sr[(c - 1) * nth] = up[c];
-		sr[P * nth] = ri;
-		sr[(P + 1) * nth] = y.x;
-		sr[(P + 2) * nth] = y.y;
+			for (int c = 1; c < NE; ++c) sr[(c - 1) * nth] = up[c];
+			sr[P * nth] = ri;
+		}
+		sr[(P + 1 + part) * nth] = y;
 #pragma unroll
 		for (int q = P - 1; q > 0; --q) {
 			yw[q] = yw[q - 1];
@@ -154,26 +151,22 @@ __global__ void __launch_bounds__(VG_THREADS) k_vg_cn_anti(double2* __restrict__
 #pragma unroll
 		for (int c = 1; c < NE; ++c) Uw[0][c] = up[c];
 	}
-	// backward: x_i = (y_i - sum_c U(i, i+c) x_{i+c}) / U(i, i); z_i := 2 x_i - z_i
-	double2 xw[P];
+	// the U rows part 0 wrote are read by both lanes: order the pair's memory accesses
+	__syncwarp(3u << (threadIdx.x & 30));
+	double xw[P];
 #pragma unroll
-	for (int q = 0; q < P; ++q) xw[q] = make_double2(0.0, 0.0);
+	for (int q = 0; q < P; ++q) xw[q] = 0.0;
 	for (int i = N - 1; i >= 0; --i) {
 		const double* sr = scr + (long)i * NS * nth + t;
-		double2 v = make_double2(sr[(P + 1) * nth], sr[(P + 2) * nth]);
+		double v = sr[(P + 1 + part) * nth];
 #pragma unroll
-		for (int c = 1; c < NE; ++c) {
-			const double u = sr[(c - 1) * nth];
-			v.x = fma(-u, xw[c - 1].x, v.x);
-			v.y = fma(-u, xw[c - 1].y, v.y);
-		}
-		const double ri = sr[P * nth];
-		const double2 x = make_double2(v.x * ri, v.y * ri);
+		for (int c = 1; c < NE; ++c) v = fma(-sr[(c - 1) * nth], xw[c - 1], v);
+		const double x = v * sr[P * nth];
 #pragma unroll
 		for (int q = P - 1; q > 0; --q) xw[q] = xw[q - 1];
 		xw[0] = x;
-		const double2 zi = z[i];
-		z[i] = make_double2(fma(2.0, x.x, -zi.x), fma(2.0, x.y, -zi.y));
+		const double zi = z[2L * i];
+		z[2L * i] = fma(2.0, x, -zi);
 	}
 }
 
@@ -712,8 +705,8 @@ int step_t(qpc_vgwr* h, long s, long ld, int nlive, int nff)
 		const unsigned grid = (unsigned)((nth + VG_THREADS - 1) / VG_THREADS);
 		cudaEvent_t pa = prof_begin(h);
 		if (anti)
-			k_vg_cn_anti<P><<<grid, VG_THREADS, 0, h->st>>>(z, (double*)h->U, h->S, h->D, h->lam[comp], -q, h->atab, ld, s, tofs, axis, sgn,
-				h->perm, h->N, h->nch, nb);
+			k_vg_cn_anti2<P><<<(unsigned)((2 * nth + VG_THREADS - 1) / VG_THREADS), VG_THREADS, 0, h->st>>>(z, (double*)h->U, h->S, h->D,
+				h->lam[comp], -q, h->atab, ld, s, tofs, axis, sgn, h->perm, h->N, h->nch, nb);
 		else
 			k_vg_cn_sym2<P><<<(unsigned)((2 * nth + VG_THREADS - 1) / VG_THREADS), VG_THREADS, 0, h->st>>>(z, (double*)h->U, h->S, h->Ri,
 				h->lam[comp], q, h->atab, ld, s, tofs, axis, sgn, h->perm, h->N, h->nch, nb);
