@@ -263,6 +263,19 @@ int qpc_hhg_spectra(int32_t n_inst, const double* z, int64_t ldz, const int64_t*
 int qpc_dgemm_slices(int64_t n, int64_t M, int64_t K, const double* A, int64_t lda, const double* B, int64_t ldb, double* C,
 	int64_t ldc, float* ms);
 
+/* The length-gauge l-space transform of the coupling step, the engine's form of cn_transform_hl
+ * (spherical/propagator/cn_1e.hpp:101-147), on the tensor cores as the engine runs it for
+ * n_l <= 48: in and out are n_pos rows of n_l complex channel values (interleaved re, im; host
+ * buffers); V [n_l/2 + 1][n_l] holds the eigenvectors of +s_k (rows k < n_l/2) and, for odd n_l, the
+ * zero-eigenvalue vector (last row).  forward != 0: slot 2k = E_k + O_k, slot 2k+1 = conj(E_k - O_k)
+ * and, for odd n_l, slot n_l - 1 = Z, with E_k, Z the sums over even l and O_k over odd l of V[k][l] c_l;
+ * forward = 0: c_l = sum_k V[k][l] x_(2k + l%2) (with Z's row for even l).  The products are formed
+ * in exact 8-bit digits (each row of real or imaginary parts under its power of two) and rounded
+ * once: each E_k, O_k is within about n_l 2^(e + f - 59) of the exact sum, 2^e and 2^f the powers of
+ * two of the input row and of V's row (an FP64 dot product rounds near n_l 2^(e + f - 53)).
+ * Errors: QPC_ERR_ARGS (n_pos < 1, n_l outside 1..48, NULL buffers), QPC_ERR_TIMEOUT. */
+int qpc_lspace_transform(int64_t n_pos, int32_t n_l, const double* V, int32_t forward, const double* in, double* out);
+
 /* Photoelectron energy spectrum (|proj|^2 binned over [emin, emax) per unit energy) and
  * ionization yield 1 - sum_{energy < thres} |proj|^2 (ionization_sph::measure_ioyd,
  * spectrum/ionization_1e.hpp:15-51) from n projections (complex) with their energies. */

@@ -27,8 +27,9 @@ def _row_exponents(M):
     return np.where(f > 0, f - 1022, -1022).astype(np.int64)
 
 
-def digits(M):
-    """(e [rows], D [NS][rows][cols] int64): the signed 7-bit digits of every row of M"""
+def digits(M, ns=NS, bits=BITS):
+    """(e [rows], D [ns][rows][cols] int64): the signed digits of every row of M (ns digits of `bits`
+    bits; 9 x 7 for the slice-product GEMM, 8 x 8 for the l-space transform)"""
     M = np.ascontiguousarray(M, dtype=np.float64)
     e = _row_exponents(M)
     b = M.view(np.int64)
@@ -42,23 +43,27 @@ def digits(M):
     right = (~left) & (sh > -64)
     Y[right] = (m[right].astype(np.uint64) >> (-sh[right]).astype(np.uint64))
     sign = np.where(b < 0, -1, 1)
-    D = np.stack([sign * ((Y >> np.uint64(BITS * (NS - 1 - s))) & np.uint64(127)).astype(np.int64) for s in range(NS)])
+    mask = np.uint64((1 << bits) - 1)
+    D = np.stack([sign * ((Y >> np.uint64(bits * (ns - 1 - s))) & mask).astype(np.int64) for s in range(ns)])
     return e, D
 
 
-def gemm(A, B):
-    """C = A B as the slice product defines it, correctly rounded from the exact digit sum"""
+def gemm(A, B, ns=NS, bits=BITS):
+    """C = A B as the slice product defines it (digit pairs s + t < ns), correctly rounded from the
+    exact digit sum"""
     A = np.asarray(A, dtype=np.float64)
     B = np.asarray(B, dtype=np.float64)
-    ea, da = digits(A)
-    eb, db = digits(B.T)
+    ea, da = digits(A, ns, bits)
+    eb, db = digits(B.T, ns, bits)
     n, M = A.shape[0], B.shape[1]
-    # exact digit-pair sums per level d = s + t (int64: each below 8 K 2^14)
-    lev = [sum(da[s] @ db[d - s].T for s in range(d + 1)) for d in range(NS)]
+    # exact digit-pair sums per level d = s + t (int64: each below ns K 2^(2 bits))
+    lev = [sum(da[s] @ db[d - s].T for s in range(d + 1)) for d in range(ns)]
+    # x = 2^(e - 63) sum_s alpha_s 2^(bits (ns - 1 - s)), so a product of two values is
+    # 2^(ea + eb - 126 + bits (ns - 1)) sum_d lev_d 2^(bits (ns - 1 - d))
     C = np.zeros((n, M))
     for i in range(n):
         for j in range(M):
-            tot = sum(int(lev[d][i, j]) << (BITS * (NS - 1 - d)) for d in range(NS))
-            e = int(ea[i] + eb[j]) - BITS * (NS + 1)
+            tot = sum(int(lev[d][i, j]) << (bits * (ns - 1 - d)) for d in range(ns))
+            e = int(ea[i] + eb[j]) - 126 + bits * (ns - 1)
             C[i, j] = float(Fraction(tot) * (Fraction(2) ** e)) if tot else 0.0
     return C

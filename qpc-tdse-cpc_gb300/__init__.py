@@ -29,7 +29,7 @@ POTENTIAL_YUKAWA = 1
 EXPORTS = (
     "qpc_last_error", "qpc_version", "qpc_set_wait_limit", "qpc_get_wait_limit", "qpc_fp64_peak",
     "qpc_lgwz_stream", "qpc_vgwr_set_profiling", "qpc_vgwr_kernel_times", "qpc_vgwr_run_dipole", "qpc_lgwz_run_ex",
-    "qpc_hhg_spectra", "qpc_dgemm_slices", "qpc_linear_knots", "qpc_radial_setup", "qpc_y10_coupling",
+    "qpc_hhg_spectra", "qpc_dgemm_slices", "qpc_lspace_transform", "qpc_linear_knots", "qpc_radial_setup", "qpc_y10_coupling",
     "qpc_y10_eigen", "qpc_ldlt_csym", "qpc_gen_eigen", "qpc_field_sinen", "qpc_lgwz_create",
     "qpc_lgwz_destroy", "qpc_lgwz_put", "qpc_lgwz_get", "qpc_lgwz_put_device", "qpc_lgwz_get_device",
     "qpc_lgwz_propagate", "qpc_lgwz_propagate_free", "qpc_lgwz_run", "qpc_lgwz_norm", "qpc_lgwz_dipole",
@@ -129,6 +129,7 @@ def load(path=None):
         "qpc_hhg_spectrum": (ctypes.c_int, [P, i64, d, d, d, d, i32, P, P]),
         "qpc_hhg_spectra": (ctypes.c_int, [i32, P, i64, P, d, d, P, P, i32, i64, P]),
         "qpc_dgemm_slices": (ctypes.c_int, [i64, i64, i64, P, i64, P, i64, P, i64, P]),
+        "qpc_lspace_transform": (ctypes.c_int, [i64, i32, P, i32, P, P]),
         "qpc_pes_bin": (ctypes.c_int, [P, P, i64, d, d, i32, d, P, P, P]),
         "qpc_cholesky_band": (ctypes.c_int, [i32, i32, P, P]),
         "qpc_lgwz_run_many": (ctypes.c_int, [i32, P, P, P, P, P, P]),
@@ -373,6 +374,19 @@ def dgemm_slices(A, B, timed=False):
     ms = np.zeros(1, np.float32)
     _check(load().qpc_dgemm_slices(n, M, K, _ptr(A), K, _ptr(B), M, _ptr(C), M, _ptr(ms)))
     return (C, float(ms[0])) if timed else C
+
+
+def lspace_transform(V, c, forward=True):
+    """The engine's l-space transform of c [n_pos][n_l] (complex) with the eigenvector table
+    V [n_l/2 + 1][n_l], on the tensor cores in exact digits (qpc_lspace_transform, n_l <= 48)."""
+    c = np.ascontiguousarray(np.atleast_2d(c), dtype=np.complex128)
+    V = _f64(np.atleast_2d(V))
+    n_pos, n_l = c.shape
+    if V.shape != (n_l // 2 + 1, n_l):
+        raise ValueError("V must be [n_l/2 + 1][n_l], got %s for n_l = %d" % (V.shape, n_l))
+    out = np.zeros_like(c)
+    _check(load().qpc_lspace_transform(n_pos, n_l, _ptr(V), 1 if forward else 0, _ptr(c), _ptr(out)))
+    return out
 
 
 def pes_bin(proj, energy, emin, emax, nbins, thres=0.0):

@@ -47,7 +47,8 @@ def build_engine(force=False, verbose=False):
     srcs = [os.path.join(CSRC, f) for f in ("qpc_engine.cu", "qpc_setup.cpp", "qpc_internal.h", "qpc_chain.cuh",
                                              "qpc_noalloc.cu", "qpc_spectra.cpp", "qpc_arnoldi.cu", "qpc_cuda_util.cuh",
                                              "qpc_mlp.cu", "qpc_vgwr.cu", "qpc_momentum.cu", "qpc_momentum.cpp",
-                                             "qpc_gemm.cuh", "qpc_hhg.cu", "qpc_ozaki.cu", "qpc_ozaki.cuh")]
+                                             "qpc_gemm.cuh", "qpc_hhg.cu", "qpc_ozaki.cu", "qpc_ozaki.cuh",
+                                             "qpc_tcgen05.cuh", "qpc_ltrans.cu", "qpc_ltrans.cuh")]
     srcs.append(os.path.join(ROOT, "include", "qpc_gb300.h"))
     if not force and not _stale(LIB, srcs):
         return LIB
@@ -63,6 +64,7 @@ def build_engine(force=False, verbose=False):
     o_mt = os.path.join(OBJDIR, "qpc_momentum.o")
     o_hh = os.path.join(OBJDIR, "qpc_hhg.o")
     o_oz = os.path.join(OBJDIR, "qpc_ozaki.o")
+    o_lt = os.path.join(OBJDIR, "qpc_ltrans.o")
     nv = [_nvcc()] + NVCC_ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC"] + os.environ.get("QPC_NVCC_EXTRA", "").split()
     jobs = [
         nv + ["-c", os.path.join(CSRC, "qpc_engine.cu"), "-o", o_cu],
@@ -73,13 +75,14 @@ def build_engine(force=False, verbose=False):
         nv + ["-c", os.path.join(CSRC, "qpc_momentum.cu"), "-o", o_mo],
         nv + ["-c", os.path.join(CSRC, "qpc_hhg.cu"), "-o", o_hh],
         nv + ["-c", os.path.join(CSRC, "qpc_ozaki.cu"), "-o", o_oz],
+        nv + ["-c", os.path.join(CSRC, "qpc_ltrans.cu"), "-o", o_lt],
         ["g++", "-O2", "-std=c++17", "-fPIC", "-c", os.path.join(CSRC, "qpc_momentum.cpp"), "-o", o_mt],
         ["g++", "-O2", "-std=c++17", "-fPIC", "-c", os.path.join(CSRC, "qpc_setup.cpp"), "-o", o_cc],
         ["g++", "-O2", "-std=c++17", "-fPIC", "-c", os.path.join(CSRC, "qpc_spectra.cpp"), "-o", o_sp],
     ]
     with cf.ThreadPoolExecutor(len(jobs)) as ex:
         outs = list(ex.map(_run, jobs))
-    _run([_nvcc()] + NVCC_ARCH + ["-shared", o_cu, o_na, o_ar, o_ml, o_vg, o_mo, o_hh, o_oz, o_mt, o_cc, o_sp, "-o", LIB + ".tmp", "-lcudart", "-lcusolver", "-lpthread"])
+    _run([_nvcc()] + NVCC_ARCH + ["-shared", o_cu, o_na, o_ar, o_ml, o_vg, o_mo, o_hh, o_oz, o_lt, o_mt, o_cc, o_sp, "-o", LIB + ".tmp", "-lcudart", "-lcusolver", "-lpthread"])
     os.replace(LIB + ".tmp", LIB)
     if verbose:
         print("".join(outs))

@@ -45,6 +45,7 @@
 #include <map>
 #include <cstdlib>
 #include "qpc_chain.cuh"
+#include "qpc_ltrans.cuh"
 
 namespace qpc {
 
@@ -73,7 +74,7 @@ double wait_limit_s()
 
 
 // device status bits (never a trap)
-enum : int { ST_PIVOT = 1, ST_NONFINITE = 2 };
+enum : int { ST_PIVOT = 1, ST_NONFINITE = 2, ST_TIMEOUT = 4 };
 
 // ============================================================================ kernels
 
@@ -459,6 +460,12 @@ struct qpc_lgwz {
 	size_t chain_smem = 0;
 	int chain_sstage = 1;	// k_chain stages the S band in shared memory (QPC_CHAIN_SSTAGE=0: read through L1)
 	int chain_warps = 4;	// warps per k_chain block, sharing one staged S band (QPC_CHAIN_WARPS)
+	// the l-space transforms on the tensor cores (qpc_ltrans.cu) for n_l <= 48, with QPC_LTRANS_TC=1:
+	// half-width of the block-diagonal product (0: the FP64 kernel k_transform), the
+	// matrices' digit planes [M][2][8][2 lt_kb][64] and exponents [M][2][2 lt_kb]
+	int lt_kb = 0;
+	uint16_t* lt_dig = nullptr;
+	int* lt_fex = nullptr;
 	// optional per-kernel timing (CUDA events around each launch on the handle's stream)
 	bool profiling = false;
 	std::vector<cudaEvent_t> evpool;
@@ -555,6 +562,7 @@ int read_status(qpc_lgwz* h)
 	if (int rc = copy_to_host(&st, h->status, sizeof(int), h->stream)) return rc;
 	if (st & ST_PIVOT) { set_error("zero pivot in a Crank-Nicolson factorisation"); return QPC_ERR_SINGULAR; }
 	if (st & ST_NONFINITE) { set_error("non-finite value in the state"); return QPC_ERR_NUMERIC; }
+	if (st & ST_TIMEOUT) { set_error("a tensor-core wait of the l-space transform ran out"); return QPC_ERR_TIMEOUT; }
 	return QPC_OK;
 }
 
@@ -761,7 +769,11 @@ void launch_group_step(qpc_lgwz* h, cudaStream_t st, int b0, long step, long ste
 		unsigned grid = (unsigned)((long)Bc * M * tiles);
 		{
 			prof_scope ps(h, QPC_KERNEL_TRANSFORM_FWD, st);
-			k_transform<<<grid, 256, smem, st>>>(h->st, h->eo, h->Vh, N, L, M, np, 1, h->ntf, step, b0, Bc, h->cmode);
+			if (h->lt_kb)
+				ltrans_launch(h->lt_kb, h->st, h->eo, h->lt_dig, h->lt_fex, N, L, M, np, 1, h->ntf, step, b0, Bc, h->cmode, h->status,
+					ST_TIMEOUT, st);
+			else
+				k_transform<<<grid, 256, smem, st>>>(h->st, h->eo, h->Vh, N, L, M, np, 1, h->ntf, step, b0, Bc, h->cmode);
 			LAUNCH(h);
 		}
 		if (np > 0) {
@@ -770,7 +782,11 @@ void launch_group_step(qpc_lgwz* h, cudaStream_t st, int b0, long step, long ste
 		}
 		{
 			prof_scope ps(h, QPC_KERNEL_TRANSFORM_BWD, st);
-			k_transform<<<grid, 256, smem, st>>>(h->eo, h->st, h->Vh, N, L, M, np, 0, h->ntf, step, b0, Bc, h->cmode);
+			if (h->lt_kb)
+				ltrans_launch(h->lt_kb, h->eo, h->st, h->lt_dig, h->lt_fex, N, L, M, np, 0, h->ntf, step, b0, Bc, h->cmode, h->status,
+					ST_TIMEOUT, st);
+			else
+				k_transform<<<grid, 256, smem, st>>>(h->eo, h->st, h->Vh, N, L, M, np, 0, h->ntf, step, b0, Bc, h->cmode);
 			LAUNCH(h);
 		}
 	}
@@ -1153,6 +1169,19 @@ static int create_impl(const qpc_dims* dims, double dt, const double* S, const d
 		}
 		h->ffmap_cur = h->ffmap_id;
 	}
+	const char* ltc = getenv("QPC_LTRANS_TC");
+	h->lt_kb = (ltc && atoi(ltc) != 0) ? ltrans_kb(L) : 0;
+	if (h->lt_kb) {
+		std::vector<uint16_t> dig(ltrans_digit_bytes(M, h->lt_kb) / 2);
+		std::vector<int> fex((size_t)M * 2 * 2 * h->lt_kb);
+		ltrans_digits(Vh.data(), M, L, np, h->lt_kb, dig.data(), fex.data());
+		if ((rc = dalloc(&h->lt_dig, dig.size())) || (rc = dalloc(&h->lt_fex, fex.size()))) return fail(rc);
+		if (cudaMemcpy(h->lt_dig, dig.data(), sizeof(uint16_t) * dig.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
+			cudaMemcpy(h->lt_fex, fex.data(), sizeof(int) * fex.size(), cudaMemcpyHostToDevice) != cudaSuccess) {
+			set_error("initial device copies failed");
+			return fail(QPC_ERR_CUDA);
+		}
+	}
 	size_t smem = sizeof(double2) * 2 * TR * (L | 1);
 	h->chain_smem = sizeof(double) * (size_t)N * NE;
 	if (const char* e = getenv("QPC_CHAIN_SSTAGE")) h->chain_sstage = atoi(e) ? 1 : 0;
@@ -1181,7 +1210,7 @@ int qpc_lgwz_destroy(qpc_lgwz* h)
 {
 	if (!h) return QPC_OK;
 	if (h->stream) cudaStreamSynchronize(h->stream);
-	cudaFree(h->S); cudaFree(h->R); cudaFree(h->Vh); cudaFree(h->lamp); cudaFree(h->ff);
+	cudaFree(h->S); cudaFree(h->R); cudaFree(h->Vh); cudaFree(h->lamp); cudaFree(h->ff); cudaFree(h->lt_dig); cudaFree(h->lt_fex);
 	cudaFree(h->ffmap); cudaFree(h->ffmap_id);
 	cudaFree(h->spf_c); cudaFree(h->spb_c); cudaFree(h->spf_ff); cudaFree(h->spb_ff);
 	cudaFree(h->st); cudaFree(h->eo); cudaFree(h->wk); cudaFree(h->hostlay); cudaFree(h->fac);

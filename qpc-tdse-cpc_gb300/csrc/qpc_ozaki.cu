@@ -3,6 +3,7 @@
 #include "qpc_internal.h"
 #include "qpc_cuda_util.cuh"
 #include "qpc_ozaki.cuh"
+#include "qpc_tcgen05.cuh"
 #include <cuda_runtime.h>
 #include <cuda.h>
 #include <vector>
@@ -97,7 +98,7 @@ constexpr int KS = 64, NSTAGE = 4;
 constexpr int STAGE_ELEMS = 2 * TM * KS;	// bf16 per stage (A tile, then B tile)
 constexpr size_t GEMM_SMEM = sizeof(__nv_bfloat16) * STAGE_ELEMS * NSTAGE;
 
-__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+using tc::smem_u32;
 
 // 16 bytes global -> shared, zero-filled when !valid
 __device__ __forceinline__ void cp16(uint32_t dst, const void* src, bool valid)
@@ -278,60 +279,16 @@ constexpr int TC_M = 128, TC_N = 128, TC_KS = 64, TC_NST = 6, TC_THREADS = 256, 
 constexpr uint32_t TC_A_BYTES = TC_M * TC_KS * 2, TC_B_BYTES = TC_N * TC_KS * 2, TC_STAGE_BYTES = TC_A_BYTES + TC_B_BYTES;
 constexpr uint32_t TC_TMEM_COLS = 128;
 constexpr size_t TC_SMEM = (size_t)TC_STAGE_BYTES * TC_NST + 1024 + 8 * TC_NST + 16;
-// instruction descriptor, kind::f16: D fp32 (bits 4-5 = 1), A and B bf16 (bits 7-9, 10-12 = 1), both
-// K-major (bits 15, 16 = 0), N >> 3 at bits 17-22, M >> 4 at bits 24-28
-constexpr uint32_t TC_IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(TC_N >> 3) << 17) | ((uint32_t)(TC_M >> 4) << 24);
-
-// shared-memory matrix descriptor of a 128-byte-swizzled K-major tile at byte address saddr: start
-// address >> 4 (bits 0-13), leading byte offset 16 (encoded 1, unused for this layout), stride byte
-// offset 1024 between 8-row groups (bits 32-45), descriptor version 1 (bits 46-47), swizzle mode
-// 128B (2 at bits 61-63)
-__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr)
-{
-	return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)1 << 16) | ((uint64_t)(1024 >> 4) << 32) | ((uint64_t)1 << 46) |
-		((uint64_t)2 << 61);
-}
-
-__device__ __forceinline__ void mbar_init(uint32_t a, uint32_t count)
-{
-	asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(a), "r"(count) : "memory");
-}
-
-// bounded wait for the completion of the phase with the given parity
-__device__ __forceinline__ bool mbar_wait(uint32_t a, uint32_t parity)
-{
-	for (long it = 0; it < (1L << 22); ++it) {
-		uint32_t ok;
-		asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n}\n"
-			: "=r"(ok) : "r"(a), "r"(parity) : "memory");
-		if (ok) return true;
-	}
-	return false;
-}
-
+constexpr uint32_t TC_IDESC = tc::idesc_bf16(TC_M, TC_N);
+using tc::sw128_desc;
+using tc::mbar_init;
+using tc::mbar_wait;
 __device__ __forceinline__ void tc_mma(uint32_t tmem, uint64_t adesc, uint64_t bdesc, uint32_t accumulate)
 {
-	asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\ttcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n"
-		::"r"(tmem), "l"(adesc), "l"(bdesc), "r"(TC_IDESC), "r"(accumulate) : "memory");
+	tc::mma_bf16(tmem, adesc, bdesc, TC_IDESC, accumulate);
 }
-
-__device__ __forceinline__ void tc_commit(uint32_t mbar)
-{
-	asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(mbar) : "memory");
-}
-
-// 32 consecutive fp32 columns of this thread's tensor-memory lane
-__device__ __forceinline__ void tc_ld32(uint32_t taddr, uint32_t (&v)[32])
-{
-	asm volatile("tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-		"%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];\n"
-		: "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]), "=r"(v[8]), "=r"(v[9]),
-		  "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]),
-		  "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]), "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]),
-		  "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
-		: "r"(taddr));
-	asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
-}
+__device__ __forceinline__ void tc_commit(uint32_t mbar) { tc::commit(mbar); }
+__device__ __forceinline__ void tc_ld32(uint32_t taddr, uint32_t (&v)[32]) { tc::ld32(taddr, v); }
 
 template <bool HI>
 __global__ void __launch_bounds__(TC_THREADS, 1) k_oz_gemm_tc(const __nv_bfloat16* __restrict__ Da, const int* __restrict__ ea,
