@@ -460,10 +460,13 @@ struct qpc_lgwz {
 	size_t chain_smem = 0;
 	int chain_sstage = 1;	// k_chain stages the S band in shared memory (QPC_CHAIN_SSTAGE=0: read through L1)
 	int chain_warps = 4;	// warps per k_chain block, sharing one staged S band (QPC_CHAIN_WARPS)
-	// the l-space transforms on the tensor cores (qpc_ltrans.cu) for n_l <= 48, with QPC_LTRANS_TC=1:
-	// half-width of the block-diagonal product (0: the FP64 kernel k_transform), the
-	// matrices' digit planes [M][2][8][2 lt_kb][64] and exponents [M][2][2 lt_kb]
+	// the l-space transforms on the tensor cores (qpc_ltrans.cu) for n_l <= 48: half-width of the
+	// block-diagonal product (0: the FP64 kernel k_transform only), the matrices' digit planes
+	// [M][2][8][2 lt_kb][64] and exponents [M][2][2 lt_kb].  A launch uses them when it has at least
+	// one 64-row tile per SM (lt_min_tiles; measured: with fewer, as for one wavefunction, the FP64
+	// kernel's shorter latency wins); QPC_LTRANS_TC=1 uses them for every launch, 0 for none.
 	int lt_kb = 0;
+	long lt_min_tiles = 0;
 	uint16_t* lt_dig = nullptr;
 	int* lt_fex = nullptr;
 	// optional per-kernel timing (CUDA events around each launch on the handle's stream)
@@ -767,9 +770,10 @@ void launch_group_step(qpc_lgwz* h, cudaStream_t st, int b0, long step, long ste
 		int tiles = (N + TR - 1) / TR;
 		size_t smem = sizeof(double2) * 2 * TR * (L | 1);
 		unsigned grid = (unsigned)((long)Bc * M * tiles);
+		const bool use_tc = h->lt_kb && (long)Bc * M * ((N + 63) / 64) >= h->lt_min_tiles;
 		{
 			prof_scope ps(h, QPC_KERNEL_TRANSFORM_FWD, st);
-			if (h->lt_kb)
+			if (use_tc)
 				ltrans_launch(h->lt_kb, h->st, h->eo, h->lt_dig, h->lt_fex, N, L, M, np, 1, h->ntf, step, b0, Bc, h->cmode, h->status,
 					ST_TIMEOUT, st);
 			else
@@ -782,7 +786,7 @@ void launch_group_step(qpc_lgwz* h, cudaStream_t st, int b0, long step, long ste
 		}
 		{
 			prof_scope ps(h, QPC_KERNEL_TRANSFORM_BWD, st);
-			if (h->lt_kb)
+			if (use_tc)
 				ltrans_launch(h->lt_kb, h->eo, h->st, h->lt_dig, h->lt_fex, N, L, M, np, 0, h->ntf, step, b0, Bc, h->cmode, h->status,
 					ST_TIMEOUT, st);
 			else
@@ -1170,7 +1174,12 @@ static int create_impl(const qpc_dims* dims, double dt, const double* S, const d
 		h->ffmap_cur = h->ffmap_id;
 	}
 	const char* ltc = getenv("QPC_LTRANS_TC");
-	h->lt_kb = (ltc && atoi(ltc) != 0) ? ltrans_kb(L) : 0;
+	h->lt_kb = (ltc && atoi(ltc) == 0) ? 0 : ltrans_kb(L);
+	if (h->lt_kb && !(ltc && atoi(ltc) == 1)) {
+		int nsm = 0;
+		if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) nsm = 152;
+		h->lt_min_tiles = nsm;
+	}
 	if (h->lt_kb) {
 		std::vector<uint16_t> dig(ltrans_digit_bytes(M, h->lt_kb) / 2);
 		std::vector<int> fex((size_t)M * 2 * 2 * h->lt_kb);

@@ -1,8 +1,8 @@
 """The length-gauge l-space transform on the tcgen05 tensor cores (qpc_ltrans.cu) through the C ABI
 (qpc_lspace_transform): bit for bit equal to its oracle (oracle/ltrans_oracle.py) for every n_l of
 the tensor-core form, ragged tile counts, rows spanning hundreds of binary orders of magnitude and
-zero rows; and the engine with the tensor-core transforms against the engine with the FP64 kernel
-(QPC_LTRANS_TC=0) over a batched run."""
+zero rows; and the engine with the tensor-core transforms for every launch (QPC_LTRANS_TC=1) against
+the engine with the FP64 kernel (QPC_LTRANS_TC=0) over a batched run."""
 import numpy as np
 import pytest
 
@@ -76,4 +76,4 @@ def test_engine_paths_agree(q, monkeypatch, n_l):
         prop.run(ftab, nt, nt + 3)
         out[mode] = prop.get()
         prop.close()
-    assert rel_l2(out["1"], out["0"]) < 1e-13
+    assert rel_l2(out["1"], out["0"]) < 1e-12	# the short-run bar of the parity tests
