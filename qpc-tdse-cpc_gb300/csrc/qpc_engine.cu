@@ -467,6 +467,7 @@ struct qpc_lgwz {
 	// kernel's shorter latency wins); QPC_LTRANS_TC=1 uses them for every launch, 0 for none.
 	int lt_kb = 0;
 	long lt_min_tiles = 0;
+	bool lt_failed = false;	// a transform launch could not be enqueued (reported by read_status)
 	uint16_t* lt_dig = nullptr;
 	int* lt_fex = nullptr;
 	// optional per-kernel timing (CUDA events around each launch on the handle's stream)
@@ -563,6 +564,11 @@ int read_status(qpc_lgwz* h)
 {
 	int st = 0;
 	if (int rc = copy_to_host(&st, h->status, sizeof(int), h->stream)) return rc;
+	if (h->lt_failed) {
+		h->lt_failed = false;
+		set_error("an l-space transform launch could not be enqueued");
+		return QPC_ERR_CUDA;
+	}
 	if (st & ST_PIVOT) { set_error("zero pivot in a Crank-Nicolson factorisation"); return QPC_ERR_SINGULAR; }
 	if (st & ST_NONFINITE) { set_error("non-finite value in the state"); return QPC_ERR_NUMERIC; }
 	if (st & ST_TIMEOUT) { set_error("a tensor-core wait of the l-space transform ran out"); return QPC_ERR_TIMEOUT; }
@@ -773,10 +779,11 @@ void launch_group_step(qpc_lgwz* h, cudaStream_t st, int b0, long step, long ste
 		const bool use_tc = h->lt_kb && (long)Bc * M * ((N + 63) / 64) >= h->lt_min_tiles;
 		{
 			prof_scope ps(h, QPC_KERNEL_TRANSFORM_FWD, st);
-			if (use_tc)
-				ltrans_launch(h->lt_kb, h->st, h->eo, h->lt_dig, h->lt_fex, N, L, M, np, 1, h->ntf, step, b0, Bc, h->cmode, h->status,
-					ST_TIMEOUT, st);
-			else
+			if (use_tc) {
+				if (ltrans_launch(h->lt_kb, h->st, h->eo, h->lt_dig, h->lt_fex, N, L, M, np, 1, h->ntf, step, b0, Bc, h->cmode, h->status,
+						ST_TIMEOUT, st))
+					h->lt_failed = true;
+			} else
 				k_transform<<<grid, 256, smem, st>>>(h->st, h->eo, h->Vh, N, L, M, np, 1, h->ntf, step, b0, Bc, h->cmode);
 			LAUNCH(h);
 		}
@@ -786,10 +793,11 @@ void launch_group_step(qpc_lgwz* h, cudaStream_t st, int b0, long step, long ste
 		}
 		{
 			prof_scope ps(h, QPC_KERNEL_TRANSFORM_BWD, st);
-			if (use_tc)
-				ltrans_launch(h->lt_kb, h->eo, h->st, h->lt_dig, h->lt_fex, N, L, M, np, 0, h->ntf, step, b0, Bc, h->cmode, h->status,
-					ST_TIMEOUT, st);
-			else
+			if (use_tc) {
+				if (ltrans_launch(h->lt_kb, h->eo, h->st, h->lt_dig, h->lt_fex, N, L, M, np, 0, h->ntf, step, b0, Bc, h->cmode, h->status,
+						ST_TIMEOUT, st))
+					h->lt_failed = true;
+			} else
 				k_transform<<<grid, 256, smem, st>>>(h->eo, h->st, h->Vh, N, L, M, np, 0, h->ntf, step, b0, Bc, h->cmode);
 			LAUNCH(h);
 		}
