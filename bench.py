@@ -298,7 +298,9 @@ def run_engine(args, sync=None):
     gpu_launches += 0
     pl.close()
 
-    cpu = cpu_baseline(q, S, R, H, c0, ftab, dt, n_l, budget_s=args.cpu_seconds) if not args.no_cpu else None
+    # the CPU sample may run up to the shortest pulse, so that it lasts its time budget
+    ftab_cpu = np.stack([t[:int(nt.min()) + 1] for t in tabs])
+    cpu = cpu_baseline(q, S, R, H, c0, ftab_cpu, dt, n_l, budget_s=args.cpu_seconds) if not args.no_cpu else None
     line = {
         "metric": "wavefunction-steps/s (batched, 256 wavefunctions)",
         "value": value, "unit": "wf-steps/s", "n_gpus": 1, "steps": K, "warmup": W,
