@@ -931,7 +931,9 @@ def main():
         print(json.dumps(run_reference(args)))
         return
     if world > 1:
-        # replicas only: every rank runs its own batch; value = sum over ranks
+        # replicas only: every rank runs its own batch; value = sum over ranks.  The CPU baseline is
+        # a 1-GPU figure (rank 0 at N = 1), so no rank takes it here.
+        args.no_cpu = True
         import torch
         import torch.distributed as dist
         dist.init_process_group("nccl")
